@@ -1,0 +1,282 @@
+/*
+ * sparq_gb300.h — C ABI of the GB300 (sm_103a) engine for SparQ's sparse-state
+ * gate-application path.
+ *
+ * The engine keeps a sparse quantum state in HBM as structure-of-arrays:
+ *   - K packed 64-bit key words per basis entry (every active register is a bit
+ *     field of width <= 64 inside one word; word-major arrays, one per word);
+ *   - one complex128 amplitude per entry (interleaved re/im, 16 bytes).
+ *
+ * Every entry point returns an sq_status (0 = success). No C++ exception crosses
+ * this boundary; sq_last_error() returns a message for the last failure on the
+ * calling thread. All calls are stream-ordered on the library's stream and are
+ * synchronous with respect to the host where they return sizes.
+ *
+ * Each declaration cites the reference interface it replaces (paths are relative
+ * to the SparQSim project root). Register ids, condition kinds, XOR-out
+ * conventions and the order of matrix elements follow the reference operators.
+ */
+#ifndef SPARQ_GB300_H
+#define SPARQ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SQ_ABI_VERSION 1
+#define SQ_MAX_REGISTERS 64     /* same cap as the reference CUDA build (basic_components.h:223-236) */
+#define SQ_MAX_KEY_WORDS 8      /* 512 packed key bits per entry */
+#define SQ_MAX_CONDITIONS 8
+#define SQ_MAX_PROGRAM 32       /* instructions per fused elementwise launch */
+
+typedef enum {
+    SQ_OK = 0,
+    SQ_ERR_INVALID = 1,        /* bad argument (reference: throw_invalid_input) */
+    SQ_ERR_CUDA = 2,           /* CUDA runtime error (reference: CUDA_CHECK) */
+    SQ_ERR_OOM = 3,            /* device allocation failed */
+    SQ_ERR_CAPACITY = 4,       /* a size exceeds a documented maximum */
+    SQ_ERR_DEVICE_TIMEOUT = 5, /* a bounded device-side wait gave up */
+    SQ_ERR_BAD_RESULT = 6,     /* NaN norm (reference: throw_bad_result, dark_magic.cpp:26-27) */
+    SQ_ERR_UNSUPPORTED = 7,    /* operation/shape not provided by this engine */
+    SQ_ERR_NO_DEVICE = 8       /* no CUDA device visible */
+} sq_status;
+
+/* Register types; reference StateStorageType (qram-simulator submodule). */
+typedef enum {
+    SQ_GENERAL = 0,
+    SQ_UNSIGNED = 1,
+    SQ_SIGNED = 2,
+    SQ_BOOLEAN = 3,
+    SQ_RATIONAL = 4
+} sq_reg_type;
+
+/* Control conditions, AND-combined; reference ClassControllable
+ * (global_macros.h:28-86, 104-284). */
+typedef enum {
+    SQ_COND_NONZERO = 0,  /* register value != 0            (conditioned_by_nonzeros) */
+    SQ_COND_ALL_ONES = 1, /* register value == 2^width - 1  (conditioned_by_all_ones) */
+    SQ_COND_BIT = 2,      /* bit `param` of register is 1   (conditioned_by_bit)      */
+    SQ_COND_VALUE = 3     /* register value == param         (conditioned_by_value)    */
+} sq_cond_kind;
+
+typedef struct {
+    uint32_t kind;   /* sq_cond_kind */
+    uint32_t reg;    /* register id */
+    uint64_t param;  /* bit position (SQ_COND_BIT) or value (SQ_COND_VALUE) */
+} sq_condition;
+
+typedef struct {
+    uint32_t count;  /* number of valid entries in c[] */
+    uint32_t reserved;
+    sq_condition c[SQ_MAX_CONDITIONS];
+} sq_cond;
+
+/* Elementwise opcodes. Each is one reference operator's per-entry update;
+ * the comment gives the reference (file:line of the CPU loop) and the
+ * operand slots used in sq_instr (reg[0..3], imm[0..2], c[0..7]). */
+typedef enum {
+    SQ_OP_NOP = 0,
+    SQ_OP_FLIP_BOOLS = 1,            /* quantum_arithmetic.cpp:11-30   reg0 = ~reg0 & mask */
+    SQ_OP_SWAP_BOOL_BOOL = 2,        /* :32-61    reg0 bit imm0 <-> reg1 bit imm1 */
+    SQ_OP_SHIFT_LEFT = 3,            /* :63-92    cyclic rotate reg0 left by imm0 */
+    SQ_OP_SHIFT_RIGHT = 4,           /* :95-121   cyclic rotate reg0 right by imm0 */
+    SQ_OP_MULT_UINT_CONST = 5,       /* :137-155  reg2 = (reg2 ^ reg0*imm0) & mask(reg2) */
+    SQ_OP_ADD_MULT_UINT_CONST = 6,   /* :157-196  reg2 = (reg2 +/- imm0*reg0) & mask */
+    SQ_OP_MOD_MULT_CONST = 7,        /* :222-285  reg0 = reg0*imm0 % imm1 (imm0 = opnum) */
+    SQ_OP_ADD_UINT_UINT = 8,         /* :287-306  reg2 ^= (reg0 + reg1) & mask */
+    SQ_OP_ADD_UINT_UINT_INPLACE = 9, /* :308-349  reg1 = (reg1 +/- reg0) & mask */
+    SQ_OP_ADD_UINT_CONST = 10,       /* :351-369  reg2 ^= (reg0 + imm0) & mask */
+    SQ_OP_ADD_CONST_INPLACE = 11,    /* :371-411  reg0 = (reg0 +/- imm0) & mask */
+    SQ_OP_SUB_UINT_UINT = 12,        /* :490-509  reg2 ^= (reg0 - reg1) & mask */
+    SQ_OP_NEG_UINT = 13,             /* :511-530  reg1 ^= (0 - reg0) & mask */
+    SQ_OP_ABS_SINT = 14,             /* :532-554  reg1 ^= |sext(reg0)| & mask */
+    SQ_OP_MUL_UINT_UINT = 15,        /* :556-575  reg2 ^= (reg0 * reg1) & mask */
+    SQ_OP_DIV_UINT_UINT = 16,        /* :577-600  reg2 ^= (reg1 ? reg0/reg1 : 0) & mask */
+    SQ_OP_SQRT_UINT = 17,            /* :602-620  reg1 ^= isqrt(reg0) & mask */
+    SQ_OP_SELECT_BOOL = 18,          /* :623-644  reg3 ^= (reg0&1 ? reg1 : reg2) & mask */
+    SQ_OP_AND_UINT_UINT = 19,        /* :646-665 */
+    SQ_OP_OR_UINT_UINT = 20,         /* :667-686 */
+    SQ_OP_XOR_UINT_UINT = 21,        /* :688-707 */
+    SQ_OP_LESS_SINT_SINT = 22,       /* :709-729  reg2 ^= sext(reg0) < sext(reg1) */
+    SQ_OP_CARRY_UINT_UINT = 23,      /* :731-754  reg3 ^= carry out of width(reg2) */
+    SQ_OP_OVERFLOW_SINT_SINT = 24,   /* :756-785  reg3 ^= signed overflow at width(reg2) */
+    SQ_OP_MULOVERFLOW_UINT_UINT = 25,/* :787-817  reg3 ^= product overflows width(reg2) */
+    SQ_OP_ISZERO_UINT = 26,          /* :819-837  reg1 ^= (reg0 == 0) */
+    SQ_OP_NEGATIVE_SINT = 27,        /* :839-857  reg1 ^= sext(reg0) < 0 */
+    SQ_OP_ADD_ANYINT_INPLACE = 28,   /* :869-907  reg0 = (reg0 +/- ext(reg1)) & mask(reg0) */
+    SQ_OP_ASSIGN = 29,               /* :909-930  reg1 = (reg1 ^ reg0) & mask(reg1) */
+    SQ_OP_COMPARE_UINT_UINT = 30,    /* :932-959  eq: reg3 ^= 1, else reg2 ^= (l < r) */
+    SQ_OP_LESS_UINT_UINT = 31,       /* :961-980  reg2 ^= (reg0 < reg1) */
+    SQ_OP_SWAP_GENERAL = 32,         /* :982-999  swap(reg0, reg1) */
+    SQ_OP_GETMID_UINT_UINT = 33,     /* :1001-1020 reg2 ^= (reg0 + reg1) / 2 */
+    SQ_OP_X_BOOL = 34,               /* basic_gates.cpp:383-401  flip bit imm0 of reg0 */
+    SQ_OP_INIT_UNSAFE = 35,          /* dark_magic.cpp:35-40     reg0 = imm0 */
+    SQ_OP_QRAM_LOAD = 36,            /* qram.cpp:15-35  reg1 ^= table[reg0 mod 2^addr_size] */
+    /* amplitude-only or key+amplitude elementwise ops */
+    SQ_OP_PHASE_BOOL = 64,           /* basic_gates.cpp:11-54  amp *= c0 if bit imm0 of reg0 */
+    SQ_OP_GLOBAL_PHASE = 65,         /* parallel_phase_operations.cpp:72-107  amp *= c0 */
+    SQ_OP_Y_BOOL = 66,               /* basic_gates.cpp:418-441 */
+    SQ_OP_REFLECTION_BOOL = 67,      /* parallel_phase_operations.cpp:46-70 regs reg0..reg[imm0-1], imm1 = inverse */
+    SQ_OP_ZERO_COND_PHASE_FLIP = 68, /* parallel_phase_operations.cpp:11-31 regs reg0..reg[imm0-1] */
+    SQ_OP_ROT_DIAGONAL = 69,         /* basic_gates.cpp:110-133 amp *= (bit ? c1 : c0) */
+    SQ_OP_ROT_OFF_DIAGONAL = 70      /* basic_gates.cpp:146-171 flip bit, amp *= (bit ? c1 : c0) */
+} sq_opcode;
+
+/* One elementwise instruction. Register ids in reg[], integer constants in
+ * imm[], complex constants as (re, im) pairs in c[]. `dag` selects the
+ * inverse for in-place ops that have one. */
+typedef struct sq_qram sq_qram;
+typedef struct {
+    uint32_t op;        /* sq_opcode */
+    uint32_t dag;       /* 1 = apply the adjoint (in-place arithmetic) */
+    uint32_t reg[4];
+    uint64_t imm[3];
+    double c[8];        /* c0 = (c[0], c[1]), c1 = (c[2], c[3]), ... */
+    const sq_qram* qram;
+    sq_cond cond;
+} sq_instr;
+
+typedef struct sq_state sq_state;
+
+/* ------------------------------------------------------------------ */
+/* Library                                                            */
+/* ------------------------------------------------------------------ */
+int sq_abi_version(void);
+const char* sq_last_error(void);
+/* Select the CUDA device and create the library stream (idempotent). */
+int sq_init(int device);
+/* Block until all work on the library stream is done; reports device-side
+ * error flags raised by bounded waits (SQ_ERR_DEVICE_TIMEOUT). */
+int sq_synchronize(void);
+/* Number of kernels this library has launched since load. */
+int sq_launch_count(uint64_t* count);
+/* The library's CUDA stream (cudaStream_t), for callers that order their own work after it. */
+int sq_get_stream(void** stream);
+
+/* ------------------------------------------------------------------ */
+/* Register table — process-global, like System::name_register_map     */
+/* (basic_components.h:239-283, basic_components.cpp:151-459).        */
+/* ------------------------------------------------------------------ */
+/* System::clear (basic_components.cpp:151-163) */
+int sq_system_clear(void);
+/* System::add_register (basic_components.cpp:330-364): reuses freed ids LIFO. */
+int sq_system_add_register(uint32_t type, uint32_t width, uint32_t* id_out);
+/* System::remove_register (basic_components.cpp:378-389) */
+int sq_system_remove_register(uint32_t id);
+/* System::type_of / size_of / status_of plus this engine's packing. */
+int sq_system_register_info(uint32_t id, uint32_t* type, uint32_t* width, uint32_t* active,
+                            uint32_t* word, uint32_t* shift);
+int sq_system_register_count(uint32_t* n);
+int sq_system_key_words(uint32_t* k);
+int sq_system_set_register_type(uint32_t id, uint32_t type);
+
+/* ------------------------------------------------------------------ */
+/* State — replaces CuSparseState (cuda/basic_components.cuh:161-328). */
+/* ------------------------------------------------------------------ */
+/* A new state holds one entry |0...0> with amplitude 1 (SparseState(),
+ * basic_components.h:604-606). `capacity` is an initial reservation. */
+int sq_state_create(uint64_t capacity, sq_state** out);
+int sq_state_destroy(sq_state* st);
+int sq_state_size(const sq_state* st, uint64_t* n);
+int sq_state_capacity(const sq_state* st, uint64_t* cap);
+int sq_state_reserve(sq_state* st, uint64_t capacity);
+/* reset_systems (system_operations.cpp:107-116): one zero entry, amplitude 1. */
+int sq_state_reset(sq_state* st);
+int sq_state_copy(sq_state* dst, const sq_state* src);
+/* Host AoS upload/download, one uint64 per register id per entry (the
+ * reference System layout): regs[i * nregs + id], amps[2*i], amps[2*i+1]. */
+int sq_state_upload(sq_state* st, uint64_t n, const uint64_t* regs, uint32_t nregs, const double* amps);
+int sq_state_download(const sq_state* st, uint64_t* regs, uint32_t nregs, double* amps);
+/* Device pointers of the live arrays (valid until the next call that resizes). */
+int sq_state_device_arrays(sq_state* st, uint64_t** key_words, uint32_t* k, double** amps);
+
+/* ------------------------------------------------------------------ */
+/* QRAM table — replaces CuQRAMCircuit::memory_dev (cuda/qram.cu:68-107) */
+/* ------------------------------------------------------------------ */
+/* qram_qutrit::QRAMCircuit(addr_size, data_size, memory): the table has
+ * 2^address_size words; it is copied to HBM once, narrowed to the smallest
+ * of u16/u32/u64 that holds every word. */
+int sq_qram_create(uint32_t address_size, uint32_t data_size, const uint64_t* memory, uint64_t n_words,
+                   sq_qram** out);
+int sq_qram_destroy(sq_qram* q);
+
+/* ------------------------------------------------------------------ */
+/* Elementwise operators                                               */
+/* ------------------------------------------------------------------ */
+/* Runs up to SQ_MAX_PROGRAM instructions over every entry in one pass
+ * (one launch); each instruction has its own conditions. */
+int sq_apply_program(sq_state* st, const sq_instr* prog, uint32_t n);
+/* Convenience entry points; each is a one-instruction program. */
+int sq_add_uint_uint(sq_state* st, uint32_t lhs, uint32_t rhs, uint32_t res, const sq_cond* cond); /* Add_UInt_UInt, quantum_arithmetic.cpp:287 */
+int sq_add_uint_uint_inplace(sq_state* st, uint32_t lhs, uint32_t rhs, const sq_cond* cond, int dag); /* :308,:327 */
+int sq_add_uint_const(sq_state* st, uint32_t lhs, uint64_t c, uint32_t res, const sq_cond* cond); /* :351 */
+int sq_add_const_inplace(sq_state* st, uint32_t reg, uint64_t c, const sq_cond* cond, int dag); /* :372,:392 */
+int sq_mult_uint_const(sq_state* st, uint32_t lhs, uint64_t c, uint32_t res, const sq_cond* cond); /* :137 */
+int sq_add_mult_uint_const(sq_state* st, uint32_t lhs, uint64_t c, uint32_t res, const sq_cond* cond, int dag); /* :157,:177 */
+int sq_mul_uint_uint(sq_state* st, uint32_t lhs, uint32_t rhs, uint32_t res, const sq_cond* cond); /* :556 */
+int sq_add_anyint_inplace(sq_state* st, uint32_t lhs, uint32_t rhs, const sq_cond* cond, int dag); /* :869,:889 */
+int sq_assign(sq_state* st, uint32_t src, uint32_t dst, const sq_cond* cond); /* :909 */
+int sq_shift(sq_state* st, uint32_t reg, uint32_t digits, int left, const sq_cond* cond); /* :63,:94 */
+int sq_swap(sq_state* st, uint32_t a, uint32_t b, const sq_cond* cond); /* :981 */
+int sq_x_bool(sq_state* st, uint32_t reg, uint32_t digit, const sq_cond* cond); /* basic_gates.cpp:383 */
+int sq_flip_bools(sq_state* st, uint32_t reg, const sq_cond* cond); /* quantum_arithmetic.cpp:11 */
+int sq_init_unsafe(sq_state* st, uint32_t reg, uint64_t value); /* dark_magic.cpp:35 */
+/* QRAMLoad::noise_free_impl (qram.cpp:15-35): data ^= memory[addr mod 2^addr_size]. */
+int sq_qram_load(sq_state* st, const sq_qram* q, uint32_t addr, uint32_t data, const sq_cond* cond);
+/* Phase_Bool (basic_gates.cpp:11-54): amp *= e^{+-i lambda} where bit `digit` of reg is set. */
+int sq_phase_bool(sq_state* st, uint32_t reg, uint32_t digit, double lambda, const sq_cond* cond, int dag);
+/* GlobalPhase (parallel_phase_operations.cpp:72-107): amp *= c (conj(c) for dag). */
+int sq_global_phase(sq_state* st, double re, double im, const sq_cond* cond, int dag);
+/* Reflection_Bool (parallel_phase_operations.cpp:46-70). */
+int sq_reflection_bool(sq_state* st, const uint32_t* regs, uint32_t nregs, int inverse, const sq_cond* cond);
+/* ZeroConditionalPhaseFlip (parallel_phase_operations.cpp:11-31). */
+int sq_zero_cond_phase_flip(sq_state* st, const uint32_t* regs, uint32_t nregs, const sq_cond* cond);
+
+/* ------------------------------------------------------------------ */
+/* Split / merge operators (group by key except target bits)           */
+/* ------------------------------------------------------------------ */
+/* Hadamard_Int (hadamard.cpp:18-162): H on the low n_digits bits of reg;
+ * groups = entries equal on every other active bit; ClearZero(eps) after. */
+int sq_hadamard_int(sq_state* st, uint32_t reg, uint32_t n_digits, const sq_cond* cond);
+/* Hadamard_Int_Full (hadamard.cpp:181-338): H on the whole register. */
+int sq_hadamard_int_full(sq_state* st, uint32_t reg, const sq_cond* cond);
+/* Hadamard_Bool (hadamard.cpp:340-439): reg must be 1 bit wide. */
+int sq_hadamard_bool(sq_state* st, uint32_t reg, const sq_cond* cond);
+/* Rot_Bool (basic_gates.cpp:74-357): 2x2 unitary mat = {m00, m01, m10, m11}
+ * as 8 doubles (re, im) on bit `digit` of reg; dag applies mat^dagger. */
+int sq_rot_bool(sq_state* st, uint32_t reg, uint32_t digit, const double* mat8, const sq_cond* cond, int dag);
+/* CondRot_Rational_Bool (condrot.cpp:12-152): angle 2*pi*in/2^width(in) on the 1-bit out. */
+int sq_condrot_rational_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, int dag);
+
+/* ------------------------------------------------------------------ */
+/* Prune / norm / merge / register surgery                              */
+/* ------------------------------------------------------------------ */
+/* clearzero_default_eps (system_operations.h:577), initially 1e-14. */
+int sq_set_clearzero_eps(double eps);
+int sq_get_clearzero_eps(double* eps);
+/* ClearZero (system_operations.cpp:371-382): drop entries with |a|^2 < eps;
+ * order of survivors is preserved. */
+int sq_clear_zero(sq_state* st, double eps);
+/* Normalize (dark_magic.cpp:11-32): a *= 1/sqrt(sum |a|^2); norm_sq_out may be NULL. */
+int sq_normalize(sq_state* st, double* norm_sq_out);
+/* Sum of |a|^2 (CheckNormalization's quantity, debugger.h). */
+int sq_norm_sq(const sq_state* st, double* out);
+/* add_systems (system_operations.h:157-175): dst += coef * src, entries with
+ * equal keys summed, |a|^2 < eps dropped. */
+int sq_add_systems(sq_state* dst, const sq_state* src, double coef);
+/* AddRegister (system_operations.cpp:269-290): new zeroed register. */
+int sq_add_register_sync(sq_state* st, uint32_t type, uint32_t width, uint32_t* id_out);
+/* RemoveRegister / remove_register_synchronous (basic_components.cpp:398-430). */
+int sq_remove_register_sync(sq_state* st, uint32_t id);
+/* SplitRegister (system_operations.cpp:121-158): low `second_size` bits become a new register. */
+int sq_split_register(sq_state* st, uint32_t first, uint32_t second_size, uint32_t* second_out);
+/* CombineRegister (system_operations.cpp:165-203): first = first << |second| | second; second removed. */
+int sq_combine_register(sq_state* st, uint32_t first, uint32_t second);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPARQ_GB300_H */

@@ -1,0 +1,724 @@
+// api.cu — the extern "C" boundary (include/sparq_gb300.h). Validates
+// arguments the way the reference operator constructors do, translates
+// register ids into packed fields and forwards to the device pipelines.
+// Exceptions never cross the boundary: every entry returns an sq_status and
+// records a message for sq_last_error().
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "sq_internal.cuh"
+
+namespace sq {
+void init_device(int device);
+uint64_t launches();
+void check_device_error();
+}  // namespace sq
+
+struct sq_state {
+    sq::State s;
+};
+struct sq_qram {
+    sq::QramTable t;
+};
+
+using namespace sq;
+
+static thread_local std::string t_err;
+
+#define SQ_API_BEGIN try {
+#define SQ_API_END                                   \
+    return SQ_OK;                                    \
+    }                                                \
+    catch (const sq::Error& e) {                     \
+        t_err = e.msg;                               \
+        return e.code;                               \
+    }                                                \
+    catch (const std::bad_alloc&) {                  \
+        t_err = "host allocation failed";            \
+        return SQ_ERR_OOM;                           \
+    }                                                \
+    catch (const std::exception& e) {                \
+        t_err = e.what();                            \
+        return SQ_ERR_INVALID;                       \
+    }
+
+static void need(bool ok, const char* msg) {
+    if (!ok) fail(SQ_ERR_INVALID, msg);
+}
+static State& S(sq_state* st) {
+    need(st != nullptr, "null state");
+    return st->s;
+}
+static const State& S(const sq_state* st) {
+    need(st != nullptr, "null state");
+    return st->s;
+}
+
+static sq_instr make_instr(uint32_t op, const sq_cond* cond) {
+    sq_instr in;
+    memset(&in, 0, sizeof(in));
+    in.op = op;
+    if (cond) in.cond = *cond;
+    return in;
+}
+static int run1(sq_state* st, const sq_instr& in) {
+    SQ_API_BEGIN
+    run_program(S(st), &in, 1);
+    SQ_API_END
+}
+
+extern "C" {
+
+int sq_abi_version(void) { return SQ_ABI_VERSION; }
+const char* sq_last_error(void) { return t_err.c_str(); }
+
+int sq_init(int device) {
+    SQ_API_BEGIN
+    init_device(device);
+    SQ_API_END
+}
+
+int sq_synchronize(void) {
+    SQ_API_BEGIN
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    check_device_error();
+    SQ_API_END
+}
+
+int sq_launch_count(uint64_t* count) {
+    SQ_API_BEGIN
+    need(count != nullptr, "null pointer");
+    *count = launches();
+    SQ_API_END
+}
+
+int sq_get_stream(void** s) {
+    SQ_API_BEGIN
+    need(s != nullptr, "null pointer");
+    *s = (void*)stream();
+    SQ_API_END
+}
+
+// ------------------------------------------------------------------ registers
+int sq_system_clear(void) {
+    SQ_API_BEGIN
+    RegTable& t = regtable();
+    double eps = 1e-14;
+    t = RegTable();
+    t.clearzero_eps = eps;
+    SQ_API_END
+}
+
+int sq_system_add_register(uint32_t type, uint32_t width, uint32_t* id_out) {
+    SQ_API_BEGIN
+    need(id_out != nullptr, "null pointer");
+    *id_out = regtable().add(type, width);
+    SQ_API_END
+}
+
+int sq_system_remove_register(uint32_t id) {
+    SQ_API_BEGIN
+    regtable().remove(id);
+    SQ_API_END
+}
+
+int sq_system_register_info(uint32_t id, uint32_t* type, uint32_t* width, uint32_t* active, uint32_t* word,
+                            uint32_t* shift) {
+    SQ_API_BEGIN
+    const RegTable& t = regtable();
+    need(id < t.regs.size(), "register not found");
+    const RegEntry& r = t.regs[id];
+    if (type) *type = r.type;
+    if (width) *width = r.width;
+    if (active) *active = r.active ? 1 : 0;
+    if (word) *word = r.word;
+    if (shift) *shift = r.shift;
+    SQ_API_END
+}
+
+int sq_system_register_count(uint32_t* n) {
+    SQ_API_BEGIN
+    need(n != nullptr, "null pointer");
+    *n = (uint32_t)regtable().regs.size();
+    SQ_API_END
+}
+
+int sq_system_key_words(uint32_t* k) {
+    SQ_API_BEGIN
+    need(k != nullptr, "null pointer");
+    *k = regtable().k;
+    SQ_API_END
+}
+
+int sq_system_set_register_type(uint32_t id, uint32_t type) {
+    SQ_API_BEGIN
+    need(type <= SQ_RATIONAL, "bad register type");
+    (void)regtable().at(id);
+    regtable().regs[id].type = type;
+    SQ_API_END
+}
+
+// ------------------------------------------------------------------ state
+int sq_state_create(uint64_t capacity, sq_state** out) {
+    SQ_API_BEGIN
+    need(out != nullptr, "null pointer");
+    sq_state* st = new sq_state();
+    try {
+        ensure_buffers(st->s.live, capacity ? capacity : 1, regtable().k, 0);
+        // one entry |0...0>, amplitude 1
+        double2 one = make_double2(1.0, 0.0);
+        SQ_CUDA(cudaMemcpyAsync(st->s.live.amp, &one, sizeof(one), cudaMemcpyHostToDevice, stream()));
+        for (uint32_t w = 0; w < st->s.live.kalloc; ++w)
+            SQ_CUDA(cudaMemsetAsync(st->s.live.keys[w], 0, 8, stream()));
+        SQ_CUDA(cudaStreamSynchronize(stream()));
+        st->s.n = 1;
+    } catch (...) {
+        free_buffers(st->s.live);
+        delete st;
+        throw;
+    }
+    *out = st;
+    SQ_API_END
+}
+
+int sq_state_destroy(sq_state* st) {
+    SQ_API_BEGIN
+    if (!st) return SQ_OK;
+    free_buffers(st->s.live);
+    free_buffers(st->s.spare);
+    delete st;
+    SQ_API_END
+}
+
+int sq_state_size(const sq_state* st, uint64_t* n) {
+    SQ_API_BEGIN
+    need(n != nullptr, "null pointer");
+    *n = S(st).n;
+    SQ_API_END
+}
+
+int sq_state_capacity(const sq_state* st, uint64_t* cap) {
+    SQ_API_BEGIN
+    need(cap != nullptr, "null pointer");
+    *cap = S(st).live.cap;
+    SQ_API_END
+}
+
+int sq_state_reserve(sq_state* st, uint64_t capacity) {
+    SQ_API_BEGIN
+    State& s = S(st);
+    ensure_buffers(s.live, capacity, regtable().k, s.n);
+    SQ_API_END
+}
+
+int sq_state_reset(sq_state* st) {
+    SQ_API_BEGIN
+    State& s = S(st);
+    sync_words(s);
+    ensure_buffers(s.live, 1, regtable().k, 0);
+    double2 one = make_double2(1.0, 0.0);
+    SQ_CUDA(cudaMemcpyAsync(s.live.amp, &one, sizeof(one), cudaMemcpyHostToDevice, stream()));
+    for (uint32_t w = 0; w < s.live.kalloc; ++w) SQ_CUDA(cudaMemsetAsync(s.live.keys[w], 0, 8, stream()));
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    s.n = 1;
+    SQ_API_END
+}
+
+int sq_state_copy(sq_state* dst, const sq_state* src) {
+    SQ_API_BEGIN
+    State& d = S(dst);
+    const State& s = S(src);
+    const uint32_t k = regtable().k;
+    ensure_buffers(d.live, std::max<uint64_t>(s.n, 1), k, 0);
+    for (uint32_t w = 0; w < k; ++w) {
+        if (w < s.live.kalloc)
+            SQ_CUDA(cudaMemcpyAsync(d.live.keys[w], s.live.keys[w], s.n * 8, cudaMemcpyDeviceToDevice, stream()));
+        else
+            SQ_CUDA(cudaMemsetAsync(d.live.keys[w], 0, s.n * 8, stream()));
+    }
+    SQ_CUDA(cudaMemcpyAsync(d.live.amp, s.live.amp, s.n * 16, cudaMemcpyDeviceToDevice, stream()));
+    d.n = s.n;
+    SQ_API_END
+}
+
+// Host packing: one uint64 per register id per entry -> K packed words.
+int sq_state_upload(sq_state* st, uint64_t n, const uint64_t* regs, uint32_t nregs, const double* amps) {
+    SQ_API_BEGIN
+    State& s = S(st);
+    need(n == 0 || (regs != nullptr || nregs == 0) , "null regs");
+    need(n == 0 || amps != nullptr, "null amps");
+    const RegTable& t = regtable();
+    const uint32_t k = t.k;
+    std::vector<uint64_t> packed((size_t)k * n, 0);
+    for (uint32_t id = 0; id < nregs && id < t.regs.size(); ++id) {
+        const RegEntry& r = t.regs[id];
+        if (!r.active || r.width == 0) continue;
+        const uint64_t m = wmask(r.width);
+        uint64_t* dst = packed.data() + (size_t)r.word * n;
+        for (uint64_t i = 0; i < n; ++i) {
+            const uint64_t v = regs[i * nregs + id];
+            if (v & ~m) fail(SQ_ERR_INVALID, "register value wider than its register");
+            dst[i] |= v << r.shift;
+        }
+    }
+    ensure_buffers(s.live, std::max<uint64_t>(n, 1), k, 0);
+    for (uint32_t w = 0; w < k; ++w)
+        SQ_CUDA(cudaMemcpyAsync(s.live.keys[w], packed.data() + (size_t)w * n, n * 8, cudaMemcpyHostToDevice, stream()));
+    SQ_CUDA(cudaMemcpyAsync(s.live.amp, amps, n * 16, cudaMemcpyHostToDevice, stream()));
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    s.n = n;
+    SQ_API_END
+}
+
+int sq_state_download(const sq_state* st, uint64_t* regs, uint32_t nregs, double* amps) {
+    SQ_API_BEGIN
+    const State& s = S(st);
+    const RegTable& t = regtable();
+    const uint64_t n = s.n;
+    const uint32_t k = std::min<uint32_t>(t.k, s.live.kalloc);
+    std::vector<uint64_t> packed((size_t)k * n);
+    for (uint32_t w = 0; w < k; ++w)
+        SQ_CUDA(cudaMemcpyAsync(packed.data() + (size_t)w * n, s.live.keys[w], n * 8, cudaMemcpyDeviceToHost, stream()));
+    if (amps) SQ_CUDA(cudaMemcpyAsync(amps, s.live.amp, n * 16, cudaMemcpyDeviceToHost, stream()));
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    if (regs) {
+        for (uint64_t i = 0; i < n; ++i)
+            for (uint32_t id = 0; id < nregs; ++id) {
+                uint64_t v = 0;
+                if (id < t.regs.size() && t.regs[id].active && t.regs[id].word < k) {
+                    const RegEntry& r = t.regs[id];
+                    v = (packed[(size_t)r.word * n + i] >> r.shift) & wmask(r.width);
+                }
+                regs[i * nregs + id] = v;
+            }
+    }
+    SQ_API_END
+}
+
+int sq_state_device_arrays(sq_state* st, uint64_t** key_words, uint32_t* k, double** amps) {
+    SQ_API_BEGIN
+    State& s = S(st);
+    sync_words(s);
+    if (key_words)
+        for (uint32_t w = 0; w < regtable().k; ++w) key_words[w] = s.live.keys[w];
+    if (k) *k = regtable().k;
+    if (amps) *amps = (double*)s.live.amp;
+    SQ_API_END
+}
+
+// ------------------------------------------------------------------ QRAM
+int sq_qram_create(uint32_t address_size, uint32_t data_size, const uint64_t* memory, uint64_t n_words,
+                   sq_qram** out) {
+    SQ_API_BEGIN
+    need(out != nullptr, "null pointer");
+    need(address_size <= 40, "QRAM address_size > 40");
+    need(data_size <= 64, "QRAM data_size > 64");
+    const uint64_t words = 1ull << address_size;
+    need(memory != nullptr && n_words >= words, "QRAM memory must hold 2^address_size words");
+    uint64_t mx = 0;
+    for (uint64_t i = 0; i < words; ++i) mx = memory[i] > mx ? memory[i] : mx;
+    uint32_t eb = mx <= 0xffffull ? 2 : (mx <= 0xffffffffull ? 4 : 8);
+    std::vector<char> buf((size_t)words * eb);
+    for (uint64_t i = 0; i < words; ++i) {
+        if (eb == 2) ((uint16_t*)buf.data())[i] = (uint16_t)memory[i];
+        else if (eb == 4) ((uint32_t*)buf.data())[i] = (uint32_t)memory[i];
+        else ((uint64_t*)buf.data())[i] = memory[i];
+    }
+    sq_qram* q = new sq_qram();
+    q->t.elem_bytes = eb;
+    q->t.address_size = address_size;
+    q->t.data_size = data_size;
+    q->t.n_words = words;
+    q->t.max_word = mx;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, buf.size());
+    if (e != cudaSuccess) {
+        delete q;
+        SQ_CUDA(e);
+    }
+    q->t.dev = p;
+    SQ_CUDA(cudaMemcpy(p, buf.data(), buf.size(), cudaMemcpyHostToDevice));
+    *out = q;
+    SQ_API_END
+}
+
+int sq_qram_destroy(sq_qram* q) {
+    SQ_API_BEGIN
+    if (!q) return SQ_OK;
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    if (q->t.dev) SQ_CUDA(cudaFree(q->t.dev));
+    delete q;
+    SQ_API_END
+}
+
+// ------------------------------------------------------------------ elementwise
+int sq_apply_program(sq_state* st, const sq_instr* prog, uint32_t n) {
+    SQ_API_BEGIN
+    need(prog != nullptr || n == 0, "null program");
+    std::vector<sq_instr> p(prog, prog + n);
+    for (auto& in : p) {
+        // the ABI carries the opaque sq_qram*; the kernel wants its table record
+        if (in.op == SQ_OP_QRAM_LOAD && in.qram) in.qram = reinterpret_cast<const sq_qram*>(&in.qram->t);
+    }
+    run_program(S(st), p.data(), n);
+    SQ_API_END
+}
+
+int sq_add_uint_uint(sq_state* st, uint32_t lhs, uint32_t rhs, uint32_t res, const sq_cond* cond) {
+    sq_instr in = make_instr(SQ_OP_ADD_UINT_UINT, cond);
+    in.reg[0] = lhs; in.reg[1] = rhs; in.reg[2] = res;
+    return run1(st, in);
+}
+int sq_add_uint_uint_inplace(sq_state* st, uint32_t lhs, uint32_t rhs, const sq_cond* cond, int dag) {
+    sq_instr in = make_instr(SQ_OP_ADD_UINT_UINT_INPLACE, cond);
+    in.reg[0] = lhs; in.reg[1] = rhs; in.dag = dag ? 1 : 0;
+    return run1(st, in);
+}
+int sq_add_uint_const(sq_state* st, uint32_t lhs, uint64_t c, uint32_t res, const sq_cond* cond) {
+    sq_instr in = make_instr(SQ_OP_ADD_UINT_CONST, cond);
+    in.reg[0] = lhs; in.reg[2] = res; in.imm[0] = c;
+    return run1(st, in);
+}
+int sq_add_const_inplace(sq_state* st, uint32_t reg, uint64_t c, const sq_cond* cond, int dag) {
+    sq_instr in = make_instr(SQ_OP_ADD_CONST_INPLACE, cond);
+    in.reg[0] = reg; in.imm[0] = c; in.dag = dag ? 1 : 0;
+    return run1(st, in);
+}
+int sq_mult_uint_const(sq_state* st, uint32_t lhs, uint64_t c, uint32_t res, const sq_cond* cond) {
+    sq_instr in = make_instr(SQ_OP_MULT_UINT_CONST, cond);
+    in.reg[0] = lhs; in.reg[2] = res; in.imm[0] = c;
+    return run1(st, in);
+}
+int sq_add_mult_uint_const(sq_state* st, uint32_t lhs, uint64_t c, uint32_t res, const sq_cond* cond, int dag) {
+    sq_instr in = make_instr(SQ_OP_ADD_MULT_UINT_CONST, cond);
+    in.reg[0] = lhs; in.reg[2] = res; in.imm[0] = c; in.dag = dag ? 1 : 0;
+    return run1(st, in);
+}
+int sq_mul_uint_uint(sq_state* st, uint32_t lhs, uint32_t rhs, uint32_t res, const sq_cond* cond) {
+    sq_instr in = make_instr(SQ_OP_MUL_UINT_UINT, cond);
+    in.reg[0] = lhs; in.reg[1] = rhs; in.reg[2] = res;
+    return run1(st, in);
+}
+int sq_add_anyint_inplace(sq_state* st, uint32_t lhs, uint32_t rhs, const sq_cond* cond, int dag) {
+    sq_instr in = make_instr(SQ_OP_ADD_ANYINT_INPLACE, cond);
+    in.reg[0] = lhs; in.reg[1] = rhs; in.dag = dag ? 1 : 0;
+    return run1(st, in);
+}
+int sq_assign(sq_state* st, uint32_t src, uint32_t dst, const sq_cond* cond) {
+    sq_instr in = make_instr(SQ_OP_ASSIGN, cond);
+    in.reg[0] = src; in.reg[1] = dst;
+    return run1(st, in);
+}
+int sq_shift(sq_state* st, uint32_t reg, uint32_t digits, int left, const sq_cond* cond) {
+    sq_instr in = make_instr(left ? SQ_OP_SHIFT_LEFT : SQ_OP_SHIFT_RIGHT, cond);
+    in.reg[0] = reg; in.imm[0] = digits;
+    return run1(st, in);
+}
+int sq_swap(sq_state* st, uint32_t a, uint32_t b, const sq_cond* cond) {
+    sq_instr in = make_instr(SQ_OP_SWAP_GENERAL, cond);
+    in.reg[0] = a; in.reg[1] = b;
+    return run1(st, in);
+}
+int sq_x_bool(sq_state* st, uint32_t reg, uint32_t digit, const sq_cond* cond) {
+    sq_instr in = make_instr(SQ_OP_X_BOOL, cond);
+    in.reg[0] = reg; in.imm[0] = digit;
+    return run1(st, in);
+}
+int sq_flip_bools(sq_state* st, uint32_t reg, const sq_cond* cond) {
+    sq_instr in = make_instr(SQ_OP_FLIP_BOOLS, cond);
+    in.reg[0] = reg;
+    return run1(st, in);
+}
+int sq_init_unsafe(sq_state* st, uint32_t reg, uint64_t value) {
+    sq_instr in = make_instr(SQ_OP_INIT_UNSAFE, nullptr);
+    in.reg[0] = reg; in.imm[0] = value;
+    return run1(st, in);
+}
+int sq_qram_load(sq_state* st, const sq_qram* q, uint32_t addr, uint32_t data, const sq_cond* cond) {
+    if (!q) {
+        t_err = "QRAMLoad: null QRAM";
+        return SQ_ERR_INVALID;
+    }
+    sq_instr in = make_instr(SQ_OP_QRAM_LOAD, cond);
+    in.reg[0] = addr; in.reg[1] = data;
+    in.qram = reinterpret_cast<const sq_qram*>(&q->t);
+    return run1(st, in);
+}
+int sq_phase_bool(sq_state* st, uint32_t reg, uint32_t digit, double lambda, const sq_cond* cond, int dag) {
+    sq_instr in = make_instr(SQ_OP_PHASE_BOOL, cond);
+    in.reg[0] = reg; in.imm[0] = digit;
+    in.c[0] = std::cos(lambda);
+    in.c[1] = dag ? -std::sin(lambda) : std::sin(lambda);
+    return run1(st, in);
+}
+int sq_global_phase(sq_state* st, double re, double im, const sq_cond* cond, int dag) {
+    sq_instr in = make_instr(SQ_OP_GLOBAL_PHASE, cond);
+    in.c[0] = re;
+    in.c[1] = dag ? -im : im;
+    return run1(st, in);
+}
+int sq_reflection_bool(sq_state* st, const uint32_t* regs, uint32_t nregs, int inverse, const sq_cond* cond) {
+    sq_instr in = make_instr(SQ_OP_REFLECTION_BOOL, cond);
+    for (uint32_t i = 0; i < nregs; ++i) {
+        if (regs[i] >= 64) { t_err = "register id >= 64"; return SQ_ERR_INVALID; }
+        in.imm[0] |= 1ull << regs[i];
+    }
+    in.imm[1] = inverse ? 1 : 0;
+    return run1(st, in);
+}
+int sq_zero_cond_phase_flip(sq_state* st, const uint32_t* regs, uint32_t nregs, const sq_cond* cond) {
+    sq_instr in = make_instr(SQ_OP_ZERO_COND_PHASE_FLIP, cond);
+    for (uint32_t i = 0; i < nregs; ++i) {
+        if (regs[i] >= 64) { t_err = "register id >= 64"; return SQ_ERR_INVALID; }
+        in.imm[0] |= 1ull << regs[i];
+    }
+    return run1(st, in);
+}
+
+// ------------------------------------------------------------------ split / merge
+static double cz_eps() { return regtable().clearzero_eps; }
+
+int sq_hadamard_int(sq_state* st, uint32_t reg, uint32_t n_digits, const sq_cond* cond) {
+    SQ_API_BEGIN
+    Field f = regtable().field(reg);
+    need(n_digits <= f.width, "Hadamard_Int: n_digits larger than the register");
+    GroupSpec g;
+    memset(&g, 0, sizeof(g));
+    g.mode = GM_HADAMARD_INT;
+    g.target = f;
+    g.target.width = (uint8_t)n_digits;
+    g.cond = resolve_cond(cond);
+    g.eps = cz_eps();
+    if (n_digits == 0) return SQ_OK;
+    group_transform(S(st), g);
+    SQ_API_END
+}
+
+int sq_hadamard_int_full(sq_state* st, uint32_t reg, const sq_cond* cond) {
+    SQ_API_BEGIN
+    Field f = regtable().field(reg);
+    GroupSpec g;
+    memset(&g, 0, sizeof(g));
+    g.mode = GM_HADAMARD_FULL;
+    g.target = f;
+    g.cond = resolve_cond(cond);
+    g.eps = cz_eps();
+    if (f.width == 0) return SQ_OK;
+    group_transform(S(st), g);
+    SQ_API_END
+}
+
+int sq_hadamard_bool(sq_state* st, uint32_t reg, const sq_cond* cond) {
+    SQ_API_BEGIN
+    Field f = regtable().field(reg);
+    need(f.width == 1, "Hadamard_Bool: size of output register must be 1");
+    GroupSpec g;
+    memset(&g, 0, sizeof(g));
+    g.mode = GM_HADAMARD_BOOL;
+    g.target = f;
+    g.cond = resolve_cond(cond);
+    g.eps = cz_eps();
+    group_transform(S(st), g);
+    SQ_API_END
+}
+
+static double abs_sqr(double re, double im) { return re * re + im * im; }
+
+int sq_rot_bool(sq_state* st, uint32_t reg, uint32_t digit, const double* m8, const sq_cond* cond, int dag) {
+    SQ_API_BEGIN
+    need(m8 != nullptr, "null matrix");
+    Field f = regtable().field(reg);
+    need(digit < f.width, "Rot_Bool: digit >= register size");
+    double m[8];
+    memcpy(m, m8, sizeof(m));
+    if (dag) {  // conjugate transpose
+        double d[8] = {m8[0], -m8[1], m8[4], -m8[5], m8[2], -m8[3], m8[6], -m8[7]};
+        memcpy(m, d, sizeof(m));
+    }
+    const double eps = 1e-14;  // Rot_Bool::_is_diagonal / _is_off_diagonal threshold (library epsilon)
+    const bool diag = abs_sqr(m[2], m[3]) < eps && abs_sqr(m[4], m[5]) < eps;
+    const bool off = abs_sqr(m[0], m[1]) < eps && abs_sqr(m[6], m[7]) < eps;
+    State& s = S(st);
+    if (diag || off) {
+        // in-place: no new entries (basic_gates.cpp:110-171), then ClearZero
+        sq_instr in = make_instr(diag ? SQ_OP_ROT_DIAGONAL : SQ_OP_ROT_OFF_DIAGONAL, cond);
+        in.reg[0] = reg;
+        in.imm[0] = digit;
+        if (diag) {
+            in.c[0] = m[0]; in.c[1] = m[1]; in.c[2] = m[6]; in.c[3] = m[7];
+        } else {  // bit 0 -> multiply by m10, bit 1 -> multiply by m01
+            in.c[0] = m[4]; in.c[1] = m[5]; in.c[2] = m[2]; in.c[3] = m[3];
+        }
+        run_program(s, &in, 1);
+        clear_zero(s, cz_eps());
+        return SQ_OK;
+    }
+    GroupSpec g;
+    memset(&g, 0, sizeof(g));
+    g.mode = GM_ROT;
+    g.target = f;
+    g.target.shift = (uint8_t)(f.shift + digit);
+    g.target.width = 1;
+    for (int i = 0; i < 4; ++i) g.m[i] = make_double2(m[2 * i], m[2 * i + 1]);
+    g.cond = resolve_cond(cond);
+    g.eps = cz_eps();
+    group_transform(s, g);
+    SQ_API_END
+}
+
+int sq_condrot_rational_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, int dag) {
+    SQ_API_BEGIN
+    need(reg_in != reg_out, "CondRot: input and output registers must differ");
+    Field fi = regtable().field(reg_in);
+    Field fo = regtable().field(reg_out);
+    need(fi.type == SQ_RATIONAL && fo.type == SQ_BOOLEAN, "CondRot_Rational_Bool: input must be Rational, output Boolean");
+    need(fo.width == 1, "CondRot_Rational_Bool: output register must be 1 bit");
+    GroupSpec g;
+    memset(&g, 0, sizeof(g));
+    g.mode = GM_CONDROT;
+    g.target = fo;
+    g.aux = fi;
+    g.sign = dag ? -1.0 : 1.0;
+    g.eps = cz_eps();
+    group_transform(S(st), g);
+    SQ_API_END
+}
+
+// ------------------------------------------------------------------ prune / norm / merge
+int sq_set_clearzero_eps(double eps) {
+    SQ_API_BEGIN
+    need(eps >= 0.0, "negative eps");
+    regtable().clearzero_eps = eps;
+    SQ_API_END
+}
+int sq_get_clearzero_eps(double* eps) {
+    SQ_API_BEGIN
+    need(eps != nullptr, "null pointer");
+    *eps = regtable().clearzero_eps;
+    SQ_API_END
+}
+
+int sq_clear_zero(sq_state* st, double eps) {
+    SQ_API_BEGIN
+    clear_zero(S(st), eps);
+    SQ_API_END
+}
+
+int sq_normalize(sq_state* st, double* norm_sq_out) {
+    SQ_API_BEGIN
+    State& s = S(st);
+    const double sum = norm_sq(s);
+    const double k = 1.0 / std::sqrt(sum);
+    if (std::isnan(k)) fail(SQ_ERR_BAD_RESULT, "Normalize: norm is NaN");
+    scale_amp(s, k);
+    if (norm_sq_out) *norm_sq_out = sum;
+    SQ_API_END
+}
+
+int sq_norm_sq(const sq_state* st, double* out) {
+    SQ_API_BEGIN
+    need(out != nullptr, "null pointer");
+    *out = norm_sq(S(st));
+    SQ_API_END
+}
+
+int sq_add_systems(sq_state* dst, const sq_state* src, double coef) {
+    SQ_API_BEGIN
+    need(dst != src, "add_systems: source and destination must differ");
+    add_systems(S(dst), S(src), coef);
+    SQ_API_END
+}
+
+int sq_add_register_sync(sq_state* st, uint32_t type, uint32_t width, uint32_t* id_out) {
+    SQ_API_BEGIN
+    need(id_out != nullptr, "null pointer");
+    State& s = S(st);
+    const uint32_t id = regtable().add(type, width);
+    *id_out = id;
+    zero_field(s, regtable().field(id));
+    SQ_API_END
+}
+
+int sq_remove_register_sync(sq_state* st, uint32_t id) {
+    SQ_API_BEGIN
+    State& s = S(st);
+    Field f = regtable().field(id);
+    zero_field(s, f);
+    regtable().remove(id);
+    SQ_API_END
+}
+
+int sq_split_register(sq_state* st, uint32_t first, uint32_t second_size, uint32_t* second_out) {
+    SQ_API_BEGIN
+    need(second_out != nullptr, "null pointer");
+    State& s = S(st);
+    RegTable& t = regtable();
+    const RegEntry fe = t.at(first);
+    need(second_size <= fe.width, "SplitRegister: second size larger than the register");
+    // The low `second_size` bits of `first` become the new register in place:
+    // no data moves. Allocate an id without bits, then hand it the low bits.
+    const uint32_t id = t.add(fe.type, 0);
+    RegEntry& se = t.regs[id];
+    RegEntry& f2 = t.regs[first];
+    se.width = second_size;
+    se.word = fe.word;
+    se.shift = fe.shift;
+    f2.width = fe.width - second_size;
+    f2.shift = fe.shift + second_size;
+    if (f2.width == 0) f2.shift = fe.shift;
+    (void)s;
+    *second_out = id;
+    SQ_API_END
+}
+
+int sq_combine_register(sq_state* st, uint32_t first, uint32_t second) {
+    SQ_API_BEGIN
+    State& s = S(st);
+    RegTable& t = regtable();
+    need(first != second, "CombineRegister: registers must differ");
+    const RegEntry a = t.at(first);
+    const RegEntry b = t.at(second);
+    need(a.width + b.width <= 64, "CombineRegister: combined width > 64");
+    if (b.width == 0) {
+        t.remove(second);
+        return SQ_OK;
+    }
+    if (a.width == 0 || (a.word == b.word && a.shift == b.shift + b.width)) {
+        // adjacent (or empty first): metadata only
+        RegEntry& fa = t.regs[first];
+        fa.word = b.word;
+        fa.shift = b.shift;
+        fa.width = a.width + b.width;
+        t.regs[second].width = 0;  // bits now belong to `first`
+        t.remove(second);
+        return SQ_OK;
+    }
+    // move both fields into a fresh field of the combined width
+    Field fa = t.field(first), fb = t.field(second);
+    t.free_bits(a.word, a.shift, a.width);
+    t.free_bits(b.word, b.shift, b.width);
+    uint32_t w, sh;
+    if (!t.alloc_bits(a.width + b.width, &w, &sh)) {
+        t.used[a.word] |= wmask(a.width) << a.shift;
+        t.used[b.word] |= wmask(b.width) << b.shift;
+        fail(SQ_ERR_CAPACITY, "packed key space exhausted");
+    }
+    Field dst;
+    dst.word = (uint8_t)w;
+    dst.shift = (uint8_t)sh;
+    dst.width = (uint8_t)(a.width + b.width);
+    dst.type = fa.type;
+    move_field(s, fa, fb, dst);
+    RegEntry& ea = t.regs[first];
+    ea.word = w;
+    ea.shift = sh;
+    ea.width = a.width + b.width;
+    t.regs[second].width = 0;
+    t.remove(second);
+    SQ_API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,218 @@
+// compact.cu — ClearZero (order-preserving single-pass stream compaction),
+// Normalize (deterministic FP64 two-level reduction + scale).
+//
+// ClearZero reads each amplitude once, and the key words of surviving entries
+// once, and writes the survivors once: N*16 + N_out*(8K+16) bytes, the
+// algorithmic minimum. Tile offsets come from a decoupled look-back, so the
+// kernel is a single pass and keeps the reference's remove_if order.
+#include <cstring>
+
+#include "lookback.cuh"
+#include "sq_internal.cuh"
+
+namespace sq {
+
+constexpr int kCzBlock = 256;
+constexpr int kCzItems = 8;
+constexpr int kCzTile = kCzBlock * kCzItems;
+
+struct LookbackWs {
+    unsigned long long* status;
+    unsigned* counter;
+    unsigned long long* total;
+};
+
+// Layout of the look-back workspace: [counter (u32) | total (u64) | pad to 256 B | status[ntiles]].
+static LookbackWs lookback_ws(long long ntiles) {
+    size_t bytes = 256 + (size_t)ntiles * 8;
+    char* p = (char*)ws().get(WS_LOOKBACK, bytes);
+    SQ_CUDA(cudaMemsetAsync(p, 0, bytes, stream()));
+    LookbackWs w;
+    w.counter = (unsigned*)p;
+    w.total = (unsigned long long*)(p + 8);
+    w.status = (unsigned long long*)(p + 256);
+    return w;
+}
+
+template <int K>
+__global__ void __launch_bounds__(kCzBlock) clearzero_kernel(ConstKeyPtrs ik, const double2* __restrict__ ia,
+                                                             KeyPtrs ok, double2* __restrict__ oa, uint64_t n,
+                                                             double eps, LookbackWs lb, long long ntiles,
+                                                             unsigned* err) {
+    __shared__ unsigned s_tile;
+    __shared__ unsigned s_cnt[kCzItems][kCzBlock / 32];
+    __shared__ unsigned long long s_prefix;
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(lb.counter, 1u);
+    __syncthreads();
+    const long long tile = s_tile;
+    const uint64_t base = (uint64_t)tile * kCzTile;
+    double2 a[kCzItems];
+    unsigned ball[kCzItems];
+#pragma unroll
+    for (int j = 0; j < kCzItems; ++j) {
+        const uint64_t i = base + (uint64_t)j * kCzBlock + tid;
+        bool keep = false;
+        if (i < n) {
+            a[j] = ia[i];
+            keep = !(a[j].x * a[j].x + a[j].y * a[j].y < eps);
+        }
+        ball[j] = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) s_cnt[j][warp] = __popc(ball[j]);
+    }
+    __syncthreads();
+    // exclusive scan of the 64 (item-row, warp) counts in index order, by warp 0
+    if (warp == 0) {
+        unsigned v0 = s_cnt[(2 * lane) / (kCzBlock / 32)][(2 * lane) % (kCzBlock / 32)];
+        unsigned v1 = s_cnt[(2 * lane + 1) / (kCzBlock / 32)][(2 * lane + 1) % (kCzBlock / 32)];
+        unsigned sum = v0 + v1, inc = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= (unsigned)o) inc += t;
+        }
+        const unsigned excl = inc - sum;
+        const unsigned total = __shfl_sync(0xffffffffu, inc, 31);
+        s_cnt[(2 * lane) / (kCzBlock / 32)][(2 * lane) % (kCzBlock / 32)] = excl;
+        s_cnt[(2 * lane + 1) / (kCzBlock / 32)][(2 * lane + 1) % (kCzBlock / 32)] = excl + v0;
+        unsigned long long pre = lb_warp_exclusive(lb.status, tile, total, err);
+        if (lane == 0) {
+            s_prefix = pre;
+            if (tile == ntiles - 1) *lb.total = pre + total;
+        }
+    }
+    __syncthreads();
+    const unsigned long long prefix = s_prefix;
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int j = 0; j < kCzItems; ++j) {
+        if (!((ball[j] >> lane) & 1u)) continue;
+        const uint64_t i = base + (uint64_t)j * kCzBlock + tid;
+        const uint64_t o = prefix + s_cnt[j][warp] + __popc(ball[j] & lt);
+#pragma unroll
+        for (int w = 0; w < K; ++w) ok.w[w][o] = ik.w[w][i];
+        oa[o] = a[j];
+    }
+}
+
+template <int K>
+static void launch_cz(const Buffers& in, Buffers& out, uint64_t n, double eps, LookbackWs lb, long long nt) {
+    ConstKeyPtrs ik;
+    KeyPtrs okp;
+    for (int w = 0; w < SQ_KMAX; ++w) {
+        ik.w[w] = in.keys[w];
+        okp.w[w] = out.keys[w];
+    }
+    clearzero_kernel<K><<<(unsigned)nt, kCzBlock, 0, stream()>>>(ik, in.amp, okp, out.amp, n, eps, lb, nt,
+                                                               device_error_word());
+    count_launch();
+    SQ_CUDA(cudaGetLastError());
+}
+
+void check_device_error() {
+    unsigned v = 0;
+    SQ_CUDA(cudaMemcpyAsync(&v, device_error_word(), 4, cudaMemcpyDeviceToHost, stream()));
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    if (v) {
+        SQ_CUDA(cudaMemsetAsync(device_error_word(), 0, 4, stream()));
+        fail(SQ_ERR_DEVICE_TIMEOUT, "a bounded device-side wait gave up (decoupled look-back)");
+    }
+}
+
+// Compacts `in` (n entries) into `out`, returns the survivor count. `out`
+// must already hold n entries of capacity.
+uint64_t compact_nonzero(const Buffers& in, Buffers& out, uint64_t n, double eps, uint32_t k) {
+    if (n == 0) return 0;
+    const long long nt = (long long)((n + kCzTile - 1) / kCzTile);
+    LookbackWs lb = lookback_ws(nt);
+    switch (k) {
+        case 1: launch_cz<1>(in, out, n, eps, lb, nt); break;
+        case 2: launch_cz<2>(in, out, n, eps, lb, nt); break;
+        case 3: launch_cz<3>(in, out, n, eps, lb, nt); break;
+        case 4: launch_cz<4>(in, out, n, eps, lb, nt); break;
+        case 5: launch_cz<5>(in, out, n, eps, lb, nt); break;
+        case 6: launch_cz<6>(in, out, n, eps, lb, nt); break;
+        case 7: launch_cz<7>(in, out, n, eps, lb, nt); break;
+        default: launch_cz<8>(in, out, n, eps, lb, nt); break;
+    }
+    unsigned long long total = 0;
+    SQ_CUDA(cudaMemcpyAsync(&total, lb.total, 8, cudaMemcpyDeviceToHost, stream()));
+    check_device_error();  // synchronizes
+    return total;
+}
+
+void clear_zero(State& s, double eps) {
+    sync_words(s);
+    if (s.n == 0) return;
+    const uint32_t k = regtable().k;
+    ensure_buffers(s.spare, s.n, k, 0);
+    uint64_t m = compact_nonzero(s.live, s.spare, s.n, eps, k);
+    swap_live_spare(s);
+    s.n = m;
+}
+
+// ------------------------------------------------------------------ norm
+constexpr int kRedBlock = 256;
+
+__global__ void __launch_bounds__(kRedBlock) norm_partial_kernel(const double2* __restrict__ a, uint64_t n,
+                                                                 double* __restrict__ partial) {
+    __shared__ double s[kRedBlock];
+    double acc = 0.0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double2 v = a[i];
+        acc += v.x * v.x + v.y * v.y;
+    }
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = kRedBlock / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
+}
+
+__global__ void __launch_bounds__(kRedBlock) norm_final_kernel(const double* __restrict__ partial, int m,
+                                                               double* __restrict__ out) {
+    __shared__ double s[kRedBlock];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < m; i += kRedBlock) acc += partial[i];
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = kRedBlock / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = s[0];
+}
+
+double norm_sq(const State& s) {
+    if (s.n == 0) return 0.0;
+    const int g = num_sms() * 4;
+    double* part = (double*)ws().get(WS_REDUCE, (size_t)(g + 1) * 8);
+    norm_partial_kernel<<<g, kRedBlock, 0, stream()>>>(s.live.amp, s.n, part);
+    norm_final_kernel<<<1, kRedBlock, 0, stream()>>>(part, g, part + g);
+    count_launch(2);
+    SQ_CUDA(cudaGetLastError());
+    double r = 0;
+    SQ_CUDA(cudaMemcpyAsync(&r, part + g, 8, cudaMemcpyDeviceToHost, stream()));
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    return r;
+}
+
+__global__ void scale_kernel(double2* __restrict__ a, uint64_t n, double k) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double2 v = a[i];
+        a[i] = make_double2(v.x * k, v.y * k);
+    }
+}
+
+void scale_amp(State& s, double k) {
+    if (s.n == 0) return;
+    scale_kernel<<<grid_for(s.n, 256), 256, 0, stream()>>>(s.live.amp, s.n, k);
+    count_launch();
+    SQ_CUDA(cudaGetLastError());
+}
+
+}  // namespace sq

@@ -1,0 +1,539 @@
+// elementwise.cu — the fused elementwise kernel.
+//
+// Every reference operator whose CPU loop touches one entry at a time
+// (register arithmetic, QRAM gather, phases, in-place rotations) is one
+// instruction of a small program. One launch streams the state once: each
+// thread loads the key words the program reads (and the amplitude if any
+// instruction needs it), runs the instructions in order with their own
+// control conditions, and stores only what changed. Consecutive operators
+// therefore cost one HBM pass instead of one pass each, and the reference's
+// partition-by-condition pass (cuda/system_operations.cu:17-66) disappears
+// because conditions are evaluated per entry in registers.
+#include <cstring>
+
+#include "sq_internal.cuh"
+
+namespace sq {
+
+struct DInstr {
+    uint16_t op;
+    uint8_t dag;
+    uint8_t pad;
+    uint32_t addr_bits;
+    Field f[4];
+    uint64_t imm[3];
+    double2 c[2];
+    const void* table;
+    uint32_t elem_bytes;
+    uint32_t pad2;
+    uint64_t zmask[SQ_KMAX];
+    DCondSet cond;
+};
+
+template <int MAXI>
+struct ProgramArgs {
+    uint32_t n;
+    uint32_t read_words;   // bit w: word w is read
+    uint32_t write_words;  // bit w: word w is written
+    uint32_t amp_mode;     // bit 0: read amplitude, bit 1: write amplitude
+    DInstr ins[MAXI];
+};
+
+__device__ __forceinline__ int64_t sext(uint64_t v, unsigned w) {
+    if (w == 0) return 0;
+    if (w >= 64) return (int64_t)v;
+    const uint64_t sign = 1ull << (w - 1);
+    return (int64_t)((v ^ sign) - sign);
+}
+
+__device__ __forceinline__ uint64_t isqrt64(uint64_t v) {
+    uint64_t res = 0, bit = 1ull << 62;
+    while (bit > v) bit >>= 2;
+    while (bit) {
+        if (v >= res + bit) {
+            v -= res + bit;
+            res = (res >> 1) + bit;
+        } else {
+            res >>= 1;
+        }
+        bit >>= 2;
+    }
+    return res;
+}
+
+// complex multiply without contraction (the library is built with --fmad=false)
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ __forceinline__ uint64_t shl(uint64_t v, unsigned s) { return s >= 64 ? 0 : v << s; }
+__device__ __forceinline__ uint64_t shr(uint64_t v, unsigned s) { return s >= 64 ? 0 : v >> s; }
+
+template <int K>
+__device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2& a) {
+    const Field* f = in.f;
+    switch (in.op) {
+        case SQ_OP_FLIP_BOOLS: fset<K>(k, f[0], ~fget<K>(k, f[0])); break;
+        case SQ_OP_SWAP_BOOL_BOOL: {
+            uint64_t x = fget<K>(k, f[0]), y = fget<K>(k, f[1]);
+            const uint64_t d1 = in.imm[0], d2 = in.imm[1];
+            const bool v1 = (x >> d1) & 1, v2 = (y >> d2) & 1;
+            if (v1 && !v2) { x -= 1ull << d1; y += 1ull << d2; }
+            if (v2 && !v1) { x += 1ull << d1; y -= 1ull << d2; }
+            fset<K>(k, f[0], x);
+            fset<K>(k, f[1], y);
+            break;
+        }
+        case SQ_OP_SHIFT_LEFT:
+        case SQ_OP_SHIFT_RIGHT: {
+            const unsigned size = f[0].width;
+            const unsigned d = (unsigned)in.imm[0];
+            const bool left = (in.op == SQ_OP_SHIFT_LEFT) != (in.dag != 0);
+            const uint64_t v = fget<K>(k, f[0]);
+            uint64_t r;
+            if (left) {
+                const uint64_t high = shr(v, size - d);
+                const uint64_t low = v - shl(high, size - d);
+                r = shl(low, d) + high;
+            } else {
+                const uint64_t high = shr(v, d);
+                const uint64_t low = v - shl(high, d);
+                r = shl(low, size - d) + high;
+            }
+            fset<K>(k, f[0], r);
+            break;
+        }
+        case SQ_OP_MULT_UINT_CONST: fset<K>(k, f[2], fget<K>(k, f[2]) ^ (fget<K>(k, f[0]) * in.imm[0])); break;
+        case SQ_OP_ADD_MULT_UINT_CONST: {
+            const uint64_t o = fget<K>(k, f[2]), l = fget<K>(k, f[0]);
+            fset<K>(k, f[2], in.dag ? o - l * in.imm[0] : o + in.imm[0] * l);
+            break;
+        }
+        case SQ_OP_MOD_MULT_CONST: fset<K>(k, f[0], (fget<K>(k, f[0]) * in.imm[0]) % in.imm[1]); break;
+        case SQ_OP_ADD_UINT_UINT: fset<K>(k, f[2], fget<K>(k, f[2]) ^ (fget<K>(k, f[0]) + fget<K>(k, f[1]))); break;
+        case SQ_OP_ADD_UINT_UINT_INPLACE: {
+            const uint64_t o = fget<K>(k, f[1]), l = fget<K>(k, f[0]);
+            fset<K>(k, f[1], in.dag ? o - l : o + l);
+            break;
+        }
+        case SQ_OP_ADD_UINT_CONST: fset<K>(k, f[2], fget<K>(k, f[2]) ^ (fget<K>(k, f[0]) + in.imm[0])); break;
+        case SQ_OP_ADD_CONST_INPLACE: {
+            const uint64_t o = fget<K>(k, f[0]);
+            fset<K>(k, f[0], in.dag ? o - in.imm[0] : o + in.imm[0]);
+            break;
+        }
+        case SQ_OP_SUB_UINT_UINT: fset<K>(k, f[2], fget<K>(k, f[2]) ^ (fget<K>(k, f[0]) - fget<K>(k, f[1]))); break;
+        case SQ_OP_NEG_UINT: fset<K>(k, f[1], fget<K>(k, f[1]) ^ (0ull - fget<K>(k, f[0]))); break;
+        case SQ_OP_ABS_SINT: {
+            const int64_t v = sext(fget<K>(k, f[0]), f[0].width);
+            const uint64_t mag = v < 0 ? (uint64_t)(-v) : (uint64_t)v;
+            fset<K>(k, f[1], fget<K>(k, f[1]) ^ mag);
+            break;
+        }
+        case SQ_OP_MUL_UINT_UINT: fset<K>(k, f[2], fget<K>(k, f[2]) ^ (fget<K>(k, f[0]) * fget<K>(k, f[1]))); break;
+        case SQ_OP_DIV_UINT_UINT: {
+            const uint64_t x = fget<K>(k, f[0]), y = fget<K>(k, f[1]);
+            fset<K>(k, f[2], fget<K>(k, f[2]) ^ (y == 0 ? 0ull : x / y));
+            break;
+        }
+        case SQ_OP_SQRT_UINT: fset<K>(k, f[1], fget<K>(k, f[1]) ^ isqrt64(fget<K>(k, f[0]))); break;
+        case SQ_OP_SELECT_BOOL: {
+            const uint64_t sel = (fget<K>(k, f[0]) & 1ull) ? fget<K>(k, f[1]) : fget<K>(k, f[2]);
+            fset<K>(k, f[3], fget<K>(k, f[3]) ^ sel);
+            break;
+        }
+        case SQ_OP_AND_UINT_UINT: fset<K>(k, f[2], fget<K>(k, f[2]) ^ (fget<K>(k, f[0]) & fget<K>(k, f[1]))); break;
+        case SQ_OP_OR_UINT_UINT: fset<K>(k, f[2], fget<K>(k, f[2]) ^ (fget<K>(k, f[0]) | fget<K>(k, f[1]))); break;
+        case SQ_OP_XOR_UINT_UINT: fset<K>(k, f[2], fget<K>(k, f[2]) ^ (fget<K>(k, f[0]) ^ fget<K>(k, f[1]))); break;
+        case SQ_OP_LESS_SINT_SINT: {
+            const bool p = sext(fget<K>(k, f[0]), f[0].width) < sext(fget<K>(k, f[1]), f[1].width);
+            fset<K>(k, f[2], fget<K>(k, f[2]) ^ (p ? 1ull : 0ull));
+            break;
+        }
+        case SQ_OP_CARRY_UINT_UINT: {
+            const uint64_t x = fget<K>(k, f[0]), y = fget<K>(k, f[1]);
+            const unsigned w = f[2].width;
+            const bool p = w >= 64 ? (x + y < x) : (x >= (1ull << w)) || (y >= (1ull << w) - x);
+            fset<K>(k, f[3], fget<K>(k, f[3]) ^ (p ? 1ull : 0ull));
+            break;
+        }
+        case SQ_OP_OVERFLOW_SINT_SINT: {
+            const unsigned w = f[2].width;
+            const uint64_t m = wmask(w);
+            const uint64_t A = (uint64_t)sext(fget<K>(k, f[0]), f[0].width) & m;
+            const uint64_t B = (uint64_t)sext(fget<K>(k, f[1]), f[1].width) & m;
+            const uint64_t S = (A + B) & m;
+            const uint64_t sa = (A >> (w - 1)) & 1, sb = (B >> (w - 1)) & 1, ss = (S >> (w - 1)) & 1;
+            const bool p = (sa == sb) && (ss != sa);
+            fset<K>(k, f[3], fget<K>(k, f[3]) ^ (p ? 1ull : 0ull));
+            break;
+        }
+        case SQ_OP_MULOVERFLOW_UINT_UINT: {
+            const uint64_t x = fget<K>(k, f[0]), y = fget<K>(k, f[1]);
+            const uint64_t lo = x * y, hi = __umul64hi(x, y);
+            const unsigned w = f[2].width;
+            const bool p = hi != 0 || (w < 64 && lo >= (1ull << w));
+            fset<K>(k, f[3], fget<K>(k, f[3]) ^ (p ? 1ull : 0ull));
+            break;
+        }
+        case SQ_OP_ISZERO_UINT: fset<K>(k, f[1], fget<K>(k, f[1]) ^ (fget<K>(k, f[0]) == 0 ? 1ull : 0ull)); break;
+        case SQ_OP_NEGATIVE_SINT:
+            fset<K>(k, f[1], fget<K>(k, f[1]) ^ (sext(fget<K>(k, f[0]), f[0].width) < 0 ? 1ull : 0ull));
+            break;
+        case SQ_OP_ADD_ANYINT_INPLACE: {
+            const uint64_t raw = fget<K>(k, f[1]);
+            const uint64_t ext = f[1].type == SQ_SIGNED ? (uint64_t)sext(raw, f[1].width) : raw;
+            const uint64_t o = fget<K>(k, f[0]);
+            fset<K>(k, f[0], in.dag ? o - ext : o + ext);
+            break;
+        }
+        case SQ_OP_ASSIGN: fset<K>(k, f[1], fget<K>(k, f[1]) ^ fget<K>(k, f[0])); break;
+        case SQ_OP_COMPARE_UINT_UINT: {
+            const uint64_t l = fget<K>(k, f[0]), r = fget<K>(k, f[1]);
+            if (l == r) fset<K>(k, f[3], fget<K>(k, f[3]) ^ 1ull);
+            else fset<K>(k, f[2], fget<K>(k, f[2]) ^ (l < r ? 1ull : 0ull));
+            break;
+        }
+        case SQ_OP_LESS_UINT_UINT:
+            fset<K>(k, f[2], fget<K>(k, f[2]) ^ (fget<K>(k, f[0]) < fget<K>(k, f[1]) ? 1ull : 0ull));
+            break;
+        case SQ_OP_SWAP_GENERAL: {
+            const uint64_t x = fget<K>(k, f[0]), y = fget<K>(k, f[1]);
+            fset<K>(k, f[0], y);
+            fset<K>(k, f[1], x);
+            break;
+        }
+        case SQ_OP_GETMID_UINT_UINT:
+            fset<K>(k, f[2], fget<K>(k, f[2]) ^ ((fget<K>(k, f[0]) + fget<K>(k, f[1])) / 2));
+            break;
+        case SQ_OP_X_BOOL: fset<K>(k, f[0], fget<K>(k, f[0]) ^ (1ull << in.imm[0])); break;
+        case SQ_OP_INIT_UNSAFE: fset<K>(k, f[0], in.imm[0]); break;
+        case SQ_OP_QRAM_LOAD: {
+            const uint64_t addr = fget<K>(k, f[0]) & wmask(in.addr_bits);
+            uint64_t word;
+            if (in.elem_bytes == 2) word = __ldg((const unsigned short*)in.table + addr);
+            else if (in.elem_bytes == 4) word = __ldg((const unsigned int*)in.table + addr);
+            else word = __ldg((const unsigned long long*)in.table + addr);
+            fset<K>(k, f[1], fget<K>(k, f[1]) ^ word);
+            break;
+        }
+        case SQ_OP_PHASE_BOOL:
+            if ((fget<K>(k, f[0]) >> in.imm[0]) & 1ull) a = cmul(a, in.c[0]);
+            break;
+        case SQ_OP_GLOBAL_PHASE: a = cmul(a, in.c[0]); break;
+        case SQ_OP_Y_BOOL: {
+            const uint64_t v = fget<K>(k, f[0]) ^ (1ull << in.imm[0]);
+            fset<K>(k, f[0], v);
+            a = cmul(a, ((v >> in.imm[0]) & 1ull) ? make_double2(0.0, 1.0) : make_double2(0.0, -1.0));
+            break;
+        }
+        case SQ_OP_REFLECTION_BOOL:
+        case SQ_OP_ZERO_COND_PHASE_FLIP: {
+            bool iszero = true;
+#pragma unroll
+            for (int w = 0; w < K; ++w) iszero = iszero && ((k[w] & in.zmask[w]) == 0);
+            bool flip = in.op == SQ_OP_ZERO_COND_PHASE_FLIP ? iszero : !((in.imm[1] != 0) ^ iszero);
+            if (flip) a = make_double2(a.x * -1.0, a.y * -1.0);
+            break;
+        }
+        case SQ_OP_ROT_DIAGONAL:
+            a = cmul(a, ((fget<K>(k, f[0]) >> in.imm[0]) & 1ull) ? in.c[1] : in.c[0]);
+            break;
+        case SQ_OP_ROT_OFF_DIAGONAL: {
+            const uint64_t v = fget<K>(k, f[0]);
+            a = cmul(a, ((v >> in.imm[0]) & 1ull) ? in.c[1] : in.c[0]);
+            fset<K>(k, f[0], v ^ (1ull << in.imm[0]));
+            break;
+        }
+        default: break;
+    }
+}
+
+template <int K, int MAXI>
+__global__ void __launch_bounds__(256) program_kernel(const __grid_constant__ ProgramArgs<MAXI> p, KeyPtrs keys,
+                                                      double2* __restrict__ amp, uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint64_t k[K];
+#pragma unroll
+        for (int w = 0; w < K; ++w) k[w] = ((p.read_words >> w) & 1u) ? keys.w[w][i] : 0ull;
+        double2 a = make_double2(0.0, 0.0);
+        if (p.amp_mode & 1u) a = amp[i];
+        for (uint32_t j = 0; j < p.n; ++j) {
+            const DInstr& in = p.ins[j];
+            if (!cond_ok<K>(k, in.cond)) continue;
+            exec<K>(in, k, a);
+        }
+#pragma unroll
+        for (int w = 0; w < K; ++w)
+            if ((p.write_words >> w) & 1u) keys.w[w][i] = k[w];
+        if (p.amp_mode & 2u) amp[i] = a;
+    }
+}
+
+template <int K, int MAXI>
+static void launch_program(const ProgramArgs<MAXI>& args, State& s) {
+    KeyPtrs kp;
+    for (int w = 0; w < SQ_KMAX; ++w) kp.w[w] = s.live.keys[w];
+    const int block = 256;
+    unsigned grid = grid_for(s.n, block, 8);
+    program_kernel<K, MAXI><<<grid, block, 0, stream()>>>(args, kp, s.live.amp, s.n);
+    count_launch();
+    SQ_CUDA(cudaGetLastError());
+}
+
+template <int MAXI>
+static void dispatch_k(const ProgramArgs<MAXI>& args, State& s, uint32_t k) {
+    switch (k) {
+        case 1: launch_program<1, MAXI>(args, s); break;
+        case 2: launch_program<2, MAXI>(args, s); break;
+        case 3: launch_program<3, MAXI>(args, s); break;
+        case 4: launch_program<4, MAXI>(args, s); break;
+        case 5: launch_program<5, MAXI>(args, s); break;
+        case 6: launch_program<6, MAXI>(args, s); break;
+        case 7: launch_program<7, MAXI>(args, s); break;
+        default: launch_program<8, MAXI>(args, s); break;
+    }
+}
+
+// ------------------------------------------------------------------ host-side translation
+static uint32_t word_bit(const Field& f) { return f.width ? (1u << f.word) : 0u; }
+
+static void need_regs(const sq_instr& in, int n) {
+    for (int i = 0; i < n; ++i) (void)regtable().at(in.reg[i]);
+}
+
+static void distinct(uint32_t a, uint32_t b, const char* what) {
+    if (a == b) fail(SQ_ERR_INVALID, std::string(what) + ": registers must be distinct");
+}
+
+// Translate one ABI instruction; returns (read words, write words, amp mode).
+static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww, uint32_t& am) {
+    memset(&d, 0, sizeof(d));
+    d.op = (uint16_t)in.op;
+    d.dag = in.dag ? 1 : 0;
+    d.imm[0] = in.imm[0];
+    d.imm[1] = in.imm[1];
+    d.imm[2] = in.imm[2];
+    d.c[0] = make_double2(in.c[0], in.c[1]);
+    d.c[1] = make_double2(in.c[2], in.c[3]);
+    d.cond = resolve_cond(&in.cond);
+    for (uint32_t i = 0; i < d.cond.n; ++i) rw |= 1u << d.cond.c[i].word;
+    RegTable& t = regtable();
+    auto F = [&](int slot) {
+        d.f[slot] = t.field(in.reg[slot]);
+        return d.f[slot];
+    };
+    auto R = [&](int slot) { rw |= word_bit(F(slot)); };
+    auto W = [&](int slot) {
+        Field f = F(slot);
+        rw |= word_bit(f);
+        ww |= word_bit(f);
+    };
+    switch (in.op) {
+        case SQ_OP_NOP: break;
+        case SQ_OP_FLIP_BOOLS: W(0); break;
+        case SQ_OP_SWAP_BOOL_BOOL:
+            W(0); W(1);
+            if (in.imm[0] >= d.f[0].width || in.imm[1] >= d.f[1].width) fail(SQ_ERR_INVALID, "Swap_Bool_Bool: digit out of range");
+            break;
+        case SQ_OP_SHIFT_LEFT:
+        case SQ_OP_SHIFT_RIGHT:
+            W(0);
+            if (in.imm[0] > d.f[0].width) fail(SQ_ERR_INVALID, "Shift: digit > register size");
+            break;
+        case SQ_OP_MULT_UINT_CONST:
+        case SQ_OP_ADD_MULT_UINT_CONST:
+            R(0); W(2);
+            distinct(in.reg[0], in.reg[2], "Mult/Add_Mult");
+            break;
+        case SQ_OP_MOD_MULT_CONST:
+            W(0);
+            if (in.imm[1] == 0) fail(SQ_ERR_INVALID, "Mod_Mult: N == 0");
+            break;
+        case SQ_OP_ADD_UINT_UINT:
+        case SQ_OP_SUB_UINT_UINT:
+        case SQ_OP_MUL_UINT_UINT:
+        case SQ_OP_DIV_UINT_UINT:
+        case SQ_OP_AND_UINT_UINT:
+        case SQ_OP_OR_UINT_UINT:
+        case SQ_OP_XOR_UINT_UINT:
+        case SQ_OP_LESS_SINT_SINT:
+        case SQ_OP_LESS_UINT_UINT:
+        case SQ_OP_GETMID_UINT_UINT:
+            R(0); R(1); W(2);
+            distinct(in.reg[0], in.reg[2], "out-of-place arithmetic");
+            distinct(in.reg[1], in.reg[2], "out-of-place arithmetic");
+            break;
+        case SQ_OP_ADD_UINT_UINT_INPLACE:
+            R(0); W(1);
+            distinct(in.reg[0], in.reg[1], "Add_UInt_UInt_InPlace");
+            break;
+        case SQ_OP_ADD_UINT_CONST: R(0); W(2); distinct(in.reg[0], in.reg[2], "Add_UInt_ConstUInt"); break;
+        case SQ_OP_ADD_CONST_INPLACE: W(0); break;
+        case SQ_OP_NEG_UINT:
+        case SQ_OP_ABS_SINT:
+        case SQ_OP_SQRT_UINT:
+        case SQ_OP_ISZERO_UINT:
+        case SQ_OP_NEGATIVE_SINT:
+            R(0); W(1);
+            distinct(in.reg[0], in.reg[1], "unary arithmetic");
+            break;
+        case SQ_OP_SELECT_BOOL: R(0); R(1); R(2); W(3); break;
+        case SQ_OP_CARRY_UINT_UINT:
+        case SQ_OP_OVERFLOW_SINT_SINT:
+        case SQ_OP_MULOVERFLOW_UINT_UINT:
+            R(0); R(1); F(2); W(3);
+            if (in.op == SQ_OP_OVERFLOW_SINT_SINT && d.f[2].width == 0) fail(SQ_ERR_INVALID, "Overflow: zero width");
+            break;
+        case SQ_OP_ADD_ANYINT_INPLACE: W(0); R(1); distinct(in.reg[0], in.reg[1], "Add_AnyInt_AnyInt_InPlace"); break;
+        case SQ_OP_ASSIGN: R(0); W(1); break;
+        case SQ_OP_COMPARE_UINT_UINT: R(0); R(1); W(2); W(3); break;
+        case SQ_OP_SWAP_GENERAL: W(0); W(1); break;
+        case SQ_OP_X_BOOL:
+        case SQ_OP_Y_BOOL:
+            W(0);
+            if (in.imm[0] >= d.f[0].width) fail(SQ_ERR_INVALID, "gate digit >= register size");
+            if (in.op == SQ_OP_Y_BOOL) am |= 3u;
+            break;
+        case SQ_OP_INIT_UNSAFE: W(0); break;
+        case SQ_OP_QRAM_LOAD: {
+            R(0); W(1);
+            distinct(in.reg[0], in.reg[1], "QRAMLoad");
+            const QramTable* q = reinterpret_cast<const QramTable*>(in.qram);
+            if (!q || !q->dev) fail(SQ_ERR_INVALID, "QRAMLoad: null table");
+            if (d.f[1].width < 64 && q->max_word > wmask(d.f[1].width))
+                fail(SQ_ERR_INVALID, "QRAMLoad: table word wider than the data register");
+            d.table = q->dev;
+            d.elem_bytes = q->elem_bytes;
+            d.addr_bits = q->address_size;
+            break;
+        }
+        case SQ_OP_PHASE_BOOL:
+            R(0);
+            if (in.imm[0] >= d.f[0].width) fail(SQ_ERR_INVALID, "Phase_Bool: digit >= register size");
+            am |= 3u;
+            break;
+        case SQ_OP_GLOBAL_PHASE: am |= 3u; break;
+        case SQ_OP_REFLECTION_BOOL:
+        case SQ_OP_ZERO_COND_PHASE_FLIP:
+            for (uint32_t id = 0; id < 64; ++id) {
+                if (!((in.imm[0] >> id) & 1ull)) continue;
+                Field f = t.field(id);
+                if (f.width) {
+                    d.zmask[f.word] |= wmask(f.width) << f.shift;
+                    rw |= 1u << f.word;
+                }
+            }
+            am |= 3u;
+            break;
+        case SQ_OP_ROT_DIAGONAL:
+            R(0);
+            if (in.imm[0] >= d.f[0].width) fail(SQ_ERR_INVALID, "Rot_Bool: digit >= register size");
+            am |= 3u;
+            break;
+        case SQ_OP_ROT_OFF_DIAGONAL:
+            W(0);
+            if (in.imm[0] >= d.f[0].width) fail(SQ_ERR_INVALID, "Rot_Bool: digit >= register size");
+            am |= 3u;
+            break;
+        default: fail(SQ_ERR_INVALID, "unknown opcode " + std::to_string(in.op));
+    }
+}
+
+void run_program(State& s, const sq_instr* prog, uint32_t n) {
+    if (n == 0) return;
+    if (n > SQ_MAX_PROGRAM) fail(SQ_ERR_CAPACITY, "program longer than SQ_MAX_PROGRAM");
+    uint32_t rw = 0, ww = 0, am = 0;
+    uint32_t k = regtable().k;
+    sync_words(s);
+    if (s.n == 0) {
+        // still validate arguments like the reference constructors would
+        DInstr tmp;
+        for (uint32_t i = 0; i < n; ++i) translate(prog[i], tmp, rw, ww, am);
+        return;
+    }
+    if (n <= 4) {
+        ProgramArgs<4> a;
+        memset(&a, 0, sizeof(a));
+        for (uint32_t i = 0; i < n; ++i) translate(prog[i], a.ins[i], rw, ww, am);
+        a.n = n;
+        a.read_words = rw;
+        a.write_words = ww;
+        a.amp_mode = am;
+        dispatch_k<4>(a, s, k);
+    } else {
+        ProgramArgs<SQ_MAX_PROGRAM>* a = new ProgramArgs<SQ_MAX_PROGRAM>;
+        memset(a, 0, sizeof(*a));
+        try {
+            for (uint32_t i = 0; i < n; ++i) translate(prog[i], a->ins[i], rw, ww, am);
+        } catch (...) {
+            delete a;
+            throw;
+        }
+        a->n = n;
+        a->read_words = rw;
+        a->write_words = ww;
+        a->amp_mode = am;
+        dispatch_k<SQ_MAX_PROGRAM>(*a, s, k);
+        delete a;
+    }
+}
+
+// Zero one register field in every entry (AddRegister on reused bits,
+// remove_register_synchronous).
+template <int K>
+__global__ void zero_field_kernel(uint64_t* __restrict__ w, uint64_t keep_mask, uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) w[i] &= keep_mask;
+}
+
+void zero_field(State& s, Field f) {
+    sync_words(s);
+    if (s.n == 0 || f.width == 0) return;
+    const uint64_t keep = ~(wmask(f.width) << f.shift);
+    zero_field_kernel<1><<<grid_for(s.n, 256), 256, 0, stream()>>>(s.live.keys[f.word], keep, s.n);
+    count_launch();
+    SQ_CUDA(cudaGetLastError());
+}
+
+// CombineRegister when the two fields are not adjacent: dst = first << |second| | second,
+// old fields cleared.
+template <int K>
+__global__ void move_field_kernel(KeyPtrs keys, Field first, Field second, Field dst, uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint64_t k[K];
+#pragma unroll
+        for (int w = 0; w < K; ++w) k[w] = keys.w[w][i];
+        const uint64_t a = fget<K>(k, first), b = fget<K>(k, second);
+        const uint64_t v = second.width >= 64 ? b : ((a << second.width) | b);
+        fset<K>(k, first, 0);
+        fset<K>(k, second, 0);
+        fset<K>(k, dst, v);
+#pragma unroll
+        for (int w = 0; w < K; ++w) keys.w[w][i] = k[w];
+    }
+}
+
+void move_field(State& s, Field first, Field second, Field dst) {
+    sync_words(s);
+    if (s.n == 0) return;
+    KeyPtrs kp;
+    for (int w = 0; w < SQ_KMAX; ++w) kp.w[w] = s.live.keys[w];
+    unsigned g = grid_for(s.n, 256);
+    switch (regtable().k) {
+        case 1: move_field_kernel<1><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
+        case 2: move_field_kernel<2><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
+        case 3: move_field_kernel<3><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
+        case 4: move_field_kernel<4><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
+        case 5: move_field_kernel<5><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
+        case 6: move_field_kernel<6><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
+        case 7: move_field_kernel<7><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
+        default: move_field_kernel<8><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
+    }
+    count_launch();
+    SQ_CUDA(cudaGetLastError());
+}
+
+}  // namespace sq

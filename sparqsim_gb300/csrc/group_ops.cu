@@ -1,0 +1,891 @@
+// group_ops.cu — split / merge operators: Hadamard_Int, Hadamard_Int_Full,
+// Hadamard_Bool, Rot_Bool (general matrix), CondRot_Rational_Bool and the
+// equal-key merge of add_systems.
+//
+// All of them act on groups of entries that agree on every active key bit
+// except a few target bits (reference grouping: sort_state.cpp:10-36,
+// compare_equal :173-188; StateLessExceptKey buckets in the SAFE_HASH paths).
+// Pipeline, every step on the GPU:
+//   1. stats: OR/AND of the group-key bits over all entries (which bits vary)
+//      and the number of entries failing the control conditions;
+//   2. extract: pack only the varying group-key bits (plus a condition-fail
+//      bit on top) into a 32- or 64-bit sort key per entry;
+//   3. onesweep radix sort of (sort key, entry index);
+//   4. segment heads -> group starts (order-preserving compaction);
+//   5. emit, count pass: per group, the number of outputs with |a|^2 >= eps;
+//      exclusive scan -> output offsets (exact count-then-scan);
+//   6. emit, write pass: recompute and write keys + amplitudes; entries that
+//      fail the conditions are copied through unchanged.
+// Output amplitudes are computed in exactly the reference's arithmetic order
+// (stage-ascending FWHT butterflies (a0 + a1) * sqrt2inv, the singleton
+// a * 2^{-n/2} shortcut, the pair formulas), so results do not depend on the
+// order entries arrive in.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "lookback.cuh"
+#include "sq_internal.cuh"
+
+namespace sq {
+
+template <typename KeyT>
+int radix_sort_pairs(KeyT* k[2], unsigned* v[2], uint64_t n, int bits);
+void check_device_error();
+
+constexpr int kMaxRuns = 64;
+
+struct Run {
+    uint8_t word;
+    uint8_t shift;
+    uint8_t len;
+    uint8_t dst;
+};
+struct Extract {
+    uint32_t nruns;
+    uint32_t flag_bit;  // 0xff: no condition bit in this chunk
+    Run runs[kMaxRuns];
+};
+
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ bool keep_amp(double2 a, double eps) { return !(a.x * a.x + a.y * a.y < eps); }
+
+// ------------------------------------------------------------------ 1. stats
+template <int K>
+__global__ void __launch_bounds__(256) stats_kernel(ConstKeyPtrs keys, uint64_t n, DCondSet cond,
+                                                    const uint64_t* __restrict__ gmask_in,
+                                                    unsigned long long* __restrict__ out /* [K or, K and, fail] */) {
+    __shared__ unsigned long long s_or[K], s_and[K];
+    __shared__ unsigned long long s_fail;
+    uint64_t gm[K];
+#pragma unroll
+    for (int w = 0; w < K; ++w) gm[w] = gmask_in[w];
+    if (threadIdx.x < K) {
+        s_or[threadIdx.x] = 0;
+        s_and[threadIdx.x] = ~0ull;
+    }
+    if (threadIdx.x == 0) s_fail = 0;
+    __syncthreads();
+    uint64_t o[K], a[K];
+#pragma unroll
+    for (int w = 0; w < K; ++w) {
+        o[w] = 0;
+        a[w] = ~0ull;
+    }
+    unsigned long long fails = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint64_t k[K];
+#pragma unroll
+        for (int w = 0; w < K; ++w) k[w] = keys.w[w][i];
+        if (!cond_ok<K>(k, cond)) {
+            ++fails;
+            continue;
+        }
+#pragma unroll
+        for (int w = 0; w < K; ++w) {
+            o[w] |= k[w] & gm[w];
+            a[w] &= k[w] & gm[w];
+        }
+    }
+#pragma unroll
+    for (int w = 0; w < K; ++w) {
+        for (int s = 16; s > 0; s >>= 1) {
+            o[w] |= __shfl_xor_sync(0xffffffffu, o[w], s);
+            a[w] &= __shfl_xor_sync(0xffffffffu, a[w], s);
+        }
+    }
+    for (int s = 16; s > 0; s >>= 1) fails += __shfl_xor_sync(0xffffffffu, fails, s);
+    if ((threadIdx.x & 31u) == 0) {
+#pragma unroll
+        for (int w = 0; w < K; ++w) {
+            atomicOr(&s_or[w], (unsigned long long)o[w]);
+            atomicAnd(&s_and[w], (unsigned long long)a[w]);
+        }
+        atomicAdd(&s_fail, fails);
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        atomicOr(&out[threadIdx.x], s_or[threadIdx.x]);
+        atomicAnd(&out[K + threadIdx.x], s_and[threadIdx.x]);
+    }
+    if (threadIdx.x == 0) atomicAdd(&out[2 * K], s_fail);
+}
+
+// ------------------------------------------------------------------ 2. extract
+template <int K, typename KeyT, bool GATHER>
+__global__ void __launch_bounds__(256) extract_kernel(ConstKeyPtrs keys, uint64_t n, const __grid_constant__ Extract ex,
+                                                      DCondSet cond, KeyT* __restrict__ sk, unsigned* __restrict__ idx) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const unsigned e = GATHER ? idx[i] : (unsigned)i;
+        uint64_t k[K];
+#pragma unroll
+        for (int w = 0; w < K; ++w) k[w] = keys.w[w][e];
+        uint64_t v = 0;
+        for (uint32_t r = 0; r < ex.nruns; ++r) {
+            const Run ru = ex.runs[r];
+            v |= ((kword<K>(k, ru.word) >> ru.shift) & wmask(ru.len)) << ru.dst;
+        }
+        if (ex.flag_bit != 0xffu && !cond_ok<K>(k, cond)) v |= 1ull << ex.flag_bit;
+        sk[i] = (KeyT)v;
+        if (!GATHER) idx[i] = (unsigned)i;
+    }
+}
+
+__global__ void iota_kernel(unsigned* __restrict__ idx, uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) idx[i] = (unsigned)i;
+}
+
+// ------------------------------------------------------------------ 4. segment heads
+struct LbWs {
+    unsigned long long* status;
+    unsigned* counter;
+    unsigned long long* total;
+};
+static LbWs make_lb(long long ntiles, int slot_offset_bytes = 0) {
+    size_t bytes = 256 + (size_t)ntiles * 8;
+    char* p = (char*)ws().get(WS_MISC, bytes);
+    SQ_CUDA(cudaMemsetAsync(p, 0, bytes, stream()));
+    LbWs w;
+    w.counter = (unsigned*)p;
+    w.total = (unsigned long long*)(p + 8);
+    w.status = (unsigned long long*)(p + 256);
+    (void)slot_offset_bytes;
+    return w;
+}
+
+constexpr int kSelBlock = 256;
+constexpr int kSelItems = 8;
+constexpr int kSelTile = kSelBlock * kSelItems;
+
+// Head of a group: first entry, or group key differs from the previous entry.
+// KEYCMP: compare sorted 1-chunk keys; otherwise gather full masked keys.
+template <int K, typename KeyT, bool KEYCMP>
+__device__ __forceinline__ bool is_head(uint64_t i, const KeyT* sk, const unsigned* idx, ConstKeyPtrs keys,
+                                        const uint64_t* gm) {
+    if (i == 0) return true;
+    if (KEYCMP) return sk[i] != sk[i - 1];
+    const unsigned a = idx[i], b = idx[i - 1];
+    bool diff = false;
+#pragma unroll
+    for (int w = 0; w < K; ++w) diff = diff || (((keys.w[w][a] ^ keys.w[w][b]) & gm[w]) != 0);
+    return diff;
+}
+
+// Order-preserving select of head positions in [0, n) into seg[]; the count
+// lands in *lb.total.
+template <int K, typename KeyT, bool KEYCMP>
+__global__ void __launch_bounds__(kSelBlock) heads_kernel(const KeyT* __restrict__ sk, const unsigned* __restrict__ idx,
+                                                          ConstKeyPtrs keys, const uint64_t* __restrict__ gmask,
+                                                          uint64_t n, unsigned* __restrict__ seg, LbWs lb,
+                                                          long long ntiles, unsigned* err) {
+    __shared__ unsigned s_tile;
+    __shared__ unsigned s_cnt[kSelItems][kSelBlock / 32];
+    __shared__ unsigned long long s_prefix;
+    uint64_t gm[K];
+#pragma unroll
+    for (int w = 0; w < K; ++w) gm[w] = gmask[w];
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(lb.counter, 1u);
+    __syncthreads();
+    const long long tile = s_tile;
+    const uint64_t base = (uint64_t)tile * kSelTile;
+    unsigned ball[kSelItems];
+#pragma unroll
+    for (int j = 0; j < kSelItems; ++j) {
+        const uint64_t i = base + (uint64_t)j * kSelBlock + tid;
+        const bool h = i < n && is_head<K, KeyT, KEYCMP>(i, sk, idx, keys, gm);
+        ball[j] = __ballot_sync(0xffffffffu, h);
+        if (lane == 0) s_cnt[j][warp] = __popc(ball[j]);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int W = kSelBlock / 32;
+        unsigned v0 = s_cnt[(2 * lane) / W][(2 * lane) % W];
+        unsigned v1 = s_cnt[(2 * lane + 1) / W][(2 * lane + 1) % W];
+        unsigned sum = v0 + v1, inc = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= (unsigned)o) inc += t;
+        }
+        const unsigned excl = inc - sum;
+        const unsigned total = __shfl_sync(0xffffffffu, inc, 31);
+        s_cnt[(2 * lane) / W][(2 * lane) % W] = excl;
+        s_cnt[(2 * lane + 1) / W][(2 * lane + 1) % W] = excl + v0;
+        unsigned long long pre = lb_warp_exclusive(lb.status, tile, total, err);
+        if (lane == 0) {
+            s_prefix = pre;
+            if (tile == ntiles - 1) *lb.total = pre + total;
+        }
+    }
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int j = 0; j < kSelItems; ++j) {
+        if (!((ball[j] >> lane) & 1u)) continue;
+        const uint64_t i = base + (uint64_t)j * kSelBlock + tid;
+        seg[s_prefix + s_cnt[j][warp] + __popc(ball[j] & lt)] = (unsigned)i;
+    }
+}
+
+// Exclusive scan of per-group counts (u32) into u64 offsets; total in *lb.total.
+__global__ void __launch_bounds__(kSelBlock) scan_counts_kernel(const unsigned* __restrict__ cnt,
+                                                                unsigned long long* __restrict__ off, uint64_t n,
+                                                                LbWs lb, long long ntiles, unsigned* err) {
+    __shared__ unsigned s_tile;
+    __shared__ unsigned long long s_w[kSelBlock / 32];
+    __shared__ unsigned long long s_prefix;
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(lb.counter, 1u);
+    __syncthreads();
+    const long long tile = s_tile;
+    const uint64_t base = (uint64_t)tile * kSelTile + (uint64_t)tid * kSelItems;  // blocked: thread owns 8 consecutive
+    unsigned long long v[kSelItems];
+    unsigned long long sum = 0;
+#pragma unroll
+    for (int j = 0; j < kSelItems; ++j) {
+        const uint64_t i = base + j;
+        v[j] = i < n ? cnt[i] : 0ull;
+        sum += v[j];
+    }
+    unsigned long long inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (unsigned)o) inc += t;
+    }
+    if (lane == 31) s_w[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long wv = lane < kSelBlock / 32 ? s_w[lane] : 0ull;
+        unsigned long long wi = wv;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= (unsigned)o) wi += t;
+        }
+        const unsigned long long total = __shfl_sync(0xffffffffu, wi, kSelBlock / 32 - 1);
+        if (lane < kSelBlock / 32) s_w[lane] = wi - wv;
+        unsigned long long pre = lb_warp_exclusive(lb.status, tile, total, err);
+        if (lane == 0) {
+            s_prefix = pre;
+            if (tile == ntiles - 1) *lb.total = pre + total;
+        }
+    }
+    __syncthreads();
+    unsigned long long run = s_prefix + s_w[warp] + inc - sum;
+#pragma unroll
+    for (int j = 0; j < kSelItems; ++j) {
+        const uint64_t i = base + j;
+        if (i < n) off[i] = run;
+        run += v[j];
+    }
+}
+
+// ------------------------------------------------------------------ 5/6. emit
+struct EmitArgs {
+    ConstKeyPtrs in_keys;
+    const double2* in_amp;
+    KeyPtrs out_keys;
+    double2* out_amp;
+    const unsigned* idx;       // sorted entry indices
+    const unsigned* seg;       // group starts, seg[G] = end
+    uint64_t groups;
+    unsigned* cnt;             // count pass output
+    const unsigned long long* off;  // write pass input
+    Field target;
+    Field aux;
+    int mode;
+    int nbits;                 // target width (1 for pair modes)
+    double extra;              // 1/sqrt(2^n)
+    double sqrt2inv;
+    double eps;
+    double sign2pi;            // CondRot: +-2*pi
+    double2 m[4];
+};
+
+template <int K>
+__device__ __forceinline__ void load_key(const ConstKeyPtrs& kp, unsigned e, uint64_t (&k)[K]) {
+#pragma unroll
+    for (int w = 0; w < K; ++w) k[w] = kp.w[w][e];
+}
+template <int K>
+__device__ __forceinline__ void store_entry(const KeyPtrs& kp, double2* amp, unsigned long long o, const uint64_t (&k)[K],
+                                            double2 a) {
+#pragma unroll
+    for (int w = 0; w < K; ++w) kp.w[w][o] = k[w];
+    amp[o] = a;
+}
+
+__device__ __forceinline__ double as_rational(uint64_t v, unsigned w) {
+    if (w >= 64) return v * 1.0 / 2 / 9223372036854775808.0;
+    return 1.0 * v / (double)(1ull << w);
+}
+
+// Pair modes (1-bit target): one thread per group.
+template <int K, bool WRITE>
+__global__ void __launch_bounds__(256) emit_pair_kernel(const __grid_constant__ EmitArgs a) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < a.groups; g += stride) {
+        const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
+        const unsigned m = s1 - s0;
+        const unsigned e0 = a.idx[s0];
+        uint64_t k0[K];
+        load_key<K>(a.in_keys, e0, k0);
+        const bool b0 = fget<K>(k0, a.target) & 1ull;
+        double2 az = make_double2(0.0, 0.0), ao = make_double2(0.0, 0.0);
+        const double2 v0 = a.in_amp[e0];
+        bool has_z = false, has_o = false;
+        if (b0) { ao = v0; has_o = true; } else { az = v0; has_z = true; }
+        if (m >= 2) {
+            const unsigned e1 = a.idx[s0 + 1];
+            const double2 v1 = a.in_amp[e1];
+            if (b0) { az = v1; has_z = true; } else { ao = v1; has_o = true; }
+        }
+        double2 rz, ro;
+        const double2 zero = make_double2(0.0, 0.0);
+        if (a.mode == GM_HADAMARD_BOOL) {
+            const double s = a.sqrt2inv;
+            if (has_z && has_o) {
+                rz = cadd(cscale(az, s), cscale(ao, s));
+                ro = csub(cscale(az, s), cscale(ao, s));
+            } else if (has_z) {
+                rz = cscale(az, s);
+                ro = cscale(az, s);
+            } else {
+                rz = cscale(ao, s);
+                ro = cscale(ao, -s);
+            }
+        } else if (a.mode == GM_ROT) {
+            if (has_z && has_o) {
+                rz = cadd(cmul2(az, a.m[0]), cmul2(ao, a.m[1]));
+                ro = cadd(cmul2(az, a.m[2]), cmul2(ao, a.m[3]));
+            } else if (has_z) {
+                rz = cmul2(az, a.m[0]);
+                ro = cmul2(az, a.m[2]);
+            } else {
+                rz = cmul2(ao, a.m[1]);
+                ro = cmul2(ao, a.m[3]);
+            }
+        } else {  // GM_CONDROT: partner amplitude 0 for singletons, as the reference inserts it
+            const double rot = as_rational(fget<K>(k0, a.aux), a.aux.width) * a.sign2pi;
+            double sn, cs;
+            sincos(rot, &sn, &cs);
+            if (!has_z) az = zero;
+            if (!has_o) ao = zero;
+            rz = csub(cscale(az, cs), cscale(ao, sn));
+            ro = cadd(cscale(az, sn), cscale(ao, cs));
+        }
+        const bool kz = keep_amp(rz, a.eps), ko = keep_amp(ro, a.eps);
+        if (!WRITE) {
+            a.cnt[g] = (unsigned)kz + (unsigned)ko;
+        } else {
+            unsigned long long o = a.off[g];
+            uint64_t kk[K];
+#pragma unroll
+            for (int w = 0; w < K; ++w) kk[w] = k0[w];
+            if (kz) {
+                fset<K>(kk, a.target, 0);
+                store_entry<K>(a.out_keys, a.out_amp, o++, kk, rz);
+            }
+            if (ko) {
+                fset<K>(kk, a.target, 1);
+                store_entry<K>(a.out_keys, a.out_amp, o, kk, ro);
+            }
+        }
+    }
+}
+
+// add_systems merge: sum each run of equal keys in sorted (stable) order.
+template <int K, bool WRITE>
+__global__ void __launch_bounds__(256) emit_merge_kernel(const __grid_constant__ EmitArgs a) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < a.groups; g += stride) {
+        const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
+        const unsigned e0 = a.idx[s0];
+        double2 acc = a.in_amp[e0];
+        for (unsigned j = s0 + 1; j < s1; ++j) acc = cadd(acc, a.in_amp[a.idx[j]]);
+        const bool keep = keep_amp(acc, a.eps);
+        if (!WRITE) {
+            a.cnt[g] = keep ? 1u : 0u;
+        } else if (keep) {
+            uint64_t k0[K];
+            load_key<K>(a.in_keys, e0, k0);
+            store_entry<K>(a.out_keys, a.out_amp, a.off[g], k0, acc);
+        }
+    }
+}
+
+// Hadamard groups: one worker (a warp, or a whole block) per group, the 2^n
+// slots of the group in shared memory.
+template <int W>
+__device__ __forceinline__ void worker_sync() {
+    if (W == 32) __syncwarp();
+    else __syncthreads();
+}
+
+// exclusive scan of a per-thread flag over a worker, in thread order; returns
+// (exclusive prefix, total) for this round.
+template <int W>
+__device__ __forceinline__ unsigned worker_rank(bool f, unsigned* s_tmp, unsigned& total) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned b = __ballot_sync(0xffffffffu, f);
+    const unsigned in_warp = __popc(b & ((1u << lane) - 1u));
+    if (W == 32) {
+        total = __popc(b);
+        return in_warp;
+    }
+    const unsigned warp = threadIdx.x >> 5;
+    if (lane == 0) s_tmp[warp] = __popc(b);
+    __syncthreads();
+    unsigned pre = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < W / 32; ++w) {
+        const unsigned c = s_tmp[w];
+        if ((unsigned)w < warp) pre += c;
+        tot += c;
+    }
+    __syncthreads();
+    total = tot;
+    return pre + in_warp;
+}
+
+template <int K, int W, bool WRITE>
+__global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constant__ EmitArgs a) {
+    extern __shared__ double2 s_slots[];
+    __shared__ unsigned s_tmp[8];
+    __shared__ uint64_t s_member_t[8][64];
+    __shared__ double2 s_member_a[8][64];
+    const unsigned S = 1u << a.nbits;
+    const unsigned wid = W == 32 ? (threadIdx.x >> 5) : 0u;
+    const unsigned t = W == 32 ? (threadIdx.x & 31u) : threadIdx.x;
+    double2* slots = s_slots + (size_t)wid * S;
+    const uint64_t workers_per_block = blockDim.x / W;
+    const uint64_t stride = (uint64_t)gridDim.x * workers_per_block;
+    const Field tg = a.target;
+    for (uint64_t g = (uint64_t)blockIdx.x * workers_per_block + wid; g < a.groups; g += stride) {
+        const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
+        const unsigned m = s1 - s0;
+        const unsigned e0 = a.idx[s0];
+        uint64_t gk[K];
+        load_key<K>(a.in_keys, e0, gk);
+        const uint64_t v0 = fget<K>(gk, tg);
+        const bool sparse_full = a.mode == GM_HADAMARD_FULL && m <= (unsigned)(a.nbits - 1);
+        if (a.mode == GM_HADAMARD_INT && m == 1) {
+            // singleton: a * 2^{-n/2}, sign (-1)^{popcount(t & v)} (hadamard.cpp:27-42)
+            const double2 base = cscale(a.in_amp[e0], a.extra);
+            const bool keep = keep_amp(base, a.eps);
+            if (!WRITE) {
+                if (t == 0) a.cnt[g] = keep ? S : 0u;
+            } else if (keep) {
+                const unsigned long long o = a.off[g];
+                for (unsigned c = t; c < S; c += W) {
+                    uint64_t kk[K];
+#pragma unroll
+                    for (int w = 0; w < K; ++w) kk[w] = gk[w];
+                    fset<K>(kk, tg, (uint64_t)c);
+                    const double2 v = (__popcll((uint64_t)c & v0) & 1) ? cscale(base, -1.0) : base;
+                    store_entry<K>(a.out_keys, a.out_amp, o + c, kk, v);
+                }
+            }
+            worker_sync<W>();
+            continue;
+        }
+        if (sparse_full) {
+            // Hadamard_Int_Full sparse bucket (hadamard.cpp:267-304): direct
+            // 2^n x m product, members summed in ascending target value.
+            for (unsigned j = t; j < m; j += W) {
+                const unsigned e = a.idx[s0 + j];
+                uint64_t kk[K];
+                load_key<K>(a.in_keys, e, kk);
+                s_member_t[wid][j] = fget<K>(kk, tg);
+                s_member_a[wid][j] = a.in_amp[e];
+            }
+            worker_sync<W>();
+            if (t == 0) {  // order members by target value (m <= 63)
+                for (unsigned i = 1; i < m; ++i) {
+                    const uint64_t kt = s_member_t[wid][i];
+                    const double2 ka = s_member_a[wid][i];
+                    int j = (int)i - 1;
+                    while (j >= 0 && s_member_t[wid][j] > kt) {
+                        s_member_t[wid][j + 1] = s_member_t[wid][j];
+                        s_member_a[wid][j + 1] = s_member_a[wid][j];
+                        --j;
+                    }
+                    s_member_t[wid][j + 1] = kt;
+                    s_member_a[wid][j + 1] = ka;
+                }
+            }
+            worker_sync<W>();
+            for (unsigned c = t; c < S; c += W) {
+                double2 acc = make_double2(0.0, 0.0);
+                for (unsigned j = 0; j < m; ++j) {
+                    double2 term = cscale(s_member_a[wid][j], (__popcll((uint64_t)c & s_member_t[wid][j]) & 1) ? -1. : 1.);
+                    term = cscale(term, a.extra);
+                    acc = cadd(acc, term);
+                }
+                slots[c] = acc;
+            }
+            worker_sync<W>();
+        } else {
+            // zero-filled slots, scatter members, stage-ascending FWHT (hadamard.cpp:44-59, 100-131)
+            for (unsigned c = t; c < S; c += W) slots[c] = make_double2(0.0, 0.0);
+            worker_sync<W>();
+            for (unsigned j = t; j < m; j += W) {
+                const unsigned e = a.idx[s0 + j];
+                uint64_t kk[K];
+                load_key<K>(a.in_keys, e, kk);
+                slots[fget<K>(kk, tg)] = a.in_amp[e];
+            }
+            worker_sync<W>();
+            for (int qn = 0; qn < a.nbits; ++qn) {
+                const unsigned h = 1u << qn;
+                for (unsigned p = t; p < S / 2; p += W) {
+                    const unsigned i0 = ((p >> qn) << (qn + 1)) | (p & (h - 1u));
+                    const unsigned i1 = i0 + h;
+                    const double2 x0 = slots[i0], x1 = slots[i1];
+                    slots[i0] = cscale(cadd(x0, x1), a.sqrt2inv);
+                    slots[i1] = cscale(csub(x0, x1), a.sqrt2inv);
+                }
+                worker_sync<W>();
+            }
+        }
+        // count / write the kept slots in ascending target order
+        unsigned long long o = WRITE ? a.off[g] : 0ull;
+        unsigned kept = 0;
+        for (unsigned r = 0; r < S; r += W) {
+            const unsigned c = r + t;
+            const bool keep = c < S && keep_amp(slots[c], a.eps);
+            unsigned tot;
+            const unsigned rank = worker_rank<W>(keep, s_tmp, tot);
+            if (WRITE && keep) {
+                uint64_t kk[K];
+#pragma unroll
+                for (int w = 0; w < K; ++w) kk[w] = gk[w];
+                fset<K>(kk, tg, (uint64_t)c);
+                store_entry<K>(a.out_keys, a.out_amp, o + kept + rank, kk, slots[c]);
+            }
+            kept += tot;
+        }
+        if (!WRITE && t == 0) a.cnt[g] = kept;
+        worker_sync<W>();
+    }
+}
+
+// Entries that fail the control conditions: copied through unchanged.
+template <int K>
+__global__ void passthrough_kernel(ConstKeyPtrs ik, const double2* __restrict__ ia, const unsigned* __restrict__ idx,
+                                   uint64_t count, KeyPtrs ok, double2* __restrict__ oa, uint64_t out_base) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
+        const unsigned e = idx[j];
+        uint64_t k[K];
+        load_key<K>(ik, e, k);
+        store_entry<K>(ok, oa, out_base + j, k, ia[e]);
+    }
+}
+
+// ------------------------------------------------------------------ host pipeline
+template <int K>
+static void run_group(State& s, const GroupSpec& gs) {
+    const uint64_t N = s.n;
+    cudaStream_t st = stream();
+    ConstKeyPtrs ik;
+    for (int w = 0; w < SQ_KMAX; ++w) ik.w[w] = s.live.keys[w];
+
+    // group mask: active bits except the target bits
+    uint64_t gmask[SQ_KMAX];
+    regtable().active_mask(gmask);
+    if (gs.target.width) gmask[gs.target.word] &= ~(wmask(gs.target.width) << gs.target.shift);
+
+    uint64_t* dg = (uint64_t*)ws().get(WS_REDUCE, 64 * 8);
+    unsigned long long* stats = (unsigned long long*)(dg + 16);
+    std::vector<unsigned long long> init(2 * K + 1, 0);
+    for (int w = 0; w < K; ++w) init[K + w] = ~0ull;
+    SQ_CUDA(cudaMemcpyAsync(dg, gmask, SQ_KMAX * 8, cudaMemcpyHostToDevice, st));
+    SQ_CUDA(cudaMemcpyAsync(stats, init.data(), init.size() * 8, cudaMemcpyHostToDevice, st));
+    stats_kernel<K><<<grid_for(N, 256, 4), 256, 0, st>>>(ik, N, gs.cond, dg, stats);
+    count_launch();
+    SQ_CUDA(cudaGetLastError());
+    std::vector<unsigned long long> res(2 * K + 1);
+    SQ_CUDA(cudaMemcpyAsync(res.data(), stats, res.size() * 8, cudaMemcpyDeviceToHost, st));
+    SQ_CUDA(cudaStreamSynchronize(st));
+    const uint64_t F = res[2 * K];
+    const uint64_t P = N - F;
+
+    // varying group-key bits -> extraction runs (least significant first)
+    std::vector<Run> runs;
+    int V = 0;
+    for (int w = 0; w < K; ++w) {
+        uint64_t vm = (res[w] ^ res[K + w]) & gmask[w];
+        int b = 0;
+        while (b < 64) {
+            if (!((vm >> b) & 1ull)) { ++b; continue; }
+            int e = b;
+            while (e < 64 && ((vm >> e) & 1ull)) ++e;
+            runs.push_back(Run{(uint8_t)w, (uint8_t)b, (uint8_t)(e - b), 0});
+            V += e - b;
+            b = e;
+        }
+    }
+    const int total_bits = V + (F ? 1 : 0);
+
+    unsigned* vbuf[2] = {(unsigned*)ws().get(WS_SORT_VAL0, N * 4 + 16), (unsigned*)ws().get(WS_SORT_VAL1, N * 4 + 16)};
+    unsigned* idx = vbuf[0];
+    const void* sorted_keys = nullptr;
+    int key_bytes = 0;
+
+    if (total_bits == 0) {
+        iota_kernel<<<grid_for(N, 256), 256, 0, st>>>(idx, N);
+        count_launch();
+    } else {
+        // split the (V + flag) bits into chunks of <= 64, sort least significant chunk first
+        struct Chunk {
+            Extract ex;
+            int bits;
+        };
+        std::vector<Chunk> chunks;
+        {
+            Chunk cur;
+            memset(&cur, 0, sizeof(cur));
+            cur.ex.flag_bit = 0xff;
+            int used = 0;
+            for (Run r : runs) {
+                int len = r.len;
+                int sh = r.shift;
+                while (len > 0) {
+                    if (used == 64 || cur.ex.nruns == kMaxRuns) {
+                        cur.bits = used;
+                        chunks.push_back(cur);
+                        memset(&cur, 0, sizeof(cur));
+                        cur.ex.flag_bit = 0xff;
+                        used = 0;
+                    }
+                    int take = std::min(len, 64 - used);
+                    cur.ex.runs[cur.ex.nruns++] = Run{r.word, (uint8_t)sh, (uint8_t)take, (uint8_t)used};
+                    used += take;
+                    sh += take;
+                    len -= take;
+                }
+            }
+            if (F) {
+                if (used == 64) {
+                    cur.bits = used;
+                    chunks.push_back(cur);
+                    memset(&cur, 0, sizeof(cur));
+                    used = 0;
+                }
+                cur.ex.flag_bit = (uint32_t)used;
+                used += 1;
+            } else {
+                cur.ex.flag_bit = 0xff;
+            }
+            cur.bits = used;
+            if (used > 0) chunks.push_back(cur);
+        }
+        const bool small = chunks.size() == 1 && chunks[0].bits <= 32;
+        if (small) {
+            uint32_t* kb[2] = {(uint32_t*)ws().get(WS_SORT_KEY0, N * 4 + 16), (uint32_t*)ws().get(WS_SORT_KEY1, N * 4 + 16)};
+            extract_kernel<K, uint32_t, false><<<grid_for(N, 256), 256, 0, st>>>(ik, N, chunks[0].ex, gs.cond, kb[0], vbuf[0]);
+            count_launch();
+            int r = radix_sort_pairs<uint32_t>(kb, vbuf, N, chunks[0].bits);
+            idx = vbuf[r];
+            sorted_keys = kb[r];
+            key_bytes = 4;
+        } else {
+            uint64_t* kb[2] = {(uint64_t*)ws().get(WS_SORT_KEY0, N * 8 + 16), (uint64_t*)ws().get(WS_SORT_KEY1, N * 8 + 16)};
+            int cur = 0;  // buffer pair holding the current (keys, indices)
+            for (size_t c = 0; c < chunks.size(); ++c) {
+                if (c == 0)
+                    extract_kernel<K, uint64_t, false><<<grid_for(N, 256), 256, 0, st>>>(ik, N, chunks[c].ex, gs.cond, kb[0], vbuf[0]);
+                else  // later chunks: key bits of the entry now at position i
+                    extract_kernel<K, uint64_t, true><<<grid_for(N, 256), 256, 0, st>>>(ik, N, chunks[c].ex, gs.cond, kb[cur], vbuf[cur]);
+                count_launch();
+                SQ_CUDA(cudaGetLastError());
+                uint64_t* kk[2] = {kb[cur], kb[cur ^ 1]};
+                unsigned* vv[2] = {vbuf[cur], vbuf[cur ^ 1]};
+                const int r = radix_sort_pairs<uint64_t>(kk, vv, N, chunks[c].bits);
+                if (r) cur ^= 1;
+            }
+            idx = vbuf[cur];
+            sorted_keys = kb[cur];
+            key_bytes = chunks.size() == 1 ? 8 : 0;
+        }
+    }
+    SQ_CUDA(cudaGetLastError());
+
+    // group starts over the first P (condition-passing) entries
+    uint64_t G = 0;
+    unsigned* seg = (unsigned*)ws().get(WS_SEG, (P + 2) * 4);
+    if (P > 0) {
+        if (total_bits == 0 || (V == 0)) {
+            unsigned h[2] = {0u, (unsigned)P};
+            SQ_CUDA(cudaMemcpyAsync(seg, h, 8, cudaMemcpyHostToDevice, st));
+            G = 1;
+        } else {
+            const long long nt = (long long)((P + kSelTile - 1) / kSelTile);
+            LbWs lb = make_lb(nt);
+            const unsigned grid = (unsigned)nt;
+            if (key_bytes == 4)
+                heads_kernel<K, uint32_t, true><<<grid, kSelBlock, 0, st>>>((const uint32_t*)sorted_keys, idx, ik, dg, P, seg, lb, nt, device_error_word());
+            else if (key_bytes == 8)
+                heads_kernel<K, uint64_t, true><<<grid, kSelBlock, 0, st>>>((const uint64_t*)sorted_keys, idx, ik, dg, P, seg, lb, nt, device_error_word());
+            else
+                heads_kernel<K, uint64_t, false><<<grid, kSelBlock, 0, st>>>(nullptr, idx, ik, dg, P, seg, lb, nt, device_error_word());
+            count_launch();
+            SQ_CUDA(cudaGetLastError());
+            unsigned long long g = 0;
+            SQ_CUDA(cudaMemcpyAsync(&g, lb.total, 8, cudaMemcpyDeviceToHost, st));
+            check_device_error();
+            G = g;
+            unsigned endv = (unsigned)P;
+            SQ_CUDA(cudaMemcpyAsync(seg + G, &endv, 4, cudaMemcpyHostToDevice, st));
+        }
+    }
+
+    // emit: count pass, scan, write pass
+    EmitArgs ea;
+    memset(&ea, 0, sizeof(ea));
+    ea.in_keys = ik;
+    ea.in_amp = s.live.amp;
+    ea.idx = idx;
+    ea.seg = seg;
+    ea.groups = G;
+    ea.target = gs.target;
+    ea.aux = gs.aux;
+    ea.mode = gs.mode;
+    ea.nbits = gs.target.width;
+    ea.extra = 1.0 / std::sqrt((double)(1ull << gs.target.width));
+    ea.sqrt2inv = 1.0 / std::sqrt(2.0);
+    ea.eps = gs.eps;
+    ea.sign2pi = gs.sign * 2 * 3.14159265358979323846;
+    for (int i = 0; i < 4; ++i) ea.m[i] = gs.m[i];
+    ea.cnt = (unsigned*)ws().get(WS_COUNT, (G + 1) * 4);
+    unsigned long long* off = (unsigned long long*)ws().get(WS_OFFSET, (G + 1) * 8);
+    ea.off = off;
+
+    const bool pair = gs.mode == GM_HADAMARD_BOOL || gs.mode == GM_ROT || gs.mode == GM_CONDROT;
+    const int nb = gs.target.width;
+    const unsigned S = 1u << nb;
+    size_t smem = 0;
+    int W = 0;
+    if (!pair && gs.mode != GM_MERGE) {
+        if (nb > 12) fail(SQ_ERR_UNSUPPORTED, "Hadamard on more than 12 bits at once is not provided by this engine");
+        W = S <= 256 ? 32 : 256;
+        smem = (size_t)(W == 32 ? 8 : 1) * S * sizeof(double2);
+    }
+    auto launch_emit = [&](bool write) {
+        if (G == 0) return;
+        if (pair) {
+            if (write) emit_pair_kernel<K, true><<<grid_for(G, 256), 256, 0, st>>>(ea);
+            else emit_pair_kernel<K, false><<<grid_for(G, 256), 256, 0, st>>>(ea);
+        } else if (gs.mode == GM_MERGE) {
+            if (write) emit_merge_kernel<K, true><<<grid_for(G, 256), 256, 0, st>>>(ea);
+            else emit_merge_kernel<K, false><<<grid_for(G, 256), 256, 0, st>>>(ea);
+        } else if (W == 32) {
+            const unsigned grid = (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8);
+            if (write) emit_hadamard_kernel<K, 32, true><<<grid, 256, smem, st>>>(ea);
+            else emit_hadamard_kernel<K, 32, false><<<grid, 256, smem, st>>>(ea);
+        } else {
+            static bool attr_set = false;
+            if (!attr_set) {
+                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+                attr_set = true;
+            }
+            const unsigned grid = (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2);
+            if (write) emit_hadamard_kernel<K, 256, true><<<grid, 256, smem, st>>>(ea);
+            else emit_hadamard_kernel<K, 256, false><<<grid, 256, smem, st>>>(ea);
+        }
+        count_launch();
+        SQ_CUDA(cudaGetLastError());
+    };
+    launch_emit(false);
+    uint64_t T = 0;
+    if (G > 0) {
+        const long long nt = (long long)((G + kSelTile - 1) / kSelTile);
+        LbWs lb = make_lb(nt);
+        scan_counts_kernel<<<(unsigned)nt, kSelBlock, 0, st>>>(ea.cnt, off, G, lb, nt, device_error_word());
+        count_launch();
+        SQ_CUDA(cudaGetLastError());
+        unsigned long long t = 0;
+        SQ_CUDA(cudaMemcpyAsync(&t, lb.total, 8, cudaMemcpyDeviceToHost, st));
+        check_device_error();
+        T = t;
+    }
+    const uint64_t out_n = T + F;
+    ensure_buffers(s.spare, std::max<uint64_t>(out_n, 1), regtable().k, 0);
+    for (int w = 0; w < SQ_KMAX; ++w) ea.out_keys.w[w] = s.spare.keys[w];
+    ea.out_amp = s.spare.amp;
+    launch_emit(true);
+    if (F) {
+        passthrough_kernel<K><<<grid_for(F, 256), 256, 0, st>>>(ik, s.live.amp, idx + P, F, ea.out_keys, ea.out_amp, T);
+        count_launch();
+        SQ_CUDA(cudaGetLastError());
+    }
+    swap_live_spare(s);
+    s.n = out_n;
+}
+
+void group_transform(State& s, const GroupSpec& g) {
+    sync_words(s);
+    if (s.n == 0) return;
+    if (s.n >= (1ull << 30)) fail(SQ_ERR_CAPACITY, "split/merge operators are limited to < 2^30 entries");
+    switch (regtable().k) {
+        case 1: run_group<1>(s, g); break;
+        case 2: run_group<2>(s, g); break;
+        case 3: run_group<3>(s, g); break;
+        case 4: run_group<4>(s, g); break;
+        case 5: run_group<5>(s, g); break;
+        case 6: run_group<6>(s, g); break;
+        case 7: run_group<7>(s, g); break;
+        default: run_group<8>(s, g); break;
+    }
+}
+
+// add_systems: dst = merge(dst ++ coef*src), equal keys summed in (dst, src) order.
+__global__ void scale_copy_kernel(const double2* __restrict__ in, double2* __restrict__ out, uint64_t n, double k,
+                                  int do_scale) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double2 v = in[i];
+        out[i] = do_scale ? make_double2(v.x * k, v.y * k) : v;
+    }
+}
+
+void add_systems(State& dst, const State& src, double coef) {
+    if (src.n == 0) return;
+    sync_words(dst);
+    const uint32_t k = regtable().k;
+    const uint64_t n0 = dst.n, n1 = src.n;
+    ensure_buffers(dst.live, n0 + n1, k, n0);
+    cudaStream_t st = stream();
+    for (uint32_t w = 0; w < k; ++w) {
+        if (w < src.live.kalloc)
+            SQ_CUDA(cudaMemcpyAsync(dst.live.keys[w] + n0, src.live.keys[w], n1 * 8, cudaMemcpyDeviceToDevice, st));
+        else
+            SQ_CUDA(cudaMemsetAsync(dst.live.keys[w] + n0, 0, n1 * 8, st));
+    }
+    const int do_scale = std::abs(coef - 1.0) > 1e-14 ? 1 : 0;
+    scale_copy_kernel<<<grid_for(n1, 256), 256, 0, st>>>(src.live.amp, dst.live.amp + n0, n1, coef, do_scale);
+    count_launch();
+    SQ_CUDA(cudaGetLastError());
+    dst.n = n0 + n1;
+    if (n0 == 0) return;
+    GroupSpec g;
+    memset(&g, 0, sizeof(g));
+    g.mode = GM_MERGE;
+    g.eps = 1e-14;
+    group_transform(dst, g);
+}
+
+}  // namespace sq

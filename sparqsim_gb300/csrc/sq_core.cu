@@ -1,0 +1,270 @@
+// sq_core.cu — host runtime of the engine: errors, the process-global register
+// table and its bit packing, the library stream, state buffers and the
+// grow-only workspace.
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <stdexcept>
+
+#include "sq_internal.cuh"
+
+namespace sq {
+
+[[noreturn]] void fail(int code, const std::string& msg) { throw Error{code, msg}; }
+
+void cuda_check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return;
+    if (e == cudaErrorMemoryAllocation) {
+        (void)cudaGetLastError();
+        fail(SQ_ERR_OOM, std::string("device allocation failed: ") + what);
+    }
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        fail(SQ_ERR_NO_DEVICE, std::string(cudaGetErrorString(e)) + " in " + what);
+    fail(SQ_ERR_CUDA, std::string(cudaGetErrorString(e)) + " in " + what);
+}
+
+// ------------------------------------------------------------------ register table
+static RegTable g_table;
+RegTable& regtable() { return g_table; }
+
+const RegEntry& RegTable::at(uint32_t id) const {
+    if (id >= regs.size() || !regs[id].active) fail(SQ_ERR_INVALID, "register id " + std::to_string(id) + " is not active");
+    return regs[id];
+}
+
+Field RegTable::field(uint32_t id) const {
+    const RegEntry& r = at(id);
+    Field f;
+    f.word = (uint8_t)r.word;
+    f.shift = (uint8_t)r.shift;
+    f.width = (uint8_t)r.width;
+    f.type = (uint8_t)r.type;
+    return f;
+}
+
+// First fit over the existing words, lowest shift first; opens a new word
+// when none has room. A register never straddles two words.
+bool RegTable::alloc_bits(uint32_t width, uint32_t* word, uint32_t* shift) {
+    if (width == 0) {
+        *word = 0;
+        *shift = 0;
+        return true;
+    }
+    const uint64_t m = wmask(width);
+    for (uint32_t w = 0; w < SQ_KMAX; ++w) {
+        for (uint32_t s = 0; s + width <= 64; ++s) {
+            if (((used[w] >> s) & m) == 0) {
+                used[w] |= m << s;
+                *word = w;
+                *shift = s;
+                if (w + 1 > k) k = w + 1;
+                return true;
+            }
+        }
+    }
+    return false;
+}
+
+void RegTable::free_bits(uint32_t word, uint32_t shift, uint32_t width) {
+    if (width == 0) return;
+    used[word] &= ~(wmask(width) << shift);
+}
+
+uint32_t RegTable::add(uint32_t type, uint32_t width) {
+    if (width > 64) fail(SQ_ERR_INVALID, "register width > 64");
+    if (type > SQ_RATIONAL) fail(SQ_ERR_INVALID, "bad register type");
+    uint32_t word, shift;
+    if (!alloc_bits(width, &word, &shift))
+        fail(SQ_ERR_CAPACITY, "packed key space exhausted (" + std::to_string(SQ_KMAX * 64) + " bits)");
+    uint32_t id;
+    if (!reusable.empty()) {
+        id = reusable.back();
+        reusable.pop_back();
+    } else {
+        if (regs.size() >= SQ_MAX_REGISTERS) {
+            free_bits(word, shift, width);
+            fail(SQ_ERR_CAPACITY, "more than SQ_MAX_REGISTERS registers");
+        }
+        regs.emplace_back();
+        id = (uint32_t)regs.size() - 1;
+    }
+    RegEntry& e = regs[id];
+    e.active = true;
+    e.type = type;
+    e.width = width;
+    e.word = word;
+    e.shift = shift;
+    return id;
+}
+
+void RegTable::remove(uint32_t id) {
+    if (id >= regs.size()) fail(SQ_ERR_INVALID, "register not found");
+    if (!regs[id].active) fail(SQ_ERR_INVALID, "register is not activated");
+    RegEntry& e = regs[id];
+    free_bits(e.word, e.shift, e.width);
+    e.active = false;
+    reusable.push_back(id);
+}
+
+void RegTable::active_mask(uint64_t out[SQ_KMAX]) const {
+    for (int w = 0; w < SQ_KMAX; ++w) out[w] = 0;
+    for (const auto& r : regs)
+        if (r.active && r.width) out[r.word] |= wmask(r.width) << r.shift;
+}
+
+DCondSet resolve_cond(const sq_cond* c) {
+    DCondSet d;
+    memset(&d, 0, sizeof(d));
+    if (!c) return d;
+    if (c->count > SQ_MAX_CONDITIONS) fail(SQ_ERR_INVALID, "too many conditions");
+    d.n = c->count;
+    for (uint32_t i = 0; i < c->count; ++i) {
+        const sq_condition& q = c->c[i];
+        if (q.kind > SQ_COND_VALUE) fail(SQ_ERR_INVALID, "bad condition kind");
+        Field f = regtable().field(q.reg);
+        d.c[i].kind = (uint8_t)q.kind;
+        d.c[i].word = f.word;
+        d.c[i].shift = f.shift;
+        d.c[i].width = f.width;
+        d.c[i].param = q.param;
+        if (q.kind == SQ_COND_BIT && q.param >= 64) fail(SQ_ERR_INVALID, "condition bit >= 64");
+    }
+    return d;
+}
+
+// ------------------------------------------------------------------ device / stream
+static cudaStream_t g_stream = nullptr;
+static int g_sms = 0;
+static int g_device = -1;
+static std::atomic<uint64_t> g_launches{0};
+
+cudaStream_t stream() {
+    if (!g_stream) {
+        int dev = g_device < 0 ? 0 : g_device;
+        SQ_CUDA(cudaSetDevice(dev));
+        g_device = dev;
+        SQ_CUDA(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+        cudaDeviceProp p;
+        SQ_CUDA(cudaGetDeviceProperties(&p, dev));
+        g_sms = p.multiProcessorCount;
+        // Keep freed stream-ordered memory in the pool instead of returning it.
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    }
+    return g_stream;
+}
+
+void init_device(int device) {
+    int n = 0;
+    SQ_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) fail(SQ_ERR_INVALID, "device index out of range");
+    if (g_stream && device != g_device) fail(SQ_ERR_INVALID, "library already bound to another device");
+    g_device = device;
+    (void)stream();
+}
+
+int num_sms() {
+    if (!g_sms) (void)stream();
+    return g_sms;
+}
+
+static unsigned int* g_err_word = nullptr;
+unsigned int* device_error_word() {
+    if (!g_err_word) {
+        (void)stream();
+        SQ_CUDA(cudaMalloc(&g_err_word, 256));
+        SQ_CUDA(cudaMemset(g_err_word, 0, 256));
+    }
+    return g_err_word;
+}
+
+void count_launch(int n) { g_launches += (uint64_t)n; }
+uint64_t launches() { return g_launches.load(); }
+
+void* dev_alloc(size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    void* p = nullptr;
+    cudaError_t e = cudaMallocAsync(&p, bytes, stream());
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        fail(SQ_ERR_OOM, "cudaMallocAsync of " + std::to_string(bytes) + " bytes failed");
+    }
+    return p;
+}
+
+void dev_free(void* p) {
+    if (p) SQ_CUDA(cudaFreeAsync(p, stream()));
+}
+
+// ------------------------------------------------------------------ buffers
+void free_buffers(Buffers& b) {
+    for (int w = 0; w < SQ_KMAX; ++w) {
+        dev_free(b.keys[w]);
+        b.keys[w] = nullptr;
+    }
+    dev_free(b.amp);
+    b.amp = nullptr;
+    b.cap = 0;
+    b.kalloc = 0;
+}
+
+void ensure_buffers(Buffers& b, uint64_t cap, uint32_t k, uint64_t keep) {
+    if (k > SQ_KMAX) fail(SQ_ERR_CAPACITY, "too many key words");
+    if (keep > b.cap) keep = b.cap;
+    if (cap <= b.cap) {
+        // capacity fine; maybe add words
+        for (uint32_t w = b.kalloc; w < k; ++w) {
+            b.keys[w] = (uint64_t*)dev_alloc(b.cap * 8);
+            SQ_CUDA(cudaMemsetAsync(b.keys[w], 0, b.cap * 8, stream()));
+        }
+        if (k > b.kalloc) b.kalloc = k;
+        return;
+    }
+    uint64_t newcap = std::max<uint64_t>(cap, b.cap + b.cap / 2);
+    newcap = std::max<uint64_t>(newcap, 1024);
+    uint32_t kk = std::max(k, b.kalloc);
+    Buffers nb;
+    nb.cap = newcap;
+    nb.kalloc = kk;
+    for (uint32_t w = 0; w < kk; ++w) {
+        nb.keys[w] = (uint64_t*)dev_alloc(newcap * 8);
+        if (w < b.kalloc && keep) {
+            SQ_CUDA(cudaMemcpyAsync(nb.keys[w], b.keys[w], keep * 8, cudaMemcpyDeviceToDevice, stream()));
+            SQ_CUDA(cudaMemsetAsync(nb.keys[w] + keep, 0, (newcap - keep) * 8, stream()));
+        } else {
+            SQ_CUDA(cudaMemsetAsync(nb.keys[w], 0, newcap * 8, stream()));
+        }
+    }
+    nb.amp = (double2*)dev_alloc(newcap * 16);
+    if (keep && b.amp) SQ_CUDA(cudaMemcpyAsync(nb.amp, b.amp, keep * 16, cudaMemcpyDeviceToDevice, stream()));
+    free_buffers(b);
+    b = nb;
+}
+
+void sync_words(State& s) {
+    uint32_t k = regtable().k;
+    if (s.live.kalloc < k) ensure_buffers(s.live, s.live.cap, k, s.n);
+}
+
+void swap_live_spare(State& s) { std::swap(s.live, s.spare); }
+
+// ------------------------------------------------------------------ workspace
+static Workspace g_ws;
+Workspace& ws() { return g_ws; }
+
+void* Workspace::get(int slot, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (sz[slot] < bytes) {
+        dev_free(p[slot]);
+        size_t n = std::max(bytes, sz[slot] + sz[slot] / 2);
+        n = (n + 255) & ~size_t(255);
+        p[slot] = dev_alloc(n);
+        sz[slot] = n;
+    }
+    return p[slot];
+}
+
+}  // namespace sq

@@ -1,0 +1,242 @@
+// sq_internal.cuh — shared device/host internals of the GB300 sparse-state engine.
+//
+// Data layout in HBM (per state):
+//   keys[w][i]  uint64, w < K: word-major arrays; each active register is a bit
+//               field (word, shift, width) inside one word.
+//   amp[i]      double2 (re, im), 16-byte aligned.
+// A state owns two such buffer sets (live + spare) so split/merge operators
+// write their output out of place and swap.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "sparq_gb300.h"
+
+#define SQ_KMAX SQ_MAX_KEY_WORDS
+
+namespace sq {
+
+// ------------------------------------------------------------------ errors
+struct Error {
+    int code;
+    std::string msg;
+};
+[[noreturn]] void fail(int code, const std::string& msg);
+void cuda_check(cudaError_t e, const char* what);
+#define SQ_CUDA(x) ::sq::cuda_check((x), #x)
+
+// Device word raised by bounded device-side waits (bit 0: a look-back gave
+// up). Allocated once per process; kernels that wait receive its address.
+unsigned int* device_error_word();
+
+// ------------------------------------------------------------------ registers
+struct Field {
+    uint8_t word;
+    uint8_t shift;
+    uint8_t width;
+    uint8_t type;
+};
+
+__host__ __device__ __forceinline__ uint64_t wmask(unsigned w) {
+    return w >= 64 ? ~0ull : ((1ull << w) - 1ull);
+}
+
+struct RegEntry {
+    bool active = false;
+    uint32_t type = 0;
+    uint32_t width = 0;
+    uint32_t word = 0;
+    uint32_t shift = 0;
+};
+
+// Process-global register table (mirrors System::name_register_map plus the
+// packing of each register into a key word).
+struct RegTable {
+    std::vector<RegEntry> regs;
+    std::vector<uint32_t> reusable;   // ids freed by remove, reused LIFO
+    uint64_t used[SQ_KMAX] = {0};     // allocated bits per word
+    uint32_t k = 1;                   // key words in use (>= 1)
+    double clearzero_eps = 1e-14;
+
+    Field field(uint32_t id) const;
+    const RegEntry& at(uint32_t id) const;
+    uint32_t add(uint32_t type, uint32_t width);
+    void remove(uint32_t id);
+    bool alloc_bits(uint32_t width, uint32_t* word, uint32_t* shift);
+    void free_bits(uint32_t word, uint32_t shift, uint32_t width);
+    void active_mask(uint64_t out[SQ_KMAX]) const;
+};
+RegTable& regtable();
+
+// ------------------------------------------------------------------ conditions
+struct DCond {
+    uint8_t kind;
+    uint8_t word;
+    uint8_t shift;
+    uint8_t width;
+    uint32_t pad;
+    uint64_t param;
+};
+struct DCondSet {
+    uint32_t n;
+    uint32_t pad;
+    DCond c[SQ_MAX_CONDITIONS];
+};
+
+template <int K>
+__device__ __forceinline__ uint64_t kword(const uint64_t (&k)[K], unsigned w) {
+    uint64_t r = 0;
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+        if ((unsigned)i == w) r = k[i];
+    return r;
+}
+template <int K>
+__device__ __forceinline__ void kword_set(uint64_t (&k)[K], unsigned w, uint64_t v) {
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+        if ((unsigned)i == w) k[i] = v;
+}
+template <int K>
+__device__ __forceinline__ uint64_t fget(const uint64_t (&k)[K], Field f) {
+    return (kword<K>(k, f.word) >> f.shift) & wmask(f.width);
+}
+template <int K>
+__device__ __forceinline__ void fset(uint64_t (&k)[K], Field f, uint64_t v) {
+    const uint64_t m = wmask(f.width) << f.shift;
+    const uint64_t w = kword<K>(k, f.word);
+    kword_set<K>(k, f.word, (w & ~m) | ((v << f.shift) & m));
+}
+
+template <int K>
+__device__ __forceinline__ bool cond_ok(const uint64_t (&k)[K], const DCondSet& cs) {
+    bool ok = true;
+    for (uint32_t i = 0; i < cs.n; ++i) {
+        const DCond& c = cs.c[i];
+        const uint64_t v = (kword<K>(k, c.word) >> c.shift) & wmask(c.width);
+        switch (c.kind) {
+            case SQ_COND_NONZERO: ok = ok && (v != 0); break;
+            case SQ_COND_ALL_ONES: ok = ok && (v == wmask(c.width)); break;
+            case SQ_COND_BIT: ok = ok && (c.param < 64) && ((v >> c.param) & 1ull); break;
+            default: ok = ok && (v == c.param); break;
+        }
+    }
+    return ok;
+}
+
+DCondSet resolve_cond(const sq_cond* c);
+
+// ------------------------------------------------------------------ QRAM
+struct QramTable {
+    void* dev = nullptr;
+    uint32_t elem_bytes = 8;
+    uint32_t address_size = 0;
+    uint32_t data_size = 0;
+    uint64_t n_words = 0;
+    uint64_t max_word = 0;
+};
+
+// ------------------------------------------------------------------ state
+struct Buffers {
+    uint64_t* keys[SQ_KMAX] = {nullptr};
+    double2* amp = nullptr;
+    uint64_t cap = 0;
+    uint32_t kalloc = 0;
+};
+
+struct State {
+    Buffers live;
+    Buffers spare;
+    uint64_t n = 0;
+};
+
+struct KeyPtrs {
+    uint64_t* w[SQ_KMAX];
+};
+struct ConstKeyPtrs {
+    const uint64_t* w[SQ_KMAX];
+};
+
+cudaStream_t stream();
+int num_sms();
+void count_launch(int n = 1);
+void* dev_alloc(size_t bytes);
+void dev_free(void* p);
+
+// Make sure `b` has at least `cap` entries and `k` key words; existing
+// contents (first `keep` entries) are preserved; new words are zero-filled.
+void ensure_buffers(Buffers& b, uint64_t cap, uint32_t k, uint64_t keep);
+// Make the state's live buffers hold K = regtable().k words.
+void sync_words(State& s);
+void free_buffers(Buffers& b);
+void swap_live_spare(State& s);
+
+// Workspace (grow-only device scratch shared by all operators).
+struct Workspace {
+    void* p[16] = {nullptr};
+    size_t sz[16] = {0};
+    void* get(int slot, size_t bytes);
+};
+Workspace& ws();
+enum WsSlot {
+    WS_SORT_KEY0 = 0,
+    WS_SORT_KEY1,
+    WS_SORT_VAL0,
+    WS_SORT_VAL1,
+    WS_LOOKBACK,
+    WS_HIST,
+    WS_SEG,
+    WS_COUNT,
+    WS_OFFSET,
+    WS_MISC,
+    WS_REDUCE,
+    WS_MERGE_KEYS,
+    WS_COUNT_MAX
+};
+
+// ------------------------------------------------------------------ launch helpers
+inline unsigned grid_for(uint64_t n, int block, int per_sm = 8) {
+    uint64_t g = (n + block - 1) / block;
+    uint64_t cap = (uint64_t)num_sms() * per_sm;
+    if (g > cap) g = cap;
+    if (g == 0) g = 1;
+    return (unsigned)g;
+}
+
+// ------------------------------------------------------------------ operators (host entry, in .cu files)
+struct DInstr;
+void run_program(State& s, const sq_instr* prog, uint32_t n);
+void clear_zero(State& s, double eps);
+double norm_sq(const State& s);
+void scale_amp(State& s, double k);
+void add_systems(State& dst, const State& src, double coef);
+
+enum GroupMode {
+    GM_HADAMARD_INT = 0,   // Hadamard_Int: singleton formula, FWHT otherwise
+    GM_HADAMARD_FULL = 1,  // Hadamard_Int_Full: sparse product below threshold, FWHT otherwise
+    GM_HADAMARD_BOOL = 2,  // Hadamard_Bool pair rules
+    GM_ROT = 3,            // Rot_Bool general 2x2
+    GM_CONDROT = 4,        // CondRot_Rational_Bool
+    GM_MERGE = 5           // sum equal keys (add_systems)
+};
+struct GroupSpec {
+    int mode;
+    Field target;        // varying bits (word, shift, n)
+    Field aux;           // CondRot input register
+    double2 m[4];        // Rot_Bool matrix
+    double sign;         // CondRot: +1 / -1 (dag)
+    DCondSet cond;
+    double eps;          // prune threshold for outputs
+    bool prune;
+};
+void group_transform(State& s, const GroupSpec& g);
+void zero_field(State& s, Field f);
+void move_field(State& s, Field first, Field second, Field dst);
+
+uint64_t* device_u64_scratch();
+
+}  // namespace sq

@@ -1,0 +1,627 @@
+"""Operators with the pysparq names and constructor arguments, executed by
+the GB300 engine.
+
+Each operator is a value object built from register names or ids (resolved
+at construction, like the reference constructors) and applied with
+``op(state)`` / ``op.dag(state)``. ``spec(dag)`` describes the operation as
+plain data; the engine call is chosen from it, and the same description is
+what a test checker consumes.
+
+Reference files (SparQ/src unless noted): quantum_arithmetic.cpp, qram.cpp,
+basic_gates.cpp, parallel_phase_operations.cpp, hadamard.cpp, condrot.cpp,
+system_operations.cpp, dark_magic.cpp; Python names from PySparQ/core.cpp.
+"""
+from __future__ import annotations
+
+import cmath
+import ctypes
+import math
+from ctypes import byref, c_double, c_uint32
+
+from ._native import OP, SQ_MAX_PROGRAM, SqInstr, call
+from .core import Controllable, QRAMCircuit_qutrit, SparseState, StateStorageType, System
+
+PI = math.pi
+U64 = 0xFFFFFFFFFFFFFFFF
+
+
+def _R(x) -> int:
+    return System.resolve(x)
+
+
+def _run(state: SparseState, spec) -> None:
+    kind = spec[0]
+    h = state._h
+    if kind == "prog":
+        instrs = spec[1]
+        for i in range(0, len(instrs), SQ_MAX_PROGRAM):
+            chunk = instrs[i:i + SQ_MAX_PROGRAM]
+            arr = (SqInstr * len(chunk))(*chunk)
+            call("sq_apply_program", h, arr, len(chunk))
+    elif kind == "hadamard_int":
+        call("sq_hadamard_int", h, spec[1], spec[2], byref(spec[3]))
+    elif kind == "hadamard_int_full":
+        call("sq_hadamard_int_full", h, spec[1], byref(spec[2]))
+    elif kind == "hadamard_bool":
+        call("sq_hadamard_bool", h, spec[1], byref(spec[2]))
+    elif kind == "rot_bool":
+        m = (c_double * 8)(*spec[3])
+        call("sq_rot_bool", h, spec[1], spec[2], m, byref(spec[4]), 0)
+    elif kind == "condrot":
+        call("sq_condrot_rational_bool", h, spec[1], spec[2], 1 if spec[3] else 0)
+    elif kind == "clear_zero":
+        call("sq_clear_zero", h, spec[1])
+    elif kind == "normalize":
+        call("sq_normalize", h, None)
+    else:
+        raise ValueError(f"unknown operation {kind}")
+
+
+class BaseOperator(Controllable):
+    """op(state) / op.dag(state) (basic_components.h:748-800)."""
+
+    self_adjoint = False
+    has_dag = True
+
+    def __init__(self):
+        self._init_controls()
+
+    def spec(self, dag: bool = False):
+        raise NotImplementedError
+
+    def __call__(self, state: SparseState) -> None:
+        _run(state, self.spec(False))
+
+    def dag(self, state: SparseState) -> None:
+        if not self.has_dag:
+            raise NotImplementedError("Dagger is not implemented.")
+        _run(state, self.spec(not self.self_adjoint))
+
+
+class SelfAdjointOperator(BaseOperator):
+    self_adjoint = True
+
+
+# ---------------------------------------------------------------------- elementwise
+class ElementwiseOperator(BaseOperator):
+    """An operator that maps each entry on its own: one instruction of the
+    fused elementwise kernel."""
+
+    opcode = "NOP"
+
+    def _fill(self, ins: SqInstr, dag: bool) -> None:
+        pass
+
+    def instr(self, dag: bool = False) -> SqInstr:
+        ins = SqInstr()
+        ins.op = OP[self.opcode]
+        ins.dag = 1 if dag else 0
+        ins.cond = self._cond()
+        self._fill(ins, dag)
+        return ins
+
+    def spec(self, dag: bool = False):
+        return ("prog", [self.instr(dag)])
+
+
+def _set_regs(ins, *regs):
+    for i, r in enumerate(regs):
+        ins.reg[i] = r
+
+
+class _Regs(ElementwiseOperator):
+    """Operators whose operands are only registers, stored in reg slots."""
+
+    def __init__(self, *regs):
+        super().__init__()
+        self.regs = [_R(r) for r in regs]
+
+    def _fill(self, ins, dag):
+        _set_regs(ins, *self.regs)
+
+
+# XOR-out (self-adjoint) three-register arithmetic: res ^= f(lhs, rhs)
+def _xor3(name, opcode, doc):
+    cls = type(name, (_Regs, SelfAdjointOperator), {"opcode": opcode, "__doc__": doc})
+    return cls
+
+
+Add_UInt_UInt = _xor3("Add_UInt_UInt", "ADD_UINT_UINT", "res ^= (lhs + rhs) mod 2^|res| (quantum_arithmetic.cpp:287-306)")
+Sub_UInt_UInt = _xor3("Sub_UInt_UInt", "SUB_UINT_UINT", "res ^= (lhs - rhs) mod 2^|res| (:490-509)")
+Mul_UInt_UInt = _xor3("Mul_UInt_UInt", "MUL_UINT_UINT", "res ^= (lhs * rhs) mod 2^|res| (:556-575)")
+Div_UInt_UInt = _xor3("Div_UInt_UInt", "DIV_UINT_UINT", "res ^= lhs / rhs (0 when rhs == 0) (:577-600)")
+And_UInt_UInt = _xor3("And_UInt_UInt", "AND_UINT_UINT", "res ^= lhs & rhs (:646-665)")
+Or_UInt_UInt = _xor3("Or_UInt_UInt", "OR_UINT_UINT", "res ^= lhs | rhs (:667-686)")
+Xor_UInt_UInt = _xor3("Xor_UInt_UInt", "XOR_UINT_UINT", "res ^= lhs ^ rhs (:688-707)")
+Less_SInt_SInt = _xor3("Less_SInt_SInt", "LESS_SINT_SINT", "flag ^= sext(lhs) < sext(rhs) (:709-729)")
+Less_UInt_UInt = _xor3("Less_UInt_UInt", "LESS_UINT_UINT", "flag ^= lhs < rhs (:961-980)")
+GetMid_UInt_UInt = _xor3("GetMid_UInt_UInt", "GETMID_UINT_UINT", "mid ^= (l + r) / 2 (:1001-1020)")
+
+Neg_UInt = _xor3("Neg_UInt", "NEG_UINT", "res ^= -reg mod 2^|res| (:511-530)")
+Abs_SInt = _xor3("Abs_SInt", "ABS_SINT", "res ^= |sext(reg)| (:532-554)")
+Sqrt_UInt = _xor3("Sqrt_UInt", "SQRT_UINT", "res ^= isqrt(reg) (:602-620)")
+IsZero_UInt = _xor3("IsZero_UInt", "ISZERO_UINT", "flag ^= (reg == 0) (:819-837)")
+Negative_SInt = _xor3("Negative_SInt", "NEGATIVE_SINT", "flag ^= sext(reg) < 0 (:839-857)")
+
+Carry_UInt_UInt = _xor3("Carry_UInt_UInt", "CARRY_UINT_UINT", "flag ^= carry of lhs + rhs at width(res) (:731-754)")
+Overflow_SInt_SInt = _xor3("Overflow_SInt_SInt", "OVERFLOW_SINT_SINT", "flag ^= signed overflow at width(res) (:756-785)")
+MulOverflow_UInt_UInt = _xor3("MulOverflow_UInt_UInt", "MULOVERFLOW_UINT_UINT", "flag ^= lhs*rhs >= 2^width(res) (:787-817)")
+Select_Bool_UInt_UInt = _xor3("Select_Bool_UInt_UInt", "SELECT_BOOL", "res ^= cond&1 ? lhs : rhs (:623-644)")
+Compare_UInt_UInt = _xor3("Compare_UInt_UInt", "COMPARE_UINT_UINT", "equal ^= 1 if l == r else less ^= l < r (:932-959)")
+Assign = _xor3("Assign", "ASSIGN", "r2 ^= r1 (:909-930)")
+Swap_General_General = _xor3("Swap_General_General", "SWAP_GENERAL", "swap(r1, r2) (:982-999)")
+
+
+class _InPlace2(_Regs):
+    """Two-register in-place ops with an inverse: dag flips the sign."""
+
+
+class Add_UInt_UInt_InPlace(_InPlace2):
+    """rhs = (rhs + lhs) mod 2^|rhs|; dag subtracts (quantum_arithmetic.cpp:308-349)."""
+
+    opcode = "ADD_UINT_UINT_INPLACE"
+
+
+class Add_AnyInt_AnyInt_InPlace(_InPlace2):
+    """lhs = (lhs + ext(rhs)) mod 2^|lhs|, rhs sign-extended if SignedInteger (:860-907)."""
+
+    opcode = "ADD_ANYINT_INPLACE"
+
+
+class FlipBools(_Regs, SelfAdjointOperator):
+    """reg = ~reg mod 2^|reg| (quantum_arithmetic.cpp:11-30)."""
+
+    opcode = "FLIP_BOOLS"
+
+
+class _RegConst(ElementwiseOperator):
+    def __init__(self, reg, const):
+        super().__init__()
+        self.reg = _R(reg)
+        self.const = int(const) & U64
+
+    def _fill(self, ins, dag):
+        ins.reg[0] = self.reg
+        ins.imm[0] = self.const
+
+
+class Add_ConstUInt_InPlace(_RegConst):
+    """reg = (reg + c) mod 2^|reg|; dag subtracts (:371-411)."""
+
+    opcode = "ADD_CONST_INPLACE"
+
+
+class ShiftLeft_InPlace(_RegConst):
+    """Cyclic left rotation by `digit` within the register (:63-92); dag rotates right."""
+
+    opcode = "SHIFT_LEFT"
+
+
+class ShiftRight_InPlace(_RegConst):
+    """Cyclic right rotation (:95-121); dag rotates left."""
+
+    opcode = "SHIFT_RIGHT"
+
+
+class _LhsConstRes(ElementwiseOperator):
+    def __init__(self, lhs, const, res):
+        super().__init__()
+        self.lhs, self.const, self.res = _R(lhs), int(const) & U64, _R(res)
+
+    def _fill(self, ins, dag):
+        ins.reg[0] = self.lhs
+        ins.reg[2] = self.res
+        ins.imm[0] = self.const
+
+
+class Add_UInt_ConstUInt(_LhsConstRes, SelfAdjointOperator):
+    """res ^= (lhs + c) mod 2^|res| (:351-369)."""
+
+    opcode = "ADD_UINT_CONST"
+
+
+class Mult_UInt_ConstUInt(_LhsConstRes, SelfAdjointOperator):
+    """res = (res ^ lhs*c) mod 2^|res| (:137-155)."""
+
+    opcode = "MULT_UINT_CONST"
+
+
+class Add_Mult_UInt_ConstUInt_InPlace(_LhsConstRes):
+    """res = (res + c*lhs) mod 2^|res|; dag subtracts (:157-196)."""
+
+    opcode = "ADD_MULT_UINT_CONST"
+
+
+class Mod_Mult_UInt_ConstUInt_InPlace(ElementwiseOperator):
+    """reg = reg * a^(2^x) mod N; dag multiplies by the modular inverse (:200-285)."""
+
+    opcode = "MOD_MULT_CONST"
+
+    def __init__(self, reg, a, x, N):
+        super().__init__()
+        self.reg, self.a, self.x, self.N = _R(reg), int(a), int(x), int(N)
+        if math.gcd(self.a, self.N) > 1:
+            raise ValueError("a and N must be coprime")
+        op = self.a % self.N
+        for _ in range(self.x):
+            op = ((op * op) & U64) % self.N
+        self.opnum = op
+
+    def _inverse(self) -> int:
+        t, nt, r, nr = 0, 1, self.N, self.opnum
+        while nr != 0:
+            q = r // nr
+            t, nt = nt, t - q * nt
+            r, nr = nr, r - q * nr
+        return t % self.N if r == 1 else 1
+
+    def _fill(self, ins, dag):
+        ins.reg[0] = self.reg
+        ins.imm[0] = self._inverse() if dag else self.opnum
+        ins.imm[1] = self.N
+        ins.dag = 0
+
+
+class Swap_Bool_Bool(ElementwiseOperator, SelfAdjointOperator):
+    """Swap bit digit1 of lhs with bit digit2 of rhs (:32-61)."""
+
+    opcode = "SWAP_BOOL_BOOL"
+
+    def __init__(self, lhs, digit1, rhs, digit2):
+        super().__init__()
+        self.lhs, self.d1, self.rhs, self.d2 = _R(lhs), int(digit1), _R(rhs), int(digit2)
+
+    def _fill(self, ins, dag):
+        ins.reg[0], ins.reg[1] = self.lhs, self.rhs
+        ins.imm[0], ins.imm[1] = self.d1, self.d2
+
+
+class _Gate(ElementwiseOperator):
+    def __init__(self, reg, digit=0):
+        super().__init__()
+        self.id = _R(reg)
+        self.digit = int(digit)
+        if self.digit >= System.size_of(self.id):
+            raise ValueError("digit out of range of the register")
+
+    def _fill(self, ins, dag):
+        ins.reg[0] = self.id
+        ins.imm[0] = self.digit
+
+
+class X_Bool(_Gate, SelfAdjointOperator):
+    """Flip bit `digit` of reg (basic_gates.cpp:383-401)."""
+
+    opcode = "X_BOOL"
+
+
+class Y_Bool(_Gate, SelfAdjointOperator):
+    """Flip bit, amplitude *= +i / -i (basic_gates.cpp:418-441)."""
+
+    opcode = "Y_BOOL"
+
+
+class Phase_Bool(ElementwiseOperator):
+    """amp *= e^{i lambda} where bit `digit` of reg is 1; dag uses e^{-i lambda}
+    (basic_gates.cpp:11-54). Phase_Bool(reg, lambda) uses digit 0."""
+
+    opcode = "PHASE_BOOL"
+
+    def __init__(self, reg, digit, lam=None):
+        super().__init__()
+        if lam is None:
+            digit, lam = 0, digit
+        self.id, self.digit, self.lam = _R(reg), int(digit), float(lam)
+        if self.digit >= System.size_of(self.id):
+            raise ValueError("digit out of range of the register")
+
+    def _fill(self, ins, dag):
+        ins.reg[0] = self.id
+        ins.imm[0] = self.digit
+        ins.c[0] = math.cos(self.lam)
+        ins.c[1] = -math.sin(self.lam) if dag else math.sin(self.lam)
+
+
+class Z_Bool(Phase_Bool):
+    def __init__(self, reg):
+        super().__init__(reg, 0, PI)
+
+
+class S_Bool(Phase_Bool):
+    def __init__(self, reg):
+        super().__init__(reg, 0, PI / 2)
+
+
+class T_Bool(Phase_Bool):
+    def __init__(self, reg):
+        super().__init__(reg, 0, PI / 4)
+
+
+class GlobalPhase(ElementwiseOperator):
+    """amp *= c (conditionable); dag uses conj(c) (parallel_phase_operations.cpp:72-107)."""
+
+    opcode = "GLOBAL_PHASE"
+
+    def __init__(self, c):
+        super().__init__()
+        self.c = complex(c)
+
+    def _fill(self, ins, dag):
+        ins.c[0] = self.c.real
+        ins.c[1] = -self.c.imag if dag else self.c.imag
+
+
+def _regmask(regs) -> int:
+    if isinstance(regs, (str, int)):
+        regs = [regs]
+    m = 0
+    for r in regs:
+        rid = _R(r)
+        if rid >= 64:
+            raise ValueError("register id >= 64")
+        m |= 1 << rid
+    return m
+
+
+class Reflection_Bool(ElementwiseOperator, SelfAdjointOperator):
+    """amp *= -1 unless (inverse XOR all-zero) (parallel_phase_operations.cpp:46-70)."""
+
+    opcode = "REFLECTION_BOOL"
+
+    def __init__(self, regs, inverse: bool = False):
+        super().__init__()
+        self.mask = _regmask(regs)
+        self.inverse = bool(inverse)
+
+    def _fill(self, ins, dag):
+        ins.imm[0] = self.mask
+        ins.imm[1] = 1 if self.inverse else 0
+
+
+class ZeroConditionalPhaseFlip(ElementwiseOperator, SelfAdjointOperator):
+    """amp *= -1 where every listed register is 0 (parallel_phase_operations.cpp:11-31)."""
+
+    opcode = "ZERO_COND_PHASE_FLIP"
+
+    def __init__(self, regs):
+        super().__init__()
+        self.mask = _regmask(regs)
+
+    def _fill(self, ins, dag):
+        ins.imm[0] = self.mask
+
+
+class Init_Unsafe(ElementwiseOperator, SelfAdjointOperator):
+    """Set reg = value in every entry (dark_magic.cpp:35-40)."""
+
+    opcode = "INIT_UNSAFE"
+
+    def __init__(self, reg, value):
+        super().__init__()
+        self.id, self.value = _R(reg), int(value) & U64
+
+    def _fill(self, ins, dag):
+        ins.reg[0] = self.id
+        ins.imm[0] = self.value
+
+
+class QRAMLoad(ElementwiseOperator, SelfAdjointOperator):
+    """data ^= memory[addr mod 2^address_size] (qram.cpp:15-35, noise-free)."""
+
+    opcode = "QRAM_LOAD"
+
+    def __init__(self, qram: QRAMCircuit_qutrit, addr, data):
+        super().__init__()
+        if qram is None:
+            raise ValueError("null QRAM")
+        self.qram, self.register_addr, self.register_data = qram, _R(addr), _R(data)
+        if self.register_addr == self.register_data:
+            raise ValueError("QRAMLoad: address and data registers must differ")
+        if System.type_of(self.register_addr) != StateStorageType.UnsignedInteger:
+            raise ValueError("QRAMLoad: address register must be UnsignedInteger")
+
+    def _fill(self, ins, dag):
+        ins.reg[0], ins.reg[1] = self.register_addr, self.register_data
+        ins.qram = self.qram._h.value
+
+
+QRAMLoadFast = QRAMLoad
+
+
+class Fused(ElementwiseOperator):
+    """A chain of elementwise operators applied in one pass over the state
+    (one kernel launch per 32 instructions). dag applies the chain's inverse:
+    the ops' adjoints in reverse order."""
+
+    def __init__(self, ops):
+        super().__init__()
+        for op in ops:
+            if not isinstance(op, ElementwiseOperator):
+                raise TypeError(f"{type(op).__name__} is not elementwise")
+        self.ops = list(ops)
+
+    def spec(self, dag: bool = False):
+        if not dag:
+            return ("prog", [op.instr(False) for op in self.ops])
+        return ("prog", [op.instr(not op.self_adjoint) for op in reversed(self.ops)])
+
+
+# ---------------------------------------------------------------------- split / merge
+class Hadamard_Int(SelfAdjointOperator):
+    """H on the low n_digits bits of reg, grouped by all other bits; ClearZero
+    after (hadamard.cpp:18-162)."""
+
+    def __init__(self, reg, n_digits):
+        super().__init__()
+        self.id, self.n_digits = _R(reg), int(n_digits)
+
+    def spec(self, dag=False):
+        return ("hadamard_int", self.id, self.n_digits, self._cond())
+
+
+class Hadamard_Int_Full(SelfAdjointOperator):
+    """H on the whole register (hadamard.cpp:181-338)."""
+
+    def __init__(self, reg):
+        super().__init__()
+        self.id = _R(reg)
+
+    def spec(self, dag=False):
+        return ("hadamard_int_full", self.id, self._cond())
+
+
+class Hadamard_Bool(SelfAdjointOperator):
+    """H on a 1-bit register (hadamard.cpp:340-439)."""
+
+    def __init__(self, reg):
+        super().__init__()
+        self.out_id = _R(reg)
+        if System.size_of(self.out_id) != 1:
+            raise ValueError("Hadamard_Bool: size of output register must be 1")
+
+    def spec(self, dag=False):
+        return ("hadamard_bool", self.out_id, self._cond())
+
+
+def _mat8(mat):
+    m = [complex(x) for x in mat]
+    if len(m) != 4:
+        raise ValueError("2x2 matrix needs 4 elements (m00, m01, m10, m11)")
+    out = []
+    for z in m:
+        out += [z.real, z.imag]
+    return out
+
+
+class Rot_Bool(BaseOperator):
+    """2x2 unitary on bit `digit` of reg (basic_gates.cpp:74-357); dag applies
+    the conjugate transpose. Rot_Bool(reg, mat) uses digit 0."""
+
+    def __init__(self, reg, digit, mat=None):
+        super().__init__()
+        if mat is None:
+            digit, mat = 0, digit
+        self.id, self.digit, self.mat = _R(reg), int(digit), [complex(x) for x in mat]
+        if self.digit >= System.size_of(self.id):
+            raise ValueError("digit out of range of the register")
+
+    def spec(self, dag=False):
+        m = self.mat
+        if dag:
+            m = [m[0].conjugate(), m[2].conjugate(), m[1].conjugate(), m[3].conjugate()]
+        return ("rot_bool", self.id, self.digit, _mat8(m), self._cond())
+
+
+class RX_Bool(Rot_Bool):
+    """RX(theta) (basic_gates.cpp:536-553)."""
+
+    def __init__(self, reg, digit, angle=None):
+        if angle is None:
+            digit, angle = 0, digit
+        c, s = math.cos(angle / 2), math.sin(angle / 2)
+        super().__init__(reg, digit, [complex(c, 0), complex(0, -s), complex(0, -s), complex(c, 0)])
+
+
+class RY_Bool(Rot_Bool):
+    """RY(theta) (basic_gates.cpp:571-588)."""
+
+    def __init__(self, reg, digit, angle=None):
+        if angle is None:
+            digit, angle = 0, digit
+        c, s = math.cos(angle / 2), math.sin(angle / 2)
+        super().__init__(reg, digit, [complex(c, 0), complex(-s, 0), complex(s, 0), complex(c, 0)])
+
+
+class CondRot_Rational_Bool(BaseOperator):
+    """Rotate the 1-bit `out` by 2*pi*in/2^|in| (condrot.cpp:12-152)."""
+
+    def __init__(self, reg_in, reg_out):
+        super().__init__()
+        self.register_in, self.register_out = _R(reg_in), _R(reg_out)
+        if (System.type_of(self.register_in) != StateStorageType.Rational
+                or System.type_of(self.register_out) != StateStorageType.Boolean):
+            raise ValueError("CondRot_Rational_Bool: input must be Rational and output Boolean")
+
+    def spec(self, dag=False):
+        return ("condrot", self.register_in, self.register_out, dag)
+
+
+CondRot_Fixed_Bool = CondRot_Rational_Bool
+
+
+class ClearZero(SelfAdjointOperator):
+    """Drop entries with |a|^2 < eps (system_operations.cpp:371-382)."""
+
+    def __init__(self, eps: float | None = None):
+        super().__init__()
+        self.eps = eps
+
+    def spec(self, dag=False):
+        from .core import get_clearzero_default_eps
+        return ("clear_zero", get_clearzero_default_eps() if self.eps is None else float(self.eps))
+
+
+class Normalize(SelfAdjointOperator):
+    """a *= 1/sqrt(sum |a|^2) (dark_magic.cpp:11-32)."""
+
+    def spec(self, dag=False):
+        return ("normalize",)
+
+
+# ---------------------------------------------------------------------- register surgery
+class AddRegister:
+    """New zero-valued register (system_operations.cpp:252-272); returns its id."""
+
+    def __init__(self, name: str, type_: StateStorageType, size: int):
+        if size > 64:
+            raise ValueError("register size > 64")
+        self.name, self.type, self.size = name, type_, int(size)
+
+    def __call__(self, state: SparseState) -> int:
+        return System.add_register_synchronous(self.name, self.type, self.size, state)
+
+
+class RemoveRegister:
+    """Zero the register in every entry and deactivate it (system_operations.cpp:310-330)."""
+
+    def __init__(self, reg):
+        self.register_id = _R(reg)
+
+    def __call__(self, state: SparseState) -> None:
+        call("sq_remove_register_sync", state._h, self.register_id)
+
+
+class SplitRegister:
+    """Low `second_size` bits of `first` become register `second_name`
+    (system_operations.cpp:124-158); returns the new id."""
+
+    def __init__(self, first, second_name: str, second_size: int):
+        self.first, self.second_name, self.second_size = first, second_name, int(second_size)
+
+    def __call__(self, state: SparseState) -> int:
+        rid = c_uint32()
+        call("sq_split_register", state._h, _R(self.first), self.second_size, byref(rid))
+        System._set_name(rid.value, self.second_name)
+        return rid.value
+
+
+class CombineRegister:
+    """first = first << |second| | second; second removed (system_operations.cpp:170-203)."""
+
+    def __init__(self, first, second):
+        self.first, self.second = first, second
+
+    def __call__(self, state: SparseState) -> int:
+        f = _R(self.first)
+        call("sq_combine_register", state._h, f, _R(self.second))
+        return f
+
+
+def add_systems(current: SparseState, new_state: SparseState, coef: float = 1.0) -> None:
+    """current += coef * new_state, equal keys merged, |a|^2 < epsilon dropped
+    (system_operations.h:157-175)."""
+    call("sq_add_systems", current._h, new_state._h, float(coef))
+
+
+def synchronize() -> None:
+    call("sq_synchronize")
