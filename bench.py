@@ -1,0 +1,468 @@
+"""bench.py — sparse-entry updates/s of the register circuit at scale on one GB300.
+
+Workload ("register circuit at scale", a 20-bit, b 32-bit, c 32-bit plus a
+32-bit scratch t): from |0>, L = 10 layers of
+    Hadamard_Int(a, h=12)                         # split: 4096 -> 2^24 entries (merge on layers >= 2)
+    QRAMLoad(T, a, b)                             # b ^= T[a], T = 2^20 seeded uniform uint32 words
+    Mul_UInt_UInt(a, b, t); Add_UInt_UInt_InPlace(t, c); Mul_UInt_UInt(a, b, t)   # c += a*b mod 2^32
+    Phase_Bool(c, 0, theta_l)                     # theta_l seeded uniform in [0, 2*pi)
+    Hadamard_Int(a, h=12)                         # split: fan-out to the 2^24-entry peak
+The five elementwise operators of a layer run as one fused launch. One step
+is the whole circuit from |0>. `updates` = sum over operator applications of
+max(N_in, N_out) (elementwise operators count N each).
+
+Arms: default = the GB300 engine; `--impl reference` = the CPU restatement of
+the reference's operator path (the reference itself does not build here)
+on the host cores, one steady-state layer per step in P concurrent processes.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "sparse-entry updates/s (register circuit at scale)"
+UNIT = "updates/s"
+A_BITS, B_BITS, C_BITS, T_BITS = 20, 32, 32, 32
+TABLE_BITS = 20
+SEED = 20261203
+
+
+def workload_config(h: int, layers: int) -> dict:
+    return {
+        "workload": (f"register circuit at scale: a{A_BITS}/b{B_BITS}/c{C_BITS} (+t{T_BITS} scratch), {layers} layers of "
+                     f"[Hadamard_Int(a,{h}); b^=QRAM[a] (2^{TABLE_BITS}-word uint32 table); c+=a*b mod 2^32; "
+                     f"phase exp(i*theta_l) on c bit 0; Hadamard_Int(a,{h})], peak 2^{2 * h} entries, complex128"),
+        "hadamard_bits": h,
+        "layers": layers,
+        "peak_entries": 1 << (2 * h),
+        "l2_policy": "inputs larger than L2: the 2^24-entry state is 0.54 GB (L2 129 MB), no flush needed",
+        "seed": SEED,
+    }
+
+
+def circuit_inputs(h: int, layers: int):
+    import numpy as np
+    rng = np.random.default_rng(SEED)
+    table = rng.integers(0, 1 << 32, 1 << TABLE_BITS, dtype=np.uint64)
+    thetas = rng.uniform(0.0, 2 * math.pi, layers)
+    return table, thetas
+
+
+# ---------------------------------------------------------------------- GB300 arm
+class Circuit:
+    def __init__(self, ps, h: int, layers: int, table, thetas):
+        self.ps, self.h, self.layers = ps, h, layers
+        ps.System.clear()
+        for name, w in (("a", A_BITS), ("b", B_BITS), ("c", C_BITS), ("t", T_BITS)):
+            ps.System.add_register(name, ps.UnsignedInteger, w)
+        self.table = table
+        self.qram = ps.QRAMCircuit_qutrit(TABLE_BITS, 32, table)
+        self.H = ps.Hadamard_Int("a", h)
+        self.mid = [ps.Fused([ps.QRAMLoad(self.qram, "a", "b"), ps.Mul_UInt_UInt("a", "b", "t"),
+                              ps.Add_UInt_UInt_InPlace("t", "c"), ps.Mul_UInt_UInt("a", "b", "t"),
+                              ps.Phase_Bool("c", 0, float(th))]) for th in thetas]
+
+    def run(self, st, count=False, qram=None, reset=True):
+        """One step from |0>. Returns the update count when count=True."""
+        ps = self.ps
+        if reset:
+            st.reset()
+        upd = 0
+        mids = self.mid if qram is None else [self._mid_with(qram, m) for m in self.mid]
+        for layer in range(self.layers):
+            n0 = st.size() if count else 0
+            self.H(st)
+            n1 = st.size() if count else 0
+            mids[layer](st)
+            self.H(st)
+            if count:
+                n2 = st.size()
+                upd += max(n0, n1) + 5 * n1 + max(n1, n2)
+        return upd
+
+    def _mid_with(self, qram, m):
+        ps = self.ps
+        ops = list(m.ops)
+        ops[0] = ps.QRAMLoad(qram, "a", "b")
+        return ps.Fused(ops)
+
+
+def sample_clocks_start(path: Path):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+    try:
+        f = open(path, "w")
+        p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "100"],
+                             stdout=f, stderr=subprocess.DEVNULL)
+        return p, f
+    except Exception:
+        return None, None
+
+
+def sample_clocks_stop(p, f, path: Path, device: int):
+    if p is None:
+        return None
+    p.terminate()
+    try:
+        p.wait(timeout=5)
+    except Exception:
+        p.kill()
+    f.close()
+    sm, mx, reasons = [], 0.0, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in path.read_text().splitlines():
+        parts = [x.strip() for x in line.split(",")]
+        if len(parts) < 9 or not parts[0].isdigit() or int(parts[0]) != device:
+            continue
+        try:
+            sm.append(float(parts[1]))
+            mx = max(mx, float(parts[2]))
+        except ValueError:
+            continue
+        for nm, v in zip(names, parts[5:9]):
+            if v.lower() == "active":
+                reasons.add(nm)
+    if not sm:
+        return None
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        return d.get(kernel)
+    except Exception:
+        return None
+
+
+def cpu_baseline_sample(h: int, table, thetas, layers_sample: int = 2):
+    """The CPU restatement of the reference path, single thread, on the first
+    `layers_sample` layers of the same full-size circuit."""
+    from oracle import oracle as O
+    from sparqsim_gb300._native import OP, SqInstr
+    import ctypes
+    O.clear()
+    a, b, c, t = (O.add_register(1, w) for w in (A_BITS, B_BITS, C_BITS, T_BITS))
+    q = O.Qram(TABLE_BITS, 32, table)
+    st = O.OracleState()
+    from sparqsim_gb300.core import SqCond
+    nocond = SqCond()
+
+    def ins(op, regs, imm=(), cc=()):
+        x = SqInstr()
+        x.op = OP[op]
+        for i, r in enumerate(regs):
+            x.reg[i] = r
+        for i, v in enumerate(imm):
+            x.imm[i] = v
+        for i, v in enumerate(cc):
+            x.c[i] = v
+        return x
+
+    t0 = time.perf_counter()
+    upd = 0
+    for layer in range(layers_sample):
+        th = float(thetas[layer])
+        n0 = st.size()
+        O._chk(O.lib().sqo_hadamard_int(st.h, a, h, ctypes.byref(nocond)))
+        n1 = st.size()
+        qi = ins("QRAM_LOAD", [a, b])
+        qi.qram = q.h
+        prog = [qi, ins("MUL_UINT_UINT", [a, b, t]), ins("ADD_UINT_UINT_INPLACE", [t, c]),
+                ins("MUL_UINT_UINT", [a, b, t]), ins("PHASE_BOOL", [c], [0], [math.cos(th), math.sin(th)])]
+        arr = (SqInstr * len(prog))(*prog)
+        O._chk(O.lib().sqo_apply(st.h, arr, len(prog)))
+        O._chk(O.lib().sqo_hadamard_int(st.h, a, h, ctypes.byref(nocond)))
+        n2 = st.size()
+        upd += max(n0, n1) + 5 * n1 + max(n1, n2)
+    dt = time.perf_counter() - t0
+    O.clear()
+    return upd, dt
+
+
+def run_gb300(args, rank: int, world: int, local_rank: int):
+    import numpy as np
+    import torch
+
+    import sparqsim_gb300 as ps
+    from sparqsim_gb300 import _native
+
+    torch.cuda.set_device(local_rank)
+    _native.call("sq_init", local_rank)
+    h, L = args.hadamard_bits, args.layers
+    table, thetas = circuit_inputs(h, L)
+    circ = Circuit(ps, h, L, table, thetas)
+    st = ps.SparseState(capacity=1 << (2 * h))
+    sp = ctypes_void_p()
+    _native.call("sq_get_stream", __import__("ctypes").byref(sp))
+    ext = torch.cuda.ExternalStream(sp.value)
+
+    # untimed: count updates (deterministic), warm up
+    updates = circ.run(st, count=True)
+    final_n = st.size()
+    for _ in range(max(args.warmup - 1, 0)):
+        circ.run(st)
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+    clocks_path = ROOT / "gpurun_out" / f"clocks_rank{rank}.csv"
+    clocks_path.parent.mkdir(exist_ok=True)
+    cp, cf = sample_clocks_start(clocks_path) if rank == 0 else (None, None)
+    launches0 = ps.launch_count()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(ext)
+    for _ in range(args.steps):
+        circ.run(st)
+    end.record(ext)
+    end.synchronize()
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end)
+    launches = ps.launch_count() - launches0
+    clocks = sample_clocks_stop(cp, cf, clocks_path, local_rank) if rank == 0 else None
+
+    t_max = ms
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+        dist.barrier()
+    ms_per_step = t_max / args.steps
+    value = world * updates * args.steps / (t_max / 1e3)
+
+    # end to end through the public API: host inputs in, final state out
+    k = ps.System.key_words()
+    host_keys = torch.empty(final_n * k, dtype=torch.int64, pin_memory=True)
+    host_amps = torch.empty(final_n * 2, dtype=torch.float64, pin_memory=True)
+    init_keys = torch.zeros(k, dtype=torch.int64, pin_memory=True)
+    init_amp = torch.tensor([1.0, 0.0], dtype=torch.float64).pin_memory()
+    host_table = torch.from_numpy(table.view(np.int64)).pin_memory()
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        q = ps.QRAMCircuit_qutrit.__new__(ps.QRAMCircuit_qutrit)
+        q.address_size, q.data_size, q.memory = TABLE_BITS, 32, table
+        hq = __import__("ctypes").c_void_p()
+        _native.call("sq_qram_create", TABLE_BITS, 32, host_table.data_ptr(), host_table.numel(),
+                     __import__("ctypes").byref(hq))
+        q._h = hq
+        _native.call("sq_state_upload_packed", st._h, 1, init_keys.data_ptr(), init_amp.data_ptr())
+        circ.run(st, qram=q, reset=False)
+        _native.call("sq_state_download_packed", st._h, host_keys.data_ptr(), host_amps.data_ptr())
+        del q
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = k * 8 + 16 + (1 << TABLE_BITS) * 4
+    d2h = final_n * (8 * k + 16)
+    e2e_value = world * updates / e2e_s
+
+    # profiled step: per-kernel device time with events on the library stream
+    _native.profile_reset()
+    _native.profile_enable(True)
+    circ.run(st)
+    _native.profile_enable(False)
+    prof = _native.profile_read()
+    total_ms = sum(v[1] for v in prof.values())
+    dom = max(prof, key=lambda k_: prof[k_][1])
+    n_l, d_ms, d_bytes = prof[dom]
+    peak, peak_kind = measured_peak_hbm()
+    achieved = d_bytes / (d_ms / 1e3) / 1e9 if d_ms > 0 else 0.0
+    traffic = ncu_traffic(dom)
+    kernels = {name: {"launches": v[0], "ms": round(v[1], 4), "share": round(v[1] / total_ms, 4) if total_ms else 0,
+                      "alg_GBps": round(v[2] / (v[1] / 1e3) / 1e9, 1) if v[1] > 0 else 0}
+               for name, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (complex128 amplitudes), u64 keys", "data": "synthetic (seeded table and angles)",
+        "config": dict(workload_config(h, L), updates_per_step=updates, final_entries=final_n,
+                       parallelism="replicas" if world > 1 else "single GPU"),
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "note": "public API: QRAM table and initial state uploaded from pinned host memory, final packed "
+                        "state downloaded, each step; wall clock"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "traffic": traffic, "alg_bytes_per_launch": d_bytes / max(n_l, 1),
+                     "avg_launch_ms": d_ms / max(n_l, 1)},
+        "kernels": kernels,
+    }
+    if clocks:
+        result["clocks"] = clocks
+    return result, (table, thetas)
+
+
+def ctypes_void_p():
+    import ctypes
+    return ctypes.c_void_p()
+
+
+# ---------------------------------------------------------------------- reference arm
+def _ref_worker(h, steps, warmup, barrier, out_q, idx):
+    try:
+        table, thetas = circuit_inputs(h, 10)
+        from oracle import oracle as O  # noqa: F401  (CPU restatement, this process only)
+        # setup: layer 1 of the circuit (|0> -> 2^{2h} entries), untimed
+        res = _ref_layers(h, table, thetas, 1 + warmup, steps, barrier)
+        out_q.put((idx, res))
+    except Exception as e:  # report, do not hang the parent
+        out_q.put((idx, ("error", repr(e))))
+
+
+def _ref_layers(h, table, thetas, untimed_layers, timed_layers, barrier):
+    import ctypes
+    from oracle import oracle as O
+    from sparqsim_gb300._native import OP, SqInstr
+    from sparqsim_gb300.core import SqCond
+    O.clear()
+    a, b, c, t = (O.add_register(1, w) for w in (A_BITS, B_BITS, C_BITS, T_BITS))
+    q = O.Qram(TABLE_BITS, 32, table)
+    st = O.OracleState()
+    nocond = SqCond()
+
+    def ins(op, regs, imm=(), cc=()):
+        x = SqInstr()
+        x.op = OP[op]
+        for i, r in enumerate(regs):
+            x.reg[i] = r
+        for i, v in enumerate(imm):
+            x.imm[i] = v
+        for i, v in enumerate(cc):
+            x.c[i] = v
+        return x
+
+    def layer(th):
+        n0 = st.size()
+        O._chk(O.lib().sqo_hadamard_int(st.h, a, h, ctypes.byref(nocond)))
+        n1 = st.size()
+        qi = ins("QRAM_LOAD", [a, b])
+        qi.qram = q.h
+        prog = [qi, ins("MUL_UINT_UINT", [a, b, t]), ins("ADD_UINT_UINT_INPLACE", [t, c]),
+                ins("MUL_UINT_UINT", [a, b, t]), ins("PHASE_BOOL", [c], [0], [math.cos(th), math.sin(th)])]
+        arr = (SqInstr * len(prog))(*prog)
+        O._chk(O.lib().sqo_apply(st.h, arr, len(prog)))
+        O._chk(O.lib().sqo_hadamard_int(st.h, a, h, ctypes.byref(nocond)))
+        n2 = st.size()
+        return max(n0, n1) + 5 * n1 + max(n1, n2)
+
+    for i in range(untimed_layers):
+        layer(float(thetas[i % len(thetas)]))
+    barrier.wait()
+    t0 = time.perf_counter()
+    upd = 0
+    for i in range(timed_layers):
+        upd += layer(float(thetas[(untimed_layers + i) % len(thetas)]))
+    return upd, time.perf_counter() - t0
+
+
+def run_reference(args):
+    h = args.hadamard_bits
+    ncpu = os.cpu_count() or 1
+    try:
+        avail_gb = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE") / 2**30
+    except Exception:
+        avail_gb = 16.0
+    per_proc_gb = 4.0 * (1 << (2 * h)) / (1 << 24)
+    P = max(1, min(ncpu, int(avail_gb * 0.6 / max(per_proc_gb, 0.1))))
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(P + 1)
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_ref_worker, args=(h, args.steps, args.warmup, barrier, q, i)) for i in range(P)]
+    for p in procs:
+        p.start()
+    barrier.wait()
+    t0 = time.perf_counter()
+    results = [q.get() for _ in procs]
+    wall = time.perf_counter() - t0
+    for p in procs:
+        p.join()
+    errs = [r for _, r in results if isinstance(r, tuple) and r and r[0] == "error"]
+    if errs:
+        print(json.dumps({"impl": "reference", "unavailable": f"CPU restatement failed: {errs[0][1]}"}))
+        return
+    upd = sum(r[0] for _, r in results)
+    value = upd / wall
+    sample = (f"{P} concurrent single-thread processes, each {args.steps} steady-state layers (2^{2 * h} -> "
+              f"2^{h} -> 2^{2 * h} entries) of the full-size circuit after {1 + args.warmup} untimed layers")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (complex128 amplitudes), u64 registers", "data": "synthetic",
+        "config": workload_config(h, 10),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": P, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# ---------------------------------------------------------------------- main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--hadamard-bits", type=int, default=12)
+    ap.add_argument("--layers", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    result, (table, thetas) = run_gb300(args, rank, world, local_rank)
+    if rank == 0:
+        if not args.no_cpu_baseline and world == 1:
+            upd, dt = cpu_baseline_sample(args.hadamard_bits, table, thetas)
+            result["cpu_baseline"] = {"value": upd / dt, "unit": UNIT, "cores": 1, "kind": "port",
+                                      "sample": f"first 2 of {args.layers} layers of the same full-size circuit, "
+                                                f"{upd} updates in {dt:.1f} s, one thread"}
+        print(json.dumps(result))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

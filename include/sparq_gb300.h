@@ -155,6 +155,15 @@ int sq_synchronize(void);
 int sq_launch_count(uint64_t* count);
 /* The library's CUDA stream (cudaStream_t), for callers that order their own work after it. */
 int sq_get_stream(void** stream);
+/* Per-kernel device timing (no counterpart in the reference, which times
+ * whole operators with std::chrono): while enabled, every launch is bracketed
+ * by CUDA events on the library stream. sq_profile_read copies up to `max`
+ * kernels: NUL-separated names into names_buf, launch counts, total ms and the
+ * total algorithmic (compulsory) HBM bytes of those launches. */
+int sq_profile_enable(int on);
+int sq_profile_reset(void);
+int sq_profile_read(char* names_buf, size_t buf_len, uint64_t* counts, double* total_ms, double* total_bytes,
+                    uint32_t max, uint32_t* n_out);
 
 /* ------------------------------------------------------------------ */
 /* Register table — process-global, like System::name_register_map     */
@@ -190,6 +199,12 @@ int sq_state_copy(sq_state* dst, const sq_state* src);
  * reference System layout): regs[i * nregs + id], amps[2*i], amps[2*i+1]. */
 int sq_state_upload(sq_state* st, uint64_t n, const uint64_t* regs, uint32_t nregs, const double* amps);
 int sq_state_download(const sq_state* st, uint64_t* regs, uint32_t nregs, double* amps);
+/* Packed transfer in the engine's own layout: keys[w * n + i] for w < K
+ * (K from sq_system_key_words), amps[2*i], amps[2*i+1]. No per-register
+ * packing on the host, so these run at copy bandwidth (CuSparseState
+ * move_to_gpu / copy_to_cpu, cuda/basic_components.cu:49-106). */
+int sq_state_upload_packed(sq_state* st, uint64_t n, const uint64_t* keys, const double* amps);
+int sq_state_download_packed(const sq_state* st, uint64_t* keys, double* amps);
 /* Device pointers of the live arrays (valid until the next call that resizes). */
 int sq_state_device_arrays(sq_state* st, uint64_t** key_words, uint32_t* k, double** amps);
 
@@ -254,6 +269,13 @@ int sq_condrot_rational_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, in
 /* ------------------------------------------------------------------ */
 /* Prune / norm / merge / register surgery                              */
 /* ------------------------------------------------------------------ */
+/* How split/merge operators group entries: 0 = automatic (hash grouping for
+ * transforms on >= 4096 entries, sort otherwise; the add_systems merge always
+ * sorts), 1 = onesweep radix sort, 2 = hash table. Results are identical;
+ * only the entry order of the output differs. No counterpart in the reference
+ * (its CPU path sorts or uses std::map buckets, its GPU path sorts). */
+int sq_set_group_strategy(int strategy);
+int sq_get_group_strategy(int* strategy);
 /* clearzero_default_eps (system_operations.h:577), initially 1e-14. */
 int sq_set_clearzero_eps(double eps);
 int sq_get_clearzero_eps(double* eps);

@@ -80,6 +80,10 @@ _SIGS = [
     ("sq_synchronize", c_int, []),
     ("sq_launch_count", c_int, [POINTER(c_uint64)]),
     ("sq_get_stream", c_int, [POINTER(c_void_p)]),
+    ("sq_profile_enable", c_int, [c_int]),
+    ("sq_profile_reset", c_int, []),
+    ("sq_profile_read", c_int, [c_void_p, ctypes.c_size_t, POINTER(c_uint64), POINTER(c_double),
+                                POINTER(c_double), c_uint32, POINTER(c_uint32)]),
     ("sq_system_clear", c_int, []),
     ("sq_system_add_register", c_int, [c_uint32, c_uint32, POINTER(c_uint32)]),
     ("sq_system_remove_register", c_int, [c_uint32]),
@@ -96,6 +100,8 @@ _SIGS = [
     ("sq_state_copy", c_int, [c_void_p, c_void_p]),
     ("sq_state_upload", c_int, [c_void_p, c_uint64, c_void_p, c_uint32, c_void_p]),
     ("sq_state_download", c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
+    ("sq_state_upload_packed", c_int, [c_void_p, c_uint64, c_void_p, c_void_p]),
+    ("sq_state_download_packed", c_int, [c_void_p, c_void_p, c_void_p]),
     ("sq_state_device_arrays", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_uint32), POINTER(c_void_p)]),
     ("sq_qram_create", c_int, [c_uint32, c_uint32, c_void_p, c_uint64, POINTER(c_void_p)]),
     ("sq_qram_destroy", c_int, [c_void_p]),
@@ -124,6 +130,8 @@ _SIGS = [
     ("sq_hadamard_bool", c_int, [c_void_p, c_uint32, POINTER(SqCond)]),
     ("sq_rot_bool", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), POINTER(SqCond), c_int]),
     ("sq_condrot_rational_bool", c_int, [c_void_p, c_uint32, c_uint32, c_int]),
+    ("sq_set_group_strategy", c_int, [c_int]),
+    ("sq_get_group_strategy", c_int, [POINTER(c_int)]),
     ("sq_set_clearzero_eps", c_int, [c_double]),
     ("sq_get_clearzero_eps", c_int, [POINTER(c_double)]),
     ("sq_clear_zero", c_int, [c_void_p, c_double]),
@@ -168,6 +176,27 @@ def check(rc: int) -> None:
 
 def call(name: str, *args) -> None:
     check(getattr(lib(), name)(*args))
+
+
+def profile_enable(on: bool) -> None:
+    call("sq_profile_enable", 1 if on else 0)
+
+
+def profile_reset() -> None:
+    call("sq_profile_reset")
+
+
+def profile_read(max_kernels: int = 64) -> dict:
+    """{kernel name: (launches, total device ms, total algorithmic bytes)} from
+    the engine's event timers."""
+    buf = ctypes.create_string_buffer(64 * max_kernels)
+    counts = (c_uint64 * max_kernels)()
+    ms = (c_double * max_kernels)()
+    nbytes = (c_double * max_kernels)()
+    n = c_uint32()
+    call("sq_profile_read", buf, len(buf), counts, ms, nbytes, max_kernels, ctypes.byref(n))
+    names = buf.raw.split(b"\0")[: n.value]
+    return {nm.decode(): (counts[i], ms[i], nbytes[i]) for i, nm in enumerate(names)}
 
 
 def launch_count() -> int:

@@ -145,6 +145,19 @@ class System:
         return k.value
 
 
+def set_group_strategy(strategy: str) -> None:
+    """'auto', 'sort' (onesweep radix sort) or 'hash' (hash-table buckets):
+    how split/merge operators group entries. Results are identical."""
+    call("sq_set_group_strategy", {"auto": 0, "sort": 1, "hash": 2}[strategy])
+
+
+def get_group_strategy() -> str:
+    from ctypes import c_int
+    v = c_int()
+    call("sq_get_group_strategy", byref(v))
+    return ["auto", "sort", "hash"][v.value]
+
+
 def set_clearzero_default_eps(eps: float) -> None:
     """clearzero_default_eps (system_operations.h:577)."""
     call("sq_set_clearzero_eps", float(eps))

@@ -95,6 +95,39 @@ int sq_launch_count(uint64_t* count) {
     SQ_API_END
 }
 
+int sq_profile_enable(int on) {
+    SQ_API_BEGIN
+    prof_enable(on != 0);
+    SQ_API_END
+}
+
+int sq_profile_reset(void) {
+    SQ_API_BEGIN
+    prof_reset();
+    SQ_API_END
+}
+
+int sq_profile_read(char* names_buf, size_t buf_len, uint64_t* counts, double* total_ms, double* total_bytes,
+                    uint32_t max, uint32_t* n_out) {
+    SQ_API_BEGIN
+    prof_collect();
+    const size_t n = std::min<size_t>(prof_count(), max);
+    size_t off = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const char* nm = prof_name(i);
+        const size_t l = strlen(nm) + 1;
+        if (names_buf && off + l <= buf_len) {
+            memcpy(names_buf + off, nm, l);
+            off += l;
+        }
+        if (counts) counts[i] = prof_launches(i);
+        if (total_ms) total_ms[i] = prof_ms(i);
+        if (total_bytes) total_bytes[i] = prof_bytes(i);
+    }
+    if (n_out) *n_out = (uint32_t)n;
+    SQ_API_END
+}
+
 int sq_get_stream(void** s) {
     SQ_API_BEGIN
     need(s != nullptr, "null pointer");
@@ -295,6 +328,37 @@ int sq_state_download(const sq_state* st, uint64_t* regs, uint32_t nregs, double
                 regs[i * nregs + id] = v;
             }
     }
+    SQ_API_END
+}
+
+int sq_state_upload_packed(sq_state* st, uint64_t n, const uint64_t* keys, const double* amps) {
+    SQ_API_BEGIN
+    State& s = S(st);
+    need(n == 0 || (keys != nullptr && amps != nullptr), "null pointer");
+    const uint32_t k = regtable().k;
+    ensure_buffers(s.live, std::max<uint64_t>(n, 1), k, 0);
+    for (uint32_t w = 0; w < k; ++w)
+        SQ_CUDA(cudaMemcpyAsync(s.live.keys[w], keys + (size_t)w * n, n * 8, cudaMemcpyHostToDevice, stream()));
+    SQ_CUDA(cudaMemcpyAsync(s.live.amp, amps, n * 16, cudaMemcpyHostToDevice, stream()));
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    s.n = n;
+    SQ_API_END
+}
+
+int sq_state_download_packed(const sq_state* st, uint64_t* keys, double* amps) {
+    SQ_API_BEGIN
+    const State& s = S(st);
+    const uint32_t k = regtable().k;
+    const uint64_t n = s.n;
+    for (uint32_t w = 0; w < k; ++w) {
+        if (!keys) break;
+        if (w < s.live.kalloc)
+            SQ_CUDA(cudaMemcpyAsync(keys + (size_t)w * n, s.live.keys[w], n * 8, cudaMemcpyDeviceToHost, stream()));
+        else
+            memset(keys + (size_t)w * n, 0, n * 8);
+    }
+    if (amps) SQ_CUDA(cudaMemcpyAsync(amps, s.live.amp, n * 16, cudaMemcpyDeviceToHost, stream()));
+    SQ_CUDA(cudaStreamSynchronize(stream()));
     SQ_API_END
 }
 
@@ -588,6 +652,18 @@ int sq_condrot_rational_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, in
 }
 
 // ------------------------------------------------------------------ prune / norm / merge
+int sq_set_group_strategy(int strategy) {
+    SQ_API_BEGIN
+    set_group_strategy(strategy);
+    SQ_API_END
+}
+int sq_get_group_strategy(int* strategy) {
+    SQ_API_BEGIN
+    need(strategy != nullptr, "null pointer");
+    *strategy = get_group_strategy();
+    SQ_API_END
+}
+
 int sq_set_clearzero_eps(double eps) {
     SQ_API_BEGIN
     need(eps >= 0.0, "negative eps");

@@ -103,9 +103,10 @@ static void launch_cz(const Buffers& in, Buffers& out, uint64_t n, double eps, L
         ik.w[w] = in.keys[w];
         okp.w[w] = out.keys[w];
     }
+    prof_begin("clearzero");
     clearzero_kernel<K><<<(unsigned)nt, kCzBlock, 0, stream()>>>(ik, in.amp, okp, out.amp, n, eps, lb, nt,
                                                                device_error_word());
-    count_launch();
+    prof_end((double)n * 16);  // every amplitude read; survivors added below
     SQ_CUDA(cudaGetLastError());
 }
 
@@ -138,6 +139,7 @@ uint64_t compact_nonzero(const Buffers& in, Buffers& out, uint64_t n, double eps
     unsigned long long total = 0;
     SQ_CUDA(cudaMemcpyAsync(&total, lb.total, 8, cudaMemcpyDeviceToHost, stream()));
     check_device_error();  // synchronizes
+    prof_add_bytes_last((double)total * (16.0 * k + 16));  // survivors: keys read + keys and amp written
     return total;
 }
 
@@ -190,9 +192,12 @@ double norm_sq(const State& s) {
     if (s.n == 0) return 0.0;
     const int g = num_sms() * 4;
     double* part = (double*)ws().get(WS_REDUCE, (size_t)(g + 1) * 8);
+    prof_begin("norm_partial");
     norm_partial_kernel<<<g, kRedBlock, 0, stream()>>>(s.live.amp, s.n, part);
+    prof_end((double)s.n * 16);
+    prof_begin("norm_final");
     norm_final_kernel<<<1, kRedBlock, 0, stream()>>>(part, g, part + g);
-    count_launch(2);
+    prof_end((double)g * 8);
     SQ_CUDA(cudaGetLastError());
     double r = 0;
     SQ_CUDA(cudaMemcpyAsync(&r, part + g, 8, cudaMemcpyDeviceToHost, stream()));
@@ -210,8 +215,9 @@ __global__ void scale_kernel(double2* __restrict__ a, uint64_t n, double k) {
 
 void scale_amp(State& s, double k) {
     if (s.n == 0) return;
+    prof_begin("scale");
     scale_kernel<<<grid_for(s.n, 256), 256, 0, stream()>>>(s.live.amp, s.n, k);
-    count_launch();
+    prof_end((double)s.n * 32);
     SQ_CUDA(cudaGetLastError());
 }
 

@@ -9,6 +9,7 @@
 // therefore cost one HBM pass instead of one pass each, and the reference's
 // partition-by-condition pass (cuda/system_operations.cu:17-66) disappears
 // because conditions are evaluated per entry in registers.
+#include <algorithm>
 #include <cstring>
 
 #include "sq_internal.cuh"
@@ -272,27 +273,37 @@ __global__ void __launch_bounds__(256) program_kernel(const __grid_constant__ Pr
 }
 
 template <int K, int MAXI>
-static void launch_program(const ProgramArgs<MAXI>& args, State& s) {
+static void launch_program(const ProgramArgs<MAXI>& args, State& s, double table_bytes) {
     KeyPtrs kp;
     for (int w = 0; w < SQ_KMAX; ++w) kp.w[w] = s.live.keys[w];
     const int block = 256;
     unsigned grid = grid_for(s.n, block, 8);
+    prof_begin("elementwise_program");
     program_kernel<K, MAXI><<<grid, block, 0, stream()>>>(args, kp, s.live.amp, s.n);
-    count_launch();
+    // compulsory traffic: words read + words written + amplitude in/out + table words touched
+    const double per = 8.0 * __builtin_popcount(args.read_words) + 8.0 * __builtin_popcount(args.write_words) +
+                       16.0 * (args.amp_mode & 1u) + 16.0 * ((args.amp_mode >> 1) & 1u);
+    prof_end((double)s.n * per + table_bytes);
     SQ_CUDA(cudaGetLastError());
 }
 
 template <int MAXI>
 static void dispatch_k(const ProgramArgs<MAXI>& args, State& s, uint32_t k) {
+    double tb = 0.0;
+    for (uint32_t i = 0; i < args.n; ++i)
+        if (args.ins[i].op == SQ_OP_QRAM_LOAD) {
+            const double words = (double)(1ull << args.ins[i].addr_bits);
+            tb += std::min((double)s.n, words) * args.ins[i].elem_bytes;
+        }
     switch (k) {
-        case 1: launch_program<1, MAXI>(args, s); break;
-        case 2: launch_program<2, MAXI>(args, s); break;
-        case 3: launch_program<3, MAXI>(args, s); break;
-        case 4: launch_program<4, MAXI>(args, s); break;
-        case 5: launch_program<5, MAXI>(args, s); break;
-        case 6: launch_program<6, MAXI>(args, s); break;
-        case 7: launch_program<7, MAXI>(args, s); break;
-        default: launch_program<8, MAXI>(args, s); break;
+        case 1: launch_program<1, MAXI>(args, s, tb); break;
+        case 2: launch_program<2, MAXI>(args, s, tb); break;
+        case 3: launch_program<3, MAXI>(args, s, tb); break;
+        case 4: launch_program<4, MAXI>(args, s, tb); break;
+        case 5: launch_program<5, MAXI>(args, s, tb); break;
+        case 6: launch_program<6, MAXI>(args, s, tb); break;
+        case 7: launch_program<7, MAXI>(args, s, tb); break;
+        default: launch_program<8, MAXI>(args, s, tb); break;
     }
 }
 
@@ -492,8 +503,9 @@ void zero_field(State& s, Field f) {
     sync_words(s);
     if (s.n == 0 || f.width == 0) return;
     const uint64_t keep = ~(wmask(f.width) << f.shift);
+    prof_begin("zero_field");
     zero_field_kernel<1><<<grid_for(s.n, 256), 256, 0, stream()>>>(s.live.keys[f.word], keep, s.n);
-    count_launch();
+    prof_end((double)s.n * 16);
     SQ_CUDA(cudaGetLastError());
 }
 
@@ -522,6 +534,7 @@ void move_field(State& s, Field first, Field second, Field dst) {
     KeyPtrs kp;
     for (int w = 0; w < SQ_KMAX; ++w) kp.w[w] = s.live.keys[w];
     unsigned g = grid_for(s.n, 256);
+    prof_begin("move_field");
     switch (regtable().k) {
         case 1: move_field_kernel<1><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
         case 2: move_field_kernel<2><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
@@ -532,7 +545,7 @@ void move_field(State& s, Field first, Field second, Field dst) {
         case 7: move_field_kernel<7><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
         default: move_field_kernel<8><<<g, 256, 0, stream()>>>(kp, first, second, dst, s.n); break;
     }
-    count_launch();
+    prof_end((double)s.n * 16.0 * regtable().k);
     SQ_CUDA(cudaGetLastError());
 }
 

@@ -297,7 +297,10 @@ struct EmitArgs {
     const double2* in_amp;
     KeyPtrs out_keys;
     double2* out_amp;
-    const unsigned* idx;       // sorted entry indices
+    const unsigned* idx;       // sort path: entry index of each member, grouped
+    const unsigned* btgt;      // hash path: target value of each member, grouped
+    const double2* bamp;       // hash path: amplitude of each member, grouped
+    const unsigned* ghead;     // hash path: one member's entry index per group (its key)
     const unsigned* seg;       // group starts, seg[G] = end
     uint64_t groups;
     unsigned* cnt;             // count pass output
@@ -331,24 +334,45 @@ __device__ __forceinline__ double as_rational(uint64_t v, unsigned w) {
     return 1.0 * v / (double)(1ull << w);
 }
 
+// Member `pos` of the grouped order: its target value and amplitude. The
+// sort path gathers them through the sorted index; the hash path reads the
+// bucket arrays, which hold them contiguously per group.
+template <bool BUCKET>
+__device__ __forceinline__ void member_at(const EmitArgs& a, unsigned pos, uint64_t& t, double2& amp) {
+    if (BUCKET) {
+        t = a.btgt[pos];
+        amp = a.bamp[pos];
+    } else {
+        const unsigned e = a.idx[pos];
+        t = (a.in_keys.w[a.target.word][e] >> a.target.shift) & wmask(a.target.width);
+        amp = a.in_amp[e];
+    }
+}
+template <bool BUCKET>
+__device__ __forceinline__ unsigned group_head(const EmitArgs& a, uint64_t g, unsigned s0) {
+    return BUCKET ? a.ghead[g] : a.idx[s0];
+}
+
 // Pair modes (1-bit target): one thread per group.
-template <int K, bool WRITE>
+template <int K, bool WRITE, bool BUCKET>
 __global__ void __launch_bounds__(256) emit_pair_kernel(const __grid_constant__ EmitArgs a) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < a.groups; g += stride) {
         const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
         const unsigned m = s1 - s0;
-        const unsigned e0 = a.idx[s0];
         uint64_t k0[K];
-        load_key<K>(a.in_keys, e0, k0);
-        const bool b0 = fget<K>(k0, a.target) & 1ull;
+        load_key<K>(a.in_keys, group_head<BUCKET>(a, g, s0), k0);
+        uint64_t t0;
+        double2 v0;
+        member_at<BUCKET>(a, s0, t0, v0);
+        const bool b0 = t0 & 1ull;
         double2 az = make_double2(0.0, 0.0), ao = make_double2(0.0, 0.0);
-        const double2 v0 = a.in_amp[e0];
         bool has_z = false, has_o = false;
         if (b0) { ao = v0; has_o = true; } else { az = v0; has_z = true; }
         if (m >= 2) {
-            const unsigned e1 = a.idx[s0 + 1];
-            const double2 v1 = a.in_amp[e1];
+            uint64_t t1;
+            double2 v1;
+            member_at<BUCKET>(a, s0 + 1, t1, v1);
             if (b0) { az = v1; has_z = true; } else { ao = v1; has_o = true; }
         }
         double2 rz, ro;
@@ -459,7 +483,7 @@ __device__ __forceinline__ unsigned worker_rank(bool f, unsigned* s_tmp, unsigne
     return pre + in_warp;
 }
 
-template <int K, int W, bool WRITE>
+template <int K, int W, bool WRITE, bool BUCKET>
 __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constant__ EmitArgs a) {
     extern __shared__ double2 s_slots[];
     __shared__ unsigned s_tmp[8];
@@ -475,14 +499,15 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
     for (uint64_t g = (uint64_t)blockIdx.x * workers_per_block + wid; g < a.groups; g += stride) {
         const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
         const unsigned m = s1 - s0;
-        const unsigned e0 = a.idx[s0];
         uint64_t gk[K];
-        load_key<K>(a.in_keys, e0, gk);
-        const uint64_t v0 = fget<K>(gk, tg);
+        load_key<K>(a.in_keys, group_head<BUCKET>(a, g, s0), gk);
         const bool sparse_full = a.mode == GM_HADAMARD_FULL && m <= (unsigned)(a.nbits - 1);
         if (a.mode == GM_HADAMARD_INT && m == 1) {
             // singleton: a * 2^{-n/2}, sign (-1)^{popcount(t & v)} (hadamard.cpp:27-42)
-            const double2 base = cscale(a.in_amp[e0], a.extra);
+            uint64_t v0;
+            double2 a0;
+            member_at<BUCKET>(a, s0, v0, a0);
+            const double2 base = cscale(a0, a.extra);
             const bool keep = keep_amp(base, a.eps);
             if (!WRITE) {
                 if (t == 0) a.cnt[g] = keep ? S : 0u;
@@ -504,11 +529,11 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
             // Hadamard_Int_Full sparse bucket (hadamard.cpp:267-304): direct
             // 2^n x m product, members summed in ascending target value.
             for (unsigned j = t; j < m; j += W) {
-                const unsigned e = a.idx[s0 + j];
-                uint64_t kk[K];
-                load_key<K>(a.in_keys, e, kk);
-                s_member_t[wid][j] = fget<K>(kk, tg);
-                s_member_a[wid][j] = a.in_amp[e];
+                uint64_t tj;
+                double2 aj;
+                member_at<BUCKET>(a, s0 + j, tj, aj);
+                s_member_t[wid][j] = tj;
+                s_member_a[wid][j] = aj;
             }
             worker_sync<W>();
             if (t == 0) {  // order members by target value (m <= 63)
@@ -541,10 +566,10 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
             for (unsigned c = t; c < S; c += W) slots[c] = make_double2(0.0, 0.0);
             worker_sync<W>();
             for (unsigned j = t; j < m; j += W) {
-                const unsigned e = a.idx[s0 + j];
-                uint64_t kk[K];
-                load_key<K>(a.in_keys, e, kk);
-                slots[fget<K>(kk, tg)] = a.in_amp[e];
+                uint64_t tj;
+                double2 aj;
+                member_at<BUCKET>(a, s0 + j, tj, aj);
+                slots[tj] = aj;
             }
             worker_sync<W>();
             for (int qn = 0; qn < a.nbits; ++qn) {
@@ -594,27 +619,215 @@ __global__ void passthrough_kernel(ConstKeyPtrs ik, const double2* __restrict__ 
     }
 }
 
-// ------------------------------------------------------------------ host pipeline
+// ------------------------------------------------------------------ hash grouping
+// Group by an open-addressing hash table keyed on the masked group key. A slot
+// holds 0 (empty), kSlotLocked (being claimed) or ((gid + 1) << 32 | head + 1)
+// where `head` is the first entry that claimed it; keys are compared against
+// the head entry's key words. Group ids are dense, in claim order. Every wait
+// on a locked slot is bounded.
+constexpr unsigned long long kSlotLocked = ~0ull;
+
+struct HashWs {
+    unsigned long long* slots;
+    unsigned long long cap_mask;
+    unsigned* gcount;     // [0]: groups, [1]: entries failing the conditions
+    unsigned* cnt;        // members per group
+    unsigned* head;       // one entry per group
+    unsigned* gid;        // group of each entry (~0u: fails the conditions)
+    unsigned* pass_list;  // entries failing the conditions
+};
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
+}
+
 template <int K>
-static void run_group(State& s, const GroupSpec& gs) {
+__global__ void __launch_bounds__(256) hash_insert_kernel(ConstKeyPtrs keys, const uint64_t* __restrict__ gmask,
+                                                          DCondSet cond, uint64_t n, HashWs h, unsigned* err) {
+    uint64_t gm[K];
+#pragma unroll
+    for (int w = 0; w < K; ++w) gm[w] = gmask[w];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint64_t k[K];
+#pragma unroll
+        for (int w = 0; w < K; ++w) k[w] = keys.w[w][i];
+        if (!cond_ok<K>(k, cond)) {
+            const unsigned p = atomicAdd(&h.gcount[1], 1u);
+            h.pass_list[p] = (unsigned)i;
+            h.gid[i] = ~0u;
+            continue;
+        }
+        unsigned long long hv = 0x9e3779b97f4a7c15ull;
+#pragma unroll
+        for (int w = 0; w < K; ++w) hv = mix64(hv ^ (k[w] & gm[w]) ^ (0x632be59bd9b4e019ull * (w + 1)));
+        unsigned long long slot = hv & h.cap_mask;
+        unsigned mygid = ~0u;
+        unsigned spins = 0;
+        for (unsigned long long probes = 0; probes <= h.cap_mask;) {
+            cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> ref(h.slots[slot]);
+            unsigned long long v = ref.load(cuda::memory_order_acquire);
+            if (v == 0ull) {
+                unsigned long long expected = 0ull;
+                if (ref.compare_exchange_strong(expected, kSlotLocked, cuda::memory_order_acq_rel)) {
+                    const unsigned g = atomicAdd(&h.gcount[0], 1u);
+                    h.head[g] = (unsigned)i;
+                    ref.store(((unsigned long long)(g + 1) << 32) | (unsigned long long)(i + 1),
+                              cuda::memory_order_release);
+                    mygid = g;
+                    break;
+                }
+                continue;  // lost the race: re-read this slot
+            }
+            if (v == kSlotLocked) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(err, 2u);
+                    break;
+                }
+                __nanosleep(20);
+                continue;
+            }
+            const unsigned hidx = (unsigned)(v & 0xffffffffull) - 1u;
+            bool same = true;
+#pragma unroll
+            for (int w = 0; w < K; ++w) same = same && (((keys.w[w][hidx] ^ k[w]) & gm[w]) == 0);
+            if (same) {
+                mygid = (unsigned)(v >> 32) - 1u;
+                break;
+            }
+            slot = (slot + 1) & h.cap_mask;
+            ++probes;
+        }
+        if (mygid == ~0u) {  // table exhausted or gave up waiting: reported, entry dropped
+            atomicOr(err, 2u);
+            h.gid[i] = ~0u;
+            continue;
+        }
+        h.gid[i] = mygid;
+        atomicAdd(&h.cnt[mygid], 1u);
+    }
+}
+
+// Partition the condition-passing entries by group: each entry's target value
+// and amplitude land in its group's range [seg[g], seg[g+1]); lanes of a warp
+// with the same group reserve consecutive slots with one atomic.
+__global__ void __launch_bounds__(256) bucket_kernel(const unsigned* __restrict__ gid, const uint64_t* __restrict__ tword,
+                                                     Field target, const double2* __restrict__ amp, uint64_t n,
+                                                     const unsigned* __restrict__ seg, unsigned* __restrict__ cnt,
+                                                     unsigned* __restrict__ btgt, double2* __restrict__ bamp) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t base0 = (uint64_t)blockIdx.x * blockDim.x;
+    for (uint64_t b = base0; b < n; b += stride) {  // warp-uniform trip count
+        const uint64_t i = b + threadIdx.x;
+        const unsigned g = i < n ? gid[i] : ~0u;
+        const bool valid = g != ~0u;
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        const unsigned peers = __match_any_sync(0xffffffffu, g) & vmask;
+        if (valid) {
+            const int leader = __ffs(peers) - 1;
+            const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+            unsigned old = 0;
+            if ((int)lane == leader) old = atomicSub(&cnt[g], (unsigned)__popc(peers));
+            old = __shfl_sync(peers, old, leader);
+            const unsigned pos = seg[g] + old - 1u - rank;
+            btgt[pos] = (unsigned)((tword[i] >> target.shift) & wmask(target.width));
+            bamp[pos] = amp[i];
+        }
+    }
+}
+
+// Exclusive scan of u32 counts into u32 group starts (seg[G] is written by the host).
+__global__ void __launch_bounds__(kSelBlock) scan_seg_kernel(const unsigned* __restrict__ cnt, unsigned* __restrict__ seg,
+                                                             uint64_t n, LbWs lb, long long ntiles, unsigned* err) {
+    __shared__ unsigned s_tile;
+    __shared__ unsigned long long s_w[kSelBlock / 32];
+    __shared__ unsigned long long s_prefix;
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(lb.counter, 1u);
+    __syncthreads();
+    const long long tile = s_tile;
+    const uint64_t base = (uint64_t)tile * kSelTile + (uint64_t)tid * kSelItems;
+    unsigned long long v[kSelItems];
+    unsigned long long sum = 0;
+#pragma unroll
+    for (int j = 0; j < kSelItems; ++j) {
+        const uint64_t i = base + j;
+        v[j] = i < n ? cnt[i] : 0ull;
+        sum += v[j];
+    }
+    unsigned long long inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (unsigned)o) inc += t;
+    }
+    if (lane == 31) s_w[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long wv = lane < kSelBlock / 32 ? s_w[lane] : 0ull;
+        unsigned long long wi = wv;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= (unsigned)o) wi += t;
+        }
+        const unsigned long long total = __shfl_sync(0xffffffffu, wi, kSelBlock / 32 - 1);
+        if (lane < kSelBlock / 32) s_w[lane] = wi - wv;
+        unsigned long long pre = lb_warp_exclusive(lb.status, tile, total, err);
+        if (lane == 0) {
+            s_prefix = pre;
+            if (tile == ntiles - 1) *lb.total = pre + total;
+        }
+    }
+    __syncthreads();
+    unsigned long long run = s_prefix + s_w[warp] + inc - sum;
+#pragma unroll
+    for (int j = 0; j < kSelItems; ++j) {
+        const uint64_t i = base + j;
+        if (i < n) seg[i] = (unsigned)run;
+        run += v[j];
+    }
+}
+
+static int g_strategy = 0;  // 0 auto, 1 sort, 2 hash
+void set_group_strategy(int s) {
+    if (s < 0 || s > 2) fail(SQ_ERR_INVALID, "group strategy must be 0 (auto), 1 (sort) or 2 (hash)");
+    g_strategy = s;
+}
+int get_group_strategy() { return g_strategy; }
+
+// ------------------------------------------------------------------ host pipeline
+struct Grouping {
+    uint64_t G = 0;      // groups among the condition-passing entries
+    uint64_t F = 0;      // entries failing the conditions
+    unsigned* seg = nullptr;
+    const unsigned* idx = nullptr;        // sort path
+    const unsigned* btgt = nullptr;       // hash path
+    const double2* bamp = nullptr;
+    const unsigned* ghead = nullptr;
+    const unsigned* pass = nullptr;       // failing entries (indices)
+    bool bucket = false;
+};
+
+template <int K>
+static Grouping group_by_sort(State& s, const GroupSpec& gs, const uint64_t* gmask, uint64_t* dg) {
     const uint64_t N = s.n;
     cudaStream_t st = stream();
     ConstKeyPtrs ik;
     for (int w = 0; w < SQ_KMAX; ++w) ik.w[w] = s.live.keys[w];
-
-    // group mask: active bits except the target bits
-    uint64_t gmask[SQ_KMAX];
-    regtable().active_mask(gmask);
-    if (gs.target.width) gmask[gs.target.word] &= ~(wmask(gs.target.width) << gs.target.shift);
-
-    uint64_t* dg = (uint64_t*)ws().get(WS_REDUCE, 64 * 8);
     unsigned long long* stats = (unsigned long long*)(dg + 16);
     std::vector<unsigned long long> init(2 * K + 1, 0);
     for (int w = 0; w < K; ++w) init[K + w] = ~0ull;
-    SQ_CUDA(cudaMemcpyAsync(dg, gmask, SQ_KMAX * 8, cudaMemcpyHostToDevice, st));
     SQ_CUDA(cudaMemcpyAsync(stats, init.data(), init.size() * 8, cudaMemcpyHostToDevice, st));
+    prof_begin("group_stats");
     stats_kernel<K><<<grid_for(N, 256, 4), 256, 0, st>>>(ik, N, gs.cond, dg, stats);
-    count_launch();
+    prof_end((double)N * 8 * K);
     SQ_CUDA(cudaGetLastError());
     std::vector<unsigned long long> res(2 * K + 1);
     SQ_CUDA(cudaMemcpyAsync(res.data(), stats, res.size() * 8, cudaMemcpyDeviceToHost, st));
@@ -645,8 +858,9 @@ static void run_group(State& s, const GroupSpec& gs) {
     int key_bytes = 0;
 
     if (total_bits == 0) {
+        prof_begin("iota");
         iota_kernel<<<grid_for(N, 256), 256, 0, st>>>(idx, N);
-        count_launch();
+        prof_end((double)N * 4);
     } else {
         // split the (V + flag) bits into chunks of <= 64, sort least significant chunk first
         struct Chunk {
@@ -695,8 +909,9 @@ static void run_group(State& s, const GroupSpec& gs) {
         const bool small = chunks.size() == 1 && chunks[0].bits <= 32;
         if (small) {
             uint32_t* kb[2] = {(uint32_t*)ws().get(WS_SORT_KEY0, N * 4 + 16), (uint32_t*)ws().get(WS_SORT_KEY1, N * 4 + 16)};
+            prof_begin("extract_sort_key");
             extract_kernel<K, uint32_t, false><<<grid_for(N, 256), 256, 0, st>>>(ik, N, chunks[0].ex, gs.cond, kb[0], vbuf[0]);
-            count_launch();
+            prof_end((double)N * (8 * K + 8));
             int r = radix_sort_pairs<uint32_t>(kb, vbuf, N, chunks[0].bits);
             idx = vbuf[r];
             sorted_keys = kb[r];
@@ -705,11 +920,12 @@ static void run_group(State& s, const GroupSpec& gs) {
             uint64_t* kb[2] = {(uint64_t*)ws().get(WS_SORT_KEY0, N * 8 + 16), (uint64_t*)ws().get(WS_SORT_KEY1, N * 8 + 16)};
             int cur = 0;  // buffer pair holding the current (keys, indices)
             for (size_t c = 0; c < chunks.size(); ++c) {
+                prof_begin("extract_sort_key");
                 if (c == 0)
                     extract_kernel<K, uint64_t, false><<<grid_for(N, 256), 256, 0, st>>>(ik, N, chunks[c].ex, gs.cond, kb[0], vbuf[0]);
                 else  // later chunks: key bits of the entry now at position i
                     extract_kernel<K, uint64_t, true><<<grid_for(N, 256), 256, 0, st>>>(ik, N, chunks[c].ex, gs.cond, kb[cur], vbuf[cur]);
-                count_launch();
+                prof_end((double)N * (8 * K + 12));
                 SQ_CUDA(cudaGetLastError());
                 uint64_t* kk[2] = {kb[cur], kb[cur ^ 1]};
                 unsigned* vv[2] = {vbuf[cur], vbuf[cur ^ 1]};
@@ -724,41 +940,137 @@ static void run_group(State& s, const GroupSpec& gs) {
     SQ_CUDA(cudaGetLastError());
 
     // group starts over the first P (condition-passing) entries
-    uint64_t G = 0;
+    Grouping out;
+    out.F = F;
+    out.idx = idx;
+    out.pass = idx + P;
     unsigned* seg = (unsigned*)ws().get(WS_SEG, (P + 2) * 4);
+    out.seg = seg;
     if (P > 0) {
-        if (total_bits == 0 || (V == 0)) {
-            unsigned h[2] = {0u, (unsigned)P};
-            SQ_CUDA(cudaMemcpyAsync(seg, h, 8, cudaMemcpyHostToDevice, st));
-            G = 1;
+        if (total_bits == 0 || V == 0) {
+            unsigned hh[2] = {0u, (unsigned)P};
+            SQ_CUDA(cudaMemcpyAsync(seg, hh, 8, cudaMemcpyHostToDevice, st));
+            out.G = 1;
         } else {
             const long long nt = (long long)((P + kSelTile - 1) / kSelTile);
             LbWs lb = make_lb(nt);
             const unsigned grid = (unsigned)nt;
+            prof_begin("group_heads");
             if (key_bytes == 4)
                 heads_kernel<K, uint32_t, true><<<grid, kSelBlock, 0, st>>>((const uint32_t*)sorted_keys, idx, ik, dg, P, seg, lb, nt, device_error_word());
             else if (key_bytes == 8)
                 heads_kernel<K, uint64_t, true><<<grid, kSelBlock, 0, st>>>((const uint64_t*)sorted_keys, idx, ik, dg, P, seg, lb, nt, device_error_word());
             else
                 heads_kernel<K, uint64_t, false><<<grid, kSelBlock, 0, st>>>(nullptr, idx, ik, dg, P, seg, lb, nt, device_error_word());
-            count_launch();
+            prof_end((double)P * (key_bytes ? key_bytes : 4 + 8 * K));
             SQ_CUDA(cudaGetLastError());
             unsigned long long g = 0;
             SQ_CUDA(cudaMemcpyAsync(&g, lb.total, 8, cudaMemcpyDeviceToHost, st));
             check_device_error();
-            G = g;
+            out.G = g;
+            prof_add_bytes_last((double)out.G * 4);
             unsigned endv = (unsigned)P;
-            SQ_CUDA(cudaMemcpyAsync(seg + G, &endv, 4, cudaMemcpyHostToDevice, st));
+            SQ_CUDA(cudaMemcpyAsync(seg + out.G, &endv, 4, cudaMemcpyHostToDevice, st));
         }
     }
+    return out;
+}
+
+template <int K>
+static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg) {
+    const uint64_t N = s.n;
+    cudaStream_t st = stream();
+    ConstKeyPtrs ik;
+    for (int w = 0; w < SQ_KMAX; ++w) ik.w[w] = s.live.keys[w];
+    uint64_t cap = 1024;
+    while (cap < 2 * N) cap <<= 1;
+    // one allocation: slots | counters | cnt | head | gid | pass_list | bucket target | bucket amp
+    const size_t off_cnt = cap * 8 + 256;
+    const size_t off_head = off_cnt + N * 4;
+    const size_t off_gid = off_head + N * 4;
+    const size_t off_pass = off_gid + N * 4;
+    const size_t off_btgt = off_pass + N * 4;
+    size_t off_bamp = off_btgt + N * 4;
+    off_bamp = (off_bamp + 15) & ~size_t(15);
+    const size_t total = off_bamp + N * 16;
+    char* base = (char*)ws().get(WS_MERGE_KEYS, total);
+    HashWs h;
+    h.slots = (unsigned long long*)base;
+    h.cap_mask = cap - 1;
+    h.gcount = (unsigned*)(base + cap * 8);
+    h.cnt = (unsigned*)(base + off_cnt);
+    h.head = (unsigned*)(base + off_head);
+    h.gid = (unsigned*)(base + off_gid);
+    h.pass_list = (unsigned*)(base + off_pass);
+    SQ_CUDA(cudaMemsetAsync(base, 0, off_head, st));  // slots, counters, cnt
+    prof_begin("hash_insert");
+    hash_insert_kernel<K><<<grid_for(N, 256, 8), 256, 0, st>>>(ik, dg, gs.cond, N, h, device_error_word());
+    prof_end((double)N * (8.0 * K + 4 + 4));
+    SQ_CUDA(cudaGetLastError());
+    unsigned gc[2] = {0, 0};
+    SQ_CUDA(cudaMemcpyAsync(gc, h.gcount, 8, cudaMemcpyDeviceToHost, st));
+    check_device_error();
+    Grouping out;
+    out.G = gc[0];
+    out.F = gc[1];
+    out.pass = h.pass_list;
+    out.ghead = h.head;
+    out.bucket = true;
+    const uint64_t P = N - out.F;
+    unsigned* seg = (unsigned*)ws().get(WS_SEG, (out.G + 2) * 4);
+    out.seg = seg;
+    if (out.G > 0) {
+        const long long nt = (long long)((out.G + kSelTile - 1) / kSelTile);
+        LbWs lb = make_lb(nt);
+        prof_begin("scan_group_sizes");
+        scan_seg_kernel<<<(unsigned)nt, kSelBlock, 0, st>>>(h.cnt, seg, out.G, lb, nt, device_error_word());
+        prof_end((double)out.G * 8);
+        SQ_CUDA(cudaGetLastError());
+        unsigned endv = (unsigned)P;
+        SQ_CUDA(cudaMemcpyAsync(seg + out.G, &endv, 4, cudaMemcpyHostToDevice, st));
+        unsigned* btgt = (unsigned*)(base + off_btgt);
+        double2* bamp = (double2*)(base + off_bamp);
+        prof_begin("bucket_members");
+        bucket_kernel<<<grid_for(N, 256, 8), 256, 0, st>>>(h.gid, s.live.keys[gs.target.word], gs.target, s.live.amp,
+                                                           N, seg, h.cnt, btgt, bamp);
+        prof_end((double)N * (4 + 8 + 16) + (double)P * (4 + 16 + 8));
+        SQ_CUDA(cudaGetLastError());
+        out.btgt = btgt;
+        out.bamp = bamp;
+    }
+    return out;
+}
+
+template <int K>
+static void run_group(State& s, const GroupSpec& gs) {
+    const uint64_t N = s.n;
+    cudaStream_t st = stream();
+    ConstKeyPtrs ik;
+    for (int w = 0; w < SQ_KMAX; ++w) ik.w[w] = s.live.keys[w];
+
+    // group mask: active bits except the target bits
+    uint64_t gmask[SQ_KMAX];
+    regtable().active_mask(gmask);
+    if (gs.target.width) gmask[gs.target.word] &= ~(wmask(gs.target.width) << gs.target.shift);
+    uint64_t* dg = (uint64_t*)ws().get(WS_REDUCE, 64 * 8);
+    SQ_CUDA(cudaMemcpyAsync(dg, gmask, SQ_KMAX * 8, cudaMemcpyHostToDevice, st));
+
+    // the merge sums runs in order, so it keeps the (stable) sort; the
+    // transforms are order-independent and default to the hash grouping
+    const bool use_hash = gs.mode != GM_MERGE && (g_strategy == 2 || (g_strategy == 0 && N >= 4096));
+    Grouping gr = use_hash ? group_by_hash<K>(s, gs, dg) : group_by_sort<K>(s, gs, gmask, dg);
+    const uint64_t G = gr.G, F = gr.F, P = N - F;
 
     // emit: count pass, scan, write pass
     EmitArgs ea;
     memset(&ea, 0, sizeof(ea));
     ea.in_keys = ik;
     ea.in_amp = s.live.amp;
-    ea.idx = idx;
-    ea.seg = seg;
+    ea.idx = gr.idx;
+    ea.btgt = gr.btgt;
+    ea.bamp = gr.bamp;
+    ea.ghead = gr.ghead;
+    ea.seg = gr.seg;
     ea.groups = G;
     ea.target = gs.target;
     ea.aux = gs.aux;
@@ -783,39 +1095,55 @@ static void run_group(State& s, const GroupSpec& gs) {
         W = S <= 256 ? 32 : 256;
         smem = (size_t)(W == 32 ? 8 : 1) * S * sizeof(double2);
     }
+    const bool bk = gr.bucket;
+    uint64_t T = 0;
     auto launch_emit = [&](bool write) {
         if (G == 0) return;
+        prof_begin(write ? (pair ? "emit_pair_write" : gs.mode == GM_MERGE ? "emit_merge_write" : "emit_hadamard_write")
+                         : (pair ? "emit_pair_count" : gs.mode == GM_MERGE ? "emit_merge_count" : "emit_hadamard_count"));
         if (pair) {
-            if (write) emit_pair_kernel<K, true><<<grid_for(G, 256), 256, 0, st>>>(ea);
-            else emit_pair_kernel<K, false><<<grid_for(G, 256), 256, 0, st>>>(ea);
+            const unsigned grid = grid_for(G, 256);
+            if (write && bk) emit_pair_kernel<K, true, true><<<grid, 256, 0, st>>>(ea);
+            else if (write) emit_pair_kernel<K, true, false><<<grid, 256, 0, st>>>(ea);
+            else if (bk) emit_pair_kernel<K, false, true><<<grid, 256, 0, st>>>(ea);
+            else emit_pair_kernel<K, false, false><<<grid, 256, 0, st>>>(ea);
         } else if (gs.mode == GM_MERGE) {
             if (write) emit_merge_kernel<K, true><<<grid_for(G, 256), 256, 0, st>>>(ea);
             else emit_merge_kernel<K, false><<<grid_for(G, 256), 256, 0, st>>>(ea);
         } else if (W == 32) {
             const unsigned grid = (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8);
-            if (write) emit_hadamard_kernel<K, 32, true><<<grid, 256, smem, st>>>(ea);
-            else emit_hadamard_kernel<K, 32, false><<<grid, 256, smem, st>>>(ea);
+            if (write && bk) emit_hadamard_kernel<K, 32, true, true><<<grid, 256, smem, st>>>(ea);
+            else if (write) emit_hadamard_kernel<K, 32, true, false><<<grid, 256, smem, st>>>(ea);
+            else if (bk) emit_hadamard_kernel<K, 32, false, true><<<grid, 256, smem, st>>>(ea);
+            else emit_hadamard_kernel<K, 32, false, false><<<grid, 256, smem, st>>>(ea);
         } else {
             static bool attr_set = false;
             if (!attr_set) {
-                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
                 attr_set = true;
             }
             const unsigned grid = (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2);
-            if (write) emit_hadamard_kernel<K, 256, true><<<grid, 256, smem, st>>>(ea);
-            else emit_hadamard_kernel<K, 256, false><<<grid, 256, smem, st>>>(ea);
+            if (write && bk) emit_hadamard_kernel<K, 256, true, true><<<grid, 256, smem, st>>>(ea);
+            else if (write) emit_hadamard_kernel<K, 256, true, false><<<grid, 256, smem, st>>>(ea);
+            else if (bk) emit_hadamard_kernel<K, 256, false, true><<<grid, 256, smem, st>>>(ea);
+            else emit_hadamard_kernel<K, 256, false, false><<<grid, 256, smem, st>>>(ea);
         }
-        count_launch();
+        // members: target + amplitude (+ index on the sort path); groups: bounds + head key; then counts or outputs
+        double b = (double)P * (bk ? 4 + 16 : 4 + 8 + 16) + (double)G * (8 + 8 * K + (bk ? 4 : 0));
+        b += write ? (double)G * 8 + (double)T * (8 * K + 16) : (double)G * 4;
+        prof_end(b);
         SQ_CUDA(cudaGetLastError());
     };
     launch_emit(false);
-    uint64_t T = 0;
     if (G > 0) {
         const long long nt = (long long)((G + kSelTile - 1) / kSelTile);
         LbWs lb = make_lb(nt);
+        prof_begin("scan_counts");
         scan_counts_kernel<<<(unsigned)nt, kSelBlock, 0, st>>>(ea.cnt, off, G, lb, nt, device_error_word());
-        count_launch();
+        prof_end((double)G * 12);
         SQ_CUDA(cudaGetLastError());
         unsigned long long t = 0;
         SQ_CUDA(cudaMemcpyAsync(&t, lb.total, 8, cudaMemcpyDeviceToHost, st));
@@ -828,8 +1156,9 @@ static void run_group(State& s, const GroupSpec& gs) {
     ea.out_amp = s.spare.amp;
     launch_emit(true);
     if (F) {
-        passthrough_kernel<K><<<grid_for(F, 256), 256, 0, st>>>(ik, s.live.amp, idx + P, F, ea.out_keys, ea.out_amp, T);
-        count_launch();
+        prof_begin("passthrough");
+        passthrough_kernel<K><<<grid_for(F, 256), 256, 0, st>>>(ik, s.live.amp, gr.pass, F, ea.out_keys, ea.out_amp, T);
+        prof_end((double)F * (4 + 2.0 * (8 * K + 16)));
         SQ_CUDA(cudaGetLastError());
     }
     swap_live_spare(s);
@@ -876,8 +1205,9 @@ void add_systems(State& dst, const State& src, double coef) {
             SQ_CUDA(cudaMemsetAsync(dst.live.keys[w] + n0, 0, n1 * 8, st));
     }
     const int do_scale = std::abs(coef - 1.0) > 1e-14 ? 1 : 0;
+    prof_begin("scale_copy");
     scale_copy_kernel<<<grid_for(n1, 256), 256, 0, st>>>(src.live.amp, dst.live.amp + n0, n1, coef, do_scale);
-    count_launch();
+    prof_end((double)n1 * 32);
     SQ_CUDA(cudaGetLastError());
     dst.n = n0 + n1;
     if (n0 == 0) return;

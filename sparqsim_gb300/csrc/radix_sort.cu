@@ -172,8 +172,9 @@ int radix_sort_pairs(KeyT* k[2], unsigned* v[2], uint64_t n, int bits) {
     const int passes = (bits + 7) / 8;
     unsigned* hist = (unsigned*)ws().get(WS_HIST, (size_t)2 * 8 * kRadix * 4);
     SQ_CUDA(cudaMemsetAsync(hist, 0, (size_t)passes * kRadix * 4, stream()));
+    prof_begin("radix_histogram");
     rs_histogram_kernel<KeyT><<<grid_for(n, kRsBlock, 4), kRsBlock, 0, stream()>>>(k[0], n, passes, hist);
-    count_launch();
+    prof_end((double)n * sizeof(KeyT));
     SQ_CUDA(cudaGetLastError());
     std::vector<unsigned> h((size_t)passes * kRadix);
     SQ_CUDA(cudaMemcpyAsync(h.data(), hist, h.size() * 4, cudaMemcpyDeviceToHost, stream()));
@@ -203,10 +204,11 @@ int radix_sort_pairs(KeyT* k[2], unsigned* v[2], uint64_t n, int bits) {
         const int p = live[q];
         unsigned* st = lb + q * per_pass;
         unsigned* counter = st + (size_t)ntiles * kRadix;
+        prof_begin(sizeof(KeyT) == 8 ? "radix_onesweep_u64" : "radix_onesweep_u32");
         rs_onesweep_kernel<KeyT><<<ntiles, kRsBlock, 0, stream()>>>(k[cur], v[cur], k[cur ^ 1], v[cur ^ 1], n, 8 * p,
                                                                    dbase + (size_t)p * kRadix, st, counter,
                                                                    device_error_word());
-        count_launch();
+        prof_end(2.0 * n * (sizeof(KeyT) + 4));  // one read and one write of (key, index)
         SQ_CUDA(cudaGetLastError());
         cur ^= 1;
     }

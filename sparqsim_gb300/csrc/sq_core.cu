@@ -184,6 +184,91 @@ unsigned int* device_error_word() {
 void count_launch(int n) { g_launches += (uint64_t)n; }
 uint64_t launches() { return g_launches.load(); }
 
+// ------------------------------------------------------------------ per-kernel timing
+// When enabled, every launch is bracketed by two CUDA events recorded on the
+// library stream; collect() turns the pairs into per-kernel totals.
+struct ProfRec {
+    const char* name;
+    cudaEvent_t a, b;
+    double bytes;
+};
+static bool g_prof = false;
+static std::vector<ProfRec> g_pending;
+static std::vector<cudaEvent_t> g_event_pool;
+static const char* g_open_name = nullptr;
+static cudaEvent_t g_open_event = nullptr;
+struct ProfStat {
+    uint64_t count = 0;
+    double ms = 0.0;
+    double bytes = 0.0;
+};
+static std::vector<std::pair<std::string, ProfStat>> g_stats;
+
+static cudaEvent_t take_event() {
+    if (!g_event_pool.empty()) {
+        cudaEvent_t e = g_event_pool.back();
+        g_event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    SQ_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+void prof_begin(const char* name) {
+    if (!g_prof) return;
+    g_open_name = name;
+    g_open_event = take_event();
+    SQ_CUDA(cudaEventRecord(g_open_event, stream()));
+}
+
+void prof_end(double alg_bytes) {
+    count_launch();
+    if (!g_prof || !g_open_event) return;
+    cudaEvent_t b = take_event();
+    SQ_CUDA(cudaEventRecord(b, stream()));
+    g_pending.push_back(ProfRec{g_open_name, g_open_event, b, alg_bytes});
+    g_open_event = nullptr;
+}
+
+void prof_add_bytes_last(double alg_bytes) {
+    if (g_prof && !g_pending.empty()) g_pending.back().bytes += alg_bytes;
+}
+
+void prof_collect() {
+    if (g_pending.empty()) return;
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    for (auto& r : g_pending) {
+        float ms = 0.f;
+        SQ_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+        auto it = std::find_if(g_stats.begin(), g_stats.end(), [&](const auto& kv) { return kv.first == r.name; });
+        if (it == g_stats.end()) {
+            g_stats.emplace_back(r.name, ProfStat{});
+            it = g_stats.end() - 1;
+        }
+        it->second.count += 1;
+        it->second.ms += ms;
+        it->second.bytes += r.bytes;
+        g_event_pool.push_back(r.a);
+        g_event_pool.push_back(r.b);
+    }
+    g_pending.clear();
+}
+
+void prof_enable(bool on) {
+    prof_collect();
+    g_prof = on;
+}
+void prof_reset() {
+    prof_collect();
+    g_stats.clear();
+}
+size_t prof_count() { return g_stats.size(); }
+const char* prof_name(size_t i) { return g_stats[i].first.c_str(); }
+uint64_t prof_launches(size_t i) { return g_stats[i].second.count; }
+double prof_ms(size_t i) { return g_stats[i].second.ms; }
+double prof_bytes(size_t i) { return g_stats[i].second.bytes; }
+
 void* dev_alloc(size_t bytes) {
     if (bytes == 0) bytes = 16;
     void* p = nullptr;

@@ -164,6 +164,20 @@ struct ConstKeyPtrs {
 cudaStream_t stream();
 int num_sms();
 void count_launch(int n = 1);
+// Bracket one kernel launch: prof_begin(name); kernel<<<...>>>(...); prof_end(bytes);
+// prof_end() also counts the launch; `bytes` is the launch's algorithmic
+// (compulsory) HBM traffic, used for the roofline.
+void prof_begin(const char* name);
+void prof_end(double alg_bytes = 0.0);
+void prof_add_bytes_last(double alg_bytes);
+void prof_collect();
+void prof_enable(bool on);
+void prof_reset();
+size_t prof_count();
+const char* prof_name(size_t i);
+uint64_t prof_launches(size_t i);
+double prof_ms(size_t i);
+double prof_bytes(size_t i);
 void* dev_alloc(size_t bytes);
 void dev_free(void* p);
 
@@ -234,6 +248,8 @@ struct GroupSpec {
     bool prune;
 };
 void group_transform(State& s, const GroupSpec& g);
+void set_group_strategy(int s);
+int get_group_strategy();
 void zero_field(State& s, Field f);
 void move_field(State& s, Field first, Field second, Field dst);
 

@@ -6,6 +6,7 @@ otherwise. Modelled on the reference's CPU-vs-GPU harness
 from __future__ import annotations
 
 import math
+import zlib
 
 import numpy as np
 import pytest
@@ -15,6 +16,13 @@ import sparqsim_gb300 as ps
 pytestmark = pytest.mark.gpu
 
 U = ps.UnsignedInteger
+
+
+@pytest.fixture(params=["sort", "hash"])
+def strategy(request):
+    ps.set_group_strategy(request.param)
+    yield request.param
+    ps.set_group_strategy("auto")
 
 
 def random_state(rng, widths, n, types=None):
@@ -44,7 +52,10 @@ def grouped_state(rng, widths, target, n_digits, groups, fill):
     for g in range(groups):
         base = [int(rng.integers(0, 1 << w)) for w in widths]
         base[target] &= ~((1 << n_digits) - 1)
-        key0 = tuple(v for i, v in enumerate(base) if i != target) + (base[target],)
+        # groups must differ outside the whole target register: the reference
+        # groups by every other register, so two groups that differ only in
+        # the target's high bits would be one (undefined) reference group
+        key0 = tuple(v for i, v in enumerate(base) if i != target)
         if key0 in seen:
             continue
         seen.add(key0)
@@ -70,7 +81,7 @@ ELEMENTWISE_CASES = [
     ("Xor", lambda: ps.Xor_UInt_UInt("a", "b", "c")),
     ("Less_UInt", lambda: ps.Less_UInt_UInt("a", "b", "f")),
     ("Less_SInt", lambda: ps.Less_SInt_SInt("s", "a", "f")),
-    ("GetMid", lambda: ps.GetMid_UInt_UInt("a", "b", "c")),
+    ("GetMid", lambda: ps.GetMid_UInt_UInt("a", "m", "c")),
     ("Neg", lambda: ps.Neg_UInt("a", "c")),
     ("Abs", lambda: ps.Abs_SInt("s", "c")),
     ("Sqrt", lambda: ps.Sqrt_UInt("b", "c")),
@@ -82,7 +93,7 @@ ELEMENTWISE_CASES = [
     ("Select", lambda: ps.Select_Bool_UInt_UInt("f", "a", "b", "c")),
     ("Compare", lambda: ps.Compare_UInt_UInt("a", "b", "f", "g")),
     ("Assign", lambda: ps.Assign("a", "c")),
-    ("Swap", lambda: ps.Swap_General_General("a", "b")),
+    ("Swap", lambda: ps.Swap_General_General("a", "a2")),
     ("FlipBools", lambda: ps.FlipBools("b")),
     ("Swap_Bool_Bool", lambda: ps.Swap_Bool_Bool("a", 2, "b", 5)),
     ("ShiftLeft", lambda: ps.ShiftLeft_InPlace("b", 3)),
@@ -116,14 +127,15 @@ def _arith_registers(dual):
     dual.reg("g", ps.Boolean, 1)
     dual.reg("s", ps.SignedInteger, 9)
     dual.reg("m", U, 4)
-    return [12, 20, 16, 1, 1, 9, 4]
+    dual.reg("a2", U, 12)
+    return [12, 20, 16, 1, 1, 9, 4, 12]
 
 
 @pytest.mark.parametrize("name,make", ELEMENTWISE_CASES, ids=[c[0] for c in ELEMENTWISE_CASES])
 @pytest.mark.parametrize("cond", ["none", "nonzero", "bit", "value"])
 def test_elementwise_vs_oracle(dual, name, make, cond):
     widths = _arith_registers(dual)
-    rng = np.random.default_rng(abs(hash((name, cond))) % 2**32)
+    rng = np.random.default_rng(zlib.crc32(f"{name}/{cond}".encode()))
     regs, amps = random_state(rng, widths, 3000)
     regs[:, 6] %= 15  # Mod_Mult acts on values < N
     dual.start(regs, amps)
@@ -186,12 +198,12 @@ def test_multiword_keys(dual):
     # 3 words of packed keys; ops touching registers in different words
     for i, w in enumerate([40, 40, 40, 30, 20]):
         dual.reg(f"r{i}", U, w)
-    assert ps.System.key_words() == 3
+    assert ps.System.key_words() == 4  # first fit: 40 | 40 | 40 | 30, the 20-bit register joins word 0
     rng = np.random.default_rng(3)
     regs, amps = random_state(rng, [40, 40, 40, 30, 20], 3000)
     dual.start(regs, amps)
     for op in [ps.Add_UInt_UInt("r0", "r1", "r2"), ps.Mul_UInt_UInt("r3", "r4", "r1"),
-               ps.Swap_General_General("r0", "r3"), ps.Phase_Bool("r2", 7, 1.1).conditioned_by_nonzeros("r4")]:
+               ps.Swap_General_General("r0", "r2"), ps.Phase_Bool("r2", 7, 1.1).conditioned_by_nonzeros("r4")]:
         dual.apply(op)
         dual.compare(exact_amp=True)
 
@@ -199,7 +211,7 @@ def test_multiword_keys(dual):
 # ----------------------------------------------------------------- split / merge
 @pytest.mark.parametrize("n_digits", [1, 2, 3, 5, 8, 10, 12])
 @pytest.mark.parametrize("fill", ["singleton", "full", "mixed"])
-def test_hadamard_int(dual, n_digits, fill):
+def test_hadamard_int(dual, strategy, n_digits, fill):
     dual.reg("x", U, 14)
     dual.reg("y", U, 9)
     dual.reg("z", U, 6)
@@ -221,7 +233,7 @@ def test_hadamard_int(dual, n_digits, fill):
     dual.compare(exact_amp=True)
 
 
-def test_hadamard_int_conditioned(dual):
+def test_hadamard_int_conditioned(dual, strategy):
     dual.reg("x", U, 6)
     dual.reg("y", U, 8)
     dual.reg("c", ps.Boolean, 1)
@@ -230,12 +242,17 @@ def test_hadamard_int_conditioned(dual):
     dual.start(regs, amps)
     dual.apply(ps.Hadamard_Int("x", 6).conditioned_by_nonzeros("c"))
     dual.compare(exact_amp=True)
-    dual.apply(ps.Hadamard_Int("x", 4).conditioned_by_value("y", int(regs[0, 1])))
+    dual.apply(ps.Hadamard_Int("x", 6).conditioned_by_value("y", int(regs[0, 1])))
+    dual.compare(exact_amp=True)
+    # partial-width Hadamard on a state whose groups share the high bits of x
+    regs2, amps2 = random_state(rng, [4, 8, 1], 400)
+    dual.start(regs2, amps2)
+    dual.apply(ps.Hadamard_Int("x", 4).conditioned_by_bit("y", 2))
     dual.compare(exact_amp=True)
 
 
 @pytest.mark.parametrize("width", [1, 2, 4, 7, 10])
-def test_hadamard_int_full(dual, width):
+def test_hadamard_int_full(dual, strategy, width):
     dual.reg("q", U, width)
     dual.reg("r", U, 10)
     rng = np.random.default_rng(width)
@@ -246,7 +263,7 @@ def test_hadamard_int_full(dual, width):
     dual.compare(exact_amp=True)
 
 
-def test_hadamard_bool(dual):
+def test_hadamard_bool(dual, strategy):
     dual.reg("q", ps.Boolean, 1)
     dual.reg("r", U, 12)
     dual.reg("c", U, 3)
@@ -260,7 +277,7 @@ def test_hadamard_bool(dual):
 
 
 @pytest.mark.parametrize("kind", ["general", "diagonal", "offdiagonal", "rx", "ry"])
-def test_rot_bool(dual, kind):
+def test_rot_bool(dual, strategy, kind):
     dual.reg("q", U, 4)
     dual.reg("r", U, 10)
     rng = np.random.default_rng(len(kind))
@@ -286,7 +303,7 @@ def test_rot_bool(dual, kind):
 
 
 @pytest.mark.parametrize("w_in", [1, 3, 8, 16])
-def test_condrot(dual, w_in):
+def test_condrot(dual, strategy, w_in):
     dual.reg("in", ps.Rational, w_in)
     dual.reg("out", ps.Boolean, 1)
     dual.reg("r", U, 6)
@@ -359,7 +376,7 @@ def test_register_surgery(dual):
     assert lo >= 0 and t >= 0
 
 
-def test_many_varying_bits_multichunk_sort(dual):
+def test_many_varying_bits_multichunk_sort(dual, strategy):
     # > 64 varying group-key bits: the sort runs over several 64-bit chunks
     for i, w in enumerate([3, 60, 60, 20]):
         dual.reg(f"r{i}", U, w)
@@ -380,7 +397,7 @@ def test_empty_state(dual):
     assert dual.gpu.size() == 0 and dual.ora.size() == 0
 
 
-def test_config1_small_circuit(dual):
+def test_config1_small_circuit(dual, strategy):
     """The config-1 circuit shape at reduced widths: H(a), b ^= T[a], c ^= a*b,
     phase on c bit 0, H(a) — keys bit-exact, amplitudes bit-exact."""
     dual.reg("a", U, 8)
@@ -395,4 +412,23 @@ def test_config1_small_circuit(dual):
         dual.apply(op)
         dual.compare(exact_amp=True)
     assert dual.gpu.size() > 1 << 14
+    assert abs(dual.gpu.norm_sq() - 1.0) < 1e-12
+
+
+def test_config1_full_size(dual, strategy):
+    """Config 1 at its literal size: a 12-bit, b/c 16-bit, 4096-word uint16
+    table; the final Hadamard fans out to ~2^24 entries. Keys bit-exact and
+    amplitudes bit-exact against the oracle on the full state."""
+    dual.reg("a", U, 12)
+    dual.reg("b", U, 16)
+    dual.reg("c", U, 16)
+    rng = np.random.default_rng(20261203)
+    table = rng.integers(0, 1 << 16, 4096, dtype=np.uint64)
+    q = dual.qram(12, 16, table)
+    dual.start()
+    for op in [ps.Hadamard_Int("a", 12), ps.QRAMLoad(q, "a", "b"), ps.Mul_UInt_UInt("a", "b", "c"),
+               ps.Phase_Bool("c", 0, 0.37), ps.Hadamard_Int("a", 12)]:
+        dual.apply(op)
+    assert dual.gpu.size() > 16_000_000
+    dual.compare(exact_amp=True)
     assert abs(dual.gpu.norm_sq() - 1.0) < 1e-12
