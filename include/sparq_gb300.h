@@ -265,6 +265,16 @@ int sq_hadamard_bool(sq_state* st, uint32_t reg, const sq_cond* cond);
 int sq_rot_bool(sq_state* st, uint32_t reg, uint32_t digit, const double* mat8, const sq_cond* cond, int dag);
 /* CondRot_Rational_Bool (condrot.cpp:12-152): angle 2*pi*in/2^width(in) on the 1-bit out. */
 int sq_condrot_rational_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, int dag);
+/* CondRot_General_Bool_Fast<F> (condrot.h:149-300): 2x2 unitary func(in) on
+ * the 1-bit out register. The callable becomes a table: table[8*v .. 8*v+7]
+ * = {m00, m01, m10, m11} as (re, im) for every v < 2^width(in) = n_values. */
+int sq_condrot_general_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, const double* table, uint64_t n_values);
+/* Rot_GeneralUnitary (rot.cpp:353-477): dense dim x dim unitary (dim = 2^width(reg),
+ * width <= 8) on the whole register, row-major (re, im) pairs; dag applies M^dagger. */
+int sq_rot_general_unitary(sq_state* st, uint32_t reg, const double* mat, uint64_t dim, const sq_cond* cond, int dag);
+/* Hadamard_Partial (hadamard.cpp:470-712): H on a set of bit positions of reg.
+ * The reference's active (hash) path is defined for one position; so is this. */
+int sq_hadamard_partial(sq_state* st, uint32_t reg, const uint32_t* positions, uint32_t n_positions, const sq_cond* cond);
 
 /* ------------------------------------------------------------------ */
 /* Prune / norm / merge / register surgery                              */
@@ -276,6 +286,12 @@ int sq_condrot_rational_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, in
  * (its CPU path sorts or uses std::map buckets, its GPU path sorts). */
 int sq_set_group_strategy(int strategy);
 int sq_get_group_strategy(int* strategy);
+/* How split operators size their output: 0 = automatic (one pass that
+ * reserves each group's output range with an atomic, when the bound "every
+ * group fully populated" fits in memory), 1 = exact count pass, scan, write
+ * pass. Same entries either way; only their order differs. */
+int sq_set_output_sizing(int mode);
+int sq_get_output_sizing(int* mode);
 /* clearzero_default_eps (system_operations.h:577), initially 1e-14. */
 int sq_set_clearzero_eps(double eps);
 int sq_get_clearzero_eps(double* eps);

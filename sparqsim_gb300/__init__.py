@@ -8,12 +8,14 @@ behind the C ABI in include/sparq_gb300.h. There is no CPU fallback.
 from ._native import SparQError, SparQInvalid, launch_count
 from .core import (Boolean, General, QRAMCircuit_qutrit, Rational, SignedInteger, SparseState,
                    StateStorageType, System, UnsignedInteger, get_clearzero_default_eps,
-                   get_group_strategy, set_clearzero_default_eps, set_group_strategy)
+                   get_group_strategy, set_clearzero_default_eps, set_group_strategy,
+                   set_output_sizing)
 from .operators import *  # noqa: F401,F403
 from .operators import (Abs_SInt, Add_AnyInt_AnyInt_InPlace, Add_ConstUInt_InPlace,
                         Add_Mult_UInt_ConstUInt_InPlace, Add_UInt_ConstUInt, Add_UInt_UInt,
                         Add_UInt_UInt_InPlace, AddRegister, And_UInt_UInt, Assign, BaseOperator,
                         Carry_UInt_UInt, ClearZero, CombineRegister, Compare_UInt_UInt, CondRot_Fixed_Bool,
+                        CondRot_General_Bool, Hadamard_Partial, Rot_GeneralUnitary,
                         CondRot_Rational_Bool, Div_UInt_UInt, ElementwiseOperator, FlipBools, Fused,
                         GetMid_UInt_UInt, GlobalPhase, Hadamard_Bool, Hadamard_Int, Hadamard_Int_Full,
                         Init_Unsafe, IsZero_UInt, Less_SInt_SInt, Less_UInt_UInt,

@@ -130,8 +130,13 @@ _SIGS = [
     ("sq_hadamard_bool", c_int, [c_void_p, c_uint32, POINTER(SqCond)]),
     ("sq_rot_bool", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), POINTER(SqCond), c_int]),
     ("sq_condrot_rational_bool", c_int, [c_void_p, c_uint32, c_uint32, c_int]),
+    ("sq_condrot_general_bool", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), c_uint64]),
+    ("sq_rot_general_unitary", c_int, [c_void_p, c_uint32, POINTER(c_double), c_uint64, POINTER(SqCond), c_int]),
+    ("sq_hadamard_partial", c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_uint32, POINTER(SqCond)]),
     ("sq_set_group_strategy", c_int, [c_int]),
     ("sq_get_group_strategy", c_int, [POINTER(c_int)]),
+    ("sq_set_output_sizing", c_int, [c_int]),
+    ("sq_get_output_sizing", c_int, [POINTER(c_int)]),
     ("sq_set_clearzero_eps", c_int, [c_double]),
     ("sq_get_clearzero_eps", c_int, [POINTER(c_double)]),
     ("sq_clear_zero", c_int, [c_void_p, c_double]),

@@ -158,6 +158,12 @@ def get_group_strategy() -> str:
     return ["auto", "sort", "hash"][v.value]
 
 
+def set_output_sizing(mode: str) -> None:
+    """'auto' (single pass with per-group atomic reservation when the output
+    bound fits) or 'exact' (count pass, scan, write pass)."""
+    call("sq_set_output_sizing", {"auto": 0, "exact": 1}[mode])
+
+
 def set_clearzero_default_eps(eps: float) -> None:
     """clearzero_default_eps (system_operations.h:577)."""
     call("sq_set_clearzero_eps", float(eps))

@@ -651,6 +651,66 @@ int sq_condrot_rational_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, in
     SQ_API_END
 }
 
+int sq_condrot_general_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, const double* table, uint64_t n_values) {
+    SQ_API_BEGIN
+    need(reg_in != reg_out, "CondRot_General_Bool: input and output registers must differ");
+    need(table != nullptr, "null matrix table");
+    Field fi = regtable().field(reg_in);
+    Field fo = regtable().field(reg_out);
+    need(fo.type == SQ_BOOLEAN && fo.width == 1, "CondRot_General_Bool: output must be a 1-bit Boolean register");
+    need(fi.width <= 24, "CondRot_General_Bool: input register wider than 24 bits");
+    need(n_values == (1ull << fi.width), "CondRot_General_Bool: table must hold 2^width(in) matrices");
+    double2* dev = (double2*)ws().get(WS_MATRIX, n_values * 4 * sizeof(double2));
+    SQ_CUDA(cudaMemcpyAsync(dev, table, n_values * 4 * sizeof(double2), cudaMemcpyHostToDevice, stream()));
+    GroupSpec g;
+    memset(&g, 0, sizeof(g));
+    g.mode = GM_ROT;
+    g.target = fo;
+    g.aux = fi;
+    g.mtable = dev;
+    g.eps = cz_eps();
+    group_transform(S(st), g);
+    SQ_API_END
+}
+
+int sq_rot_general_unitary(sq_state* st, uint32_t reg, const double* mat, uint64_t dim, const sq_cond* cond, int dag) {
+    SQ_API_BEGIN
+    need(mat != nullptr, "null matrix");
+    Field f = regtable().field(reg);
+    need(f.width >= 1 && f.width <= 8, "Rot_GeneralUnitary: register width must be 1..8");
+    need(dim == (1ull << f.width), "Rot_GeneralUnitary: matrix size does not match the register's size");
+    double2* dev = (double2*)ws().get(WS_MATRIX, dim * dim * sizeof(double2));
+    SQ_CUDA(cudaMemcpyAsync(dev, mat, dim * dim * sizeof(double2), cudaMemcpyHostToDevice, stream()));
+    GroupSpec g;
+    memset(&g, 0, sizeof(g));
+    g.mode = GM_UNITARY;
+    g.target = f;
+    g.umat = dev;
+    g.udag = dag ? 1 : 0;
+    g.cond = resolve_cond(cond);
+    g.eps = cz_eps();
+    group_transform(S(st), g);
+    SQ_API_END
+}
+
+int sq_hadamard_partial(sq_state* st, uint32_t reg, const uint32_t* positions, uint32_t n_positions, const sq_cond* cond) {
+    SQ_API_BEGIN
+    need(positions != nullptr && n_positions == 1,
+         "Hadamard_Partial: exactly one qubit position (the reference's active path handles one)");
+    Field f = regtable().field(reg);
+    need(positions[0] < f.width, "Hadamard_Partial: position >= register size");
+    GroupSpec g;
+    memset(&g, 0, sizeof(g));
+    g.mode = GM_HADAMARD_BOOL;
+    g.target = f;
+    g.target.shift = (uint8_t)(f.shift + positions[0]);
+    g.target.width = 1;
+    g.cond = resolve_cond(cond);
+    g.eps = cz_eps();
+    group_transform(S(st), g);
+    SQ_API_END
+}
+
 // ------------------------------------------------------------------ prune / norm / merge
 int sq_set_group_strategy(int strategy) {
     SQ_API_BEGIN
@@ -661,6 +721,18 @@ int sq_get_group_strategy(int* strategy) {
     SQ_API_BEGIN
     need(strategy != nullptr, "null pointer");
     *strategy = get_group_strategy();
+    SQ_API_END
+}
+
+int sq_set_output_sizing(int mode) {
+    SQ_API_BEGIN
+    set_output_sizing(mode);
+    SQ_API_END
+}
+int sq_get_output_sizing(int* mode) {
+    SQ_API_BEGIN
+    need(mode != nullptr, "null pointer");
+    *mode = get_output_sizing();
     SQ_API_END
 }
 

@@ -305,6 +305,7 @@ struct EmitArgs {
     uint64_t groups;
     unsigned* cnt;             // count pass output
     const unsigned long long* off;  // write pass input
+    unsigned long long* cursor;     // single-pass mode: output slots reserved so far
     Field target;
     Field aux;
     int mode;
@@ -314,6 +315,9 @@ struct EmitArgs {
     double eps;
     double sign2pi;            // CondRot: +-2*pi
     double2 m[4];
+    const double2* mtable;     // CondRot_General_Bool: 4 matrix elements per input value
+    const double2* umat;       // Rot_GeneralUnitary: S x S row-major
+    int udag;                  // Rot_GeneralUnitary: apply the conjugate transpose
 };
 
 template <int K>
@@ -390,15 +394,23 @@ __global__ void __launch_bounds__(256) emit_pair_kernel(const __grid_constant__ 
                 ro = cscale(ao, -s);
             }
         } else if (a.mode == GM_ROT) {
+            double2 m0 = a.m[0], m1 = a.m[1], m2 = a.m[2], m3 = a.m[3];
+            if (a.mtable) {  // CondRot_General_Bool: matrix chosen by the input register's value
+                const double2* mt = a.mtable + 4 * fget<K>(k0, a.aux);
+                m0 = mt[0];
+                m1 = mt[1];
+                m2 = mt[2];
+                m3 = mt[3];
+            }
             if (has_z && has_o) {
-                rz = cadd(cmul2(az, a.m[0]), cmul2(ao, a.m[1]));
-                ro = cadd(cmul2(az, a.m[2]), cmul2(ao, a.m[3]));
+                rz = cadd(cmul2(az, m0), cmul2(ao, m1));
+                ro = cadd(cmul2(az, m2), cmul2(ao, m3));
             } else if (has_z) {
-                rz = cmul2(az, a.m[0]);
-                ro = cmul2(az, a.m[2]);
+                rz = cmul2(az, m0);
+                ro = cmul2(az, m2);
             } else {
-                rz = cmul2(ao, a.m[1]);
-                ro = cmul2(ao, a.m[3]);
+                rz = cmul2(ao, m1);
+                ro = cmul2(ao, m3);
             }
         } else {  // GM_CONDROT: partner amplitude 0 for singletons, as the reference inserts it
             const double rot = as_rational(fget<K>(k0, a.aux), a.aux.width) * a.sign2pi;
@@ -572,7 +584,30 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
                 slots[tj] = aj;
             }
             worker_sync<W>();
-            for (int qn = 0; qn < a.nbits; ++qn) {
+            if (a.mode == GM_UNITARY) {
+                // Rot_GeneralUnitary (rot.cpp:353-389): out[i] = sum_j M(i,j) * amp[j], j ascending
+                double2 r[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const unsigned c = t + (unsigned)q * W;
+                    double2 acc = make_double2(0.0, 0.0);
+                    if (c < S)
+                        for (unsigned j = 0; j < S; ++j) {
+                            const double2 mij = a.udag ? make_double2(a.umat[(size_t)j * S + c].x, -a.umat[(size_t)j * S + c].y)
+                                                       : a.umat[(size_t)c * S + j];
+                            acc = cadd(acc, cmul2(mij, slots[j]));
+                        }
+                    r[q] = acc;
+                }
+                worker_sync<W>();
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const unsigned c = t + (unsigned)q * W;
+                    if (c < S) slots[c] = r[q];
+                }
+                worker_sync<W>();
+            }
+            for (int qn = 0; a.mode != GM_UNITARY && qn < a.nbits; ++qn) {
                 const unsigned h = 1u << qn;
                 for (unsigned p = t; p < S / 2; p += W) {
                     const unsigned i0 = ((p >> qn) << (qn + 1)) | (p & (h - 1u));
@@ -603,6 +638,213 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
         }
         if (!WRITE && t == 0) a.cnt[g] = kept;
         worker_sync<W>();
+    }
+}
+
+// Hadamard on 12 bits (4096 slots), one CTA of 256 threads per group. The
+// stage-ascending FWHT runs mostly in registers: each thread holds 16 slots.
+// Layout A: slot = j << 8 | warp << 5 | lane (j = 0..15); layout B:
+// slot = warp << 9 | j << 5 | lane. Stages 0-4 are warp shuffles in layout A,
+// stages 5-8 are in-register in layout B, stages 9-11 in-register in layout A;
+// shared memory is used only to scatter the members and for two transposes.
+// Every butterfly is (x0 + x1) * sqrt2inv, (x0 - x1) * sqrt2inv in the
+// reference's stage order, so results are bit-identical to the smem version.
+// MODE 0 counts kept outputs, 1 writes at offsets from the count pass, 2
+// reserves each group's range with one atomic (single pass; the order of
+// groups in the output is then not fixed, the values are).
+enum { EMIT_COUNT = 0, EMIT_WRITE = 1, EMIT_ATOMIC = 2 };
+
+__device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
+    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
+template <int K, int MODE, bool BUCKET>
+__global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constant__ EmitArgs a) {
+    extern __shared__ double2 sl[];  // 4096 slots
+    __shared__ unsigned s_cnt[16][8];
+    __shared__ unsigned long long s_base;
+    __shared__ uint64_t s_mt[64];
+    __shared__ double2 s_ma[64];
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const Field tg = a.target;
+    const double s2 = a.sqrt2inv;
+    for (uint64_t g = blockIdx.x; g < a.groups; g += gridDim.x) {
+        const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
+        const unsigned m = s1 - s0;
+        uint64_t gk[K];
+        load_key<K>(a.in_keys, group_head<BUCKET>(a, g, s0), gk);
+        if (a.mode == GM_HADAMARD_INT && m == 1) {
+            uint64_t v0;
+            double2 a0;
+            member_at<BUCKET>(a, s0, v0, a0);
+            const double2 base = cscale(a0, a.extra);
+            const bool keep = keep_amp(base, a.eps);
+            if (MODE == EMIT_COUNT) {
+                if (tid == 0) a.cnt[g] = keep ? 4096u : 0u;
+            } else if (keep) {
+                if (MODE == EMIT_ATOMIC) {
+                    if (tid == 0) s_base = atomicAdd(a.cursor, 4096ull);
+                    __syncthreads();
+                }
+                const unsigned long long o = MODE == EMIT_WRITE ? a.off[g] : s_base;
+                for (unsigned c = tid; c < 4096u; c += 256u) {
+                    uint64_t kk[K];
+#pragma unroll
+                    for (int w = 0; w < K; ++w) kk[w] = gk[w];
+                    fset<K>(kk, tg, (uint64_t)c);
+                    const double2 v = (__popcll((uint64_t)c & v0) & 1) ? cscale(base, -1.0) : base;
+                    store_entry<K>(a.out_keys, a.out_amp, o + c, kk, v);
+                }
+            }
+            __syncthreads();
+            continue;
+        }
+        double2 v[16];
+        if (a.mode == GM_HADAMARD_FULL && m <= 11u) {
+            // sparse bucket: direct product, members in ascending target order (hadamard.cpp:267-304)
+            for (unsigned j = tid; j < m; j += 256u) {
+                uint64_t tj;
+                double2 aj;
+                member_at<BUCKET>(a, s0 + j, tj, aj);
+                s_mt[j] = tj;
+                s_ma[j] = aj;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                for (unsigned i = 1; i < m; ++i) {
+                    const uint64_t kt = s_mt[i];
+                    const double2 ka = s_ma[i];
+                    int j = (int)i - 1;
+                    while (j >= 0 && s_mt[j] > kt) {
+                        s_mt[j + 1] = s_mt[j];
+                        s_ma[j + 1] = s_ma[j];
+                        --j;
+                    }
+                    s_mt[j + 1] = kt;
+                    s_ma[j + 1] = ka;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const unsigned c = ((unsigned)j << 8) | tid;
+                double2 acc = make_double2(0.0, 0.0);
+                for (unsigned q = 0; q < m; ++q) {
+                    double2 term = cscale(s_ma[q], (__popcll((uint64_t)c & s_mt[q]) & 1) ? -1. : 1.);
+                    term = cscale(term, a.extra);
+                    acc = cadd(acc, term);
+                }
+                v[j] = acc;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) sl[((unsigned)j << 8) | tid] = make_double2(0.0, 0.0);
+            __syncthreads();
+            for (unsigned j = tid; j < m; j += 256u) {
+                uint64_t tj;
+                double2 aj;
+                member_at<BUCKET>(a, s0 + j, tj, aj);
+                sl[tj] = aj;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = sl[((unsigned)j << 8) | tid];
+            // stages 0..4: partner lane = lane ^ h
+#pragma unroll
+            for (int qn = 0; qn < 5; ++qn) {
+                const int h = 1 << qn;
+                const bool lower = !(lane & (unsigned)h);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const double2 p = shfl_xor_d2(v[j], h);
+                    v[j] = lower ? cscale(cadd(v[j], p), s2) : cscale(csub(p, v[j]), s2);
+                }
+            }
+            // transpose A -> B
+#pragma unroll
+            for (int j = 0; j < 16; ++j) sl[((unsigned)j << 8) | tid] = v[j];
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = sl[(warp << 9) | ((unsigned)j << 5) | lane];
+            // stages 5..8: slot bit qn = bit (qn - 5) of j
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    if (j & (1 << b)) continue;
+                    const double2 x0 = v[j], x1 = v[j | (1 << b)];
+                    v[j] = cscale(cadd(x0, x1), s2);
+                    v[j | (1 << b)] = cscale(csub(x0, x1), s2);
+                }
+            }
+            // transpose B -> A (each thread rewrites the slots it read)
+#pragma unroll
+            for (int j = 0; j < 16; ++j) sl[(warp << 9) | ((unsigned)j << 5) | lane] = v[j];
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = sl[((unsigned)j << 8) | tid];
+            // stages 9..11: slot bit qn = bit (qn - 8) of j
+#pragma unroll
+            for (int b = 1; b < 4; ++b) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    if (j & (1 << b)) continue;
+                    const double2 x0 = v[j], x1 = v[j | (1 << b)];
+                    v[j] = cscale(cadd(x0, x1), s2);
+                    v[j | (1 << b)] = cscale(csub(x0, x1), s2);
+                }
+            }
+        }
+        // kept slots in ascending slot order: row j (slot bits 8..11), then warp, then lane
+        unsigned ball[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            ball[j] = __ballot_sync(0xffffffffu, keep_amp(v[j], a.eps));
+            if (lane == 0) s_cnt[j][warp] = __popc(ball[j]);
+        }
+        __syncthreads();
+        if (warp == 0) {
+            unsigned c4[4], sum = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const unsigned idx = lane * 4 + q;
+                c4[q] = s_cnt[idx >> 3][idx & 7];
+                sum += c4[q];
+            }
+            unsigned inc = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= (unsigned)o) inc += t;
+            }
+            unsigned run = inc - sum;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const unsigned idx = lane * 4 + q;
+                s_cnt[idx >> 3][idx & 7] = run;
+                run += c4[q];
+            }
+            const unsigned total = __shfl_sync(0xffffffffu, inc, 31);
+            if (lane == 0) {
+                if (MODE == EMIT_COUNT) a.cnt[g] = total;
+                else if (MODE == EMIT_ATOMIC) s_base = total ? atomicAdd(a.cursor, (unsigned long long)total) : 0ull;
+            }
+        }
+        __syncthreads();
+        if (MODE != EMIT_COUNT) {
+            const unsigned long long o = MODE == EMIT_WRITE ? a.off[g] : s_base;
+            const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                if (!((ball[j] >> lane) & 1u)) continue;
+                uint64_t kk[K];
+#pragma unroll
+                for (int w = 0; w < K; ++w) kk[w] = gk[w];
+                fset<K>(kk, tg, (uint64_t)(((unsigned)j << 8) | tid));
+                store_entry<K>(a.out_keys, a.out_amp, o + s_cnt[j][warp] + __popc(ball[j] & lt), kk, v[j]);
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -796,6 +1038,12 @@ __global__ void __launch_bounds__(kSelBlock) scan_seg_kernel(const unsigned* __r
 }
 
 static int g_strategy = 0;  // 0 auto, 1 sort, 2 hash
+static int g_sizing = 0;    // 0 auto (single pass when the output bound fits), 1 exact count-then-scan
+void set_output_sizing(int m) {
+    if (m < 0 || m > 1) fail(SQ_ERR_INVALID, "output sizing must be 0 (auto) or 1 (count then scan)");
+    g_sizing = m;
+}
+int get_output_sizing() { return g_sizing; }
 void set_group_strategy(int s) {
     if (s < 0 || s > 2) fail(SQ_ERR_INVALID, "group strategy must be 0 (auto), 1 (sort) or 2 (hash)");
     g_strategy = s;
@@ -1081,6 +1329,9 @@ static void run_group(State& s, const GroupSpec& gs) {
     ea.eps = gs.eps;
     ea.sign2pi = gs.sign * 2 * 3.14159265358979323846;
     for (int i = 0; i < 4; ++i) ea.m[i] = gs.m[i];
+    ea.mtable = gs.mtable;
+    ea.umat = gs.umat;
+    ea.udag = gs.udag;
     ea.cnt = (unsigned*)ws().get(WS_COUNT, (G + 1) * 4);
     unsigned long long* off = (unsigned long long*)ws().get(WS_OFFSET, (G + 1) * 8);
     ea.off = off;
@@ -1092,12 +1343,76 @@ static void run_group(State& s, const GroupSpec& gs) {
     int W = 0;
     if (!pair && gs.mode != GM_MERGE) {
         if (nb > 12) fail(SQ_ERR_UNSUPPORTED, "Hadamard on more than 12 bits at once is not provided by this engine");
+        if (gs.mode == GM_UNITARY && nb > 8) fail(SQ_ERR_UNSUPPORTED, "Rot_GeneralUnitary on more than 8 bits");
         W = S <= 256 ? 32 : 256;
         smem = (size_t)(W == 32 ? 8 : 1) * S * sizeof(double2);
     }
     const bool bk = gr.bucket;
     uint64_t T = 0;
+    // Hadamard on 12 bits: register FWHT kernel; single pass when the output
+    // bound (every group fully populated) fits a modest multiple of the input
+    const bool h4096 = !pair && gs.mode != GM_MERGE && gs.mode != GM_UNITARY && nb == 12;
+    const uint64_t bound = G * 4096ull + F;
+    const bool single_pass = h4096 && g_sizing == 0 && bound <= std::max<uint64_t>(4 * N, 1ull << 27);
+    if (h4096) {
+        static bool attr4096 = false;
+        if (!attr4096) {
+            const int sm = 4096 * (int)sizeof(double2);
+            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_COUNT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_WRITE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_ATOMIC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_COUNT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_WRITE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_ATOMIC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+            attr4096 = true;
+        }
+    }
+    auto launch_h4096 = [&](int mode) {
+        const unsigned grid = (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2);
+        const size_t sm = 4096 * sizeof(double2);
+        prof_begin(mode == EMIT_COUNT ? "emit_h4096_count" : mode == EMIT_WRITE ? "emit_h4096_write" : "emit_h4096_single_pass");
+        if (bk) {
+            if (mode == EMIT_COUNT) emit_h4096_kernel<K, EMIT_COUNT, true><<<grid, 256, sm, st>>>(ea);
+            else if (mode == EMIT_WRITE) emit_h4096_kernel<K, EMIT_WRITE, true><<<grid, 256, sm, st>>>(ea);
+            else emit_h4096_kernel<K, EMIT_ATOMIC, true><<<grid, 256, sm, st>>>(ea);
+        } else {
+            if (mode == EMIT_COUNT) emit_h4096_kernel<K, EMIT_COUNT, false><<<grid, 256, sm, st>>>(ea);
+            else if (mode == EMIT_WRITE) emit_h4096_kernel<K, EMIT_WRITE, false><<<grid, 256, sm, st>>>(ea);
+            else emit_h4096_kernel<K, EMIT_ATOMIC, false><<<grid, 256, sm, st>>>(ea);
+        }
+        double b = (double)P * (bk ? 4 + 16 : 4 + 8 + 16) + (double)G * (8 + 8 * K + (bk ? 4 : 0));
+        b += mode == EMIT_COUNT ? (double)G * 4 : (double)T * (8 * K + 16) + (mode == EMIT_WRITE ? (double)G * 8 : 0.0);
+        prof_end(b);
+        SQ_CUDA(cudaGetLastError());
+    };
+    if (single_pass) {
+        ensure_buffers(s.spare, std::max<uint64_t>(bound, 1), regtable().k, 0);
+        for (int w = 0; w < SQ_KMAX; ++w) ea.out_keys.w[w] = s.spare.keys[w];
+        ea.out_amp = s.spare.amp;
+        unsigned long long* cur = (unsigned long long*)ws().get(WS_COUNT, (G + 1) * 4 + 64);
+        ea.cursor = cur;
+        SQ_CUDA(cudaMemsetAsync(cur, 0, 8, st));
+        if (G > 0) launch_h4096(EMIT_ATOMIC);
+        unsigned long long t = 0;
+        SQ_CUDA(cudaMemcpyAsync(&t, cur, 8, cudaMemcpyDeviceToHost, st));
+        SQ_CUDA(cudaStreamSynchronize(st));
+        T = t;
+        prof_add_bytes_last((double)T * (8 * K + 16));
+        if (F) {
+            prof_begin("passthrough");
+            passthrough_kernel<K><<<grid_for(F, 256), 256, 0, st>>>(ik, s.live.amp, gr.pass, F, ea.out_keys, ea.out_amp, T);
+            prof_end((double)F * (4 + 2.0 * (8 * K + 16)));
+            SQ_CUDA(cudaGetLastError());
+        }
+        swap_live_spare(s);
+        s.n = T + F;
+        return;
+    }
     auto launch_emit = [&](bool write) {
+        if (h4096) {
+            if (G > 0) launch_h4096(write ? EMIT_WRITE : EMIT_COUNT);
+            return;
+        }
         if (G == 0) return;
         prof_begin(write ? (pair ? "emit_pair_write" : gs.mode == GM_MERGE ? "emit_merge_write" : "emit_hadamard_write")
                          : (pair ? "emit_pair_count" : gs.mode == GM_MERGE ? "emit_merge_count" : "emit_hadamard_count"));

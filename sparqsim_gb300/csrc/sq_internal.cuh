@@ -209,6 +209,7 @@ enum WsSlot {
     WS_MISC,
     WS_REDUCE,
     WS_MERGE_KEYS,
+    WS_MATRIX,
     WS_COUNT_MAX
 };
 
@@ -235,7 +236,8 @@ enum GroupMode {
     GM_HADAMARD_BOOL = 2,  // Hadamard_Bool pair rules
     GM_ROT = 3,            // Rot_Bool general 2x2
     GM_CONDROT = 4,        // CondRot_Rational_Bool
-    GM_MERGE = 5           // sum equal keys (add_systems)
+    GM_MERGE = 5,          // sum equal keys (add_systems)
+    GM_UNITARY = 6         // Rot_GeneralUnitary: dense 2^k x 2^k per group
 };
 struct GroupSpec {
     int mode;
@@ -246,10 +248,15 @@ struct GroupSpec {
     DCondSet cond;
     double eps;          // prune threshold for outputs
     bool prune;
+    const double2* mtable;  // device: CondRot_General_Bool matrices (4 per input value)
+    const double2* umat;    // device: Rot_GeneralUnitary matrix
+    int udag;
 };
 void group_transform(State& s, const GroupSpec& g);
 void set_group_strategy(int s);
 int get_group_strategy();
+void set_output_sizing(int m);
+int get_output_sizing();
 void zero_field(State& s, Field f);
 void move_field(State& s, Field first, Field second, Field dst);
 

@@ -49,6 +49,16 @@ def _run(state: SparseState, spec) -> None:
         call("sq_rot_bool", h, spec[1], spec[2], m, byref(spec[4]), 0)
     elif kind == "condrot":
         call("sq_condrot_rational_bool", h, spec[1], spec[2], 1 if spec[3] else 0)
+    elif kind == "condrot_general":
+        tab = spec[3]
+        call("sq_condrot_general_bool", h, spec[1], spec[2], tab.ctypes.data_as(ctypes.POINTER(c_double)), tab.size // 8)
+    elif kind == "rot_general_unitary":
+        mat = spec[2]
+        call("sq_rot_general_unitary", h, spec[1], mat.ctypes.data_as(ctypes.POINTER(c_double)), spec[3],
+             byref(spec[4]), 1 if spec[5] else 0)
+    elif kind == "hadamard_partial":
+        pos = (c_uint32 * len(spec[2]))(*spec[2])
+        call("sq_hadamard_partial", h, spec[1], pos, len(spec[2]), byref(spec[3]))
     elif kind == "clear_zero":
         call("sq_clear_zero", h, spec[1])
     elif kind == "normalize":
@@ -547,6 +557,65 @@ class CondRot_Rational_Bool(BaseOperator):
 
 
 CondRot_Fixed_Bool = CondRot_Rational_Bool
+
+
+class CondRot_General_Bool(BaseOperator):
+    """2x2 unitary func(v) on the 1-bit `out`, v = value of `in`
+    (CondRot_General_Bool_Fast<F>, condrot.h:149-300). `func(v)` returns the
+    four elements (m00, m01, m10, m11); it is evaluated on the host for every
+    v < 2^width(in) and the table is uploaded."""
+
+    has_dag = False
+
+    def __init__(self, reg_in, reg_out, func):
+        super().__init__()
+        import numpy as np
+        self.in_id, self.out_id = _R(reg_in), _R(reg_out)
+        if System.type_of(self.out_id) != StateStorageType.Boolean or System.size_of(self.out_id) != 1:
+            raise ValueError("CondRot_General_Bool: output must be a 1-bit Boolean register")
+        n = 1 << System.size_of(self.in_id)
+        tab = np.zeros((n, 8), dtype=np.float64)
+        for v in range(n):
+            m = [complex(x) for x in func(v)]
+            tab[v] = [m[0].real, m[0].imag, m[1].real, m[1].imag, m[2].real, m[2].imag, m[3].real, m[3].imag]
+        self.table = np.ascontiguousarray(tab.reshape(-1))
+
+    def spec(self, dag=False):
+        return ("condrot_general", self.in_id, self.out_id, self.table)
+
+
+class Rot_GeneralUnitary(BaseOperator):
+    """Dense 2^k x 2^k unitary on a k-bit register (rot.cpp:353-477); dag
+    applies the conjugate transpose."""
+
+    def __init__(self, reg, mat):
+        super().__init__()
+        import numpy as np
+        self.id = _R(reg)
+        m = np.asarray(mat, dtype=np.complex128)
+        dim = 1 << System.size_of(self.id)
+        if m.shape != (dim, dim):
+            raise ValueError("Matrix size does not match the register's size.")
+        self.dim = dim
+        self.mat = np.ascontiguousarray(m).view(np.float64).reshape(-1).copy()
+
+    def spec(self, dag=False):
+        return ("rot_general_unitary", self.id, self.mat, self.dim, self._cond(), dag)
+
+
+class Hadamard_Partial(SelfAdjointOperator):
+    """H on one bit position of a register (hadamard.cpp:470-712; the
+    reference's active path is defined for a single position)."""
+
+    def __init__(self, reg, positions):
+        super().__init__()
+        self.id = _R(reg)
+        self.positions = sorted(int(p) for p in positions)
+        if len(self.positions) != 1:
+            raise ValueError("Hadamard_Partial: exactly one position is supported")
+
+    def spec(self, dag=False):
+        return ("hadamard_partial", self.id, self.positions, self._cond())
 
 
 class ClearZero(SelfAdjointOperator):

@@ -18,11 +18,13 @@ pytestmark = pytest.mark.gpu
 U = ps.UnsignedInteger
 
 
-@pytest.fixture(params=["sort", "hash"])
+@pytest.fixture(params=["sort", "hash", "hash-exact"])
 def strategy(request):
-    ps.set_group_strategy(request.param)
+    ps.set_group_strategy(request.param.split("-")[0])
+    ps.set_output_sizing("exact" if request.param.endswith("exact") else "auto")
     yield request.param
     ps.set_group_strategy("auto")
+    ps.set_output_sizing("auto")
 
 
 def random_state(rng, widths, n, types=None):
