@@ -298,6 +298,22 @@ int sq_get_clearzero_eps(double* eps);
 /* ClearZero (system_operations.cpp:371-382): drop entries with |a|^2 < eps;
  * order of survivors is preserved. */
 int sq_clear_zero(sq_state* st, double eps);
+/* ClearZero for callers that must not have the library allocate device
+ * memory (programs that own every device buffer through their own pool or
+ * framework allocator; loops where an implicit cudaMalloc, which may
+ * synchronize the device, is not allowed). No counterpart in the reference.
+ * Inputs and outputs are the caller's device arrays: k key-word arrays of n
+ * words each plus n interleaved complex amplitudes in, the same layout out
+ * (capacity >= n), survivor count to *n_out (host). The only scratch is a
+ * fixed 262,400-byte static device array inside this library, so n is capped
+ * at SQ_NOALLOC_MAX_ENTRIES; larger n returns SQ_ERR_CAPACITY. Work is issued
+ * on `stream` (NULL = the default stream) and the call waits for it. The
+ * first call on each device looks up that array's device address with the
+ * device current; make that first call before capturing any stream. All calls
+ * share the array: calls that overlap on the GPU race. */
+#define SQ_NOALLOC_MAX_ENTRIES (1ull << 26)
+int sq_clear_zero_noalloc(const uint64_t* const* keys_in, const double* amps_in, uint32_t k, uint64_t n, double eps,
+                          uint64_t* const* keys_out, double* amps_out, uint64_t* n_out, void* stream);
 /* Normalize (dark_magic.cpp:11-32): a *= 1/sqrt(sum |a|^2); norm_sq_out may be NULL. */
 int sq_normalize(sq_state* st, double* norm_sq_out);
 /* Sum of |a|^2 (CheckNormalization's quantity, debugger.h). */

@@ -140,6 +140,8 @@ _SIGS = [
     ("sq_set_clearzero_eps", c_int, [c_double]),
     ("sq_get_clearzero_eps", c_int, [POINTER(c_double)]),
     ("sq_clear_zero", c_int, [c_void_p, c_double]),
+    ("sq_clear_zero_noalloc", c_int, [POINTER(c_void_p), c_void_p, c_uint32, c_uint64, c_double, POINTER(c_void_p),
+                                      c_void_p, POINTER(c_uint64), c_void_p]),
     ("sq_normalize", c_int, [c_void_p, POINTER(c_double)]),
     ("sq_norm_sq", c_int, [c_void_p, POINTER(c_double)]),
     ("sq_add_systems", c_int, [c_void_p, c_void_p, c_double]),

@@ -28,6 +28,10 @@ using namespace sq;
 
 static thread_local std::string t_err;
 
+namespace sq {
+void set_last_error(const std::string& msg) { t_err = msg; }
+}  // namespace sq
+
 #define SQ_API_BEGIN try {
 #define SQ_API_END                                   \
     return SQ_OK;                                    \

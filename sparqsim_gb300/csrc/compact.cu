@@ -221,4 +221,97 @@ void scale_amp(State& s, double k) {
     SQ_CUDA(cudaGetLastError());
 }
 
+// ------------------------------------------------------------------ ClearZero without allocation
+// Some callers may not let a library allocate device memory on their behalf:
+// programs that hand out all GPU memory from their own pre-planned pool or
+// framework allocator, and latency-critical loops where a hidden cudaMalloc
+// (which can synchronize the device) is not acceptable. For them this entry
+// point compacts caller-owned arrays into caller-owned arrays and takes its
+// only scratch, the decoupled look-back status, from one fixed device array
+// declared below: 8 * (32 + 32768) bytes, enough for up to 2^26 entries.
+// That array lives in every GPU that loads this library until the process
+// exits, and all calls share it, so two calls whose work overlaps on the GPU
+// (different streams, different host threads) race on it.
+constexpr uint64_t kNoAllocMaxEntries = 1ull << 26;
+constexpr uint64_t kNoAllocTiles = kNoAllocMaxEntries / kCzTile;
+constexpr uint64_t kNoAllocHeaderWords = 32;  // [0] tile counter, [1] survivor total, [2] error word
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocHeaderWords + kNoAllocTiles];
+
+constexpr int kNoAllocMaxDevices = 64;
+static unsigned long long* g_noalloc_dev_ptr[kNoAllocMaxDevices] = {nullptr};
+
+template <int K>
+static void launch_cz_noalloc(const uint64_t* const* keys_in, const double* amps_in, uint64_t* const* keys_out,
+                              double* amps_out, uint64_t n, double eps, unsigned long long* scratch, long long nt,
+                              cudaStream_t s) {
+    ConstKeyPtrs ik;
+    KeyPtrs okp;
+    for (int w = 0; w < SQ_KMAX; ++w) {
+        ik.w[w] = w < K ? keys_in[w] : nullptr;
+        okp.w[w] = w < K ? keys_out[w] : nullptr;
+    }
+    LookbackWs lb;
+    lb.counter = (unsigned*)scratch;
+    lb.total = scratch + 1;
+    lb.status = scratch + kNoAllocHeaderWords;
+    clearzero_kernel<K><<<(unsigned)nt, kCzBlock, 0, s>>>(ik, (const double2*)amps_in, okp, (double2*)amps_out, n, eps,
+                                                          lb, nt, (unsigned*)(scratch + 2));
+    count_launch();
+}
+
 }  // namespace sq
+
+extern "C" int sq_clear_zero_noalloc(const uint64_t* const* keys_in, const double* amps_in, uint32_t k, uint64_t n,
+                                     double eps, uint64_t* const* keys_out, double* amps_out, uint64_t* n_out,
+                                     void* stream_handle) {
+    using namespace sq;
+    auto bad = [&](int code, const char* msg) {
+        set_last_error(std::string("sq_clear_zero_noalloc: ") + msg);
+        return code;
+    };
+    if (!n_out) return bad(SQ_ERR_INVALID, "null n_out");
+    if (k < 1 || k > SQ_KMAX) return bad(SQ_ERR_INVALID, "k must be 1..SQ_MAX_KEY_WORDS");
+    if (n > kNoAllocMaxEntries) return bad(SQ_ERR_CAPACITY, "n exceeds SQ_NOALLOC_MAX_ENTRIES (2^26)");
+    if (n > 0 && (!keys_in || !amps_in || !keys_out || !amps_out)) return bad(SQ_ERR_INVALID, "null array");
+    for (uint32_t w = 0; n > 0 && w < k; ++w)
+        if (!keys_in[w] || !keys_out[w]) return bad(SQ_ERR_INVALID, "null key-word array");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
+        return bad(SQ_ERR_CUDA, "no current CUDA device");
+    // One-time set-up per device, with that device current: the host-side name
+    // of a __device__ array is not its device address, so ask the runtime.
+    if (!g_noalloc_dev_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return bad(SQ_ERR_CUDA, cudaGetErrorString(e));
+        g_noalloc_dev_ptr[dev] = (unsigned long long*)p;
+    }
+    if (n == 0) {
+        *n_out = 0;
+        return SQ_OK;
+    }
+    cudaStream_t s = (cudaStream_t)stream_handle;
+    unsigned long long* scratch = g_noalloc_dev_ptr[dev];
+    const long long nt = (long long)((n + kCzTile - 1) / kCzTile);
+    // the look-back status, tile counter, total and error word must start at zero
+    if (cudaMemsetAsync(scratch, 0, (size_t)(kNoAllocHeaderWords + nt) * 8, s) != cudaSuccess)
+        return bad(SQ_ERR_CUDA, "cudaMemsetAsync failed");
+    switch (k) {
+        case 1: launch_cz_noalloc<1>(keys_in, amps_in, keys_out, amps_out, n, eps, scratch, nt, s); break;
+        case 2: launch_cz_noalloc<2>(keys_in, amps_in, keys_out, amps_out, n, eps, scratch, nt, s); break;
+        case 3: launch_cz_noalloc<3>(keys_in, amps_in, keys_out, amps_out, n, eps, scratch, nt, s); break;
+        case 4: launch_cz_noalloc<4>(keys_in, amps_in, keys_out, amps_out, n, eps, scratch, nt, s); break;
+        case 5: launch_cz_noalloc<5>(keys_in, amps_in, keys_out, amps_out, n, eps, scratch, nt, s); break;
+        case 6: launch_cz_noalloc<6>(keys_in, amps_in, keys_out, amps_out, n, eps, scratch, nt, s); break;
+        case 7: launch_cz_noalloc<7>(keys_in, amps_in, keys_out, amps_out, n, eps, scratch, nt, s); break;
+        default: launch_cz_noalloc<8>(keys_in, amps_in, keys_out, amps_out, n, eps, scratch, nt, s); break;
+    }
+    if (cudaGetLastError() != cudaSuccess) return bad(SQ_ERR_CUDA, "kernel launch failed");
+    unsigned long long hdr[3] = {0, 0, 0};
+    if (cudaMemcpyAsync(hdr, scratch, sizeof(hdr), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return bad(SQ_ERR_CUDA, "reading the survivor count failed");
+    if (hdr[2] & 0xffffffffull) return bad(SQ_ERR_DEVICE_TIMEOUT, "a bounded look-back wait gave up");
+    *n_out = hdr[1];
+    return SQ_OK;
+}

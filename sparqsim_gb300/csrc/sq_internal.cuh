@@ -26,6 +26,8 @@ struct Error {
     std::string msg;
 };
 [[noreturn]] void fail(int code, const std::string& msg);
+// Message returned by sq_last_error() on this thread.
+void set_last_error(const std::string& msg);
 void cuda_check(cudaError_t e, const char* what);
 #define SQ_CUDA(x) ::sq::cuda_check((x), #x)
 
