@@ -122,7 +122,14 @@ typedef enum {
     SQ_OP_REFLECTION_BOOL = 67,      /* parallel_phase_operations.cpp:46-70 regs reg0..reg[imm0-1], imm1 = inverse */
     SQ_OP_ZERO_COND_PHASE_FLIP = 68, /* parallel_phase_operations.cpp:11-31 regs reg0..reg[imm0-1] */
     SQ_OP_ROT_DIAGONAL = 69,         /* basic_gates.cpp:110-133 amp *= (bit ? c1 : c0) */
-    SQ_OP_ROT_OFF_DIAGONAL = 70      /* basic_gates.cpp:146-171 flip bit, amp *= (bit ? c1 : c0) */
+    SQ_OP_ROT_OFF_DIAGONAL = 70,     /* basic_gates.cpp:146-171 flip bit, amp *= (bit ? c1 : c0) */
+    /* Per-trajectory Pauli noise for batched trajectories (no single reference
+     * operator; equivalent to X_Bool / Z_Bool conditioned_by_value on the
+     * trajectory register): t = reg0; if t < imm0, with masks
+     * w[6t .. 6t+5] = (xa, xb, xc, za, zb, zc) read from `qram`:
+     * reg1 ^= xa, reg2 ^= xb, reg3 ^= xc, then
+     * amp *= (-1)^(popcount(reg1 & za) + popcount(reg2 & zb) + popcount(reg3 & zc)). */
+    SQ_OP_PAULI_NOISE = 71
 } sq_opcode;
 
 /* One elementwise instruction. Register ids in reg[], integer constants in
@@ -256,6 +263,11 @@ int sq_zero_cond_phase_flip(sq_state* st, const uint32_t* regs, uint32_t nregs, 
 /* Hadamard_Int (hadamard.cpp:18-162): H on the low n_digits bits of reg;
  * groups = entries equal on every other active bit; ClearZero(eps) after. */
 int sq_hadamard_int(sq_state* st, uint32_t reg, uint32_t n_digits, const sq_cond* cond);
+/* Batched Hadamard_Int: H on the low n bits of reg where n is each entry's
+ * value of `width_reg` (n <= max_digits <= 8). Equivalent to applying
+ * Hadamard_Int(reg, h).conditioned_by_value(width_reg, h) for every h, in one
+ * pass; used to run trajectories of different widths in one state. */
+int sq_hadamard_int_batched(sq_state* st, uint32_t reg, uint32_t width_reg, uint32_t max_digits, const sq_cond* cond);
 /* Hadamard_Int_Full (hadamard.cpp:181-338): H on the whole register. */
 int sq_hadamard_int_full(sq_state* st, uint32_t reg, const sq_cond* cond);
 /* Hadamard_Bool (hadamard.cpp:340-439): reg must be 1 bit wide. */

@@ -46,6 +46,9 @@ def lib():
             "sqo_rot_bool": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), POINTER(SqCond), c_int]),
             "sqo_condrot": (c_int, [c_void_p, c_uint32, c_uint32, c_int]),
             "sqo_clear_zero": (c_int, [c_void_p, c_double]),
+            "sqo_condrot_general": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), c_uint64]),
+            "sqo_rot_general_unitary": (c_int, [c_void_p, c_uint32, POINTER(c_double), c_uint64, POINTER(SqCond), c_int]),
+            "sqo_hadamard_partial": (c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_uint32, POINTER(SqCond)]),
             "sqo_normalize": (c_int, [c_void_p, POINTER(c_double)]),
             "sqo_add_systems": (c_int, [c_void_p, c_void_p, c_double]),
             "sqo_add_register_sync": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_uint32)]),
@@ -179,6 +182,20 @@ def apply(state: OracleState, spec) -> None:
         _chk(L.sqo_apply(h, arr, len(instrs)))
     elif kind == "hadamard_int":
         _chk(L.sqo_hadamard_int(h, spec[1], spec[2], byref(spec[3])))
+    elif kind == "hadamard_int_batched":
+        # reference composition: Hadamard_Int(reg, h).conditioned_by_value(width_reg, h) for each h
+        from sparqsim_gb300._native import COND_VALUE, SqCond
+        reg, wreg, maxd, cond = spec[1], spec[2], spec[3], spec[4]
+        for hd in range(1, maxd + 1):
+            c = SqCond()
+            ctypes.pointer(c)[0] = cond
+            if c.count >= 8:
+                raise ValueError("too many conditions")
+            c.c[c.count].kind = COND_VALUE
+            c.c[c.count].reg = wreg
+            c.c[c.count].param = hd
+            c.count += 1
+            _chk(L.sqo_hadamard_int(h, reg, hd, byref(c)))
     elif kind == "hadamard_int_full":
         _chk(L.sqo_hadamard_int_full(h, spec[1], byref(spec[2])))
     elif kind == "hadamard_bool":
@@ -188,6 +205,16 @@ def apply(state: OracleState, spec) -> None:
         _chk(L.sqo_rot_bool(h, spec[1], spec[2], m, byref(spec[4]), 0))
     elif kind == "condrot":
         _chk(L.sqo_condrot(h, spec[1], spec[2], 1 if spec[3] else 0))
+    elif kind == "condrot_general":
+        tab = spec[3]
+        _chk(L.sqo_condrot_general(h, spec[1], spec[2], tab.ctypes.data_as(POINTER(c_double)), tab.size // 8))
+    elif kind == "rot_general_unitary":
+        mat = spec[2]
+        _chk(L.sqo_rot_general_unitary(h, spec[1], mat.ctypes.data_as(POINTER(c_double)), spec[3], byref(spec[4]),
+                                       1 if spec[5] else 0))
+    elif kind == "hadamard_partial":
+        pos = (c_uint32 * len(spec[2]))(*spec[2])
+        _chk(L.sqo_hadamard_partial(h, spec[1], pos, len(spec[2]), byref(spec[3])))
     elif kind == "clear_zero":
         _chk(L.sqo_clear_zero(h, spec[1]))
     elif kind == "normalize":

@@ -402,6 +402,19 @@ static void apply_instr_entry(System& s, const sq_instr& in) {
             v ^= pow2(in.imm[0]);
             return;
         }
+        case SQ_OP_PAULI_NOISE: {  // per-trajectory X then Z masks (batched trajectories)
+            const Qram* q = reinterpret_cast<const Qram*>(in.qram);
+            uint64_t t = get_as(s, r[0]);
+            if (t >= in.imm[0]) return;
+            int parity = 0;
+            for (int k = 0; k < 3; ++k) {
+                uint64_t& v = s.get(r[k + 1]);
+                v ^= q->memory[t * 6 + k];
+                parity += bitcount(v & q->memory[t * 6 + 3 + k]);
+            }
+            if (parity & 1) s.amplitude = complex_t(s.amplitude.real() * -1.0, s.amplitude.imag() * -1.0);
+            return;
+        }
         default:
             throw std::invalid_argument("unknown opcode " + std::to_string(in.op));
     }
@@ -768,6 +781,140 @@ static void condrot(State& st, size_t reg_in, size_t reg_out, bool dag) {
     clear_zero(st, g_clearzero_eps);
 }
 
+// ---------------------------------------------------------------- CondRot_General_Bool_Fast
+// condrot.h:149-300 with SAFE_HASH; the callable is a table of 2x2 matrices
+static void condrot_general(State& st, size_t in_id, size_t out_id, const complex_t* table) {
+    if (st.empty()) return;
+    std::map<System, size_t, LessExceptKey> buckets(LessExceptKey{out_id});
+    auto mat_of = [&](size_t k) { return table + 4 * as_u64(st[k].get(in_id), size_of(in_id)); };
+    auto op_pair = [&](size_t zero, size_t one) {
+        const complex_t* m = mat_of(zero);
+        complex_t a = st[zero].amplitude, b = st[one].amplitude;
+        st[zero].amplitude = cmul(a, m[0]) + cmul(b, m[1]);
+        st[one].amplitude = cmul(a, m[2]) + cmul(b, m[3]);
+    };
+    size_t current_size = st.size();
+    for (size_t i = 0; i < current_size; ++i) {
+        auto iter = buckets.find(st[i]);
+        if (iter == buckets.end()) { buckets.insert({st[i], i}); continue; }
+        if (as_u64(st[iter->second].get(out_id), 1)) op_pair(i, iter->second);
+        else op_pair(iter->second, i);
+        buckets.erase(iter);
+    }
+    for (auto& kv : buckets) {
+        size_t k = kv.second;
+        const complex_t* m = mat_of(k);
+        System c = st[k];
+        if (as_u64(st[k].get(out_id), 1)) {  // operate_alone_one
+            st.push_back(c);
+            st.back().get(out_id) = 0;
+            st.back().amplitude = cmul(st.back().amplitude, m[1]);
+            st[k].amplitude = cmul(st[k].amplitude, m[3]);
+        } else {  // operate_alone_zero
+            st.push_back(c);
+            st.back().get(out_id) = 1;
+            st[k].amplitude = cmul(st[k].amplitude, m[0]);
+            st.back().amplitude = cmul(st.back().amplitude, m[2]);
+        }
+    }
+    clear_zero(st, g_clearzero_eps);
+}
+
+// ---------------------------------------------------------------- Rot_GeneralUnitary
+// rot.cpp:353-477 with SAFE_HASH
+static void rot_general_unitary(State& st, size_t id, const complex_t* mat, bool dagger, const sq_cond* cond) {
+    if (st.empty()) return;
+    size_t full_size = (size_t)pow2(size_of(id));
+    auto bucket_op = [&](const std::vector<size_t>& positions) {
+        std::vector<complex_t> amps(positions.size());
+        for (size_t i = 0; i < positions.size(); ++i) amps[i] = st[positions[i]].amplitude;
+        std::vector<complex_t> new_amps(positions.size(), 0);
+        for (size_t i = 0; i < full_size; ++i)
+            for (size_t j = 0; j < full_size; ++j) {
+                complex_t m = dagger ? std::conj(mat[j * full_size + i]) : mat[i * full_size + j];
+                new_amps[i] += cmul(m, amps[j]);
+            }
+        for (size_t i = 0; i < positions.size(); ++i) st[positions[i]].amplitude = new_amps[i];
+    };
+    std::map<System, std::pair<size_t, std::vector<size_t>>, LessExceptKey> buckets(LessExceptKey{id});
+    size_t current_size = st.size();
+    for (size_t i = 0; i < current_size; ++i) {
+        if (!condition_satisfied(st[i], cond)) continue;
+        uint64_t val = get_as(st[i], id);
+        auto res = buckets.insert({st[i], {0, std::vector<size_t>(full_size, (size_t)-1)}});
+        auto iter = res.first;
+        iter->second.second[val] = i;
+        iter->second.first += 1;
+        if (iter->second.first == full_size) {
+            bucket_op(iter->second.second);
+            buckets.erase(iter);
+        }
+    }
+    for (auto& kv : buckets) {
+        auto& all_pos = kv.second.second;
+        for (size_t i = 0; i < all_pos.size(); ++i)
+            if (all_pos[i] == (size_t)-1) {
+                st.push_back(kv.first);
+                st.back().get(id) = i;
+                st.back().amplitude = 0;
+                all_pos[i] = st.size() - 1;
+            }
+        bucket_op(all_pos);
+    }
+    clear_zero(st, g_clearzero_eps);
+}
+
+// ---------------------------------------------------------------- Hadamard_Partial (one position)
+// hadamard.cpp:619-711 (use_hash path): buckets equal except the chosen bit
+static void hadamard_partial1(State& st, size_t id, size_t pos) {
+    if (st.empty()) return;
+    uint64_t bit = pow2(pos);
+    struct Less {
+        size_t id;
+        uint64_t bit;
+        bool operator()(const System& a, const System& b) const {
+            for (size_t i = 0; i < g_regs.size(); ++i) {
+                if (!status_of(i)) continue;
+                uint64_t x = a.get(i), y = b.get(i);
+                if (i == id) { x &= ~bit; y &= ~bit; }
+                if (x < y) return true;
+                if (x > y) return false;
+            }
+            return false;
+        }
+    };
+    std::map<System, size_t, Less> buckets(Less{id, bit});
+    auto op_pair = [&](size_t zero, size_t one) {
+        complex_t a = st[zero].amplitude, b = st[one].amplitude;
+        st[zero].amplitude = cscale(a, kSqrt2Inv) + cscale(b, kSqrt2Inv);
+        st[one].amplitude = cscale(a, kSqrt2Inv) - cscale(b, kSqrt2Inv);
+    };
+    size_t current_size = st.size();
+    for (size_t i = 0; i < current_size; ++i) {
+        auto iter = buckets.find(st[i]);
+        if (iter == buckets.end()) { buckets.insert({st[i], i}); continue; }
+        if (st[iter->second].get(id) & bit) op_pair(i, iter->second);
+        else op_pair(iter->second, i);
+        buckets.erase(iter);
+    }
+    for (auto& kv : buckets) {
+        size_t k = kv.second;
+        System c = st[k];
+        if (st[k].get(id) & bit) {  // operate_alone_one
+            st.push_back(c);
+            st.back().get(id) &= ~bit;
+            st.back().amplitude = cscale(st.back().amplitude, kSqrt2Inv);
+            st[k].amplitude = cscale(st[k].amplitude, -kSqrt2Inv);
+        } else {  // operate_alone_zero
+            st.push_back(c);
+            st.back().get(id) |= bit;
+            st[k].amplitude = cscale(st[k].amplitude, kSqrt2Inv);
+            st.back().amplitude = cscale(st.back().amplitude, kSqrt2Inv);
+        }
+    }
+    clear_zero(st, g_clearzero_eps);
+}
+
 // ---------------------------------------------------------------- Normalize / add_systems
 static double normalize(State& st) {  // dark_magic.cpp:11-32
     double sum_prob = 0.0;
@@ -925,6 +1072,29 @@ int sqo_rot_bool(void* h, uint32_t reg, uint32_t digit, const double* m8, const 
 }
 int sqo_condrot(void* h, uint32_t reg_in, uint32_t reg_out, int dag) {
     SQO_TRY(condrot(*static_cast<State*>(h), reg_in, reg_out, dag != 0))
+}
+int sqo_condrot_general(void* h, uint32_t reg_in, uint32_t reg_out, const double* table, uint64_t n_values) {
+    SQO_TRY({
+        if (n_values != pow2(size_of(reg_in))) throw std::invalid_argument("table size");
+        std::vector<complex_t> t(4 * n_values);
+        for (uint64_t i = 0; i < 4 * n_values; ++i) t[i] = complex_t(table[2 * i], table[2 * i + 1]);
+        condrot_general(*static_cast<State*>(h), reg_in, reg_out, t.data());
+    })
+}
+int sqo_rot_general_unitary(void* h, uint32_t reg, const double* mat, uint64_t dim, const sq_cond* cond, int dag) {
+    SQO_TRY({
+        if (dim != pow2(size_of(reg))) throw std::invalid_argument("matrix size");
+        std::vector<complex_t> m(dim * dim);
+        for (uint64_t i = 0; i < dim * dim; ++i) m[i] = complex_t(mat[2 * i], mat[2 * i + 1]);
+        rot_general_unitary(*static_cast<State*>(h), reg, m.data(), dag != 0, cond);
+    })
+}
+int sqo_hadamard_partial(void* h, uint32_t reg, const uint32_t* positions, uint32_t n, const sq_cond* cond) {
+    SQO_TRY({
+        if (n != 1) throw std::invalid_argument("one position");
+        (void)cond;
+        hadamard_partial1(*static_cast<State*>(h), reg, positions[0]);
+    })
 }
 int sqo_clear_zero(void* h, double eps) { SQO_TRY(clear_zero(*static_cast<State*>(h), eps)) }
 int sqo_normalize(void* h, double* norm_sq) {

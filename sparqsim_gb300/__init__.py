@@ -15,7 +15,8 @@ from .operators import (Abs_SInt, Add_AnyInt_AnyInt_InPlace, Add_ConstUInt_InPla
                         Add_Mult_UInt_ConstUInt_InPlace, Add_UInt_ConstUInt, Add_UInt_UInt,
                         Add_UInt_UInt_InPlace, AddRegister, And_UInt_UInt, Assign, BaseOperator,
                         Carry_UInt_UInt, ClearZero, CombineRegister, Compare_UInt_UInt, CondRot_Fixed_Bool,
-                        CondRot_General_Bool, Hadamard_Partial, Rot_GeneralUnitary,
+                        CondRot_General_Bool, Hadamard_Partial, Rot_GeneralUnitary, Hadamard_Int_Batched,
+                        NoiseTable, PauliNoise,
                         CondRot_Rational_Bool, Div_UInt_UInt, ElementwiseOperator, FlipBools, Fused,
                         GetMid_UInt_UInt, GlobalPhase, Hadamard_Bool, Hadamard_Int, Hadamard_Int_Full,
                         Init_Unsafe, IsZero_UInt, Less_SInt_SInt, Less_UInt_UInt,

@@ -34,6 +34,7 @@ OP = dict(
     ADD_ANYINT_INPLACE=28, ASSIGN=29, COMPARE_UINT_UINT=30, LESS_UINT_UINT=31, SWAP_GENERAL=32,
     GETMID_UINT_UINT=33, X_BOOL=34, INIT_UNSAFE=35, QRAM_LOAD=36, PHASE_BOOL=64, GLOBAL_PHASE=65,
     Y_BOOL=66, REFLECTION_BOOL=67, ZERO_COND_PHASE_FLIP=68, ROT_DIAGONAL=69, ROT_OFF_DIAGONAL=70,
+    PAULI_NOISE=71,
 )
 
 
@@ -126,6 +127,7 @@ _SIGS = [
     ("sq_reflection_bool", c_int, [c_void_p, POINTER(c_uint32), c_uint32, c_int, POINTER(SqCond)]),
     ("sq_zero_cond_phase_flip", c_int, [c_void_p, POINTER(c_uint32), c_uint32, POINTER(SqCond)]),
     ("sq_hadamard_int", c_int, [c_void_p, c_uint32, c_uint32, POINTER(SqCond)]),
+    ("sq_hadamard_int_batched", c_int, [c_void_p, c_uint32, c_uint32, c_uint32, POINTER(SqCond)]),
     ("sq_hadamard_int_full", c_int, [c_void_p, c_uint32, POINTER(SqCond)]),
     ("sq_hadamard_bool", c_int, [c_void_p, c_uint32, POINTER(SqCond)]),
     ("sq_rot_bool", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), POINTER(SqCond), c_int]),

@@ -565,6 +565,26 @@ int sq_hadamard_int(sq_state* st, uint32_t reg, uint32_t n_digits, const sq_cond
     SQ_API_END
 }
 
+int sq_hadamard_int_batched(sq_state* st, uint32_t reg, uint32_t width_reg, uint32_t max_digits, const sq_cond* cond) {
+    SQ_API_BEGIN
+    need(reg != width_reg, "batched Hadamard: width register must differ from the target");
+    Field f = regtable().field(reg);
+    Field w = regtable().field(width_reg);
+    need(max_digits >= 1 && max_digits <= 8, "batched Hadamard: max_digits must be 1..8");
+    need(max_digits <= f.width, "batched Hadamard: max_digits larger than the register");
+    need(w.width >= 1, "batched Hadamard: empty width register");
+    GroupSpec g;
+    memset(&g, 0, sizeof(g));
+    g.mode = GM_HADAMARD_INT;
+    g.target = f;
+    g.target.width = (uint8_t)max_digits;
+    g.varw = w;
+    g.cond = resolve_cond(cond);
+    g.eps = cz_eps();
+    group_transform(S(st), g);
+    SQ_API_END
+}
+
 int sq_hadamard_int_full(sq_state* st, uint32_t reg, const sq_cond* cond) {
     SQ_API_BEGIN
     Field f = regtable().field(reg);

@@ -116,6 +116,8 @@ void check_device_error() {
     SQ_CUDA(cudaStreamSynchronize(stream()));
     if (v) {
         SQ_CUDA(cudaMemsetAsync(device_error_word(), 0, 4, stream()));
+        if (v & 4u) fail(SQ_ERR_INVALID, "batched Hadamard: an entry's digit count exceeds max_digits");
+        if (v & 2u) fail(SQ_ERR_DEVICE_TIMEOUT, "hash grouping gave up (table full or a bounded wait expired)");
         fail(SQ_ERR_DEVICE_TIMEOUT, "a bounded device-side wait gave up (decoupled look-back)");
     }
 }

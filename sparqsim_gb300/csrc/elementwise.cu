@@ -246,6 +246,27 @@ __device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2
             fset<K>(k, f[0], v ^ (1ull << in.imm[0]));
             break;
         }
+        case SQ_OP_PAULI_NOISE: {
+            const uint64_t t = fget<K>(k, f[0]);
+            if (t >= in.imm[0]) break;
+            uint64_t m[6];
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                const uint64_t idx = t * 6 + r;
+                if (in.elem_bytes == 2) m[r] = __ldg((const unsigned short*)in.table + idx);
+                else if (in.elem_bytes == 4) m[r] = __ldg((const unsigned int*)in.table + idx);
+                else m[r] = __ldg((const unsigned long long*)in.table + idx);
+            }
+            int parity = 0;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                const uint64_t v = fget<K>(k, f[r + 1]) ^ m[r];
+                fset<K>(k, f[r + 1], v);
+                parity += __popcll(v & m[r + 3]);
+            }
+            if (parity & 1) a = make_double2(a.x * -1.0, a.y * -1.0);
+            break;
+        }
         default: break;
     }
 }
@@ -448,6 +469,16 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
             if (in.imm[0] >= d.f[0].width) fail(SQ_ERR_INVALID, "Rot_Bool: digit >= register size");
             am |= 3u;
             break;
+        case SQ_OP_PAULI_NOISE: {
+            R(0); W(1); W(2); W(3);
+            const QramTable* q = reinterpret_cast<const QramTable*>(in.qram);
+            if (!q || !q->dev) fail(SQ_ERR_INVALID, "Pauli noise: null mask table");
+            if (q->n_words < 6 * in.imm[0]) fail(SQ_ERR_INVALID, "Pauli noise: table smaller than 6 words per trajectory");
+            d.table = q->dev;
+            d.elem_bytes = q->elem_bytes;
+            am |= 3u;
+            break;
+        }
         default: fail(SQ_ERR_INVALID, "unknown opcode " + std::to_string(in.op));
     }
 }

@@ -318,6 +318,7 @@ struct EmitArgs {
     const double2* mtable;     // CondRot_General_Bool: 4 matrix elements per input value
     const double2* umat;       // Rot_GeneralUnitary: S x S row-major
     int udag;                  // Rot_GeneralUnitary: apply the conjugate transpose
+    Field varw;                // batched Hadamard: each group's digit count is this field of its key
 };
 
 template <int K>
@@ -501,25 +502,30 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
     __shared__ unsigned s_tmp[8];
     __shared__ uint64_t s_member_t[8][64];
     __shared__ double2 s_member_a[8][64];
-    const unsigned S = 1u << a.nbits;
+    const unsigned Smax = 1u << a.nbits;
     const unsigned wid = W == 32 ? (threadIdx.x >> 5) : 0u;
     const unsigned t = W == 32 ? (threadIdx.x & 31u) : threadIdx.x;
-    double2* slots = s_slots + (size_t)wid * S;
+    double2* slots = s_slots + (size_t)wid * Smax;
     const uint64_t workers_per_block = blockDim.x / W;
     const uint64_t stride = (uint64_t)gridDim.x * workers_per_block;
-    const Field tg = a.target;
     for (uint64_t g = (uint64_t)blockIdx.x * workers_per_block + wid; g < a.groups; g += stride) {
         const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
         const unsigned m = s1 - s0;
         uint64_t gk[K];
         load_key<K>(a.in_keys, group_head<BUCKET>(a, g, s0), gk);
-        const bool sparse_full = a.mode == GM_HADAMARD_FULL && m <= (unsigned)(a.nbits - 1);
+        // batched Hadamard: this group's digit count comes from its key
+        const int nbits = a.varw.width ? (int)fget<K>(gk, a.varw) : a.nbits;
+        const unsigned S = 1u << nbits;
+        const double extra = a.varw.width ? 1.0 / sqrt((double)S) : a.extra;
+        Field tg = a.target;
+        tg.width = (uint8_t)nbits;
+        const bool sparse_full = a.mode == GM_HADAMARD_FULL && m <= (unsigned)(nbits - 1);
         if (a.mode == GM_HADAMARD_INT && m == 1) {
             // singleton: a * 2^{-n/2}, sign (-1)^{popcount(t & v)} (hadamard.cpp:27-42)
             uint64_t v0;
             double2 a0;
             member_at<BUCKET>(a, s0, v0, a0);
-            const double2 base = cscale(a0, a.extra);
+            const double2 base = cscale(a0, extra);
             const bool keep = keep_amp(base, a.eps);
             if (!WRITE) {
                 if (t == 0) a.cnt[g] = keep ? S : 0u;
@@ -567,7 +573,7 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
                 double2 acc = make_double2(0.0, 0.0);
                 for (unsigned j = 0; j < m; ++j) {
                     double2 term = cscale(s_member_a[wid][j], (__popcll((uint64_t)c & s_member_t[wid][j]) & 1) ? -1. : 1.);
-                    term = cscale(term, a.extra);
+                    term = cscale(term, extra);
                     acc = cadd(acc, term);
                 }
                 slots[c] = acc;
@@ -607,7 +613,7 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
                 }
                 worker_sync<W>();
             }
-            for (int qn = 0; a.mode != GM_UNITARY && qn < a.nbits; ++qn) {
+            for (int qn = 0; a.mode != GM_UNITARY && qn < nbits; ++qn) {
                 const unsigned h = 1u << qn;
                 for (unsigned p = t; p < S / 2; p += W) {
                     const unsigned i0 = ((p >> qn) << (qn + 1)) | (p & (h - 1u));
@@ -740,11 +746,20 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
 #pragma unroll
             for (int j = 0; j < 16; ++j) sl[((unsigned)j << 8) | tid] = make_double2(0.0, 0.0);
             __syncthreads();
-            for (unsigned j = tid; j < m; j += 256u) {
-                uint64_t tj;
-                double2 aj;
-                member_at<BUCKET>(a, s0 + j, tj, aj);
-                sl[tj] = aj;
+            // members: 8 independent loads in flight per thread, then scatter
+            for (unsigned j0 = 0; j0 < m; j0 += 8u * 256u) {
+                uint64_t tq[8];
+                double2 aq[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const unsigned j = j0 + (unsigned)q * 256u + tid;
+                    if (j < m) member_at<BUCKET>(a, s0 + j, tq[q], aq[q]);
+                }
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const unsigned j = j0 + (unsigned)q * 256u + tid;
+                    if (j < m) sl[tq[q]] = aq[q];
+                }
             }
             __syncthreads();
 #pragma unroll
@@ -872,7 +887,7 @@ constexpr unsigned long long kSlotLocked = ~0ull;
 struct HashWs {
     unsigned long long* slots;
     unsigned long long cap_mask;
-    unsigned* gcount;     // [0]: groups, [1]: entries failing the conditions
+    unsigned* gcount;     // [0]: groups, [1]: entries failing the conditions, [2]: table overflow
     unsigned* cnt;        // members per group
     unsigned* head;       // one entry per group
     unsigned* gid;        // group of each entry (~0u: fails the conditions)
@@ -890,68 +905,115 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
 
 template <int K>
 __global__ void __launch_bounds__(256) hash_insert_kernel(ConstKeyPtrs keys, const uint64_t* __restrict__ gmask,
-                                                          DCondSet cond, uint64_t n, HashWs h, unsigned* err) {
+                                                          DCondSet cond, uint64_t n, HashWs h, unsigned gmax,
+                                                          Field tgt, Field varw, unsigned max_digits, unsigned* err) {
     uint64_t gm[K];
 #pragma unroll
     for (int w = 0; w < K; ++w) gm[w] = gmask[w];
+    const unsigned lane = threadIdx.x & 31u;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x; b < n; b += stride) {  // warp-uniform trip count
+        const uint64_t i = b + threadIdx.x;
+        const bool valid = i < n;
         uint64_t k[K];
 #pragma unroll
-        for (int w = 0; w < K; ++w) k[w] = keys.w[w][i];
-        if (!cond_ok<K>(k, cond)) {
-            const unsigned p = atomicAdd(&h.gcount[1], 1u);
-            h.pass_list[p] = (unsigned)i;
-            h.gid[i] = ~0u;
-            continue;
+        for (int w = 0; w < K; ++w) k[w] = valid ? (keys.w[w][i] & gm[w]) : 0ull;
+        bool pass = false;
+        if (valid) {
+            uint64_t full[K];
+#pragma unroll
+            for (int w = 0; w < K; ++w) full[w] = keys.w[w][i];
+            pass = cond_ok<K>(full, cond);
+            if (pass && varw.width) {  // batched Hadamard: drop this entry's own n low target bits
+                const unsigned nd = (unsigned)fget<K>(full, varw);
+                if (nd > max_digits) {
+                    atomicOr(err, 4u);
+                    pass = false;
+                } else {
+                    kword_set<K>(k, tgt.word, kword<K>(k, tgt.word) & ~(wmask(nd) << tgt.shift));
+                }
+            }
+            if (!pass) {
+                const unsigned p = atomicAdd(&h.gcount[1], 1u);
+                h.pass_list[p] = (unsigned)i;
+                h.gid[i] = ~0u;
+            }
         }
         unsigned long long hv = 0x9e3779b97f4a7c15ull;
 #pragma unroll
-        for (int w = 0; w < K; ++w) hv = mix64(hv ^ (k[w] & gm[w]) ^ (0x632be59bd9b4e019ull * (w + 1)));
-        unsigned long long slot = hv & h.cap_mask;
-        unsigned mygid = ~0u;
-        unsigned spins = 0;
-        for (unsigned long long probes = 0; probes <= h.cap_mask;) {
-            cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> ref(h.slots[slot]);
-            unsigned long long v = ref.load(cuda::memory_order_acquire);
-            if (v == 0ull) {
-                unsigned long long expected = 0ull;
-                if (ref.compare_exchange_strong(expected, kSlotLocked, cuda::memory_order_acq_rel)) {
-                    const unsigned g = atomicAdd(&h.gcount[0], 1u);
-                    h.head[g] = (unsigned)i;
-                    ref.store(((unsigned long long)(g + 1) << 32) | (unsigned long long)(i + 1),
-                              cuda::memory_order_release);
-                    mygid = g;
-                    break;
-                }
-                continue;  // lost the race: re-read this slot
-            }
-            if (v == kSlotLocked) {
-                if (++spins > kSpinLimit) {
-                    atomicOr(err, 2u);
-                    break;
-                }
-                __nanosleep(20);
-                continue;
-            }
-            const unsigned hidx = (unsigned)(v & 0xffffffffull) - 1u;
-            bool same = true;
+        for (int w = 0; w < K; ++w) hv = mix64(hv ^ k[w] ^ (0x632be59bd9b4e019ull * (w + 1)));
+        // lanes whose group key hashes equal share one table probe (entries of
+        // a group usually arrive together); a lane whose key differs from its
+        // leader's despite the equal hash probes on its own
+        const unsigned pm = __ballot_sync(0xffffffffu, pass);
+        const unsigned peers = __match_any_sync(0xffffffffu, hv) & pm;
+        const int leader = pass ? __ffs(peers) - 1 : (int)lane;
+        bool same = true;
 #pragma unroll
-            for (int w = 0; w < K; ++w) same = same && (((keys.w[w][hidx] ^ k[w]) & gm[w]) == 0);
-            if (same) {
-                mygid = (unsigned)(v >> 32) - 1u;
-                break;
+        for (int w = 0; w < K; ++w) same = same && (__shfl_sync(0xffffffffu, k[w], leader) == k[w]);
+        const unsigned same_mask = __ballot_sync(0xffffffffu, pass && same);
+        const bool probe = pass && (!same || (int)lane == leader);
+        unsigned mygid = ~0u;
+        if (probe) {
+            unsigned long long slot = hv & h.cap_mask;
+            unsigned spins = 0;
+            for (unsigned long long probes = 0; probes <= h.cap_mask;) {
+                if (h.gcount[2]) break;  // table overflowed: the host retries with a larger one
+                cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> ref(h.slots[slot]);
+                unsigned long long v = ref.load(cuda::memory_order_relaxed);
+                if (v == 0ull) {
+                    unsigned long long expected = 0ull;
+                    if (ref.compare_exchange_strong(expected, kSlotLocked, cuda::memory_order_relaxed)) {
+                        const unsigned g = atomicAdd(&h.gcount[0], 1u);
+                        if (g >= gmax) {
+                            atomicExch(&h.gcount[2], 1u);
+                            break;
+                        }
+                        h.head[g] = (unsigned)i;
+                        ref.store(((unsigned long long)(g + 1) << 32) | (unsigned long long)(i + 1),
+                                  cuda::memory_order_relaxed);
+                        mygid = g;
+                        break;
+                    }
+                    continue;  // lost the race: re-read this slot
+                }
+                if (v == kSlotLocked) {
+                    if (++spins > kSpinLimit) {
+                        atomicOr(err, 2u);
+                        break;
+                    }
+                    __nanosleep(20);
+                    continue;
+                }
+                const unsigned hidx = (unsigned)(v & 0xffffffffull) - 1u;
+                uint64_t hk[K];
+#pragma unroll
+                for (int w = 0; w < K; ++w) hk[w] = keys.w[w][hidx] & gm[w];
+                if (varw.width) {
+                    const unsigned hn = (unsigned)fget<K>(hk, varw);
+                    kword_set<K>(hk, tgt.word, kword<K>(hk, tgt.word) & ~(wmask(hn) << tgt.shift));
+                }
+                bool eq = true;
+#pragma unroll
+                for (int w = 0; w < K; ++w) eq = eq && ((hk[w] ^ k[w]) == 0);
+                if (eq) {
+                    mygid = (unsigned)(v >> 32) - 1u;
+                    break;
+                }
+                slot = (slot + 1) & h.cap_mask;
+                ++probes;
             }
-            slot = (slot + 1) & h.cap_mask;
-            ++probes;
+            if (mygid != ~0u) {
+                const unsigned c = (int)lane == leader ? __popc(peers & same_mask) : 1u;
+                atomicAdd(&h.cnt[mygid], c);
+            }
         }
-        if (mygid == ~0u) {  // table exhausted or gave up waiting: reported, entry dropped
-            atomicOr(err, 2u);
-            h.gid[i] = ~0u;
-            continue;
+        const unsigned lg = __shfl_sync(0xffffffffu, mygid, leader);
+        if (pass) {
+            if (!probe) mygid = lg;
+            h.gid[i] = mygid;
+            if (mygid == ~0u && !h.gcount[2]) atomicOr(err, 2u);  // probe gave up: reported
         }
-        h.gid[i] = mygid;
-        atomicAdd(&h.cnt[mygid], 1u);
     }
 }
 
@@ -961,7 +1023,8 @@ __global__ void __launch_bounds__(256) hash_insert_kernel(ConstKeyPtrs keys, con
 __global__ void __launch_bounds__(256) bucket_kernel(const unsigned* __restrict__ gid, const uint64_t* __restrict__ tword,
                                                      Field target, const double2* __restrict__ amp, uint64_t n,
                                                      const unsigned* __restrict__ seg, unsigned* __restrict__ cnt,
-                                                     unsigned* __restrict__ btgt, double2* __restrict__ bamp) {
+                                                     unsigned* __restrict__ btgt, double2* __restrict__ bamp,
+                                                     const uint64_t* __restrict__ wword, Field varw) {
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t base0 = (uint64_t)blockIdx.x * blockDim.x;
@@ -978,7 +1041,8 @@ __global__ void __launch_bounds__(256) bucket_kernel(const unsigned* __restrict_
             if ((int)lane == leader) old = atomicSub(&cnt[g], (unsigned)__popc(peers));
             old = __shfl_sync(peers, old, leader);
             const unsigned pos = seg[g] + old - 1u - rank;
-            btgt[pos] = (unsigned)((tword[i] >> target.shift) & wmask(target.width));
+            const unsigned nd = varw.width ? (unsigned)((wword[i] >> varw.shift) & wmask(varw.width)) : target.width;
+            btgt[pos] = (unsigned)((tword[i] >> target.shift) & wmask(nd));
             bamp[pos] = amp[i];
         }
     }
@@ -1224,40 +1288,58 @@ static Grouping group_by_sort(State& s, const GroupSpec& gs, const uint64_t* gma
     return out;
 }
 
+static uint64_t g_hash_groups_hint = 1ull << 20;
+void set_hash_groups_hint(uint64_t g) { g_hash_groups_hint = g ? g : (1ull << 20); }
+
 template <int K>
 static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg) {
     const uint64_t N = s.n;
     cudaStream_t st = stream();
     ConstKeyPtrs ik;
     for (int w = 0; w < SQ_KMAX; ++w) ik.w[w] = s.live.keys[w];
-    uint64_t cap = 1024;
-    while (cap < 2 * N) cap <<= 1;
-    // one allocation: slots | counters | cnt | head | gid | pass_list | bucket target | bucket amp
-    const size_t off_cnt = cap * 8 + 256;
-    const size_t off_head = off_cnt + N * 4;
-    const size_t off_gid = off_head + N * 4;
-    const size_t off_pass = off_gid + N * 4;
-    const size_t off_btgt = off_pass + N * 4;
-    size_t off_bamp = off_btgt + N * 4;
-    off_bamp = (off_bamp + 15) & ~size_t(15);
-    const size_t total = off_bamp + N * 16;
-    char* base = (char*)ws().get(WS_MERGE_KEYS, total);
+    // Table sized for the expected number of groups (load factor <= 1/2);
+    // if more groups show up the kernel flags overflow and we retry with a
+    // table that fits every entry.
+    uint64_t want = std::min<uint64_t>(N, g_hash_groups_hint);
     HashWs h;
-    h.slots = (unsigned long long*)base;
-    h.cap_mask = cap - 1;
-    h.gcount = (unsigned*)(base + cap * 8);
-    h.cnt = (unsigned*)(base + off_cnt);
-    h.head = (unsigned*)(base + off_head);
-    h.gid = (unsigned*)(base + off_gid);
-    h.pass_list = (unsigned*)(base + off_pass);
-    SQ_CUDA(cudaMemsetAsync(base, 0, off_head, st));  // slots, counters, cnt
-    prof_begin("hash_insert");
-    hash_insert_kernel<K><<<grid_for(N, 256, 8), 256, 0, st>>>(ik, dg, gs.cond, N, h, device_error_word());
-    prof_end((double)N * (8.0 * K + 4 + 4));
-    SQ_CUDA(cudaGetLastError());
+    char* base = nullptr;
+    size_t off_btgt = 0, off_bamp = 0;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        uint64_t cap = 1024;
+        while (cap < 2 * want) cap <<= 1;
+        const uint64_t gmax = cap / 2;
+        // one allocation: slots | counters | cnt | head | gid | pass_list | bucket target | bucket amp
+        const size_t off_cnt = cap * 8 + 256;
+        const size_t off_head = off_cnt + gmax * 4;
+        const size_t off_gid = off_head + gmax * 4;
+        const size_t off_pass = off_gid + N * 4;
+        off_btgt = off_pass + N * 4;
+        off_bamp = (off_btgt + N * 4 + 15) & ~size_t(15);
+        const size_t total = off_bamp + N * 16;
+        base = (char*)ws().get(WS_MERGE_KEYS, total);
+        h.slots = (unsigned long long*)base;
+        h.cap_mask = cap - 1;
+        h.gcount = (unsigned*)(base + cap * 8);
+        h.cnt = (unsigned*)(base + off_cnt);
+        h.head = (unsigned*)(base + off_head);
+        h.gid = (unsigned*)(base + off_gid);
+        h.pass_list = (unsigned*)(base + off_pass);
+        SQ_CUDA(cudaMemsetAsync(base, 0, off_head, st));  // slots, counters, cnt
+        prof_begin("hash_insert");
+        hash_insert_kernel<K><<<grid_for(N, 256, 8), 256, 0, st>>>(ik, dg, gs.cond, N, h, (unsigned)gmax, gs.target,
+                                                                   gs.varw, gs.target.width, device_error_word());
+        prof_end((double)N * (8.0 * K + 4));
+        SQ_CUDA(cudaGetLastError());
+        unsigned gc[3] = {0, 0, 0};
+        SQ_CUDA(cudaMemcpyAsync(gc, h.gcount, 12, cudaMemcpyDeviceToHost, st));
+        check_device_error();
+        if (!gc[2]) break;
+        if (attempt == 1) fail(SQ_ERR_DEVICE_TIMEOUT, "hash grouping overflowed a table sized for every entry");
+        want = N;
+    }
     unsigned gc[2] = {0, 0};
     SQ_CUDA(cudaMemcpyAsync(gc, h.gcount, 8, cudaMemcpyDeviceToHost, st));
-    check_device_error();
+    SQ_CUDA(cudaStreamSynchronize(st));
     Grouping out;
     out.G = gc[0];
     out.F = gc[1];
@@ -1280,7 +1362,8 @@ static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg) {
         double2* bamp = (double2*)(base + off_bamp);
         prof_begin("bucket_members");
         bucket_kernel<<<grid_for(N, 256, 8), 256, 0, st>>>(h.gid, s.live.keys[gs.target.word], gs.target, s.live.amp,
-                                                           N, seg, h.cnt, btgt, bamp);
+                                                           N, seg, h.cnt, btgt, bamp,
+                                                           s.live.keys[gs.varw.width ? gs.varw.word : 0], gs.varw);
         prof_end((double)N * (4 + 8 + 16) + (double)P * (4 + 16 + 8));
         SQ_CUDA(cudaGetLastError());
         out.btgt = btgt;
@@ -1299,13 +1382,16 @@ static void run_group(State& s, const GroupSpec& gs) {
     // group mask: active bits except the target bits
     uint64_t gmask[SQ_KMAX];
     regtable().active_mask(gmask);
-    if (gs.target.width) gmask[gs.target.word] &= ~(wmask(gs.target.width) << gs.target.shift);
+    // fixed width: the target bits never belong to the group key; batched
+    // width: the hash kernel clears each entry's own low n bits
+    if (gs.target.width && !gs.varw.width) gmask[gs.target.word] &= ~(wmask(gs.target.width) << gs.target.shift);
     uint64_t* dg = (uint64_t*)ws().get(WS_REDUCE, 64 * 8);
     SQ_CUDA(cudaMemcpyAsync(dg, gmask, SQ_KMAX * 8, cudaMemcpyHostToDevice, st));
 
     // the merge sums runs in order, so it keeps the (stable) sort; the
     // transforms are order-independent and default to the hash grouping
-    const bool use_hash = gs.mode != GM_MERGE && (g_strategy == 2 || (g_strategy == 0 && N >= 4096));
+    const bool use_hash = gs.varw.width ||
+                          (gs.mode != GM_MERGE && (g_strategy == 2 || (g_strategy == 0 && N >= 4096)));
     Grouping gr = use_hash ? group_by_hash<K>(s, gs, dg) : group_by_sort<K>(s, gs, gmask, dg);
     const uint64_t G = gr.G, F = gr.F, P = N - F;
 
@@ -1332,6 +1418,7 @@ static void run_group(State& s, const GroupSpec& gs) {
     ea.mtable = gs.mtable;
     ea.umat = gs.umat;
     ea.udag = gs.udag;
+    ea.varw = gs.varw;
     ea.cnt = (unsigned*)ws().get(WS_COUNT, (G + 1) * 4);
     unsigned long long* off = (unsigned long long*)ws().get(WS_OFFSET, (G + 1) * 8);
     ea.off = off;

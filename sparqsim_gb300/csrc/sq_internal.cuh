@@ -253,6 +253,7 @@ struct GroupSpec {
     const double2* mtable;  // device: CondRot_General_Bool matrices (4 per input value)
     const double2* umat;    // device: Rot_GeneralUnitary matrix
     int udag;
+    Field varw;             // batched Hadamard: register holding each entry's digit count (width 0: unused)
 };
 void group_transform(State& s, const GroupSpec& g);
 void set_group_strategy(int s);

@@ -40,6 +40,8 @@ def _run(state: SparseState, spec) -> None:
             call("sq_apply_program", h, arr, len(chunk))
     elif kind == "hadamard_int":
         call("sq_hadamard_int", h, spec[1], spec[2], byref(spec[3]))
+    elif kind == "hadamard_int_batched":
+        call("sq_hadamard_int_batched", h, spec[1], spec[2], spec[3], byref(spec[4]))
     elif kind == "hadamard_int_full":
         call("sq_hadamard_int_full", h, spec[1], byref(spec[2]))
     elif kind == "hadamard_bool":
@@ -467,6 +469,57 @@ class Hadamard_Int(SelfAdjointOperator):
 
     def spec(self, dag=False):
         return ("hadamard_int", self.id, self.n_digits, self._cond())
+
+
+class Hadamard_Int_Batched(SelfAdjointOperator):
+    """Hadamard_Int on the low n bits of `reg`, n read per entry from
+    `width_reg` (n <= max_digits <= 8): many trajectories of different widths
+    transformed in one pass. Same result as Hadamard_Int(reg, h)
+    .conditioned_by_value(width_reg, h) for every h."""
+
+    def __init__(self, reg, width_reg, max_digits):
+        super().__init__()
+        self.id, self.width_id, self.max_digits = _R(reg), _R(width_reg), int(max_digits)
+
+    def spec(self, dag=False):
+        return ("hadamard_int_batched", self.id, self.width_id, self.max_digits, self._cond())
+
+
+class NoiseTable:
+    """Per-trajectory Pauli masks: masks[t] = (xa, xb, xc, za, zb, zc)."""
+
+    def __init__(self, masks):
+        import numpy as np
+        m = np.ascontiguousarray(np.asarray(masks, dtype=np.uint64).reshape(-1, 6))
+        self.n_traj = m.shape[0]
+        words = m.reshape(-1)
+        bits = max(1, int(np.ceil(np.log2(max(words.size, 2)))))
+        padded = np.zeros(1 << bits, dtype=np.uint64)
+        padded[: words.size] = words
+        self.masks = m
+        self.table = QRAMCircuit_qutrit(bits, 64, padded)
+
+
+class PauliNoise(ElementwiseOperator):
+    """Per-trajectory Pauli X then Z errors on three registers, selected by the
+    trajectory register's value (batched noisy trajectories)."""
+
+    opcode = "PAULI_NOISE"
+
+    def __init__(self, traj_reg, regs, table: NoiseTable):
+        super().__init__()
+        if len(regs) != 3:
+            raise ValueError("PauliNoise acts on three registers")
+        self.traj = _R(traj_reg)
+        self.regs = [_R(r) for r in regs]
+        self.noise = table
+
+    def _fill(self, ins, dag):
+        ins.reg[0] = self.traj
+        for i, r in enumerate(self.regs):
+            ins.reg[i + 1] = r
+        ins.imm[0] = self.noise.n_traj
+        ins.qram = self.noise.table._h.value
 
 
 class Hadamard_Int_Full(SelfAdjointOperator):

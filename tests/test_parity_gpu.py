@@ -434,3 +434,51 @@ def test_config1_full_size(dual, strategy):
     assert dual.gpu.size() > 16_000_000
     dual.compare(exact_amp=True)
     assert abs(dual.gpu.norm_sq() - 1.0) < 1e-12
+
+
+def _random_unitary(rng, dim):
+    z = rng.normal(size=(dim, dim)) + 1j * rng.normal(size=(dim, dim))
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+@pytest.mark.parametrize("width", [1, 2, 3, 5])
+def test_rot_general_unitary(dual, strategy, width):
+    dual.reg("q", U, width)
+    dual.reg("r", U, 9)
+    rng = np.random.default_rng(100 + width)
+    S = 1 << width
+    regs, amps = grouped_state(rng, [width, 9], 0, width, 80, lambda g: int(rng.integers(1, S + 1)))
+    dual.start(regs, amps)
+    op = ps.Rot_GeneralUnitary("q", _random_unitary(rng, S))
+    dual.apply(op)
+    dual.compare(exact_amp=True)
+    dual.apply(op, dag=True)
+    dual.compare(exact_amp=True)
+    dual.apply(op.conditioned_by_bit("r", 3))
+    dual.compare(exact_amp=True)
+
+
+@pytest.mark.parametrize("w_in", [1, 4, 10])
+def test_condrot_general_bool(dual, strategy, w_in):
+    dual.reg("in", U, w_in)
+    dual.reg("out", ps.Boolean, 1)
+    dual.reg("r", U, 7)
+    rng = np.random.default_rng(200 + w_in)
+    regs, amps = random_state(rng, [w_in, 1, 7], 3000)
+    dual.start(regs, amps)
+    mats = [_random_unitary(rng, 2) for _ in range(1 << w_in)]
+    op = ps.CondRot_General_Bool("in", "out", lambda v: mats[v].reshape(-1))
+    dual.apply(op)
+    dual.compare(exact_amp=True)
+
+
+def test_hadamard_partial(dual, strategy):
+    dual.reg("q", U, 6)
+    dual.reg("r", U, 10)
+    rng = np.random.default_rng(300)
+    regs, amps = random_state(rng, [6, 10], 3000)
+    dual.start(regs, amps)
+    for pos in (0, 3, 5):
+        dual.apply(ps.Hadamard_Partial("q", [pos]))
+        dual.compare(exact_amp=True)
