@@ -206,6 +206,94 @@ def cpu_baseline_sample(h: int, table, thetas, layers_sample: int = 2):
     return upd, dt
 
 
+def run_trajectories(args, ext) -> dict:
+    """Batched noisy trajectories (4096 instances, a/b/c 16-bit, per-instance
+    Hadamard width h_t in [4, 8], Pauli X/Z at p = 1e-3 per bit per layer,
+    6 layers): the batched form, the plain GPU form (one state per instance)
+    on a sample of instances, and the oracle on a smaller sample."""
+    import numpy as np
+    import torch
+
+    import sparqsim_gb300 as ps
+    from sparqsim_gb300.workloads import NoisyTrajectories
+    wl = NoisyTrajectories(n_traj=args.trajectories, layers=6, p=1e-3, h_min=4, h_max=8, seed=SEED)
+    wl.build_batched()
+    st = ps.SparseState(capacity=1 << 20)
+    upd = wl.run_batched(st, count=True)
+    peak_hint = st.size()
+    for _ in range(2):
+        wl.run_batched(st)
+    steps = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(ext)
+    for _ in range(steps):
+        wl.run_batched(st)
+    e.record(ext)
+    e.synchronize()
+    batched_ms = s.elapsed_time(e) / steps
+    batched_wall = (time.perf_counter() - t0) / steps
+    # plain GPU form: instance by instance, on a sample of instances
+    n_sample = min(args.plain_sample, wl.n_traj)
+    wl.build_plain()
+    sp = ps.SparseState(capacity=1 << 17)
+    upd_p = sum(wl.run_plain(sp, t, count=True) for t in range(n_sample))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for t in range(n_sample):
+        wl.run_plain(sp, t)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    # the oracle, one thread, plain form, on a smaller sample
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.clear()
+        for rid in ps.System.active_ids():
+            O.add_register(int(ps.System.type_of(rid)), ps.System.size_of(rid))
+        _, qram, noise, mids, Hs = wl._built
+        O.register_qram(qram)
+        for nt in noise:
+            O.register_qram(nt.table)
+        n_cpu = min(args.cpu_sample, wl.n_traj)
+        upd_c = 0
+        t0 = time.perf_counter()
+        for t in range(n_cpu):
+            ost = O.OracleState()
+            ost.set(np.array([[t, 0, 0, 0]], dtype=np.uint64), np.ones(1, dtype=np.complex128))
+            H = Hs[int(wl.widths[t])]
+            for mid in mids:
+                n0 = ost.size()
+                O.apply(ost, H.spec())
+                n1 = ost.size()
+                O.apply(ost, mid.spec())
+                O.apply(ost, H.spec())
+                upd_c += max(n0, n1) + 4 * n1 + max(n1, ost.size())
+        cpu_s = time.perf_counter() - t0
+        O.clear()
+        cpu = {"value": upd_c / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"instances 0..{n_cpu - 1}, plain form, {upd_c} updates in {cpu_s:.1f} s, one thread"}
+    batched_ups = upd / (batched_ms / 1e3)
+    plain_ups = upd_p / plain_s
+    out = {
+        "workload": (f"{wl.n_traj} noisy instances of the register circuit (a/b/c 16-bit, 2^16-word uint16 table), "
+                     "Hadamard width h_t in [4,8] per instance, Pauli X/Z p=1e-3 per bit per layer, 6 layers, "
+                     "support 2^h..2^2h per instance"),
+        "updates_per_step": upd, "peak_entries": peak_hint,
+        "batched": {"value": batched_ups, "unit": UNIT, "ms_per_step": batched_ms,
+                    "wall_ms_per_step": batched_wall * 1e3},
+        "plain_gpu": {"value": plain_ups, "unit": UNIT,
+                      "sample": f"instances 0..{n_sample - 1}, {upd_p} updates in {plain_s:.2f} s (wall clock)"},
+        "batched_over_plain": batched_ups / plain_ups,
+        "fwht_arithmetic": ps.get_fwht_arithmetic(),
+    }
+    if cpu:
+        out["cpu"] = cpu
+        out["batched_over_cpu"] = batched_ups / cpu["value"]
+    return out
+
+
 def run_gb300(args, rank: int, world: int, local_rank: int):
     import numpy as np
     import torch
@@ -215,6 +303,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
 
     torch.cuda.set_device(local_rank)
     _native.call("sq_init", local_rank)
+    ps.set_fwht_arithmetic(args.fwht_arithmetic)
     h, L = args.hadamard_bits, args.layers
     table, thetas = circuit_inputs(h, L)
     circ = Circuit(ps, h, L, table, thetas)
@@ -258,6 +347,21 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         dist.barrier()
     ms_per_step = t_max / args.steps
     value = world * updates * args.steps / (t_max / 1e3)
+
+    # the same steps in the other butterfly arithmetic (same keys; amplitudes
+    # bit-identical to the reference in 'reference', within 1e-12 in 'exact-sum')
+    other = "reference" if args.fwht_arithmetic == "exact-sum" else "exact-sum"
+    ps.set_fwht_arithmetic(other)
+    circ.run(st)
+    torch.cuda.synchronize()
+    s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s2.record(ext)
+    for _ in range(args.steps):
+        circ.run(st)
+    e2.record(ext)
+    e2.synchronize()
+    other_ms = s2.elapsed_time(e2) / args.steps
+    ps.set_fwht_arithmetic(args.fwht_arithmetic)
 
     # end to end through the public API: host inputs in, final state out
     k = ps.System.key_words()
@@ -308,6 +412,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         "config": dict(workload_config(h, L), updates_per_step=updates, final_entries=final_n,
                        parallelism="replicas" if world > 1 else "single GPU"),
         "gpu_launches": launches,
+        "fwht_arithmetic": args.fwht_arithmetic,
+        f"{other}_arithmetic": {"value": world * updates / (other_ms / 1e3), "unit": UNIT, "ms_per_step": other_ms},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "note": "public API: QRAM table and initial state uploaded from pinned host memory, final packed "
                         "state downloaded, each step; wall clock"},
@@ -319,6 +425,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     }
     if clocks:
         result["clocks"] = clocks
+    if args.trajectories and rank == 0:
+        result["batched_trajectories"] = run_trajectories(args, ext)
     return result, (table, thetas)
 
 
@@ -434,6 +542,12 @@ def main():
     ap.add_argument("--hadamard-bits", type=int, default=12)
     ap.add_argument("--layers", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--trajectories", type=int, default=4096,
+                    help="instances in the batched noisy-trajectory leg (0 skips it)")
+    ap.add_argument("--plain-sample", type=int, default=256, help="instances timed in the plain GPU form")
+    ap.add_argument("--cpu-sample", type=int, default=16, help="instances timed in the oracle")
+    ap.add_argument("--fwht-arithmetic", default="exact-sum", choices=["exact-sum", "reference"],
+                    help="Hadamard butterfly arithmetic of the headline run (the other one is timed too)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 

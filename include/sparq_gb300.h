@@ -304,6 +304,18 @@ int sq_get_group_strategy(int* strategy);
  * pass. Same entries either way; only their order differs. */
 int sq_set_output_sizing(int mode);
 int sq_get_output_sizing(int* mode);
+/* Arithmetic of the Hadamard butterfly networks (Hadamard_Int, the full
+ * buckets of Hadamard_Int_Full, Hadamard_Int_Batched):
+ * SQ_ARITH_REFERENCE = FP64 butterflies (a0 +- a1) * sqrt2inv in the
+ * reference's stage order (hadamard.cpp:44-59,100-131): bit-identical to the
+ * reference's CPU results; SQ_ARITH_EXACT_SUM (the default) = each group's
+ * amplitudes on one 64-bit integer grid, exact sums, one FP64 rounding per
+ * output. Exact-sum results differ from the reference's by at most a few units
+ * in the last place of the group's largest amplitude; keys are identical. It
+ * exists because FP64 runs at a small fraction of the integer rate on GB300. */
+enum { SQ_ARITH_REFERENCE = 0, SQ_ARITH_EXACT_SUM = 1 };
+int sq_set_fwht_arithmetic(int mode);
+int sq_get_fwht_arithmetic(int* mode);
 /* clearzero_default_eps (system_operations.h:577), initially 1e-14. */
 int sq_set_clearzero_eps(double eps);
 int sq_get_clearzero_eps(double* eps);

@@ -175,7 +175,7 @@ def apply(state: OracleState, spec) -> None:
         for ins in spec[1]:
             c = SqInstr()
             ctypes.pointer(c)[0] = ins
-            if ins.op == OP["QRAM_LOAD"]:
+            if ins.op in (OP["QRAM_LOAD"], OP["PAULI_NOISE"]):
                 c.qram = _qram_map[ins.qram].h
             instrs.append(c)
         arr = (SqInstr * len(instrs))(*instrs)

@@ -139,6 +139,8 @@ _SIGS = [
     ("sq_get_group_strategy", c_int, [POINTER(c_int)]),
     ("sq_set_output_sizing", c_int, [c_int]),
     ("sq_get_output_sizing", c_int, [POINTER(c_int)]),
+    ("sq_set_fwht_arithmetic", c_int, [c_int]),
+    ("sq_get_fwht_arithmetic", c_int, [POINTER(c_int)]),
     ("sq_set_clearzero_eps", c_int, [c_double]),
     ("sq_get_clearzero_eps", c_int, [POINTER(c_double)]),
     ("sq_clear_zero", c_int, [c_void_p, c_double]),

@@ -23,6 +23,10 @@ BUILD = PKG / "_build"
 LIB = PKG / "libsparq_gb300.so"
 
 SOURCES = ["sq_core.cu", "elementwise.cu", "compact.cu", "radix_sort.cu", "group_ops.cu", "api.cu"]
+# group_ops.cu is also compiled once per key width K (its kernels are templates
+# on K), so that the objects build in parallel: (source, object stem, defines)
+UNITS = [(s, Path(s).stem, []) for s in SOURCES] + \
+        [("group_ops.cu", f"group_ops_k{k}", [f"-DSQ_GROUP_K={k}"]) for k in range(1, 9)]
 HEADERS = ["sq_internal.cuh", "lookback.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -42,9 +46,10 @@ def _newest_input() -> float:
     return max(f.stat().st_mtime for f in files)
 
 
-def _compile(src: str) -> Path:
-    obj = BUILD / (Path(src).stem + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(obj)]
+def _compile(unit) -> Path:
+    src, stem, defines = unit
+    obj = BUILD / (stem + ".o")
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *defines, "-c", str(CSRC / src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -56,8 +61,10 @@ def build(force: bool = False, verbose: bool = True) -> Path:
     if LIB.exists() and not force and LIB.stat().st_mtime >= _newest_input():
         return LIB
     BUILD.mkdir(exist_ok=True)
-    with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(_compile, SOURCES))
+    # longest units first so the pool stays busy
+    units = sorted(UNITS, key=lambda u: (u[0] not in ("group_ops.cu", "elementwise.cu"), u[1]))
+    with cf.ThreadPoolExecutor(max_workers=min(len(units), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(_compile, units))
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", *map(str, objs), "-o", str(tmp), "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -164,6 +164,20 @@ def set_output_sizing(mode: str) -> None:
     call("sq_set_output_sizing", {"auto": 0, "exact": 1}[mode])
 
 
+def set_fwht_arithmetic(mode: str) -> None:
+    """Arithmetic of the Hadamard butterflies: 'reference' (FP64 in the
+    reference's stage order, bit-identical results) or 'exact-sum' (default:
+    exact integer sums on a per-group grid, one rounding per output)."""
+    call("sq_set_fwht_arithmetic", {"reference": 0, "exact-sum": 1}[mode])
+
+
+def get_fwht_arithmetic() -> str:
+    from ctypes import c_int
+    v = c_int()
+    call("sq_get_fwht_arithmetic", byref(v))
+    return ["reference", "exact-sum"][v.value]
+
+
 def set_clearzero_default_eps(eps: float) -> None:
     """clearzero_default_eps (system_operations.h:577)."""
     call("sq_set_clearzero_eps", float(eps))

@@ -226,6 +226,7 @@ int sq_state_destroy(sq_state* st) {
     if (!st) return SQ_OK;
     free_buffers(st->s.live);
     free_buffers(st->s.spare);
+    free_group_cache(st->s.groups);
     delete st;
     SQ_API_END
 }
@@ -247,6 +248,7 @@ int sq_state_capacity(const sq_state* st, uint64_t* cap) {
 int sq_state_reserve(sq_state* st, uint64_t capacity) {
     SQ_API_BEGIN
     State& s = S(st);
+    drop_groups(s);
     ensure_buffers(s.live, capacity, regtable().k, s.n);
     SQ_API_END
 }
@@ -254,6 +256,7 @@ int sq_state_reserve(sq_state* st, uint64_t capacity) {
 int sq_state_reset(sq_state* st) {
     SQ_API_BEGIN
     State& s = S(st);
+    drop_groups(s);
     sync_words(s);
     ensure_buffers(s.live, 1, regtable().k, 0);
     double2 one = make_double2(1.0, 0.0);
@@ -268,6 +271,7 @@ int sq_state_copy(sq_state* dst, const sq_state* src) {
     SQ_API_BEGIN
     State& d = S(dst);
     const State& s = S(src);
+    drop_groups(d);
     const uint32_t k = regtable().k;
     ensure_buffers(d.live, std::max<uint64_t>(s.n, 1), k, 0);
     for (uint32_t w = 0; w < k; ++w) {
@@ -285,6 +289,7 @@ int sq_state_copy(sq_state* dst, const sq_state* src) {
 int sq_state_upload(sq_state* st, uint64_t n, const uint64_t* regs, uint32_t nregs, const double* amps) {
     SQ_API_BEGIN
     State& s = S(st);
+    drop_groups(s);
     need(n == 0 || (regs != nullptr || nregs == 0) , "null regs");
     need(n == 0 || amps != nullptr, "null amps");
     const RegTable& t = regtable();
@@ -338,6 +343,7 @@ int sq_state_download(const sq_state* st, uint64_t* regs, uint32_t nregs, double
 int sq_state_upload_packed(sq_state* st, uint64_t n, const uint64_t* keys, const double* amps) {
     SQ_API_BEGIN
     State& s = S(st);
+    drop_groups(s);
     need(n == 0 || (keys != nullptr && amps != nullptr), "null pointer");
     const uint32_t k = regtable().k;
     ensure_buffers(s.live, std::max<uint64_t>(n, 1), k, 0);
@@ -369,6 +375,7 @@ int sq_state_download_packed(const sq_state* st, uint64_t* keys, double* amps) {
 int sq_state_device_arrays(sq_state* st, uint64_t** key_words, uint32_t* k, double** amps) {
     SQ_API_BEGIN
     State& s = S(st);
+    drop_groups(s);  // the caller may write the arrays
     sync_words(s);
     if (key_words)
         for (uint32_t w = 0; w < regtable().k; ++w) key_words[w] = s.live.keys[w];
@@ -760,6 +767,18 @@ int sq_get_output_sizing(int* mode) {
     SQ_API_END
 }
 
+int sq_set_fwht_arithmetic(int mode) {
+    SQ_API_BEGIN
+    set_fwht_arithmetic(mode);
+    SQ_API_END
+}
+int sq_get_fwht_arithmetic(int* mode) {
+    SQ_API_BEGIN
+    need(mode != nullptr, "null pointer");
+    *mode = get_fwht_arithmetic();
+    SQ_API_END
+}
+
 int sq_set_clearzero_eps(double eps) {
     SQ_API_BEGIN
     need(eps >= 0.0, "negative eps");
@@ -800,6 +819,7 @@ int sq_norm_sq(const sq_state* st, double* out) {
 int sq_add_systems(sq_state* dst, const sq_state* src, double coef) {
     SQ_API_BEGIN
     need(dst != src, "add_systems: source and destination must differ");
+    drop_groups(S(dst));
     add_systems(S(dst), S(src), coef);
     SQ_API_END
 }
@@ -808,6 +828,7 @@ int sq_add_register_sync(sq_state* st, uint32_t type, uint32_t width, uint32_t* 
     SQ_API_BEGIN
     need(id_out != nullptr, "null pointer");
     State& s = S(st);
+    drop_groups(s);
     const uint32_t id = regtable().add(type, width);
     *id_out = id;
     zero_field(s, regtable().field(id));
@@ -817,6 +838,7 @@ int sq_add_register_sync(sq_state* st, uint32_t type, uint32_t width, uint32_t* 
 int sq_remove_register_sync(sq_state* st, uint32_t id) {
     SQ_API_BEGIN
     State& s = S(st);
+    drop_groups(s);
     Field f = regtable().field(id);
     zero_field(s, f);
     regtable().remove(id);
@@ -827,6 +849,7 @@ int sq_split_register(sq_state* st, uint32_t first, uint32_t second_size, uint32
     SQ_API_BEGIN
     need(second_out != nullptr, "null pointer");
     State& s = S(st);
+    drop_groups(s);
     RegTable& t = regtable();
     const RegEntry fe = t.at(first);
     need(second_size <= fe.width, "SplitRegister: second size larger than the register");
@@ -849,6 +872,7 @@ int sq_split_register(sq_state* st, uint32_t first, uint32_t second_size, uint32
 int sq_combine_register(sq_state* st, uint32_t first, uint32_t second) {
     SQ_API_BEGIN
     State& s = S(st);
+    drop_groups(s);
     RegTable& t = regtable();
     need(first != second, "CombineRegister: registers must differ");
     const RegEntry a = t.at(first);

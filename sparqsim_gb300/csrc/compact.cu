@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kCzBlock) clearzero_kernel(ConstKeyPtrs ik, co
         bool keep = false;
         if (i < n) {
             a[j] = ia[i];
-            keep = !(a[j].x * a[j].x + a[j].y * a[j].y < eps);
+            keep = sq_keep_amp(a[j].x, a[j].y, eps);
         }
         ball[j] = __ballot_sync(0xffffffffu, keep);
         if (lane == 0) s_cnt[j][warp] = __popc(ball[j]);
@@ -146,6 +146,7 @@ uint64_t compact_nonzero(const Buffers& in, Buffers& out, uint64_t n, double eps
 }
 
 void clear_zero(State& s, double eps) {
+    drop_groups(s);
     sync_words(s);
     if (s.n == 0) return;
     const uint32_t k = regtable().k;

@@ -503,6 +503,7 @@ void run_program(State& s, const sq_instr* prog, uint32_t n) {
         a.read_words = rw;
         a.write_words = ww;
         a.amp_mode = am;
+        if (ww) drop_groups(s);  // key values change: cached group ranges no longer hold
         dispatch_k<4>(a, s, k);
     } else {
         ProgramArgs<SQ_MAX_PROGRAM>* a = new ProgramArgs<SQ_MAX_PROGRAM>;
@@ -517,6 +518,7 @@ void run_program(State& s, const sq_instr* prog, uint32_t n) {
         a->read_words = rw;
         a->write_words = ww;
         a->amp_mode = am;
+        if (ww) drop_groups(s);
         dispatch_k<SQ_MAX_PROGRAM>(*a, s, k);
         delete a;
     }
@@ -531,6 +533,7 @@ __global__ void zero_field_kernel(uint64_t* __restrict__ w, uint64_t keep_mask, 
 }
 
 void zero_field(State& s, Field f) {
+    drop_groups(s);
     sync_words(s);
     if (s.n == 0 || f.width == 0) return;
     const uint64_t keep = ~(wmask(f.width) << f.shift);
@@ -560,6 +563,7 @@ __global__ void move_field_kernel(KeyPtrs keys, Field first, Field second, Field
 }
 
 void move_field(State& s, Field first, Field second, Field dst) {
+    drop_groups(s);
     sync_words(s);
     if (s.n == 0) return;
     KeyPtrs kp;

@@ -36,6 +36,10 @@ void check_device_error();
 
 constexpr int kMaxRuns = 64;
 
+// Kernels and device helpers have internal linkage: the file is compiled once
+// per key width K (-DSQ_GROUP_K=K) plus once for the dispatcher, in parallel.
+namespace {
+
 struct Run {
     uint8_t word;
     uint8_t shift;
@@ -54,7 +58,79 @@ __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_doub
 __device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-__device__ __forceinline__ bool keep_amp(double2 a, double eps) { return !(a.x * a.x + a.y * a.y < eps); }
+__device__ __forceinline__ bool keep_amp(double2 a, double eps) { return sq_keep_amp(a.x, a.y, eps); }
+// a * -1.0 without the FP64 pipe (same bits for every non-NaN value)
+__device__ __forceinline__ double2 cneg(double2 a) {
+    return make_double2(__longlong_as_double(__double_as_longlong(a.x) ^ (long long)0x8000000000000000ull),
+                        __longlong_as_double(__double_as_longlong(a.y) ^ (long long)0x8000000000000000ull));
+}
+
+// ------------------------------------------------------------------ exact-sum FWHT arithmetic
+// FP64 runs at a small fraction of the integer rate on this part, and an
+// n-stage butterfly network costs 4n FP64 operations per slot. In the
+// exact-sum arithmetic a group's amplitudes are put on one integer grid,
+//     X = round(x * 2^(F - E)),  E = emax - 1022,  F = 62 - n,
+// where emax is the largest biased exponent among the group's components (so
+// every |x| < 2^E and |X| < 2^F); the n stages of sums and differences are then
+// exact in int64 (|partial sum| < 2^62), and each output is rounded once:
+//     y = Y * 2^(E - F) * 2^(-n/2)  (times 1/sqrt(2) once more for odd n).
+// The only other error is the grid rounding of each input, at most
+// 2^(E - F - 1) per component. Zero or subnormal components count as biased
+// exponent 1; a group holding inf or NaN gives unspecified amplitudes.
+__device__ __forceinline__ int amp_exp(double2 v) {
+    const int ex = (int)((unsigned long long)__double_as_longlong(v.x) >> 52) & 0x7ff;
+    const int ey = (int)((unsigned long long)__double_as_longlong(v.y) >> 52) & 0x7ff;
+    const int e = ex > ey ? ex : ey;
+    return e ? e : 1;
+}
+__device__ __forceinline__ long long to_fixed(double x, int emax, int F) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)(b >> 52) & 0x7ff;
+    unsigned long long mant = b & 0xfffffffffffffull;
+    if (ex) mant |= 1ull << 52;
+    const int r = emax - (ex ? ex : 1) + 53 - F;  // right shift; >= n - 9
+    unsigned long long q;
+    if (r <= 0) q = mant << (-r);
+    else if (r >= 64) q = 0;
+    else q = (mant + (1ull << (r - 1))) >> r;  // half away from zero
+    return (b >> 63) ? -(long long)q : (long long)q;
+}
+__device__ __forceinline__ longlong2 to_fixed2(double2 v, int emax, int F) {
+    return make_longlong2(to_fixed(v.x, emax, F), to_fixed(v.y, emax, F));
+}
+// Y * 2^e2 rounded to nearest even (|Y| < 2^63)
+__device__ __forceinline__ double fixed_to_double(long long Y, int e2) {
+    if (Y == 0) return 0.0;
+    const unsigned long long sign = (unsigned long long)Y & 0x8000000000000000ull;
+    const unsigned long long m = sign ? 0ull - (unsigned long long)Y : (unsigned long long)Y;
+    const int top = 63 - __clzll((long long)m);
+    int ex = top;
+    unsigned long long q;
+    if (top > 52) {
+        const int sh = top - 52;
+        q = m >> sh;
+        const unsigned long long rem = m & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        q += (rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull;
+        if (q >> 53) {
+            q >>= 1;
+            ++ex;
+        }
+    } else {
+        q = m << (52 - top);
+    }
+    const int be = ex + e2 + 1023;
+    if (be <= 0 || be >= 2047) return scalbn((double)Y, e2);  // outside the normal range (two roundings)
+    return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (q & 0xfffffffffffffull)));
+}
+__device__ __forceinline__ double2 from_fixed2(longlong2 v, int e2, bool odd, double s2) {
+    double2 r = make_double2(fixed_to_double(v.x, e2), fixed_to_double(v.y, e2));
+    if (odd) r = cscale(r, s2);
+    return r;
+}
+__device__ __forceinline__ longlong2 ladd(longlong2 a, longlong2 b) { return make_longlong2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ longlong2 lsub(longlong2 a, longlong2 b) { return make_longlong2(a.x - b.x, a.y - b.y); }
+// output scale exponent of an n-stage exact-sum FWHT: E - F - floor(n/2)
+__device__ __forceinline__ int fix_out_exp(int emax, int n) { return emax - 1022 - (62 - n) - (n >> 1); }
 
 // ------------------------------------------------------------------ 1. stats
 template <int K>
@@ -319,6 +395,13 @@ struct EmitArgs {
     const double2* umat;       // Rot_GeneralUnitary: S x S row-major
     int udag;                  // Rot_GeneralUnitary: apply the conjugate transpose
     Field varw;                // batched Hadamard: each group's digit count is this field of its key
+    const unsigned long long* rstart;  // cached group ranges (access mode 2)
+    const unsigned* rcnt;
+    unsigned long long* ostart;  // single-pass mode: each group's output range, for the next split
+    unsigned* ocnt;
+    unsigned long long capacity;  // single-pass mode: output entries available; a group whose
+                                  // reservation ends past it writes nothing (the host reruns exactly)
+    int fix;                   // FWHT arithmetic: 0 the reference's FP64 butterflies, 1 exact sums
 };
 
 template <int K>
@@ -342,20 +425,33 @@ __device__ __forceinline__ double as_rational(uint64_t v, unsigned w) {
 // Member `pos` of the grouped order: its target value and amplitude. The
 // sort path gathers them through the sorted index; the hash path reads the
 // bucket arrays, which hold them contiguously per group.
-template <bool BUCKET>
+// Member access: AM 0 = sort path (entry index per member), 1 = hash path
+// (bucketed target + amplitude per member), 2 = cached group ranges (members
+// are the entries start[g] .. start[g] + cnt[g] - 1 themselves).
+template <int AM>
 __device__ __forceinline__ void member_at(const EmitArgs& a, unsigned pos, uint64_t& t, double2& amp) {
-    if (BUCKET) {
+    if (AM == 1) {
         t = a.btgt[pos];
         amp = a.bamp[pos];
     } else {
-        const unsigned e = a.idx[pos];
+        const unsigned e = AM == 2 ? pos : a.idx[pos];
         t = (a.in_keys.w[a.target.word][e] >> a.target.shift) & wmask(a.target.width);
         amp = a.in_amp[e];
     }
 }
-template <bool BUCKET>
+template <int AM>
 __device__ __forceinline__ unsigned group_head(const EmitArgs& a, uint64_t g, unsigned s0) {
-    return BUCKET ? a.ghead[g] : a.idx[s0];
+    return AM == 1 ? a.ghead[g] : AM == 2 ? s0 : a.idx[s0];
+}
+template <int AM>
+__device__ __forceinline__ void group_range(const EmitArgs& a, uint64_t g, unsigned& s0, unsigned& m) {
+    if (AM == 2) {
+        s0 = (unsigned)a.rstart[g];
+        m = a.rcnt[g];
+    } else {
+        s0 = a.seg[g];
+        m = a.seg[g + 1] - s0;
+    }
 }
 
 // Pair modes (1-bit target): one thread per group.
@@ -470,6 +566,48 @@ __device__ __forceinline__ void worker_sync() {
     else __syncthreads();
 }
 
+// max of an int over a worker (a warp or the whole block); s_tmp holds 8 words
+template <int W>
+__device__ __forceinline__ int worker_max(int v, unsigned* s_tmp) {
+    v = (int)__reduce_max_sync(0xffffffffu, (unsigned)v);
+    if (W == 32) return v;
+    __syncthreads();
+    if ((threadIdx.x & 31u) == 0) s_tmp[threadIdx.x >> 5] = (unsigned)v;
+    __syncthreads();
+    unsigned r = s_tmp[0];
+#pragma unroll
+    for (int i = 1; i < 8; ++i) r = max(r, s_tmp[i]);
+    __syncthreads();
+    return (int)r;
+}
+
+// Single-pass output: one thread of the worker reserves `total` output slots
+// with an atomic on the cursor and publishes the range for the next split.
+// `fits` is false when the range ends past the output capacity.
+template <int W>
+__device__ __forceinline__ unsigned long long reserve_out(const EmitArgs& a, uint64_t g, unsigned total, bool& fits,
+                                                          unsigned long long* s_base) {
+    const unsigned t = W == 32 ? (threadIdx.x & 31u) : threadIdx.x;
+    unsigned long long base = 0;
+    if (t == 0) {
+        base = total ? atomicAdd(a.cursor, (unsigned long long)total) : 0ull;
+        if (a.ocnt) {
+            a.ostart[g] = base;
+            a.ocnt[g] = total;
+        }
+    }
+    if (W == 32) {
+        base = __shfl_sync(0xffffffffu, base, 0);
+    } else {
+        if (t == 0) *s_base = base;
+        __syncthreads();
+        base = *s_base;
+        __syncthreads();
+    }
+    fits = base + total <= a.capacity;
+    return base;
+}
+
 // exclusive scan of a per-thread flag over a worker, in thread order; returns
 // (exclusive prefix, total) for this round.
 template <int W>
@@ -496,12 +634,13 @@ __device__ __forceinline__ unsigned worker_rank(bool f, unsigned* s_tmp, unsigne
     return pre + in_warp;
 }
 
-template <int K, int W, bool WRITE, bool BUCKET>
+template <int K, int W, bool WRITE, int AM>
 __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constant__ EmitArgs a) {
     extern __shared__ double2 s_slots[];
     __shared__ unsigned s_tmp[8];
     __shared__ uint64_t s_member_t[8][64];
     __shared__ double2 s_member_a[8][64];
+    __shared__ unsigned long long s_base;
     const unsigned Smax = 1u << a.nbits;
     const unsigned wid = W == 32 ? (threadIdx.x >> 5) : 0u;
     const unsigned t = W == 32 ? (threadIdx.x & 31u) : threadIdx.x;
@@ -509,10 +648,14 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
     const uint64_t workers_per_block = blockDim.x / W;
     const uint64_t stride = (uint64_t)gridDim.x * workers_per_block;
     for (uint64_t g = (uint64_t)blockIdx.x * workers_per_block + wid; g < a.groups; g += stride) {
-        const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
-        const unsigned m = s1 - s0;
+        unsigned s0, m;
+        group_range<AM>(a, g, s0, m);
+        if (m == 0) {  // an emptied cached range
+            if (!WRITE && t == 0) a.cnt[g] = 0u;
+            continue;
+        }
         uint64_t gk[K];
-        load_key<K>(a.in_keys, group_head<BUCKET>(a, g, s0), gk);
+        load_key<K>(a.in_keys, group_head<AM>(a, g, s0), gk);
         // batched Hadamard: this group's digit count comes from its key
         const int nbits = a.varw.width ? (int)fget<K>(gk, a.varw) : a.nbits;
         const unsigned S = 1u << nbits;
@@ -524,19 +667,22 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
             // singleton: a * 2^{-n/2}, sign (-1)^{popcount(t & v)} (hadamard.cpp:27-42)
             uint64_t v0;
             double2 a0;
-            member_at<BUCKET>(a, s0, v0, a0);
+            member_at<AM>(a, s0, v0, a0);
             const double2 base = cscale(a0, extra);
-            const bool keep = keep_amp(base, a.eps);
+            // batched width 0: the entry is left as it is, never pruned
+            const bool keep = (a.varw.width && nbits == 0) || keep_amp(base, a.eps);
+            bool fits = true;
+            unsigned long long o = 0;
+            if (WRITE) o = a.cursor ? reserve_out<W>(a, g, keep ? S : 0u, fits, &s_base) : a.off[g];
             if (!WRITE) {
                 if (t == 0) a.cnt[g] = keep ? S : 0u;
-            } else if (keep) {
-                const unsigned long long o = a.off[g];
+            } else if (keep && fits) {
                 for (unsigned c = t; c < S; c += W) {
                     uint64_t kk[K];
 #pragma unroll
                     for (int w = 0; w < K; ++w) kk[w] = gk[w];
                     fset<K>(kk, tg, (uint64_t)c);
-                    const double2 v = (__popcll((uint64_t)c & v0) & 1) ? cscale(base, -1.0) : base;
+                    const double2 v = (__popcll((uint64_t)c & v0) & 1) ? cneg(base) : base;
                     store_entry<K>(a.out_keys, a.out_amp, o + c, kk, v);
                 }
             }
@@ -549,7 +695,7 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
             for (unsigned j = t; j < m; j += W) {
                 uint64_t tj;
                 double2 aj;
-                member_at<BUCKET>(a, s0 + j, tj, aj);
+                member_at<AM>(a, s0 + j, tj, aj);
                 s_member_t[wid][j] = tj;
                 s_member_a[wid][j] = aj;
             }
@@ -583,13 +729,38 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
             // zero-filled slots, scatter members, stage-ascending FWHT (hadamard.cpp:44-59, 100-131)
             for (unsigned c = t; c < S; c += W) slots[c] = make_double2(0.0, 0.0);
             worker_sync<W>();
+            int emax = 1;
             for (unsigned j = t; j < m; j += W) {
                 uint64_t tj;
                 double2 aj;
-                member_at<BUCKET>(a, s0 + j, tj, aj);
+                member_at<AM>(a, s0 + j, tj, aj);
                 slots[tj] = aj;
+                emax = max(emax, amp_exp(aj));
             }
+            const bool fix = a.fix && a.mode != GM_UNITARY;
+            if (fix) emax = worker_max<W>(emax, s_tmp);
             worker_sync<W>();
+            if (fix) {
+                // exact-sum arithmetic: integer grid, n exact stages, one rounding
+                longlong2* ls = reinterpret_cast<longlong2*>(slots);
+                const int F = 62 - nbits;
+                for (unsigned c = t; c < S; c += W) ls[c] = to_fixed2(slots[c], emax, F);
+                worker_sync<W>();
+                for (int qn = 0; qn < nbits; ++qn) {
+                    const unsigned h = 1u << qn;
+                    for (unsigned p = t; p < S / 2; p += W) {
+                        const unsigned i0 = ((p >> qn) << (qn + 1)) | (p & (h - 1u));
+                        const unsigned i1 = i0 + h;
+                        const longlong2 x0 = ls[i0], x1 = ls[i1];
+                        ls[i0] = ladd(x0, x1);
+                        ls[i1] = lsub(x0, x1);
+                    }
+                    worker_sync<W>();
+                }
+                const int e2 = fix_out_exp(emax, nbits);
+                for (unsigned c = t; c < S; c += W) slots[c] = from_fixed2(ls[c], e2, nbits & 1, a.sqrt2inv);
+                worker_sync<W>();
+            }
             if (a.mode == GM_UNITARY) {
                 // Rot_GeneralUnitary (rot.cpp:353-389): out[i] = sum_j M(i,j) * amp[j], j ascending
                 double2 r[8];
@@ -613,7 +784,7 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
                 }
                 worker_sync<W>();
             }
-            for (int qn = 0; a.mode != GM_UNITARY && qn < nbits; ++qn) {
+            for (int qn = 0; a.mode != GM_UNITARY && !fix && qn < nbits; ++qn) {
                 const unsigned h = 1u << qn;
                 for (unsigned p = t; p < S / 2; p += W) {
                     const unsigned i0 = ((p >> qn) << (qn + 1)) | (p & (h - 1u));
@@ -626,14 +797,27 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
             }
         }
         // count / write the kept slots in ascending target order
-        unsigned long long o = WRITE ? a.off[g] : 0ull;
+        unsigned long long o = 0;
+        bool fits = true;
+        if (WRITE && a.cursor) {  // single pass: count, reserve, then write
+            unsigned total = 0;
+            for (unsigned r = 0; r < S; r += W) {
+                const unsigned c = r + t;
+                unsigned tot;
+                worker_rank<W>(c < S && keep_amp(slots[c], a.eps), s_tmp, tot);
+                total += tot;
+            }
+            o = reserve_out<W>(a, g, total, fits, &s_base);
+        } else if (WRITE) {
+            o = a.off[g];
+        }
         unsigned kept = 0;
         for (unsigned r = 0; r < S; r += W) {
             const unsigned c = r + t;
             const bool keep = c < S && keep_amp(slots[c], a.eps);
             unsigned tot;
             const unsigned rank = worker_rank<W>(keep, s_tmp, tot);
-            if (WRITE && keep) {
+            if (WRITE && keep && fits) {
                 uint64_t kk[K];
 #pragma unroll
                 for (int w = 0; w < K; ++w) kk[w] = gk[w];
@@ -664,41 +848,65 @@ __device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
     return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
 }
 
-template <int K, int MODE, bool BUCKET>
+template <int K, int MODE, int AM>
 __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constant__ EmitArgs a) {
     extern __shared__ double2 sl[];  // 4096 slots
     __shared__ unsigned s_cnt[16][8];
     __shared__ unsigned long long s_base;
     __shared__ uint64_t s_mt[64];
     __shared__ double2 s_ma[64];
+    __shared__ unsigned s_emax[8];
+    __shared__ bool s_fits;
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const Field tg = a.target;
     const double s2 = a.sqrt2inv;
     for (uint64_t g = blockIdx.x; g < a.groups; g += gridDim.x) {
-        const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
-        const unsigned m = s1 - s0;
+        unsigned s0, m;
+        group_range<AM>(a, g, s0, m);
+        if (m == 0) {  // an emptied cached range
+            if (tid == 0) {
+                if (MODE == EMIT_COUNT) a.cnt[g] = 0u;
+                else if (MODE == EMIT_ATOMIC && a.ocnt) {
+                    a.ostart[g] = 0ull;
+                    a.ocnt[g] = 0u;
+                }
+            }
+            continue;
+        }
         uint64_t gk[K];
-        load_key<K>(a.in_keys, group_head<BUCKET>(a, g, s0), gk);
+        load_key<K>(a.in_keys, group_head<AM>(a, g, s0), gk);
         if (a.mode == GM_HADAMARD_INT && m == 1) {
             uint64_t v0;
             double2 a0;
-            member_at<BUCKET>(a, s0, v0, a0);
+            member_at<AM>(a, s0, v0, a0);
             const double2 base = cscale(a0, a.extra);
             const bool keep = keep_amp(base, a.eps);
             if (MODE == EMIT_COUNT) {
                 if (tid == 0) a.cnt[g] = keep ? 4096u : 0u;
+            } else if (MODE == EMIT_ATOMIC && !keep) {
+                if (tid == 0 && a.ocnt) {
+                    a.ostart[g] = 0ull;
+                    a.ocnt[g] = 0u;
+                }
             } else if (keep) {
                 if (MODE == EMIT_ATOMIC) {
-                    if (tid == 0) s_base = atomicAdd(a.cursor, 4096ull);
+                    if (tid == 0) {
+                        s_base = atomicAdd(a.cursor, 4096ull);
+                        if (a.ocnt) {
+                            a.ostart[g] = s_base;
+                            a.ocnt[g] = 4096u;
+                        }
+                    }
                     __syncthreads();
                 }
                 const unsigned long long o = MODE == EMIT_WRITE ? a.off[g] : s_base;
-                for (unsigned c = tid; c < 4096u; c += 256u) {
+                const bool fits = MODE != EMIT_ATOMIC || o + 4096ull <= a.capacity;
+                for (unsigned c = tid; fits && c < 4096u; c += 256u) {
                     uint64_t kk[K];
 #pragma unroll
                     for (int w = 0; w < K; ++w) kk[w] = gk[w];
                     fset<K>(kk, tg, (uint64_t)c);
-                    const double2 v = (__popcll((uint64_t)c & v0) & 1) ? cscale(base, -1.0) : base;
+                    const double2 v = (__popcll((uint64_t)c & v0) & 1) ? cneg(base) : base;
                     store_entry<K>(a.out_keys, a.out_amp, o + c, kk, v);
                 }
             }
@@ -711,7 +919,7 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
             for (unsigned j = tid; j < m; j += 256u) {
                 uint64_t tj;
                 double2 aj;
-                member_at<BUCKET>(a, s0 + j, tj, aj);
+                member_at<AM>(a, s0 + j, tj, aj);
                 s_mt[j] = tj;
                 s_ma[j] = aj;
             }
@@ -747,21 +955,83 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
             for (int j = 0; j < 16; ++j) sl[((unsigned)j << 8) | tid] = make_double2(0.0, 0.0);
             __syncthreads();
             // members: 8 independent loads in flight per thread, then scatter
+            int emax = 1;
             for (unsigned j0 = 0; j0 < m; j0 += 8u * 256u) {
                 uint64_t tq[8];
                 double2 aq[8];
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
                     const unsigned j = j0 + (unsigned)q * 256u + tid;
-                    if (j < m) member_at<BUCKET>(a, s0 + j, tq[q], aq[q]);
+                    if (j < m) member_at<AM>(a, s0 + j, tq[q], aq[q]);
                 }
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
                     const unsigned j = j0 + (unsigned)q * 256u + tid;
-                    if (j < m) sl[tq[q]] = aq[q];
+                    if (j < m) {
+                        sl[tq[q]] = aq[q];
+                        emax = max(emax, amp_exp(aq[q]));
+                    }
                 }
             }
+            if (a.fix) {
+                emax = (int)__reduce_max_sync(0xffffffffu, (unsigned)emax);
+                if (lane == 0) s_emax[warp] = (unsigned)emax;
+            }
             __syncthreads();
+            if (a.fix) {
+                // exact-sum arithmetic: same stage layout on the int64 grid, one rounding at the end
+#pragma unroll
+                for (int i = 0; i < 8; ++i) emax = max(emax, (int)s_emax[i]);
+                longlong2* ls = reinterpret_cast<longlong2*>(sl);
+                longlong2 x[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) x[j] = to_fixed2(sl[((unsigned)j << 8) | tid], emax, 50);
+#pragma unroll
+                for (int qn = 0; qn < 5; ++qn) {
+                    const int h = 1 << qn;
+                    const bool lower = !(lane & (unsigned)h);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const longlong2 p = make_longlong2(__shfl_xor_sync(0xffffffffu, x[j].x, h),
+                                                           __shfl_xor_sync(0xffffffffu, x[j].y, h));
+                        x[j] = lower ? ladd(x[j], p) : lsub(p, x[j]);
+                    }
+                }
+                __syncthreads();  // every thread has read its slots as doubles
+#pragma unroll
+                for (int j = 0; j < 16; ++j) ls[((unsigned)j << 8) | tid] = x[j];
+                __syncthreads();
+#pragma unroll
+                for (int j = 0; j < 16; ++j) x[j] = ls[(warp << 9) | ((unsigned)j << 5) | lane];
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        if (j & (1 << b)) continue;
+                        const longlong2 x0 = x[j], x1 = x[j | (1 << b)];
+                        x[j] = ladd(x0, x1);
+                        x[j | (1 << b)] = lsub(x0, x1);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) ls[(warp << 9) | ((unsigned)j << 5) | lane] = x[j];
+                __syncthreads();
+#pragma unroll
+                for (int j = 0; j < 16; ++j) x[j] = ls[((unsigned)j << 8) | tid];
+#pragma unroll
+                for (int b = 1; b < 4; ++b) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        if (j & (1 << b)) continue;
+                        const longlong2 x0 = x[j], x1 = x[j | (1 << b)];
+                        x[j] = ladd(x0, x1);
+                        x[j | (1 << b)] = lsub(x0, x1);
+                    }
+                }
+                const int e2 = fix_out_exp(emax, 12);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = from_fixed2(x[j], e2, false, s2);
+            } else {
 #pragma unroll
             for (int j = 0; j < 16; ++j) v[j] = sl[((unsigned)j << 8) | tid];
             // stages 0..4: partner lane = lane ^ h
@@ -809,6 +1079,7 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
                     v[j | (1 << b)] = cscale(csub(x0, x1), s2);
                 }
             }
+            }  // FP64 butterflies
         }
         // kept slots in ascending slot order: row j (slot bits 8..11), then warp, then lane
         unsigned ball[16];
@@ -842,16 +1113,25 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
             const unsigned total = __shfl_sync(0xffffffffu, inc, 31);
             if (lane == 0) {
                 if (MODE == EMIT_COUNT) a.cnt[g] = total;
-                else if (MODE == EMIT_ATOMIC) s_base = total ? atomicAdd(a.cursor, (unsigned long long)total) : 0ull;
+                else if (MODE == EMIT_ATOMIC) {
+                    s_base = total ? atomicAdd(a.cursor, (unsigned long long)total) : 0ull;
+                    s_fits = s_base + total <= a.capacity;
+                    if (a.ocnt) {
+                        a.ostart[g] = s_base;
+                        a.ocnt[g] = total;
+                    }
+                }
             }
         }
         __syncthreads();
         if (MODE != EMIT_COUNT) {
             const unsigned long long o = MODE == EMIT_WRITE ? a.off[g] : s_base;
             const unsigned lt = (1u << lane) - 1u;
+            // past the output capacity (uniform over the CTA): nothing is written, the host reruns exactly
+            const bool fits = MODE != EMIT_ATOMIC || s_fits;
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-                if (!((ball[j] >> lane) & 1u)) continue;
+                if (!fits || !((ball[j] >> lane) & 1u)) continue;
                 uint64_t kk[K];
 #pragma unroll
                 for (int w = 0; w < K; ++w) kk[w] = gk[w];
@@ -1101,6 +1381,9 @@ __global__ void __launch_bounds__(kSelBlock) scan_seg_kernel(const unsigned* __r
     }
 }
 
+}  // namespace
+
+#ifndef SQ_GROUP_K
 static int g_strategy = 0;  // 0 auto, 1 sort, 2 hash
 static int g_sizing = 0;    // 0 auto (single pass when the output bound fits), 1 exact count-then-scan
 void set_output_sizing(int m) {
@@ -1108,11 +1391,33 @@ void set_output_sizing(int m) {
     g_sizing = m;
 }
 int get_output_sizing() { return g_sizing; }
+static int g_arith = SQ_ARITH_EXACT_SUM;
+void set_fwht_arithmetic(int m) {
+    if (m != SQ_ARITH_REFERENCE && m != SQ_ARITH_EXACT_SUM)
+        fail(SQ_ERR_INVALID, "FWHT arithmetic must be 0 (reference FP64) or 1 (exact sum)");
+    g_arith = m;
+}
+int get_fwht_arithmetic() { return g_arith; }
 void set_group_strategy(int s) {
     if (s < 0 || s > 2) fail(SQ_ERR_INVALID, "group strategy must be 0 (auto), 1 (sort) or 2 (hash)");
     g_strategy = s;
 }
 int get_group_strategy() { return g_strategy; }
+static uint64_t g_hash_groups_hint = 1ull << 20;
+void set_hash_groups_hint(uint64_t g) { g_hash_groups_hint = g ? g : (1ull << 20); }
+uint64_t hash_groups_hint() { return g_hash_groups_hint; }
+static uint64_t g_out_hint = 0;
+void hint_output_size(uint64_t outputs) { g_out_hint = outputs; }
+uint64_t take_output_size_hint() {
+    const uint64_t h = g_out_hint;
+    g_out_hint = 0;
+    return h;
+}
+static uint64_t g_overflows = 0;
+void note_single_pass_overflow() { ++g_overflows; }
+uint64_t single_pass_overflows() { return g_overflows; }
+void note_output_size(int, uint64_t, uint64_t, uint64_t) {}
+#else
 
 // ------------------------------------------------------------------ host pipeline
 struct Grouping {
@@ -1288,9 +1593,6 @@ static Grouping group_by_sort(State& s, const GroupSpec& gs, const uint64_t* gma
     return out;
 }
 
-static uint64_t g_hash_groups_hint = 1ull << 20;
-void set_hash_groups_hint(uint64_t g) { g_hash_groups_hint = g ? g : (1ull << 20); }
-
 template <int K>
 static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg) {
     const uint64_t N = s.n;
@@ -1300,7 +1602,7 @@ static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg) {
     // Table sized for the expected number of groups (load factor <= 1/2);
     // if more groups show up the kernel flags overflow and we retry with a
     // table that fits every entry.
-    uint64_t want = std::min<uint64_t>(N, g_hash_groups_hint);
+    uint64_t want = std::min<uint64_t>(N, hash_groups_hint());
     HashWs h;
     char* base = nullptr;
     size_t off_btgt = 0, off_bamp = 0;
@@ -1372,6 +1674,50 @@ static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg) {
     return out;
 }
 
+template <int K, int MODE>
+static void launch_h4096(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
+    if (am == 2) emit_h4096_kernel<K, MODE, 2><<<grid, 256, sm, st>>>(ea);
+    else if (am == 1) emit_h4096_kernel<K, MODE, 1><<<grid, 256, sm, st>>>(ea);
+    else emit_h4096_kernel<K, MODE, 0><<<grid, 256, sm, st>>>(ea);
+}
+template <int K, int W, bool WRITE>
+static void launch_hadamard(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
+    if (am == 2) emit_hadamard_kernel<K, W, WRITE, 2><<<grid, 256, sm, st>>>(ea);
+    else if (am == 1) emit_hadamard_kernel<K, W, WRITE, 1><<<grid, 256, sm, st>>>(ea);
+    else emit_hadamard_kernel<K, W, WRITE, 0><<<grid, 256, sm, st>>>(ea);
+}
+template <int K>
+static void set_emit_smem_limits() {
+    const int sm = 4096 * (int)sizeof(double2);
+    const int g = 96 * 1024;
+#define SQ_SMEM(f, b) SQ_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, b))
+    SQ_SMEM((emit_h4096_kernel<K, EMIT_COUNT, 0>), sm); SQ_SMEM((emit_h4096_kernel<K, EMIT_COUNT, 1>), sm);
+    SQ_SMEM((emit_h4096_kernel<K, EMIT_COUNT, 2>), sm); SQ_SMEM((emit_h4096_kernel<K, EMIT_WRITE, 0>), sm);
+    SQ_SMEM((emit_h4096_kernel<K, EMIT_WRITE, 1>), sm); SQ_SMEM((emit_h4096_kernel<K, EMIT_WRITE, 2>), sm);
+    SQ_SMEM((emit_h4096_kernel<K, EMIT_ATOMIC, 0>), sm); SQ_SMEM((emit_h4096_kernel<K, EMIT_ATOMIC, 1>), sm);
+    SQ_SMEM((emit_h4096_kernel<K, EMIT_ATOMIC, 2>), sm);
+    SQ_SMEM((emit_hadamard_kernel<K, 256, true, 0>), g); SQ_SMEM((emit_hadamard_kernel<K, 256, true, 1>), g);
+    SQ_SMEM((emit_hadamard_kernel<K, 256, true, 2>), g); SQ_SMEM((emit_hadamard_kernel<K, 256, false, 0>), g);
+    SQ_SMEM((emit_hadamard_kernel<K, 256, false, 1>), g); SQ_SMEM((emit_hadamard_kernel<K, 256, false, 2>), g);
+#undef SQ_SMEM
+}
+
+static bool same_field(const Field& a, const Field& b) {
+    return a.word == b.word && a.shift == b.shift && a.width == b.width;
+}
+static void ensure_cache_set(GroupCache& c, int i, uint64_t G) {
+    if (c.cap[i] >= G) return;
+    const uint64_t cap = std::max<uint64_t>(G + G / 4, 1024);
+    dev_free(c.start[i]);
+    dev_free(c.cnt[i]);
+    c.start[i] = nullptr;
+    c.cnt[i] = nullptr;
+    c.cap[i] = 0;
+    c.start[i] = (unsigned long long*)dev_alloc(cap * 8);
+    c.cnt[i] = (unsigned*)dev_alloc(cap * 4);
+    c.cap[i] = cap;
+}
+
 template <int K>
 static void run_group(State& s, const GroupSpec& gs) {
     const uint64_t N = s.n;
@@ -1391,8 +1737,21 @@ static void run_group(State& s, const GroupSpec& gs) {
     // the merge sums runs in order, so it keeps the (stable) sort; the
     // transforms are order-independent and default to the hash grouping
     const bool use_hash = gs.varw.width ||
-                          (gs.mode != GM_MERGE && (g_strategy == 2 || (g_strategy == 0 && N >= 4096)));
-    Grouping gr = use_hash ? group_by_hash<K>(s, gs, dg) : group_by_sort<K>(s, gs, gmask, dg);
+                          (gs.mode != GM_MERGE && (get_group_strategy() == 2 || (get_group_strategy() == 0 && N >= 4096)));
+    // A Hadamard on the same bits as the split that produced this state (no
+    // key change since, no conditions) takes that split's output ranges as
+    // its groups: every member is still read and transformed, only the
+    // grouping pass is not needed.
+    GroupCache& gc = s.groups;
+    const bool cache_out = (gs.mode == GM_HADAMARD_INT || gs.mode == GM_HADAMARD_FULL) && !gs.varw.width;
+    const bool reuse = gc.valid && cache_out && gs.cond.n == 0 && same_field(gc.target, gs.target) &&
+                       std::equal(gmask, gmask + SQ_KMAX, gc.gmask);
+    gc.valid = false;
+    Grouping gr;
+    if (reuse) gr.G = gc.G;
+    else gr = use_hash ? group_by_hash<K>(s, gs, dg) : group_by_sort<K>(s, gs, gmask, dg);
+    const int am = reuse ? 2 : gr.bucket ? 1 : 0;
+    const int out_set = 1 - gc.cur;
     const uint64_t G = gr.G, F = gr.F, P = N - F;
 
     // emit: count pass, scan, write pass
@@ -1419,6 +1778,25 @@ static void run_group(State& s, const GroupSpec& gs) {
     ea.umat = gs.umat;
     ea.udag = gs.udag;
     ea.varw = gs.varw;
+    ea.fix = get_fwht_arithmetic() == SQ_ARITH_EXACT_SUM ? 1 : 0;
+    if (reuse) {
+        ea.rstart = gc.start[gc.cur];
+        ea.rcnt = gc.cnt[gc.cur];
+    }
+    if (cache_out && gr.F == 0 && gr.G > 0) {
+        ensure_cache_set(gc, out_set, gr.G);
+        ea.ostart = gc.start[out_set];
+        ea.ocnt = gc.cnt[out_set];
+    }
+    // the ranges are kept when every entry landed in one (no pass-through)
+    auto keep_ranges = [&]() {
+        if (!ea.ocnt) return;
+        gc.valid = true;
+        gc.cur = out_set;
+        gc.G = gr.G;
+        gc.target = gs.target;
+        std::copy(gmask, gmask + SQ_KMAX, gc.gmask);
+    };
     ea.cnt = (unsigned*)ws().get(WS_COUNT, (G + 1) * 4);
     unsigned long long* off = (unsigned long long*)ws().get(WS_OFFSET, (G + 1) * 8);
     ea.off = off;
@@ -1439,65 +1817,89 @@ static void run_group(State& s, const GroupSpec& gs) {
     // Hadamard on 12 bits: register FWHT kernel; single pass when the output
     // bound (every group fully populated) fits a modest multiple of the input
     const bool h4096 = !pair && gs.mode != GM_MERGE && gs.mode != GM_UNITARY && nb == 12;
-    const uint64_t bound = G * 4096ull + F;
-    const bool single_pass = h4096 && g_sizing == 0 && bound <= std::max<uint64_t>(4 * N, 1ull << 27);
-    if (h4096) {
-        static bool attr4096 = false;
-        if (!attr4096) {
-            const int sm = 4096 * (int)sizeof(double2);
-            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_COUNT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_WRITE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_ATOMIC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_COUNT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_WRITE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-            SQ_CUDA(cudaFuncSetAttribute(emit_h4096_kernel<K, EMIT_ATOMIC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-            attr4096 = true;
+    // Output sizing. Single pass (each group reserves its outputs with one
+    // atomic) when an output capacity is known up front: the bound "every
+    // group fully populated" when it fits a modest multiple of the input, else
+    // a predicted size when one was given (size_hint_outputs). A single pass
+    // whose outputs overflow the capacity writes nothing past it and the
+    // exact count-then-scan path runs instead, so results never depend on
+    // the capacity.
+    const bool generic = !pair && gs.mode != GM_MERGE;
+    const uint64_t boundT = generic ? G * (uint64_t)S : 0;
+    const uint64_t policy = std::max<uint64_t>(4 * N, 1ull << 27);
+    uint64_t capT = 0;
+    if (generic && get_output_sizing() == 0 && G > 0) {
+        if (boundT <= policy) capT = boundT;
+        else if (const uint64_t hint = take_output_size_hint()) capT = std::min<uint64_t>(hint, boundT);
+    }
+    const bool single_pass = capT > 0;
+    {
+        static bool limits_set = false;
+        if (!limits_set) {
+            set_emit_smem_limits<K>();
+            limits_set = true;
         }
     }
-    auto launch_h4096 = [&](int mode) {
+    // algorithmic bytes of the member reads: cached ranges read the target's
+    // key word and the amplitude of each entry; the hash path its bucketed
+    // (target, amplitude); the sort path index, target word and amplitude
+    const double member_bytes = am == 2 ? 8 + 16 : am == 1 ? 4 + 16 : 4 + 8 + 16;
+    const double group_bytes = am == 2 ? 8 + 4 + 8 * K : 8 + 8 * K + (am == 1 ? 4 : 0);
+    auto launch_h4096_mode = [&](int mode) {
         const unsigned grid = (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2);
         const size_t sm = 4096 * sizeof(double2);
         prof_begin(mode == EMIT_COUNT ? "emit_h4096_count" : mode == EMIT_WRITE ? "emit_h4096_write" : "emit_h4096_single_pass");
-        if (bk) {
-            if (mode == EMIT_COUNT) emit_h4096_kernel<K, EMIT_COUNT, true><<<grid, 256, sm, st>>>(ea);
-            else if (mode == EMIT_WRITE) emit_h4096_kernel<K, EMIT_WRITE, true><<<grid, 256, sm, st>>>(ea);
-            else emit_h4096_kernel<K, EMIT_ATOMIC, true><<<grid, 256, sm, st>>>(ea);
-        } else {
-            if (mode == EMIT_COUNT) emit_h4096_kernel<K, EMIT_COUNT, false><<<grid, 256, sm, st>>>(ea);
-            else if (mode == EMIT_WRITE) emit_h4096_kernel<K, EMIT_WRITE, false><<<grid, 256, sm, st>>>(ea);
-            else emit_h4096_kernel<K, EMIT_ATOMIC, false><<<grid, 256, sm, st>>>(ea);
-        }
-        double b = (double)P * (bk ? 4 + 16 : 4 + 8 + 16) + (double)G * (8 + 8 * K + (bk ? 4 : 0));
-        b += mode == EMIT_COUNT ? (double)G * 4 : (double)T * (8 * K + 16) + (mode == EMIT_WRITE ? (double)G * 8 : 0.0);
+        if (mode == EMIT_COUNT) launch_h4096<K, EMIT_COUNT>(am, grid, sm, st, ea);
+        else if (mode == EMIT_WRITE) launch_h4096<K, EMIT_WRITE>(am, grid, sm, st, ea);
+        else launch_h4096<K, EMIT_ATOMIC>(am, grid, sm, st, ea);
+        double b = (double)P * member_bytes + (double)G * group_bytes;
+        b += mode == EMIT_COUNT ? (double)G * 4 : (double)T * (8 * K + 16) + (mode == EMIT_WRITE ? (double)G * 8 : (double)G * 12);
         prof_end(b);
         SQ_CUDA(cudaGetLastError());
     };
     if (single_pass) {
-        ensure_buffers(s.spare, std::max<uint64_t>(bound, 1), regtable().k, 0);
+        ensure_buffers(s.spare, capT + F, regtable().k, 0);
         for (int w = 0; w < SQ_KMAX; ++w) ea.out_keys.w[w] = s.spare.keys[w];
         ea.out_amp = s.spare.amp;
-        unsigned long long* cur = (unsigned long long*)ws().get(WS_COUNT, (G + 1) * 4 + 64);
+        unsigned long long* cur = (unsigned long long*)ws().get(WS_CURSOR, 64);
         ea.cursor = cur;
+        ea.capacity = capT;
         SQ_CUDA(cudaMemsetAsync(cur, 0, 8, st));
-        if (G > 0) launch_h4096(EMIT_ATOMIC);
+        if (h4096) {
+            launch_h4096_mode(EMIT_ATOMIC);
+        } else {
+            prof_begin("emit_hadamard_single_pass");
+            if (W == 32) launch_hadamard<K, 32, true>(am, (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8), smem, st, ea);
+            else launch_hadamard<K, 256, true>(am, (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2), smem, st, ea);
+            prof_end((double)P * member_bytes + (double)G * (group_bytes + 12));
+            SQ_CUDA(cudaGetLastError());
+        }
         unsigned long long t = 0;
         SQ_CUDA(cudaMemcpyAsync(&t, cur, 8, cudaMemcpyDeviceToHost, st));
         SQ_CUDA(cudaStreamSynchronize(st));
-        T = t;
-        prof_add_bytes_last((double)T * (8 * K + 16));
-        if (F) {
-            prof_begin("passthrough");
-            passthrough_kernel<K><<<grid_for(F, 256), 256, 0, st>>>(ik, s.live.amp, gr.pass, F, ea.out_keys, ea.out_amp, T);
-            prof_end((double)F * (4 + 2.0 * (8 * K + 16)));
-            SQ_CUDA(cudaGetLastError());
+        ea.cursor = nullptr;
+        ea.capacity = 0;
+        note_output_size(gs.mode, N, G, t);
+        if (t <= capT) {
+            T = t;
+            prof_add_bytes_last((double)T * (8 * K + 16));
+            if (F) {
+                prof_begin("passthrough");
+                passthrough_kernel<K><<<grid_for(F, 256), 256, 0, st>>>(ik, s.live.amp, gr.pass, F, ea.out_keys, ea.out_amp, T);
+                prof_end((double)F * (4 + 2.0 * (8 * K + 16)));
+                SQ_CUDA(cudaGetLastError());
+            }
+            swap_live_spare(s);
+            s.n = T + F;
+            keep_ranges();
+            return;
         }
-        swap_live_spare(s);
-        s.n = T + F;
-        return;
+        // the capacity was too small: nothing usable was written, run exactly
+        note_single_pass_overflow();
     }
     auto launch_emit = [&](bool write) {
         if (h4096) {
-            if (G > 0) launch_h4096(write ? EMIT_WRITE : EMIT_COUNT);
+            if (G > 0) launch_h4096_mode(write ? EMIT_WRITE : EMIT_COUNT);
             return;
         }
         if (G == 0) return;
@@ -1514,27 +1916,15 @@ static void run_group(State& s, const GroupSpec& gs) {
             else emit_merge_kernel<K, false><<<grid_for(G, 256), 256, 0, st>>>(ea);
         } else if (W == 32) {
             const unsigned grid = (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8);
-            if (write && bk) emit_hadamard_kernel<K, 32, true, true><<<grid, 256, smem, st>>>(ea);
-            else if (write) emit_hadamard_kernel<K, 32, true, false><<<grid, 256, smem, st>>>(ea);
-            else if (bk) emit_hadamard_kernel<K, 32, false, true><<<grid, 256, smem, st>>>(ea);
-            else emit_hadamard_kernel<K, 32, false, false><<<grid, 256, smem, st>>>(ea);
+            if (write) launch_hadamard<K, 32, true>(am, grid, smem, st, ea);
+            else launch_hadamard<K, 32, false>(am, grid, smem, st, ea);
         } else {
-            static bool attr_set = false;
-            if (!attr_set) {
-                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-                SQ_CUDA(cudaFuncSetAttribute(emit_hadamard_kernel<K, 256, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-                attr_set = true;
-            }
             const unsigned grid = (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2);
-            if (write && bk) emit_hadamard_kernel<K, 256, true, true><<<grid, 256, smem, st>>>(ea);
-            else if (write) emit_hadamard_kernel<K, 256, true, false><<<grid, 256, smem, st>>>(ea);
-            else if (bk) emit_hadamard_kernel<K, 256, false, true><<<grid, 256, smem, st>>>(ea);
-            else emit_hadamard_kernel<K, 256, false, false><<<grid, 256, smem, st>>>(ea);
+            if (write) launch_hadamard<K, 256, true>(am, grid, smem, st, ea);
+            else launch_hadamard<K, 256, false>(am, grid, smem, st, ea);
         }
         // members: target + amplitude (+ index on the sort path); groups: bounds + head key; then counts or outputs
-        double b = (double)P * (bk ? 4 + 16 : 4 + 8 + 16) + (double)G * (8 + 8 * K + (bk ? 4 : 0));
+        double b = (double)P * member_bytes + (double)G * group_bytes;
         b += write ? (double)G * 8 + (double)T * (8 * K + 16) : (double)G * 4;
         prof_end(b);
         SQ_CUDA(cudaGetLastError());
@@ -1552,6 +1942,7 @@ static void run_group(State& s, const GroupSpec& gs) {
         check_device_error();
         T = t;
     }
+    if (generic) note_output_size(gs.mode, N, G, T);
     const uint64_t out_n = T + F;
     ensure_buffers(s.spare, std::max<uint64_t>(out_n, 1), regtable().k, 0);
     for (int w = 0; w < SQ_KMAX; ++w) ea.out_keys.w[w] = s.spare.keys[w];
@@ -1563,23 +1954,43 @@ static void run_group(State& s, const GroupSpec& gs) {
         prof_end((double)F * (4 + 2.0 * (8 * K + 16)));
         SQ_CUDA(cudaGetLastError());
     }
+    if (ea.ocnt) {  // count-then-scan: the counts and offsets are the output ranges
+        SQ_CUDA(cudaMemcpyAsync(ea.ocnt, ea.cnt, G * 4, cudaMemcpyDeviceToDevice, st));
+        SQ_CUDA(cudaMemcpyAsync(ea.ostart, off, G * 8, cudaMemcpyDeviceToDevice, st));
+    }
     swap_live_spare(s);
     s.n = out_n;
+    keep_ranges();
 }
+
+#define SQ_CAT2(a, b) a##b
+#define SQ_CAT(a, b) SQ_CAT2(a, b)
+void SQ_CAT(run_group_k, SQ_GROUP_K)(State& s, const GroupSpec& g) { run_group<SQ_GROUP_K>(s, g); }
+#endif  // SQ_GROUP_K
+
+#ifndef SQ_GROUP_K
+void run_group_k1(State&, const GroupSpec&);
+void run_group_k2(State&, const GroupSpec&);
+void run_group_k3(State&, const GroupSpec&);
+void run_group_k4(State&, const GroupSpec&);
+void run_group_k5(State&, const GroupSpec&);
+void run_group_k6(State&, const GroupSpec&);
+void run_group_k7(State&, const GroupSpec&);
+void run_group_k8(State&, const GroupSpec&);
 
 void group_transform(State& s, const GroupSpec& g) {
     sync_words(s);
     if (s.n == 0) return;
     if (s.n >= (1ull << 30)) fail(SQ_ERR_CAPACITY, "split/merge operators are limited to < 2^30 entries");
     switch (regtable().k) {
-        case 1: run_group<1>(s, g); break;
-        case 2: run_group<2>(s, g); break;
-        case 3: run_group<3>(s, g); break;
-        case 4: run_group<4>(s, g); break;
-        case 5: run_group<5>(s, g); break;
-        case 6: run_group<6>(s, g); break;
-        case 7: run_group<7>(s, g); break;
-        default: run_group<8>(s, g); break;
+        case 1: run_group_k1(s, g); break;
+        case 2: run_group_k2(s, g); break;
+        case 3: run_group_k3(s, g); break;
+        case 4: run_group_k4(s, g); break;
+        case 5: run_group_k5(s, g); break;
+        case 6: run_group_k6(s, g); break;
+        case 7: run_group_k7(s, g); break;
+        default: run_group_k8(s, g); break;
     }
 }
 
@@ -1619,5 +2030,6 @@ void add_systems(State& dst, const State& src, double coef) {
     g.eps = 1e-14;
     group_transform(dst, g);
 }
+#endif  // !SQ_GROUP_K
 
 }  // namespace sq

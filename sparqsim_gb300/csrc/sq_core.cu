@@ -296,6 +296,17 @@ void free_buffers(Buffers& b) {
     b.kalloc = 0;
 }
 
+void free_group_cache(GroupCache& c) {
+    for (int i = 0; i < 2; ++i) {
+        dev_free(c.start[i]);
+        dev_free(c.cnt[i]);
+        c.start[i] = nullptr;
+        c.cnt[i] = nullptr;
+        c.cap[i] = 0;
+    }
+    c.valid = false;
+}
+
 void ensure_buffers(Buffers& b, uint64_t cap, uint32_t k, uint64_t keep) {
     if (k > SQ_KMAX) fail(SQ_ERR_CAPACITY, "too many key words");
     if (keep > b.cap) keep = b.cap;

@@ -36,6 +36,26 @@ void cuda_check(cudaError_t e, const char* what);
 unsigned int* device_error_word();
 
 // ------------------------------------------------------------------ registers
+// Prune predicate of ClearZero and of every split: keep unless
+// x*x + y*y < eps, evaluated in FP64 with that exact rounding. The result is
+// first decided from the exponent fields where they settle it (FP64 runs at a
+// small fraction of the integer rate on this part, and most amplitudes are far
+// from the threshold): with M = max(|x|,|y|) of biased exponent e,
+// M >= 2^(e-1023) gives fl(x*x + y*y) >= 2^(2e-2046), and M < 2^(e-1022) gives
+// fl(x*x + y*y) <= 2^(2e-2043); eps lies in [2^(ee-1023), 2^(ee-1022)).
+#ifdef __CUDACC__
+__device__ __forceinline__ bool sq_keep_amp(double x, double y, double eps) {
+    const int ex = (int)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ff;
+    const int ey = (int)((unsigned long long)__double_as_longlong(y) >> 52) & 0x7ff;
+    const int e = ex > ey ? ex : ey;
+    const long long eb = __double_as_longlong(eps);
+    const int ee = (int)(eb >> 52) & 0x7ff;
+    if (2 * e >= ee + 1024) return true;              // also inf/NaN amplitudes, as the formula does
+    if (eb > 0 && ee > 0 && 2 * e < ee + 1020) return false;  // eps positive and normal
+    return !(x * x + y * y < eps);
+}
+#endif
+
 struct Field {
     uint8_t word;
     uint8_t shift;
@@ -150,11 +170,31 @@ struct Buffers {
     uint32_t kalloc = 0;
 };
 
+// Group ranges left by the last Hadamard split: the entries of each group of
+// that operation's output (equal keys outside the low `target.width` bits of
+// `target`) sit in one contiguous range [start[g], start[g] + cnt[g]). A
+// following split on the same bits takes its groups from here instead of
+// grouping again. Anything that changes key values or entry positions drops
+// the ranges (drop_groups).
+struct GroupCache {
+    bool valid = false;
+    Field target{};
+    uint64_t gmask[SQ_KMAX] = {0};
+    uint64_t G = 0;
+    int cur = 0;                               // the valid set; the other one is written next
+    unsigned long long* start[2] = {nullptr, nullptr};
+    unsigned* cnt[2] = {nullptr, nullptr};
+    uint64_t cap[2] = {0, 0};
+};
+
 struct State {
     Buffers live;
     Buffers spare;
     uint64_t n = 0;
+    GroupCache groups;
 };
+inline void drop_groups(State& s) { s.groups.valid = false; }
+void free_group_cache(GroupCache& c);
 
 struct KeyPtrs {
     uint64_t* w[SQ_KMAX];
@@ -212,6 +252,7 @@ enum WsSlot {
     WS_REDUCE,
     WS_MERGE_KEYS,
     WS_MATRIX,
+    WS_CURSOR,
     WS_COUNT_MAX
 };
 
@@ -260,6 +301,17 @@ void set_group_strategy(int s);
 int get_group_strategy();
 void set_output_sizing(int m);
 int get_output_sizing();
+void set_fwht_arithmetic(int m);
+int get_fwht_arithmetic();
+void set_hash_groups_hint(uint64_t groups);
+uint64_t hash_groups_hint();
+// Output-size hints for the next split (0: none); taken once.
+void hint_output_size(uint64_t outputs);
+uint64_t take_output_size_hint();
+// Split outcomes, for the size predictor's training log and its overflow rate.
+void note_output_size(int mode, uint64_t n_in, uint64_t groups, uint64_t n_out);
+void note_single_pass_overflow();
+uint64_t single_pass_overflows();
 void zero_field(State& s, Field f);
 void move_field(State& s, Field first, Field second, Field dst);
 

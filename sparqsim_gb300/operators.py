@@ -18,7 +18,7 @@ import ctypes
 import math
 from ctypes import byref, c_double, c_uint32
 
-from ._native import OP, SQ_MAX_PROGRAM, SqInstr, call
+from ._native import OP, SQ_ERR_INVALID, SQ_MAX_PROGRAM, SparQInvalid, SqInstr, call
 from .core import Controllable, QRAMCircuit_qutrit, SparseState, StateStorageType, System
 
 PI = math.pi
@@ -513,6 +513,11 @@ class PauliNoise(ElementwiseOperator):
         self.traj = _R(traj_reg)
         self.regs = [_R(r) for r in regs]
         self.noise = table
+        for j, r in enumerate(self.regs):
+            w = System.size_of(r)
+            lim = (1 << w) - 1 if w < 64 else (1 << 64) - 1
+            if int(table.masks[:, j].max(initial=0)) > lim or int(table.masks[:, j + 3].max(initial=0)) > lim:
+                raise SparQInvalid(SQ_ERR_INVALID, f"PauliNoise: a mask of register {r} is wider than its {w} bits")
 
     def _fill(self, ins, dag):
         ins.reg[0] = self.traj

@@ -47,13 +47,28 @@ def _built():
 
 @pytest.fixture(autouse=True)
 def fresh_system():
+    """Fresh register tables; Hadamard butterflies in the reference's FP64
+    order (bit-identical results) unless a test selects exact-sum."""
     import sparqsim_gb300 as ps
     from oracle import oracle as O
     ps.System.clear()
     O.clear()
+    ps.set_fwht_arithmetic("reference")
     yield
     ps.System.clear()
     O.clear()
+    ps.set_fwht_arithmetic("reference")
+
+
+# amplitude errors against the FP64 oracle, per FWHT arithmetic, reported at the end
+AMP_ERRORS: dict = {}
+
+
+def pytest_terminal_summary(terminalreporter):
+    if AMP_ERRORS:
+        terminalreporter.write_line("amplitude error vs the FP64 oracle (max |a_gpu - a_oracle| / max|a|):")
+        for mode, errs in sorted(AMP_ERRORS.items()):
+            terminalreporter.write_line(f"  {mode}: {len(errs)} comparisons, max {max(errs):.3e}")
 
 
 class Dual:
@@ -66,6 +81,7 @@ class Dual:
         self.ps, self.O = ps, O
         self.gpu = None
         self.ora = None
+        self.relaxed = False  # exact-sum FWHT: amplitudes within tolerance instead of bit-exact
 
     def reg(self, name, type_, width):
         rid = self.ps.System.add_register(name, type_, width)
@@ -129,7 +145,9 @@ class Dual:
             raise AssertionError(f"keys differ at rows {bad}: gpu {gk[bad]} oracle {ok[bad]}")
         scale = max(float(np.max(np.abs(oa))) if oa.size else 0.0, 1e-300)
         err = float(np.max(np.abs(ga - oa))) / scale if oa.size else 0.0
-        if exact_amp:
+        mode = self.ps.get_fwht_arithmetic()
+        AMP_ERRORS.setdefault(mode, []).append(err)
+        if exact_amp and not self.relaxed:
             assert np.array_equal(ga.view(np.float64), oa.view(np.float64)), f"amplitudes not bit-exact (rel {err})"
         assert err <= rel, f"amplitude rel error {err} > {rel}"
         return err

@@ -18,10 +18,16 @@ pytestmark = pytest.mark.gpu
 U = ps.UnsignedInteger
 
 
-@pytest.fixture(params=["sort", "hash", "hash-exact"])
-def strategy(request):
+@pytest.fixture(params=["sort", "hash", "hash-exact", "sort-fix", "hash-fix"])
+def strategy(request, dual):
+    """Grouping strategy x output sizing x FWHT arithmetic. The '-fix' cases
+    run the Hadamard butterflies in exact-sum arithmetic: keys stay bit-exact,
+    amplitudes are held to 1e-12 relative (of the largest) instead of bit-exact."""
     ps.set_group_strategy(request.param.split("-")[0])
     ps.set_output_sizing("exact" if request.param.endswith("exact") else "auto")
+    if request.param.endswith("fix"):
+        ps.set_fwht_arithmetic("exact-sum")
+        dual.relaxed = True
     yield request.param
     ps.set_group_strategy("auto")
     ps.set_output_sizing("auto")
@@ -434,6 +440,10 @@ def test_config1_full_size(dual, strategy):
     assert dual.gpu.size() > 16_000_000
     dual.compare(exact_amp=True)
     assert abs(dual.gpu.norm_sq() - 1.0) < 1e-12
+    # and back: 4096 full 4096-member groups merge (the 12-stage FWHT at scale)
+    dual.apply(ps.Hadamard_Int("a", 12))
+    assert dual.gpu.size() == 4096
+    dual.compare(exact_amp=True)
 
 
 def _random_unitary(rng, dim):
