@@ -351,17 +351,19 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     # the same steps in the other butterfly arithmetic (same keys; amplitudes
     # bit-identical to the reference in 'reference', within 1e-12 in 'exact-sum')
     other = "reference" if args.fwht_arithmetic == "exact-sum" else "exact-sum"
-    ps.set_fwht_arithmetic(other)
-    circ.run(st)
-    torch.cuda.synchronize()
-    s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s2.record(ext)
-    for _ in range(args.steps):
+    other_ms = None
+    if not args.skip_other_arithmetic:
+        ps.set_fwht_arithmetic(other)
         circ.run(st)
-    e2.record(ext)
-    e2.synchronize()
-    other_ms = s2.elapsed_time(e2) / args.steps
-    ps.set_fwht_arithmetic(args.fwht_arithmetic)
+        torch.cuda.synchronize()
+        s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s2.record(ext)
+        for _ in range(args.steps):
+            circ.run(st)
+        e2.record(ext)
+        e2.synchronize()
+        other_ms = s2.elapsed_time(e2) / args.steps
+        ps.set_fwht_arithmetic(args.fwht_arithmetic)
 
     # end to end through the public API: host inputs in, final state out
     k = ps.System.key_words()
@@ -413,7 +415,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
                        parallelism="replicas" if world > 1 else "single GPU"),
         "gpu_launches": launches,
         "fwht_arithmetic": args.fwht_arithmetic,
-        f"{other}_arithmetic": {"value": world * updates / (other_ms / 1e3), "unit": UNIT, "ms_per_step": other_ms},
+        f"{other}_arithmetic": ({"value": world * updates / (other_ms / 1e3), "unit": UNIT, "ms_per_step": other_ms}
+                                if other_ms else None),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "note": "public API: QRAM table and initial state uploaded from pinned host memory, final packed "
                         "state downloaded, each step; wall clock"},
@@ -542,6 +545,8 @@ def main():
     ap.add_argument("--hadamard-bits", type=int, default=12)
     ap.add_argument("--layers", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-other-arithmetic", action="store_true",
+                    help="do not also time the other Hadamard butterfly arithmetic")
     ap.add_argument("--trajectories", type=int, default=4096,
                     help="instances in the batched noisy-trajectory leg (0 skips it)")
     ap.add_argument("--plain-sample", type=int, default=256, help="instances timed in the plain GPU form")

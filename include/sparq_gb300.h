@@ -314,6 +314,51 @@ int sq_get_output_sizing(int* mode);
  * in the last place of the group's largest amplitude; keys are identical. It
  * exists because FP64 runs at a small fraction of the integer rate on GB300. */
 enum { SQ_ARITH_REFERENCE = 0, SQ_ARITH_EXACT_SUM = 1 };
+
+/* ------------------------------------------------------------------ size model
+ * A learned model of split-operator output sizes (no counterpart in the
+ * reference): a 3-layer FP32 MLP, SQ_PRED_FEATURES inputs -> 64 -> 64 -> 2,
+ * ReLU, trained on the GPU by this library's own kernels on sizes logged by
+ * the split operators. Features (per operator, before it runs): operator kind
+ * one-hot [0..6] (Hadamard_Int, Hadamard_Int_Full, Hadamard_Bool, Rot_Bool,
+ * CondRot, Rot_GeneralUnitary, merge), [7] per-entry width, [8] target
+ * width / 16, [9] key words / 8, [10] log2 N / 32, [11] cached group ranges
+ * usable, [12] log2(cached groups + 1) / 32, [13] conditions / 8, [15] 1, and
+ * [16..47] a 32-register sketch (max leading-zero rank per hash bucket, / 32)
+ * of the group keys of up to 65536 sampled entries. Outputs:
+ * log2(groups / N) / 16 and log2((outputs + 1) / N) / 16. When enabled, the
+ * predicted group count sizes the hash table and the predicted output count
+ * gives a single-pass capacity where the fully populated bound is too large;
+ * an overflow reruns the operator exactly, so results never depend on it.
+ * Parameters are one float array: W1[48][64], b1[64], W2[64][64], b2[64],
+ * W3[64][2], b3[2] (row-major, [in][out]). */
+#define SQ_PRED_FEATURES 48
+#define SQ_PRED_PARAMS 7426
+int sq_predictor_reset(uint64_t seed);
+int sq_predictor_get_params(float* out, uint64_t n);
+int sq_predictor_set_params(const float* in, uint64_t n);
+/* Mean-squared-error loss and its gradient (same layout as the parameters)
+ * over n rows of features x[n][48] and targets t[n][2]; no update. */
+int sq_predictor_gradient(const float* x, const float* t, uint64_t n, float* grad, float* loss);
+int sq_predictor_predict(const float* x, uint64_t n, float* y);
+/* Adam, `epochs` passes over n rows in shuffled minibatches of `batch`. */
+int sq_predictor_train(const float* x, const float* t, uint64_t n, uint32_t epochs, uint32_t batch, float lr,
+                       uint64_t seed, float* final_loss);
+int sq_predictor_enable(int on);
+/* Logging of (features, sizes) rows by the split operators (host memory). */
+int sq_predictor_log_enable(int on);
+int sq_predictor_log_size(uint64_t* rows);
+int sq_predictor_log_read(float* x, float* t, uint64_t max_rows, uint64_t* rows);
+int sq_predictor_log_clear(void);
+/* Predictions made, and single passes that overflowed their capacity. */
+int sq_predictor_stats(uint64_t* predictions, uint64_t* overflows);
+/* Output entries a single-pass split may allocate by the fully populated
+ * bound (a memory budget); 0 restores the default, max(4 N, 2^27). Beyond
+ * it a split uses a predicted capacity, or else the exact count pass. */
+int sq_set_single_pass_limit(uint64_t entries);
+/* Groups the hash grouping's first table is sized for when no prediction is
+ * made (default 2^20); more groups cost a second, larger attempt. */
+int sq_set_hash_groups_hint(uint64_t groups);
 int sq_set_fwht_arithmetic(int mode);
 int sq_get_fwht_arithmetic(int* mode);
 /* clearzero_default_eps (system_operations.h:577), initially 1e-14. */

@@ -6,7 +6,7 @@ device is visible, calls raise instead of computing anything on the host.
 from __future__ import annotations
 
 import ctypes
-from ctypes import POINTER, c_double, c_int, c_uint32, c_uint64, c_void_p
+from ctypes import POINTER, c_double, c_float, c_int, c_uint32, c_uint64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().with_name("libsparq_gb300.so")
@@ -140,6 +140,21 @@ _SIGS = [
     ("sq_set_output_sizing", c_int, [c_int]),
     ("sq_get_output_sizing", c_int, [POINTER(c_int)]),
     ("sq_set_fwht_arithmetic", c_int, [c_int]),
+    ("sq_set_single_pass_limit", c_int, [c_uint64]),
+    ("sq_set_hash_groups_hint", c_int, [c_uint64]),
+    ("sq_predictor_reset", c_int, [c_uint64]),
+    ("sq_predictor_get_params", c_int, [c_void_p, c_uint64]),
+    ("sq_predictor_set_params", c_int, [c_void_p, c_uint64]),
+    ("sq_predictor_gradient", c_int, [c_void_p, c_void_p, c_uint64, c_void_p, POINTER(c_float)]),
+    ("sq_predictor_predict", c_int, [c_void_p, c_uint64, c_void_p]),
+    ("sq_predictor_train", c_int, [c_void_p, c_void_p, c_uint64, c_uint32, c_uint32, c_float, c_uint64,
+                                   POINTER(c_float)]),
+    ("sq_predictor_enable", c_int, [c_int]),
+    ("sq_predictor_log_enable", c_int, [c_int]),
+    ("sq_predictor_log_size", c_int, [POINTER(c_uint64)]),
+    ("sq_predictor_log_read", c_int, [c_void_p, c_void_p, c_uint64, POINTER(c_uint64)]),
+    ("sq_predictor_log_clear", c_int, []),
+    ("sq_predictor_stats", c_int, [POINTER(c_uint64), POINTER(c_uint64)]),
     ("sq_get_fwht_arithmetic", c_int, [POINTER(c_int)]),
     ("sq_set_clearzero_eps", c_int, [c_double]),
     ("sq_get_clearzero_eps", c_int, [POINTER(c_double)]),

@@ -22,7 +22,7 @@ INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libsparq_gb300.so"
 
-SOURCES = ["sq_core.cu", "elementwise.cu", "compact.cu", "radix_sort.cu", "group_ops.cu", "api.cu"]
+SOURCES = ["sq_core.cu", "elementwise.cu", "compact.cu", "radix_sort.cu", "group_ops.cu", "api.cu", "predictor.cu"]
 # group_ops.cu is also compiled once per key width K (its kernels are templates
 # on K), so that the objects build in parallel: (source, object stem, defines)
 UNITS = [(s, Path(s).stem, []) for s in SOURCES] + \

@@ -393,29 +393,27 @@ int sq_qram_create(uint32_t address_size, uint32_t data_size, const uint64_t* me
     need(data_size <= 64, "QRAM data_size > 64");
     const uint64_t words = 1ull << address_size;
     need(memory != nullptr && n_words >= words, "QRAM memory must hold 2^address_size words");
-    uint64_t mx = 0;
-    for (uint64_t i = 0; i < words; ++i) mx = memory[i] > mx ? memory[i] : mx;
-    uint32_t eb = mx <= 0xffffull ? 2 : (mx <= 0xffffffffull ? 4 : 8);
-    std::vector<char> buf((size_t)words * eb);
-    for (uint64_t i = 0; i < words; ++i) {
-        if (eb == 2) ((uint16_t*)buf.data())[i] = (uint16_t)memory[i];
-        else if (eb == 4) ((uint32_t*)buf.data())[i] = (uint32_t)memory[i];
-        else ((uint64_t*)buf.data())[i] = memory[i];
-    }
+    // the highest bit any word uses decides the stored width (and is checked
+    // against the data register at use); the narrowing runs on the GPU
+    uint64_t all = 0;
+    for (uint64_t i = 0; i < words; ++i) all |= memory[i];
+    const uint32_t eb = all <= 0xffffull ? 2 : (all <= 0xffffffffull ? 4 : 8);
     sq_qram* q = new sq_qram();
     q->t.elem_bytes = eb;
     q->t.address_size = address_size;
     q->t.data_size = data_size;
     q->t.n_words = words;
-    q->t.max_word = mx;
-    void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, buf.size());
-    if (e != cudaSuccess) {
+    q->t.max_word = all;
+    try {
+        q->t.dev = dev_alloc((size_t)words * eb);
+        qram_pack(memory, words, eb, q->t.dev);
+        // the caller's buffer may be pinned: the copy completes before return
+        SQ_CUDA(cudaStreamSynchronize(stream()));
+    } catch (...) {
+        dev_free(q->t.dev);
         delete q;
-        SQ_CUDA(e);
+        throw;
     }
-    q->t.dev = p;
-    SQ_CUDA(cudaMemcpy(p, buf.data(), buf.size(), cudaMemcpyHostToDevice));
     *out = q;
     SQ_API_END
 }
@@ -423,8 +421,7 @@ int sq_qram_create(uint32_t address_size, uint32_t data_size, const uint64_t* me
 int sq_qram_destroy(sq_qram* q) {
     SQ_API_BEGIN
     if (!q) return SQ_OK;
-    SQ_CUDA(cudaStreamSynchronize(stream()));
-    if (q->t.dev) SQ_CUDA(cudaFree(q->t.dev));
+    dev_free(q->t.dev);  // stream-ordered: after every launch that reads it
     delete q;
     SQ_API_END
 }
@@ -764,6 +761,18 @@ int sq_get_output_sizing(int* mode) {
     SQ_API_BEGIN
     need(mode != nullptr, "null pointer");
     *mode = get_output_sizing();
+    SQ_API_END
+}
+
+int sq_set_hash_groups_hint(uint64_t groups) {
+    SQ_API_BEGIN
+    set_hash_groups_hint(groups);
+    SQ_API_END
+}
+
+int sq_set_single_pass_limit(uint64_t entries) {
+    SQ_API_BEGIN
+    set_single_pass_limit(entries);
     SQ_API_END
 }
 

@@ -524,6 +524,31 @@ void run_program(State& s, const sq_instr* prog, uint32_t n) {
     }
 }
 
+// QRAM tables are stored at the narrowest width that holds every word.
+__global__ void qram_pack_kernel(const uint64_t* __restrict__ src, uint64_t n, uint32_t eb, void* __restrict__ dst) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint64_t v = src[i];
+        if (eb == 2) ((unsigned short*)dst)[i] = (unsigned short)v;
+        else ((unsigned int*)dst)[i] = (unsigned int)v;
+    }
+}
+
+void qram_pack(const uint64_t* host_words, uint64_t n, uint32_t eb, void* dst) {
+    cudaStream_t st = stream();
+    if (eb == 8) {
+        SQ_CUDA(cudaMemcpyAsync(dst, host_words, n * 8, cudaMemcpyHostToDevice, st));
+        return;
+    }
+    uint64_t* tmp = (uint64_t*)dev_alloc(n * 8);
+    SQ_CUDA(cudaMemcpyAsync(tmp, host_words, n * 8, cudaMemcpyHostToDevice, st));
+    prof_begin("qram_pack");
+    qram_pack_kernel<<<grid_for(n, 256), 256, 0, st>>>(tmp, n, eb, dst);
+    prof_end((double)n * (8 + eb));
+    SQ_CUDA(cudaGetLastError());
+    dev_free(tmp);
+}
+
 // Zero one register field in every entry (AddRegister on reused bits,
 // remove_register_synchronous).
 template <int K>

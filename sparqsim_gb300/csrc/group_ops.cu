@@ -59,10 +59,16 @@ __device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 __device__ __forceinline__ bool keep_amp(double2 a, double eps) { return sq_keep_amp(a.x, a.y, eps); }
-// a * -1.0 without the FP64 pipe (same bits for every non-NaN value)
-__device__ __forceinline__ double2 cneg(double2 a) {
-    return make_double2(__longlong_as_double(__double_as_longlong(a.x) ^ (long long)0x8000000000000000ull),
-                        __longlong_as_double(__double_as_longlong(a.y) ^ (long long)0x8000000000000000ull));
+// Store of a or -a (the bits of a * -1.0 for every non-NaN a) as integer
+// bits: a negation kept in double registers would be issued as an FP64 add.
+template <int K>
+__device__ __forceinline__ void store_entry_sign(const KeyPtrs& kp, double2* amp, unsigned long long o,
+                                                 const uint64_t (&k)[K], double2 a, bool negate) {
+#pragma unroll
+    for (int w = 0; w < K; ++w) kp.w[w][o] = k[w];
+    const unsigned long long s = negate ? 0x8000000000000000ull : 0ull;
+    reinterpret_cast<ulonglong2*>(amp)[o] = make_ulonglong2((unsigned long long)__double_as_longlong(a.x) ^ s,
+                                                            (unsigned long long)__double_as_longlong(a.y) ^ s);
 }
 
 // ------------------------------------------------------------------ exact-sum FWHT arithmetic
@@ -95,9 +101,23 @@ __device__ __forceinline__ long long to_fixed(double x, int emax, int F) {
     else q = (mant + (1ull << (r - 1))) >> r;  // half away from zero
     return (b >> 63) ? -(long long)q : (long long)q;
 }
+// The same for F <= 52 (n >= 10), where the shift is always a right shift:
+// branch-free (a shift past the mantissa rounds to 0 at 63 just as at 64+).
+__device__ __forceinline__ long long to_fixed_right(double x, int emax, int F) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)(b >> 52) & 0x7ff;
+    const unsigned long long mant = (b & 0xfffffffffffffull) | (ex ? (1ull << 52) : 0ull);
+    const int r = min(emax - (ex ? ex : 1) + 53 - F, 63);
+    const unsigned long long q = (mant + (1ull << (r - 1))) >> r;
+    const unsigned long long sg = 0ull - (b >> 63);  // all ones when negative
+    return (long long)((q ^ sg) - sg);
+}
 __device__ __forceinline__ longlong2 to_fixed2(double2 v, int emax, int F) {
     return make_longlong2(to_fixed(v.x, emax, F), to_fixed(v.y, emax, F));
 }
+// outside the normal range (two roundings); a call of its own, so that the
+// conversion is not issued for every slot
+static __device__ __noinline__ double fixed_to_double_scaled(long long Y, int e2) { return scalbn((double)Y, e2); }
 // Y * 2^e2 rounded to nearest even (|Y| < 2^63)
 __device__ __forceinline__ double fixed_to_double(long long Y, int e2) {
     if (Y == 0) return 0.0;
@@ -119,7 +139,7 @@ __device__ __forceinline__ double fixed_to_double(long long Y, int e2) {
         q = m << (52 - top);
     }
     const int be = ex + e2 + 1023;
-    if (be <= 0 || be >= 2047) return scalbn((double)Y, e2);  // outside the normal range (two roundings)
+    if (be <= 0 || be >= 2047) return fixed_to_double_scaled(Y, e2);
     return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (q & 0xfffffffffffffull)));
 }
 __device__ __forceinline__ double2 from_fixed2(longlong2 v, int e2, bool odd, double s2) {
@@ -682,8 +702,7 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
 #pragma unroll
                     for (int w = 0; w < K; ++w) kk[w] = gk[w];
                     fset<K>(kk, tg, (uint64_t)c);
-                    const double2 v = (__popcll((uint64_t)c & v0) & 1) ? cneg(base) : base;
-                    store_entry<K>(a.out_keys, a.out_amp, o + c, kk, v);
+                    store_entry_sign<K>(a.out_keys, a.out_amp, o + c, kk, base, __popcll((uint64_t)c & v0) & 1);
                 }
             }
             worker_sync<W>();
@@ -734,7 +753,7 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
                 uint64_t tj;
                 double2 aj;
                 member_at<AM>(a, s0 + j, tj, aj);
-                slots[tj] = aj;
+                slots[tj & (S - 1u)] = aj;  // cached ranges of a batched split: only the group's own n bits
                 emax = max(emax, amp_exp(aj));
             }
             const bool fix = a.fix && a.mode != GM_UNITARY;
@@ -844,11 +863,36 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
 // groups in the output is then not fixed, the values are).
 enum { EMIT_COUNT = 0, EMIT_WRITE = 1, EMIT_ATOMIC = 2 };
 
+// lower ? p : -v, chosen on the bit patterns
+__device__ __forceinline__ double2 sel_neg(bool lower, double2 p, double2 v) {
+    const unsigned long long sx = (unsigned long long)__double_as_longlong(v.x) ^ 0x8000000000000000ull;
+    const unsigned long long sy = (unsigned long long)__double_as_longlong(v.y) ^ 0x8000000000000000ull;
+    return make_double2(__longlong_as_double((long long)(lower ? (unsigned long long)__double_as_longlong(p.x) : sx)),
+                        __longlong_as_double((long long)(lower ? (unsigned long long)__double_as_longlong(p.y) : sy)));
+}
+
+// The 4-stage exact-sum FWHT of 16 values held by one thread (index bits
+// 0-3 of j), stages in ascending order.
+__device__ __forceinline__ void fwht16(longlong2 (&x)[16]) {
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            if (j & (1 << b)) continue;
+            const longlong2 x0 = x[j], x1 = x[j | (1 << b)];
+            x[j] = ladd(x0, x1);
+            x[j | (1 << b)] = lsub(x0, x1);
+        }
+    }
+}
+
 __device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
     return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
 }
 
-template <int K, int MODE, int AM>
+// FIX selects the exact-sum arithmetic at compile time: one arithmetic per
+// instantiation keeps the unrolled code within the instruction cache.
+template <int K, int MODE, int AM, bool FIX>
 __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constant__ EmitArgs a) {
     extern __shared__ double2 sl[];  // 4096 slots
     __shared__ unsigned s_cnt[16][8];
@@ -906,14 +950,14 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
 #pragma unroll
                     for (int w = 0; w < K; ++w) kk[w] = gk[w];
                     fset<K>(kk, tg, (uint64_t)c);
-                    const double2 v = (__popcll((uint64_t)c & v0) & 1) ? cneg(base) : base;
-                    store_entry<K>(a.out_keys, a.out_amp, o + c, kk, v);
+                    store_entry_sign<K>(a.out_keys, a.out_amp, o + c, kk, base, __popcll((uint64_t)c & v0) & 1);
                 }
             }
             __syncthreads();
             continue;
         }
         double2 v[16];
+        unsigned rows = 0xffffu;  // rows j that may hold a kept slot (warp-uniform)
         if (a.mode == GM_HADAMARD_FULL && m <= 11u) {
             // sparse bucket: direct product, members in ascending target order (hadamard.cpp:267-304)
             for (unsigned j = tid; j < m; j += 256u) {
@@ -951,12 +995,24 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
                 v[j] = acc;
             }
         } else {
+            // A full cached range holds its members in ascending target order
+            // (every emit writes a group's outputs in slot order), so member c
+            // has target c: the 16 slots of a thread load straight into
+            // registers, 16 coalesced loads in flight, no scatter.
+            const bool direct = AM == 2 && m == 4096u;
+            int emax = 1;
+            if (direct) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = __ldcs(a.in_amp + s0 + (((unsigned)j << 8) | tid));
+#pragma unroll
+                for (int j = 0; j < 16; ++j) emax = max(emax, amp_exp(v[j]));
+            } else {
 #pragma unroll
             for (int j = 0; j < 16; ++j) sl[((unsigned)j << 8) | tid] = make_double2(0.0, 0.0);
             __syncthreads();
+            }
             // members: 8 independent loads in flight per thread, then scatter
-            int emax = 1;
-            for (unsigned j0 = 0; j0 < m; j0 += 8u * 256u) {
+            for (unsigned j0 = 0; !direct && j0 < m; j0 += 8u * 256u) {
                 uint64_t tq[8];
                 double2 aq[8];
 #pragma unroll
@@ -973,67 +1029,65 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
                     }
                 }
             }
-            if (a.fix) {
+            if (FIX) {
                 emax = (int)__reduce_max_sync(0xffffffffu, (unsigned)emax);
                 if (lane == 0) s_emax[warp] = (unsigned)emax;
             }
             __syncthreads();
-            if (a.fix) {
-                // exact-sum arithmetic: same stage layout on the int64 grid, one rounding at the end
+            if (FIX) {
+                // exact-sum arithmetic on the int64 grid, one rounding at the end.
+                // Every stage runs in registers: a thread holds 16 slots that
+                // differ in bits 0-3 (layout P: slot = tid << 4 | j), then bits
+                // 4-7 (layout Q: slot = tid_hi << 8 | j << 4 | tid_lo), then
+                // bits 8-11 (layout A); two shared-memory transposes in between.
+                // Slots are stored at s ^ ((s >> 4) & 7) (16-byte units), which
+                // keeps all three layouts free of bank conflicts.
 #pragma unroll
                 for (int i = 0; i < 8; ++i) emax = max(emax, (int)s_emax[i]);
                 longlong2* ls = reinterpret_cast<longlong2*>(sl);
                 longlong2 x[16];
 #pragma unroll
-                for (int j = 0; j < 16; ++j) x[j] = to_fixed2(sl[((unsigned)j << 8) | tid], emax, 50);
-#pragma unroll
-                for (int qn = 0; qn < 5; ++qn) {
-                    const int h = 1 << qn;
-                    const bool lower = !(lane & (unsigned)h);
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        const longlong2 p = make_longlong2(__shfl_xor_sync(0xffffffffu, x[j].x, h),
-                                                           __shfl_xor_sync(0xffffffffu, x[j].y, h));
-                        x[j] = lower ? ladd(x[j], p) : lsub(p, x[j]);
-                    }
+                for (int j = 0; j < 16; ++j) {
+                    const double2 d = direct ? v[j] : sl[((unsigned)j << 8) | tid];
+                    x[j] = make_longlong2(to_fixed_right(d.x, emax, 50), to_fixed_right(d.y, emax, 50));
                 }
+                auto sw = [](unsigned q) { return q ^ ((q >> 4) & 7u); };
                 __syncthreads();  // every thread has read its slots as doubles
 #pragma unroll
-                for (int j = 0; j < 16; ++j) ls[((unsigned)j << 8) | tid] = x[j];
+                for (int j = 0; j < 16; ++j) ls[sw(((unsigned)j << 8) | tid)] = x[j];
                 __syncthreads();
 #pragma unroll
-                for (int j = 0; j < 16; ++j) x[j] = ls[(warp << 9) | ((unsigned)j << 5) | lane];
+                for (int j = 0; j < 16; ++j) x[j] = ls[sw((tid << 4) | (unsigned)j)];
+                fwht16(x);  // stages 0-3
 #pragma unroll
-                for (int b = 0; b < 4; ++b) {
+                for (int j = 0; j < 16; ++j) ls[sw((tid << 4) | (unsigned)j)] = x[j];
+                __syncthreads();
+                const unsigned qb = ((tid >> 4) << 8) | (tid & 15u);
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        if (j & (1 << b)) continue;
-                        const longlong2 x0 = x[j], x1 = x[j | (1 << b)];
-                        x[j] = ladd(x0, x1);
-                        x[j | (1 << b)] = lsub(x0, x1);
-                    }
-                }
+                for (int j = 0; j < 16; ++j) x[j] = ls[sw(qb | ((unsigned)j << 4))];
+                fwht16(x);  // stages 4-7
 #pragma unroll
-                for (int j = 0; j < 16; ++j) ls[(warp << 9) | ((unsigned)j << 5) | lane] = x[j];
+                for (int j = 0; j < 16; ++j) ls[sw(qb | ((unsigned)j << 4))] = x[j];
                 __syncthreads();
 #pragma unroll
-                for (int j = 0; j < 16; ++j) x[j] = ls[((unsigned)j << 8) | tid];
-#pragma unroll
-                for (int b = 1; b < 4; ++b) {
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        if (j & (1 << b)) continue;
-                        const longlong2 x0 = x[j], x1 = x[j | (1 << b)];
-                        x[j] = ladd(x0, x1);
-                        x[j | (1 << b)] = lsub(x0, x1);
-                    }
-                }
+                for (int j = 0; j < 16; ++j) x[j] = ls[sw(((unsigned)j << 8) | tid)];
+                fwht16(x);  // stages 8-11
                 const int e2 = fix_out_exp(emax, 12);
 #pragma unroll
-                for (int j = 0; j < 16; ++j) v[j] = from_fixed2(x[j], e2, false, s2);
+                for (int j = 0; j < 16; ++j) {
+                    // merges leave most slots exactly zero: skip the conversion
+                    // and the prune test row by row
+                    const bool nz = (x[j].x | x[j].y) != 0;
+                    if (__any_sync(0xffffffffu, nz)) {
+                        v[j] = from_fixed2(x[j], e2, false, s2);
+                    } else {
+                        v[j] = make_double2(0.0, 0.0);
+                        rows &= ~(1u << j);
+                    }
+                }
             } else {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) v[j] = sl[((unsigned)j << 8) | tid];
+            for (int j = 0; !direct && j < 16; ++j) v[j] = sl[((unsigned)j << 8) | tid];
             // stages 0..4: partner lane = lane ^ h
 #pragma unroll
             for (int qn = 0; qn < 5; ++qn) {
@@ -1042,7 +1096,9 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const double2 p = shfl_xor_d2(v[j], h);
-                    v[j] = lower ? cscale(cadd(v[j], p), s2) : cscale(csub(p, v[j]), s2);
+                    // lower: (v + p) * s2; upper: (p - v) * s2 = (p + (-v)) * s2, the
+                    // same rounding; operands picked as bits so that one add is issued
+                    v[j] = cscale(cadd(lower ? v[j] : p, sel_neg(lower, p, v[j])), s2);
                 }
             }
             // transpose A -> B
@@ -1085,7 +1141,7 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
         unsigned ball[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-            ball[j] = __ballot_sync(0xffffffffu, keep_amp(v[j], a.eps));
+            ball[j] = ((rows >> j) & 1u) ? __ballot_sync(0xffffffffu, keep_amp(v[j], a.eps)) : 0u;
             if (lane == 0) s_cnt[j][warp] = __popc(ball[j]);
         }
         __syncthreads();
@@ -1164,6 +1220,19 @@ __global__ void passthrough_kernel(ConstKeyPtrs ik, const double2* __restrict__ 
 // on a locked slot is bounded.
 constexpr unsigned long long kSlotLocked = ~0ull;
 
+// atomicAdd(ctr, 1) for each calling lane, one atomic per group of lanes that
+// execute the call together (new group ids: every lane of a warp of
+// singleton groups would otherwise hit the same counter)
+__device__ __forceinline__ unsigned warp_aggregated_add(unsigned* ctr) {
+    const unsigned am = __activemask();
+    const unsigned lane = threadIdx.x & 31u;
+    const int leader = __ffs(am) - 1;
+    unsigned base = 0;
+    if ((int)lane == leader) base = atomicAdd(ctr, (unsigned)__popc(am));
+    base = __shfl_sync(am, base, leader);
+    return base + (unsigned)__popc(am & ((1u << lane) - 1u));
+}
+
 struct HashWs {
     unsigned long long* slots;
     unsigned long long cap_mask;
@@ -1173,6 +1242,14 @@ struct HashWs {
     unsigned* gid;        // group of each entry (~0u: fails the conditions)
     unsigned* pass_list;  // entries failing the conditions
 };
+
+// The overflow flag is read coherently (another SM sets it while this lane
+// may be waiting on a slot that the setter locked and will never fill).
+__device__ __forceinline__ bool overflowed(const HashWs& h) {
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> f(h.gcount[2]);
+    return f.load(cuda::memory_order_relaxed) != 0u;
+}
+
 
 __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
     x ^= x >> 30;
@@ -1214,8 +1291,7 @@ __global__ void __launch_bounds__(256) hash_insert_kernel(ConstKeyPtrs keys, con
                 }
             }
             if (!pass) {
-                const unsigned p = atomicAdd(&h.gcount[1], 1u);
-                h.pass_list[p] = (unsigned)i;
+                h.pass_list[warp_aggregated_add(&h.gcount[1])] = (unsigned)i;
                 h.gid[i] = ~0u;
             }
         }
@@ -1238,13 +1314,13 @@ __global__ void __launch_bounds__(256) hash_insert_kernel(ConstKeyPtrs keys, con
             unsigned long long slot = hv & h.cap_mask;
             unsigned spins = 0;
             for (unsigned long long probes = 0; probes <= h.cap_mask;) {
-                if (h.gcount[2]) break;  // table overflowed: the host retries with a larger one
+                if (overflowed(h)) break;  // table overflowed: the host retries with a larger one
                 cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> ref(h.slots[slot]);
                 unsigned long long v = ref.load(cuda::memory_order_relaxed);
                 if (v == 0ull) {
                     unsigned long long expected = 0ull;
                     if (ref.compare_exchange_strong(expected, kSlotLocked, cuda::memory_order_relaxed)) {
-                        const unsigned g = atomicAdd(&h.gcount[0], 1u);
+                        const unsigned g = warp_aggregated_add(&h.gcount[0]);
                         if (g >= gmax) {
                             atomicExch(&h.gcount[2], 1u);
                             break;
@@ -1292,8 +1368,178 @@ __global__ void __launch_bounds__(256) hash_insert_kernel(ConstKeyPtrs keys, con
         if (pass) {
             if (!probe) mygid = lg;
             h.gid[i] = mygid;
-            if (mygid == ~0u && !h.gcount[2]) atomicOr(err, 2u);  // probe gave up: reported
+            if (mygid == ~0u && !overflowed(h)) atomicOr(err, 2u);  // probe gave up: reported
         }
+    }
+}
+
+// Sketch of the group keys for the size model: 32 registers, each the largest
+// leading-zero rank (+1) of the hashed keys falling in its bucket (the
+// HyperLogLog register update), over `samples` entries taken at a stride.
+template <int K>
+__global__ void __launch_bounds__(256) sketch_kernel(ConstKeyPtrs keys, const uint64_t* __restrict__ gmask,
+                                                     uint64_t stride, unsigned samples, unsigned* __restrict__ regs) {
+    __shared__ unsigned sr[32];
+    if (threadIdx.x < 32) sr[threadIdx.x] = 0;
+    __syncthreads();
+    for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < samples; s += gridDim.x * blockDim.x) {
+        const uint64_t i = (uint64_t)s * stride;
+        unsigned long long hv = 0x9e3779b97f4a7c15ull;
+#pragma unroll
+        for (int w = 0; w < K; ++w) hv = mix64(hv ^ (keys.w[w][i] & gmask[w]) ^ (0x632be59bd9b4e019ull * (w + 1)));
+        const unsigned bucket = (unsigned)(hv >> 59);
+        const unsigned rank = (unsigned)__clzll((long long)((hv << 5) | 1ull)) + 1u;
+        atomicMax(&sr[bucket], rank);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) atomicMax(&regs[threadIdx.x], sr[threadIdx.x]);
+}
+
+// Grouping of a small state in one CTA: the hash table, the member counts and
+// the group starts live in shared memory, so grouping is one launch instead of
+// the table clear, insert, scan and bucket launches. A slot holds its head
+// entry + 1 (claimed by one compare-and-swap, never locked); later entries
+// compare their masked key with the head's. Outputs match the multi-CTA hash
+// path: group starts, one head per group, members' (target, amplitude)
+// contiguous per group, and the entries that fail the conditions.
+constexpr unsigned kSmallGroupMax = 8192;  // entries
+constexpr unsigned kSmallPer = kSmallGroupMax / 1024;
+
+template <int K>
+__device__ __forceinline__ void group_key(const ConstKeyPtrs& keys, unsigned e, const uint64_t (&gm)[K], Field tgt,
+                                          Field varw, uint64_t (&k)[K]) {
+#pragma unroll
+    for (int w = 0; w < K; ++w) k[w] = keys.w[w][e] & gm[w];
+    if (varw.width) {
+        uint64_t full[K];
+#pragma unroll
+        for (int w = 0; w < K; ++w) full[w] = keys.w[w][e];
+        const unsigned nd = (unsigned)fget<K>(full, varw);
+        kword_set<K>(k, tgt.word, kword<K>(k, tgt.word) & ~(wmask(nd) << tgt.shift));
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(1024) group_small_kernel(ConstKeyPtrs keys, const uint64_t* __restrict__ gmask,
+                                                           DCondSet cond, const double2* __restrict__ amp,
+                                                           unsigned n, unsigned cap, Field tgt, Field varw,
+                                                           unsigned max_digits, unsigned* __restrict__ counts,
+                                                           unsigned* __restrict__ seg, unsigned* __restrict__ ghead,
+                                                           unsigned* __restrict__ btgt, double2* __restrict__ bamp,
+                                                           unsigned* __restrict__ pass_list, unsigned* err) {
+    extern __shared__ unsigned s_tab[];  // cap slots | cap counts
+    unsigned* table = s_tab;
+    unsigned* cnt = s_tab + cap;
+    __shared__ unsigned s_F, s_scan[32][2];
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    for (unsigned i = tid; i < 2 * cap; i += 1024u) s_tab[i] = 0u;
+    if (tid == 0) s_F = 0u;
+    uint64_t gm[K];
+#pragma unroll
+    for (int w = 0; w < K; ++w) gm[w] = gmask[w];
+    __syncthreads();
+    unsigned myslot[kSmallPer];
+#pragma unroll
+    for (unsigned q = 0; q < kSmallPer; ++q) {
+        const unsigned e = tid + q * 1024u;
+        myslot[q] = ~0u;
+        if (e >= n) continue;
+        uint64_t full[K];
+#pragma unroll
+        for (int w = 0; w < K; ++w) full[w] = keys.w[w][e];
+        bool pass = cond_ok<K>(full, cond);
+        if (pass && varw.width && (unsigned)fget<K>(full, varw) > max_digits) {
+            atomicOr(err, 4u);
+            pass = false;
+        }
+        if (!pass) {
+            pass_list[atomicAdd(&s_F, 1u)] = e;
+            continue;
+        }
+        uint64_t k[K];
+        group_key<K>(keys, e, gm, tgt, varw, k);
+        unsigned long long hv = 0x9e3779b97f4a7c15ull;
+#pragma unroll
+        for (int w = 0; w < K; ++w) hv = mix64(hv ^ k[w] ^ (0x632be59bd9b4e019ull * (w + 1)));
+        unsigned slot = (unsigned)hv & (cap - 1u);
+        for (unsigned probes = 0; probes < cap; ++probes) {  // the table holds 2x the entries: always ends
+            const unsigned old = atomicCAS(&table[slot], 0u, e + 1u);
+            if (old == 0u) break;
+            uint64_t hk[K];
+            group_key<K>(keys, old - 1u, gm, tgt, varw, hk);
+            bool eq = true;
+#pragma unroll
+            for (int w = 0; w < K; ++w) eq = eq && hk[w] == k[w];
+            if (eq) break;
+            slot = (slot + 1u) & (cap - 1u);
+        }
+        myslot[q] = slot;
+        atomicAdd(&cnt[slot], 1u);
+    }
+    __syncthreads();
+    // dense group ids and member offsets: one block-wide scan over the slots in order
+    const unsigned per = cap / 1024u;  // cap >= 1024
+    const unsigned s0 = tid * per;
+    unsigned occ = 0, mem = 0;
+    for (unsigned i = 0; i < per; ++i) {
+        occ += table[s0 + i] ? 1u : 0u;
+        mem += cnt[s0 + i];
+    }
+    unsigned io = occ, im = mem;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned a = __shfl_up_sync(0xffffffffu, io, o), b = __shfl_up_sync(0xffffffffu, im, o);
+        if (lane >= (unsigned)o) {
+            io += a;
+            im += b;
+        }
+    }
+    if (lane == 31) {
+        s_scan[warp][0] = io;
+        s_scan[warp][1] = im;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        unsigned a = s_scan[lane][0], b = s_scan[lane][1];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned x = __shfl_up_sync(0xffffffffu, a, o), y = __shfl_up_sync(0xffffffffu, b, o);
+            if (lane >= (unsigned)o) {
+                a += x;
+                b += y;
+            }
+        }
+        s_scan[lane][0] = a;
+        s_scan[lane][1] = b;
+    }
+    __syncthreads();
+    unsigned gid = io - occ + (warp ? s_scan[warp - 1][0] : 0u);
+    unsigned off = im - mem + (warp ? s_scan[warp - 1][1] : 0u);
+    for (unsigned i = 0; i < per; ++i) {
+        const unsigned h = table[s0 + i];
+        if (!h) continue;
+        seg[gid] = off;
+        ghead[gid] = h - 1u;
+        off += cnt[s0 + i];
+        cnt[s0 + i] = seg[gid];  // fill cursor of the slot's group
+        ++gid;
+    }
+    if (tid == 1023) {
+        counts[0] = s_scan[31][0];
+        counts[1] = s_F;
+        seg[s_scan[31][0]] = s_scan[31][1];
+    }
+    __syncthreads();
+    // members, contiguous per group
+#pragma unroll
+    for (unsigned q = 0; q < kSmallPer; ++q) {
+        const unsigned e = tid + q * 1024u;
+        if (myslot[q] == ~0u) continue;
+        const unsigned pos = atomicAdd(&cnt[myslot[q]], 1u);
+        const unsigned nd = varw.width ? (unsigned)((keys.w[varw.word][e] >> varw.shift) & wmask(varw.width))
+                                       : tgt.width;
+        btgt[pos] = (unsigned)((keys.w[tgt.word][e] >> tgt.shift) & wmask(nd));
+        bamp[pos] = amp[e];
     }
 }
 
@@ -1413,6 +1659,9 @@ uint64_t take_output_size_hint() {
     g_out_hint = 0;
     return h;
 }
+static uint64_t g_single_limit = 0;  // 0: max(4 N, 2^27)
+void set_single_pass_limit(uint64_t entries) { g_single_limit = entries; }
+uint64_t single_pass_limit() { return g_single_limit; }
 static uint64_t g_overflows = 0;
 void note_single_pass_overflow() { ++g_overflows; }
 uint64_t single_pass_overflows() { return g_overflows; }
@@ -1594,15 +1843,49 @@ static Grouping group_by_sort(State& s, const GroupSpec& gs, const uint64_t* gma
 }
 
 template <int K>
-static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg) {
+static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg, uint64_t want_groups) {
     const uint64_t N = s.n;
     cudaStream_t st = stream();
     ConstKeyPtrs ik;
     for (int w = 0; w < SQ_KMAX; ++w) ik.w[w] = s.live.keys[w];
+    if (N <= kSmallGroupMax) {
+        unsigned cap = 1024;
+        while (cap < 2 * N) cap <<= 1;
+        // one allocation: counts | seg | head | pass | bucket target | bucket amp
+        const size_t o_seg = 64, o_head = o_seg + (N + 2) * 4, o_pass = o_head + N * 4, o_btgt = o_pass + N * 4;
+        const size_t o_bamp = (o_btgt + N * 4 + 15) & ~size_t(15), total = o_bamp + N * 16;
+        char* base = (char*)ws().get(WS_MERGE_KEYS, total);
+        static bool smem_set = false;
+        if (!smem_set) {
+            SQ_CUDA(cudaFuncSetAttribute(group_small_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(2 * 2 * kSmallGroupMax * 4)));
+            smem_set = true;
+        }
+        prof_begin("group_small");
+        group_small_kernel<K><<<1, 1024, 2 * cap * 4, st>>>(
+            ik, dg, gs.cond, s.live.amp, (unsigned)N, cap, gs.target, gs.varw, gs.target.width, (unsigned*)base,
+            (unsigned*)(base + o_seg), (unsigned*)(base + o_head), (unsigned*)(base + o_btgt),
+            (double2*)(base + o_bamp), (unsigned*)(base + o_pass), device_error_word());
+        prof_end((double)N * (8.0 * K + 16) * 2);
+        SQ_CUDA(cudaGetLastError());
+        unsigned gc[2] = {0, 0};
+        SQ_CUDA(cudaMemcpyAsync(gc, base, 8, cudaMemcpyDeviceToHost, st));
+        check_device_error();  // synchronizes
+        Grouping out;
+        out.G = gc[0];
+        out.F = gc[1];
+        out.seg = (unsigned*)(base + o_seg);
+        out.ghead = (unsigned*)(base + o_head);
+        out.btgt = (unsigned*)(base + o_btgt);
+        out.bamp = (double2*)(base + o_bamp);
+        out.pass = (unsigned*)(base + o_pass);
+        out.bucket = true;
+        return out;
+    }
     // Table sized for the expected number of groups (load factor <= 1/2);
     // if more groups show up the kernel flags overflow and we retry with a
     // table that fits every entry.
-    uint64_t want = std::min<uint64_t>(N, hash_groups_hint());
+    uint64_t want = std::min<uint64_t>(N, want_groups ? want_groups : hash_groups_hint());
     HashWs h;
     char* base = nullptr;
     size_t off_btgt = 0, off_bamp = 0;
@@ -1674,11 +1957,49 @@ static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg) {
     return out;
 }
 
+constexpr uint64_t kModelMinEntries = 1ull << 15;  // below this a prediction costs more than it saves
+
+// Features of the size model (layout in sparq_gb300.h).
+template <int K>
+static void split_features(State& s, const GroupSpec& gs, uint64_t N, const uint64_t* dg, bool cached,
+                           uint64_t cached_groups, float* f) {
+    const int kind = gs.mode == GM_HADAMARD_INT ? 0 : gs.mode == GM_HADAMARD_FULL ? 1 : gs.mode == GM_HADAMARD_BOOL ? 2
+                   : gs.mode == GM_ROT ? 3 : (gs.mode == GM_CONDROT) ? 4 : gs.mode == GM_UNITARY ? 5 : 6;
+    f[kind] = 1.f;
+    f[7] = gs.varw.width ? 1.f : 0.f;
+    f[8] = (float)gs.target.width / 16.f;
+    f[9] = (float)K / 8.f;
+    f[10] = (float)(std::log2((double)N) / 32.0);
+    f[11] = cached ? 1.f : 0.f;
+    f[12] = cached ? (float)(std::log2((double)cached_groups + 1.0) / 32.0) : 0.f;
+    f[13] = (float)gs.cond.n / 8.f;
+    f[15] = 1.f;
+    cudaStream_t st = stream();
+    unsigned* regs = (unsigned*)ws().get(WS_SKETCH, 32 * 4);
+    SQ_CUDA(cudaMemsetAsync(regs, 0, 32 * 4, st));
+    const unsigned samples = (unsigned)std::min<uint64_t>(N, 65536);
+    ConstKeyPtrs ik;
+    for (int w = 0; w < SQ_KMAX; ++w) ik.w[w] = s.live.keys[w];
+    prof_begin("size_sketch");
+    sketch_kernel<K><<<64, 256, 0, st>>>(ik, dg, N / samples, samples, regs);
+    prof_end((double)samples * 8 * K);
+    SQ_CUDA(cudaGetLastError());
+    unsigned h[32];
+    SQ_CUDA(cudaMemcpyAsync(h, regs, sizeof(h), cudaMemcpyDeviceToHost, st));
+    SQ_CUDA(cudaStreamSynchronize(st));
+    for (int i = 0; i < 32; ++i) f[16 + i] = (float)h[i] / 32.f;
+}
+
+template <int K, int MODE, bool FIX>
+static void launch_h4096_arith(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
+    if (am == 2) emit_h4096_kernel<K, MODE, 2, FIX><<<grid, 256, sm, st>>>(ea);
+    else if (am == 1) emit_h4096_kernel<K, MODE, 1, FIX><<<grid, 256, sm, st>>>(ea);
+    else emit_h4096_kernel<K, MODE, 0, FIX><<<grid, 256, sm, st>>>(ea);
+}
 template <int K, int MODE>
 static void launch_h4096(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
-    if (am == 2) emit_h4096_kernel<K, MODE, 2><<<grid, 256, sm, st>>>(ea);
-    else if (am == 1) emit_h4096_kernel<K, MODE, 1><<<grid, 256, sm, st>>>(ea);
-    else emit_h4096_kernel<K, MODE, 0><<<grid, 256, sm, st>>>(ea);
+    if (ea.fix) launch_h4096_arith<K, MODE, true>(am, grid, sm, st, ea);
+    else launch_h4096_arith<K, MODE, false>(am, grid, sm, st, ea);
 }
 template <int K, int W, bool WRITE>
 static void launch_hadamard(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
@@ -1691,11 +2012,14 @@ static void set_emit_smem_limits() {
     const int sm = 4096 * (int)sizeof(double2);
     const int g = 96 * 1024;
 #define SQ_SMEM(f, b) SQ_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, b))
-    SQ_SMEM((emit_h4096_kernel<K, EMIT_COUNT, 0>), sm); SQ_SMEM((emit_h4096_kernel<K, EMIT_COUNT, 1>), sm);
-    SQ_SMEM((emit_h4096_kernel<K, EMIT_COUNT, 2>), sm); SQ_SMEM((emit_h4096_kernel<K, EMIT_WRITE, 0>), sm);
-    SQ_SMEM((emit_h4096_kernel<K, EMIT_WRITE, 1>), sm); SQ_SMEM((emit_h4096_kernel<K, EMIT_WRITE, 2>), sm);
-    SQ_SMEM((emit_h4096_kernel<K, EMIT_ATOMIC, 0>), sm); SQ_SMEM((emit_h4096_kernel<K, EMIT_ATOMIC, 1>), sm);
-    SQ_SMEM((emit_h4096_kernel<K, EMIT_ATOMIC, 2>), sm);
+#define SQ_SMEM_H(m)                                                                                           \
+    SQ_SMEM((emit_h4096_kernel<K, m, 0, false>), sm); SQ_SMEM((emit_h4096_kernel<K, m, 1, false>), sm);       \
+    SQ_SMEM((emit_h4096_kernel<K, m, 2, false>), sm); SQ_SMEM((emit_h4096_kernel<K, m, 0, true>), sm);        \
+    SQ_SMEM((emit_h4096_kernel<K, m, 1, true>), sm); SQ_SMEM((emit_h4096_kernel<K, m, 2, true>), sm);
+    SQ_SMEM_H(EMIT_COUNT)
+    SQ_SMEM_H(EMIT_WRITE)
+    SQ_SMEM_H(EMIT_ATOMIC)
+#undef SQ_SMEM_H
     SQ_SMEM((emit_hadamard_kernel<K, 256, true, 0>), g); SQ_SMEM((emit_hadamard_kernel<K, 256, true, 1>), g);
     SQ_SMEM((emit_hadamard_kernel<K, 256, true, 2>), g); SQ_SMEM((emit_hadamard_kernel<K, 256, false, 0>), g);
     SQ_SMEM((emit_hadamard_kernel<K, 256, false, 1>), g); SQ_SMEM((emit_hadamard_kernel<K, 256, false, 2>), g);
@@ -1743,13 +2067,34 @@ static void run_group(State& s, const GroupSpec& gs) {
     // its groups: every member is still read and transformed, only the
     // grouping pass is not needed.
     GroupCache& gc = s.groups;
-    const bool cache_out = (gs.mode == GM_HADAMARD_INT || gs.mode == GM_HADAMARD_FULL) && !gs.varw.width;
+    const bool cache_out = gs.mode == GM_HADAMARD_INT || gs.mode == GM_HADAMARD_FULL;
     const bool reuse = gc.valid && cache_out && gs.cond.n == 0 && same_field(gc.target, gs.target) &&
-                       std::equal(gmask, gmask + SQ_KMAX, gc.gmask);
+                       same_field(gc.varw, gs.varw) && std::equal(gmask, gmask + SQ_KMAX, gc.gmask);
     gc.valid = false;
+
+    // the size model: features before the operator, sizes after it
+    const bool model_on = (predictor_enabled() || predictor_logging()) && N >= kModelMinEntries;
+    float feat[SQ_PRED_FEATURES] = {0.f};
+    float pred[2] = {0.f, 0.f};
+    bool have_pred = false;
+    if (model_on) {
+        split_features<K>(s, gs, N, dg, reuse, gc.G, feat);
+        have_pred = predictor_predict(feat, pred);
+    }
+    const double g_pred = have_pred ? (double)N * std::exp2(16.0 * pred[0]) : 0.0;
+    const double t_pred = have_pred ? (double)N * std::exp2(16.0 * pred[1]) : 0.0;
+
     Grouping gr;
     if (reuse) gr.G = gc.G;
-    else gr = use_hash ? group_by_hash<K>(s, gs, dg) : group_by_sort<K>(s, gs, gmask, dg);
+    else if (use_hash) gr = group_by_hash<K>(s, gs, dg, have_pred ? (uint64_t)(g_pred * 1.5) + 1024 : 0);
+    else gr = group_by_sort<K>(s, gs, gmask, dg);
+    // logged once the output size is known
+    auto log_sizes = [&](uint64_t T_out) {
+        if (!model_on || !predictor_logging()) return;
+        const float t[2] = {(float)(std::log2((double)std::max<uint64_t>(gr.G, 1) / (double)N) / 16.0),
+                            (float)(std::log2((double)(T_out + 1) / (double)N) / 16.0)};
+        predictor_log(feat, t);
+    };
     const int am = reuse ? 2 : gr.bucket ? 1 : 0;
     const int out_set = 1 - gc.cur;
     const uint64_t G = gr.G, F = gr.F, P = N - F;
@@ -1795,6 +2140,7 @@ static void run_group(State& s, const GroupSpec& gs) {
         gc.cur = out_set;
         gc.G = gr.G;
         gc.target = gs.target;
+        gc.varw = gs.varw;
         std::copy(gmask, gmask + SQ_KMAX, gc.gmask);
     };
     ea.cnt = (unsigned*)ws().get(WS_COUNT, (G + 1) * 4);
@@ -1826,11 +2172,16 @@ static void run_group(State& s, const GroupSpec& gs) {
     // the capacity.
     const bool generic = !pair && gs.mode != GM_MERGE;
     const uint64_t boundT = generic ? G * (uint64_t)S : 0;
-    const uint64_t policy = std::max<uint64_t>(4 * N, 1ull << 27);
+    const uint64_t policy = single_pass_limit() ? single_pass_limit() : std::max<uint64_t>(4 * N, 1ull << 27);
     uint64_t capT = 0;
-    if (generic && get_output_sizing() == 0 && G > 0) {
+    // every group reserves its outputs with one atomic on one cursor: past a
+    // few thousand small groups that serialisation costs more than a count pass
+    const uint64_t max_single_groups = h4096 ? (1ull << 16) : 8192;
+    if (generic && get_output_sizing() == 0 && G > 0 && G <= max_single_groups) {
+        const uint64_t hint = take_output_size_hint();
         if (boundT <= policy) capT = boundT;
-        else if (const uint64_t hint = take_output_size_hint()) capT = std::min<uint64_t>(hint, boundT);
+        else if (hint) capT = std::min<uint64_t>(hint, boundT);
+        else if (have_pred) capT = std::min<uint64_t>((uint64_t)(t_pred * 1.25) + 4096, boundT);
     }
     const bool single_pass = capT > 0;
     {
@@ -1840,11 +2191,12 @@ static void run_group(State& s, const GroupSpec& gs) {
             limits_set = true;
         }
     }
-    // algorithmic bytes of the member reads: cached ranges read the target's
-    // key word and the amplitude of each entry; the hash path its bucketed
-    // (target, amplitude); the sort path index, target word and amplitude
-    const double member_bytes = am == 2 ? 8 + 16 : am == 1 ? 4 + 16 : 4 + 8 + 16;
-    const double group_bytes = am == 2 ? 8 + 4 + 8 * K : 8 + 8 * K + (am == 1 ? 4 : 0);
+    // Algorithmic bytes of a split, as the operator is defined: every entry
+    // in and every entry out once, E = 8K + 16 bytes each, (P + T) * E, booked
+    // on the launch that writes the outputs; a count pass books its re-read
+    // of the inputs, P * E. (What the kernels physically move differs by
+    // access mode: a full cached range is read as amplitudes only.)
+    const double E = 8.0 * K + 16.0;
     auto launch_h4096_mode = [&](int mode) {
         const unsigned grid = (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2);
         const size_t sm = 4096 * sizeof(double2);
@@ -1852,9 +2204,7 @@ static void run_group(State& s, const GroupSpec& gs) {
         if (mode == EMIT_COUNT) launch_h4096<K, EMIT_COUNT>(am, grid, sm, st, ea);
         else if (mode == EMIT_WRITE) launch_h4096<K, EMIT_WRITE>(am, grid, sm, st, ea);
         else launch_h4096<K, EMIT_ATOMIC>(am, grid, sm, st, ea);
-        double b = (double)P * member_bytes + (double)G * group_bytes;
-        b += mode == EMIT_COUNT ? (double)G * 4 : (double)T * (8 * K + 16) + (mode == EMIT_WRITE ? (double)G * 8 : (double)G * 12);
-        prof_end(b);
+        prof_end(mode == EMIT_COUNT ? (double)P * E : (double)(P + T) * E);
         SQ_CUDA(cudaGetLastError());
     };
     if (single_pass) {
@@ -1871,7 +2221,7 @@ static void run_group(State& s, const GroupSpec& gs) {
             prof_begin("emit_hadamard_single_pass");
             if (W == 32) launch_hadamard<K, 32, true>(am, (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8), smem, st, ea);
             else launch_hadamard<K, 256, true>(am, (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2), smem, st, ea);
-            prof_end((double)P * member_bytes + (double)G * (group_bytes + 12));
+            prof_end((double)P * E);
             SQ_CUDA(cudaGetLastError());
         }
         unsigned long long t = 0;
@@ -1882,6 +2232,7 @@ static void run_group(State& s, const GroupSpec& gs) {
         note_output_size(gs.mode, N, G, t);
         if (t <= capT) {
             T = t;
+            log_sizes(T);
             prof_add_bytes_last((double)T * (8 * K + 16));
             if (F) {
                 prof_begin("passthrough");
@@ -1923,10 +2274,7 @@ static void run_group(State& s, const GroupSpec& gs) {
             if (write) launch_hadamard<K, 256, true>(am, grid, smem, st, ea);
             else launch_hadamard<K, 256, false>(am, grid, smem, st, ea);
         }
-        // members: target + amplitude (+ index on the sort path); groups: bounds + head key; then counts or outputs
-        double b = (double)P * member_bytes + (double)G * group_bytes;
-        b += write ? (double)G * 8 + (double)T * (8 * K + 16) : (double)G * 4;
-        prof_end(b);
+        prof_end(write ? (double)(P + T) * E : (double)P * E);
         SQ_CUDA(cudaGetLastError());
     };
     launch_emit(false);
@@ -1943,6 +2291,7 @@ static void run_group(State& s, const GroupSpec& gs) {
         T = t;
     }
     if (generic) note_output_size(gs.mode, N, G, T);
+    log_sizes(T);
     const uint64_t out_n = T + F;
     ensure_buffers(s.spare, std::max<uint64_t>(out_n, 1), regtable().k, 0);
     for (int w = 0; w < SQ_KMAX; ++w) ea.out_keys.w[w] = s.spare.keys[w];

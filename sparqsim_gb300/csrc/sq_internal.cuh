@@ -44,6 +44,11 @@ unsigned int* device_error_word();
 // M >= 2^(e-1023) gives fl(x*x + y*y) >= 2^(2e-2046), and M < 2^(e-1022) gives
 // fl(x*x + y*y) <= 2^(2e-2043); eps lies in [2^(ee-1023), 2^(ee-1022)).
 #ifdef __CUDACC__
+// The FP64 evaluation sits in a function of its own so that the compiler
+// branches around it instead of issuing it, predicated off, for every entry.
+static __device__ __noinline__ bool sq_keep_amp_fp64(double x, double y, double eps) {
+    return !(x * x + y * y < eps);
+}
 __device__ __forceinline__ bool sq_keep_amp(double x, double y, double eps) {
     const int ex = (int)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ff;
     const int ey = (int)((unsigned long long)__double_as_longlong(y) >> 52) & 0x7ff;
@@ -52,7 +57,7 @@ __device__ __forceinline__ bool sq_keep_amp(double x, double y, double eps) {
     const int ee = (int)(eb >> 52) & 0x7ff;
     if (2 * e >= ee + 1024) return true;              // also inf/NaN amplitudes, as the formula does
     if (eb > 0 && ee > 0 && 2 * e < ee + 1020) return false;  // eps positive and normal
-    return !(x * x + y * y < eps);
+    return sq_keep_amp_fp64(x, y, eps);
 }
 #endif
 
@@ -159,7 +164,7 @@ struct QramTable {
     uint32_t address_size = 0;
     uint32_t data_size = 0;
     uint64_t n_words = 0;
-    uint64_t max_word = 0;
+    uint64_t max_word = 0;  // OR of every word: the highest bit any word uses
 };
 
 // ------------------------------------------------------------------ state
@@ -179,6 +184,7 @@ struct Buffers {
 struct GroupCache {
     bool valid = false;
     Field target{};
+    Field varw{};                              // batched width register (width 0: none)
     uint64_t gmask[SQ_KMAX] = {0};
     uint64_t G = 0;
     int cur = 0;                               // the valid set; the other one is written next
@@ -195,6 +201,8 @@ struct State {
 };
 inline void drop_groups(State& s) { s.groups.valid = false; }
 void free_group_cache(GroupCache& c);
+// Copy a host table of 64-bit words to `dst` on the device as eb-byte words.
+void qram_pack(const uint64_t* host_words, uint64_t n, uint32_t eb, void* dst);
 
 struct KeyPtrs {
     uint64_t* w[SQ_KMAX];
@@ -253,6 +261,7 @@ enum WsSlot {
     WS_MERGE_KEYS,
     WS_MATRIX,
     WS_CURSOR,
+    WS_SKETCH,
     WS_COUNT_MAX
 };
 
@@ -312,6 +321,13 @@ uint64_t take_output_size_hint();
 void note_output_size(int mode, uint64_t n_in, uint64_t groups, uint64_t n_out);
 void note_single_pass_overflow();
 uint64_t single_pass_overflows();
+void set_single_pass_limit(uint64_t entries);
+uint64_t single_pass_limit();
+// The learned size model (predictor.cu).
+bool predictor_enabled();
+bool predictor_logging();
+bool predictor_predict(const float* features, float* out);
+void predictor_log(const float* features, const float* sizes);
 void zero_field(State& s, Field f);
 void move_field(State& s, Field first, Field second, Field dst);
 

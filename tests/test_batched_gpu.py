@@ -51,7 +51,13 @@ def test_hadamard_int_batched(dual, maxd, arith):
     op = ps.Hadamard_Int_Batched("a", "w", maxd)
     dual.apply(op)
     dual.compare(exact_amp=True)
-    dual.apply(op)  # H.H merges every trajectory back
+    from sparqsim_gb300 import _native
+    _native.profile_reset()
+    _native.profile_enable(True)
+    dual.apply(op)  # H.H merges every trajectory back, on the first split's cached group ranges
+    _native.profile_enable(False)
+    names = _native.profile_read()
+    assert "hash_insert" not in names and "group_small" not in names
     dual.compare(exact_amp=True)
 
 

@@ -14,7 +14,7 @@ from sparqsim_gb300 import _native
 pytestmark = pytest.mark.gpu
 
 U = ps.UnsignedInteger
-GROUPING_KERNELS = ("hash_insert", "bucket_members", "radix_onesweep", "radix_histogram", "group_stats")
+GROUPING_KERNELS = ("hash_insert", "bucket_members", "radix_onesweep", "radix_histogram", "group_stats", "group_small")
 
 
 def _grouping_ran(fn) -> bool:
