@@ -2174,9 +2174,9 @@ static void run_group(State& s, const GroupSpec& gs) {
     const uint64_t boundT = generic ? G * (uint64_t)S : 0;
     const uint64_t policy = single_pass_limit() ? single_pass_limit() : std::max<uint64_t>(4 * N, 1ull << 27);
     uint64_t capT = 0;
-    // every group reserves its outputs with one atomic on one cursor: past a
-    // few thousand small groups that serialisation costs more than a count pass
-    const uint64_t max_single_groups = h4096 ? (1ull << 16) : 8192;
+    // every group reserves its outputs with one atomic on one cursor; past
+    // about a million groups that serialisation costs more than a count pass
+    const uint64_t max_single_groups = 1ull << 20;
     if (generic && get_output_sizing() == 0 && G > 0 && G <= max_single_groups) {
         const uint64_t hint = take_output_size_hint();
         if (boundT <= policy) capT = boundT;
