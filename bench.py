@@ -294,6 +294,61 @@ def run_trajectories(args, ext) -> dict:
     return out
 
 
+def run_qda(args, ext) -> dict:
+    """QDA walk steps at N = 2^16 (config 3's size) with the tridiagonal block
+    encoding: A = alpha I + beta (S + S^T) with kappa(A) about 50, b uniform,
+    on the schedule of a 2000-step walk. The first `--qda-steps` steps are run
+    once with size counting (untimed), then again from the start, timed."""
+    import torch
+
+    import sparqsim_gb300 as ps
+    from sparqsim_gb300 import qda
+    n_bits, beta = 16, 1.0
+    alpha = 2 * beta * 51 / 49  # eigenvalues alpha + 2 beta cos(k pi / (N+1)): kappa about 50
+    kappa, p, total_steps, sample = 50.0, 0.5, 2000, args.qda_steps
+
+    class Counting(qda.Runner):
+        def __init__(self, state, count):
+            super().__init__(state)
+            self.count, self.updates = count, 0
+
+        def op(self, o, dag=False):
+            n0 = self.state.size() if self.count else 0
+            super().op(o, dag)
+            if self.count:
+                self.updates += max(n0, self.state.size())
+
+    def walk(count):
+        ps.System.clear()
+        run = Counting(ps.SparseState(capacity=1 << 22), count)
+        qda.declare_registers(run, n_bits)
+        run.op(ps.Hadamard_Int_Full("main_reg"))
+        enc_A = qda.BlockEncodingTridiagonal("main_reg", "anc_UA", alpha, beta)
+        enc_b = qda.StatePrepHadamard("main_reg")
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        s.record(ext)
+        for n in range(sample):
+            qda.WalkS(enc_A, enc_b, *qda.REGS, n / total_steps, kappa, p).apply(run)
+            run.op(ps.ClearZero())
+        e.record(ext)
+        e.synchronize()
+        return run, s.elapsed_time(e), time.perf_counter() - t0
+
+    counted, _, _ = walk(True)
+    run, ms, wall = walk(False)
+    return {
+        "workload": (f"QDA walk, N=2^{n_bits}, tridiagonal block encoding of alpha I + beta (S + S^T) "
+                     f"(alpha={alpha:.4f}, beta={beta}, kappa about 50), b uniform, schedule of a "
+                     f"{total_steps}-step walk (p={p}); its first {sample} steps timed"),
+        "steps_timed": sample, "entries_after": run.state.size(),
+        "updates": counted.updates, "value": counted.updates / (ms / 1e3), "unit": UNIT,
+        "ms_per_walk_step": ms / sample, "wall_ms_per_walk_step": wall * 1e3 / sample,
+        "projected_2000_step_walk_s": ms / sample * total_steps / 1e3,
+    }
+
+
 def run_gb300(args, rank: int, world: int, local_rank: int):
     import numpy as np
     import torch
@@ -430,6 +485,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         result["clocks"] = clocks
     if args.trajectories and rank == 0:
         result["batched_trajectories"] = run_trajectories(args, ext)
+    if args.qda_steps and rank == 0:
+        result["qda_walk"] = run_qda(args, ext)
     return result, (table, thetas)
 
 
@@ -551,6 +608,7 @@ def main():
                     help="instances in the batched noisy-trajectory leg (0 skips it)")
     ap.add_argument("--plain-sample", type=int, default=256, help="instances timed in the plain GPU form")
     ap.add_argument("--cpu-sample", type=int, default=16, help="instances timed in the oracle")
+    ap.add_argument("--qda-steps", type=int, default=20, help="QDA walk steps timed at N=2^16 (0 skips)")
     ap.add_argument("--fwht-arithmetic", default="exact-sum", choices=["exact-sum", "reference"],
                     help="Hadamard butterfly arithmetic of the headline run (the other one is timed too)")
     args = ap.parse_args()

@@ -115,6 +115,8 @@ typedef enum {
     SQ_OP_X_BOOL = 34,               /* basic_gates.cpp:383-401  flip bit imm0 of reg0 */
     SQ_OP_INIT_UNSAFE = 35,          /* dark_magic.cpp:35-40     reg0 = imm0 */
     SQ_OP_QRAM_LOAD = 36,            /* qram.cpp:15-35  reg1 ^= table[reg0 mod 2^addr_size] */
+    SQ_OP_PLUS_ONE_OVERFLOW = 37,    /* SparQ_Algorithm/src/BlockEncoding/block_encoding_tridiagonal.cpp:20-83
+                                        reg0 = reg0 +/- 1 mod 2^width; on the wrap reg1 = (reg1 + 1) % 2 */
     /* amplitude-only or key+amplitude elementwise ops */
     SQ_OP_PHASE_BOOL = 64,           /* basic_gates.cpp:11-54  amp *= c0 if bit imm0 of reg0 */
     SQ_OP_GLOBAL_PHASE = 65,         /* parallel_phase_operations.cpp:72-107  amp *= c0 */

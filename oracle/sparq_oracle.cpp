@@ -222,6 +222,27 @@ static void apply_instr_entry(System& s, const sq_instr& in) {
             else o = (o - in.imm[0]) & m;
             return;
         }
+        case SQ_OP_PLUS_ONE_OVERFLOW: {  // block_encoding_tridiagonal.cpp:20-83
+            uint64_t& v = s.get(r[0]);
+            uint64_t& ov = s.get(r[1]);
+            const uint64_t top = width_mask(size_of(r[0]));
+            if (!in.dag) {
+                if (v == top) {
+                    ov = (ov + 1) % 2;
+                    v = 0;
+                } else {
+                    v += 1;
+                }
+            } else {
+                if (v == 0) {
+                    ov = (ov + 1) % 2;
+                    v = top;
+                } else {
+                    v -= 1;
+                }
+            }
+            return;
+        }
         case SQ_OP_SUB_UINT_UINT: {  // :490-509
             uint64_t& o = s.get(r[2]);
             o = (o ^ (get_as(s, r[0]) - get_as(s, r[1]))) & width_mask(size_of(r[2]));

@@ -32,7 +32,7 @@ OP = dict(
     OR_UINT_UINT=20, XOR_UINT_UINT=21, LESS_SINT_SINT=22, CARRY_UINT_UINT=23,
     OVERFLOW_SINT_SINT=24, MULOVERFLOW_UINT_UINT=25, ISZERO_UINT=26, NEGATIVE_SINT=27,
     ADD_ANYINT_INPLACE=28, ASSIGN=29, COMPARE_UINT_UINT=30, LESS_UINT_UINT=31, SWAP_GENERAL=32,
-    GETMID_UINT_UINT=33, X_BOOL=34, INIT_UNSAFE=35, QRAM_LOAD=36, PHASE_BOOL=64, GLOBAL_PHASE=65,
+    GETMID_UINT_UINT=33, X_BOOL=34, INIT_UNSAFE=35, QRAM_LOAD=36, PLUS_ONE_OVERFLOW=37, PHASE_BOOL=64, GLOBAL_PHASE=65,
     Y_BOOL=66, REFLECTION_BOOL=67, ZERO_COND_PHASE_FLIP=68, ROT_DIAGONAL=69, ROT_OFF_DIAGONAL=70,
     PAULI_NOISE=71,
 )

@@ -553,19 +553,32 @@ int sq_zero_cond_phase_flip(sq_state* st, const uint32_t* regs, uint32_t nregs, 
 // ------------------------------------------------------------------ split / merge
 static double cz_eps() { return regtable().clearzero_eps; }
 
+// H on more than 12 bits: H^(x)n factorises over disjoint bit sets, so the
+// low 12 bits run first, then the next (up to 12) bits, each pass grouping by
+// every other bit. In the reference arithmetic each slot sees the same
+// stage-ascending butterflies as in one pass; groups that one pass would treat
+// as a singleton or a sparse bucket are rounded as in the FWHT instead (within
+// 1e-15 relative).
+static void hadamard_passes(State& s, Field f, uint32_t n, int mode, const DCondSet& cond) {
+    for (uint32_t lo = 0; lo < n; lo += 12) {
+        GroupSpec g;
+        memset(&g, 0, sizeof(g));
+        g.mode = mode;
+        g.target = f;
+        g.target.shift = (uint8_t)(f.shift + lo);
+        g.target.width = (uint8_t)std::min<uint32_t>(12, n - lo);
+        g.cond = cond;
+        g.eps = cz_eps();
+        group_transform(s, g);
+    }
+}
+
 int sq_hadamard_int(sq_state* st, uint32_t reg, uint32_t n_digits, const sq_cond* cond) {
     SQ_API_BEGIN
     Field f = regtable().field(reg);
     need(n_digits <= f.width, "Hadamard_Int: n_digits larger than the register");
-    GroupSpec g;
-    memset(&g, 0, sizeof(g));
-    g.mode = GM_HADAMARD_INT;
-    g.target = f;
-    g.target.width = (uint8_t)n_digits;
-    g.cond = resolve_cond(cond);
-    g.eps = cz_eps();
     if (n_digits == 0) return SQ_OK;
-    group_transform(S(st), g);
+    hadamard_passes(S(st), f, n_digits, GM_HADAMARD_INT, resolve_cond(cond));
     SQ_API_END
 }
 
@@ -599,6 +612,10 @@ int sq_hadamard_int_full(sq_state* st, uint32_t reg, const sq_cond* cond) {
     g.cond = resolve_cond(cond);
     g.eps = cz_eps();
     if (f.width == 0) return SQ_OK;
+    if (f.width > 12) {  // the register in passes of 12 bits
+        hadamard_passes(S(st), f, f.width, GM_HADAMARD_INT, g.cond);
+        return SQ_OK;
+    }
     group_transform(S(st), g);
     SQ_API_END
 }

@@ -123,6 +123,14 @@ __device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2
             fset<K>(k, f[0], in.dag ? o - in.imm[0] : o + in.imm[0]);
             break;
         }
+        case SQ_OP_PLUS_ONE_OVERFLOW: {
+            const uint64_t v = fget<K>(k, f[0]);
+            const uint64_t top = wmask(f[0].width);
+            const bool wrap = in.dag ? v == 0 : v == top;
+            fset<K>(k, f[0], in.dag ? v - 1 : v + 1);  // stored modulo 2^width
+            if (wrap) fset<K>(k, f[1], (fget<K>(k, f[1]) + 1) % 2);
+            break;
+        }
         case SQ_OP_SUB_UINT_UINT: fset<K>(k, f[2], fget<K>(k, f[2]) ^ (fget<K>(k, f[0]) - fget<K>(k, f[1]))); break;
         case SQ_OP_NEG_UINT: fset<K>(k, f[1], fget<K>(k, f[1]) ^ (0ull - fget<K>(k, f[0]))); break;
         case SQ_OP_ABS_SINT: {
@@ -403,6 +411,10 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
             break;
         case SQ_OP_ADD_UINT_CONST: R(0); W(2); distinct(in.reg[0], in.reg[2], "Add_UInt_ConstUInt"); break;
         case SQ_OP_ADD_CONST_INPLACE: W(0); break;
+        case SQ_OP_PLUS_ONE_OVERFLOW:
+            W(0); W(1);
+            distinct(in.reg[0], in.reg[1], "PlusOneAndOverflow");
+            break;
         case SQ_OP_NEG_UINT:
         case SQ_OP_ABS_SINT:
         case SQ_OP_SQRT_UINT:

@@ -475,13 +475,13 @@ __device__ __forceinline__ void group_range(const EmitArgs& a, uint64_t g, unsig
 }
 
 // Pair modes (1-bit target): one thread per group.
-template <int K, bool WRITE, bool BUCKET>
-__global__ void __launch_bounds__(256) emit_pair_kernel(const __grid_constant__ EmitArgs a) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < a.groups; g += stride) {
+// The two outputs of pair group g and whether each survives the prune.
+template <int K, bool BUCKET>
+__device__ __forceinline__ void pair_outputs(const EmitArgs& a, uint64_t g, uint64_t (&k0)[K], double2& rz,
+                                             double2& ro, bool& kz, bool& ko) {
+    {
         const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
         const unsigned m = s1 - s0;
-        uint64_t k0[K];
         load_key<K>(a.in_keys, group_head<BUCKET>(a, g, s0), k0);
         uint64_t t0;
         double2 v0;
@@ -496,7 +496,6 @@ __global__ void __launch_bounds__(256) emit_pair_kernel(const __grid_constant__ 
             member_at<BUCKET>(a, s0 + 1, t1, v1);
             if (b0) { az = v1; has_z = true; } else { ao = v1; has_o = true; }
         }
-        double2 rz, ro;
         const double2 zero = make_double2(0.0, 0.0);
         if (a.mode == GM_HADAMARD_BOOL) {
             const double s = a.sqrt2inv;
@@ -538,25 +537,64 @@ __global__ void __launch_bounds__(256) emit_pair_kernel(const __grid_constant__ 
             rz = csub(cscale(az, cs), cscale(ao, sn));
             ro = cadd(cscale(az, sn), cscale(ao, cs));
         }
-        const bool kz = keep_amp(rz, a.eps), ko = keep_amp(ro, a.eps);
+        kz = keep_amp(rz, a.eps);
+        ko = keep_amp(ro, a.eps);
+    }
+}
+
+// One thread per group of at most two members (the target is one bit). In
+// the single-pass mode (WRITE with a cursor) the lanes of a warp reserve
+// their outputs with one atomic, in lane order.
+template <int K, bool WRITE, bool BUCKET>
+__global__ void __launch_bounds__(256) emit_pair_kernel(const __grid_constant__ EmitArgs a) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint64_t gb = (uint64_t)blockIdx.x * blockDim.x; gb < a.groups; gb += stride) {  // warp-uniform trips
+        const uint64_t g = gb + threadIdx.x;
+        const bool valid = g < a.groups;
+        bool kz = false, ko = false;
+        double2 rz = make_double2(0.0, 0.0), ro = make_double2(0.0, 0.0);
+        uint64_t k0[K];
+        if (valid) pair_outputs<K, BUCKET>(a, g, k0, rz, ro, kz, ko);
         if (!WRITE) {
-            a.cnt[g] = (unsigned)kz + (unsigned)ko;
-        } else {
-            unsigned long long o = a.off[g];
-            uint64_t kk[K];
+            if (valid) a.cnt[g] = (unsigned)kz + (unsigned)ko;
+            continue;
+        }
+        unsigned long long o = 0;
+        bool fits = true;
+        if (a.cursor) {
+            const unsigned c = (unsigned)kz + (unsigned)ko;
+            unsigned inc = c;
 #pragma unroll
-            for (int w = 0; w < K; ++w) kk[w] = k0[w];
-            if (kz) {
-                fset<K>(kk, a.target, 0);
-                store_entry<K>(a.out_keys, a.out_amp, o++, kk, rz);
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned t = __shfl_up_sync(0xffffffffu, inc, d);
+                if (lane >= (unsigned)d) inc += t;
             }
-            if (ko) {
-                fset<K>(kk, a.target, 1);
-                store_entry<K>(a.out_keys, a.out_amp, o, kk, ro);
-            }
+            const unsigned total = __shfl_sync(0xffffffffu, inc, 31);
+            unsigned long long base = 0;
+            if (lane == 31 && total) base = atomicAdd(a.cursor, (unsigned long long)total);
+            base = __shfl_sync(0xffffffffu, base, 31);
+            fits = base + total <= a.capacity;
+            o = base + (inc - c);
+        } else if (valid) {
+            o = a.off[g];
+        }
+        if (!valid || !fits) continue;
+        uint64_t kk[K];
+#pragma unroll
+        for (int w = 0; w < K; ++w) kk[w] = k0[w];
+        if (kz) {
+            fset<K>(kk, a.target, 0);
+            store_entry<K>(a.out_keys, a.out_amp, o++, kk, rz);
+        }
+        if (ko) {
+            fset<K>(kk, a.target, 1);
+            store_entry<K>(a.out_keys, a.out_amp, o, kk, ro);
         }
     }
 }
+
+
 
 // add_systems merge: sum each run of equal keys in sorted (stable) order.
 template <int K, bool WRITE>
@@ -2171,13 +2209,14 @@ static void run_group(State& s, const GroupSpec& gs) {
     // exact count-then-scan path runs instead, so results never depend on
     // the capacity.
     const bool generic = !pair && gs.mode != GM_MERGE;
-    const uint64_t boundT = generic ? G * (uint64_t)S : 0;
+    const bool sizable = gs.mode != GM_MERGE;  // pairs: at most two outputs per group
+    const uint64_t boundT = sizable ? G * (uint64_t)S : 0;
     const uint64_t policy = single_pass_limit() ? single_pass_limit() : std::max<uint64_t>(4 * N, 1ull << 27);
     uint64_t capT = 0;
     // every group reserves its outputs with one atomic on one cursor; past
     // about a million groups that serialisation costs more than a count pass
     const uint64_t max_single_groups = 1ull << 20;
-    if (generic && get_output_sizing() == 0 && G > 0 && G <= max_single_groups) {
+    if (sizable && get_output_sizing() == 0 && G > 0 && (pair || G <= max_single_groups)) {
         const uint64_t hint = take_output_size_hint();
         if (boundT <= policy) capT = boundT;
         else if (hint) capT = std::min<uint64_t>(hint, boundT);
@@ -2217,6 +2256,12 @@ static void run_group(State& s, const GroupSpec& gs) {
         SQ_CUDA(cudaMemsetAsync(cur, 0, 8, st));
         if (h4096) {
             launch_h4096_mode(EMIT_ATOMIC);
+        } else if (pair) {  // one atomic per warp of groups
+            prof_begin("emit_pair_single_pass");
+            if (bk) emit_pair_kernel<K, true, true><<<grid_for(G, 256), 256, 0, st>>>(ea);
+            else emit_pair_kernel<K, true, false><<<grid_for(G, 256), 256, 0, st>>>(ea);
+            prof_end((double)P * E);
+            SQ_CUDA(cudaGetLastError());
         } else {
             prof_begin("emit_hadamard_single_pass");
             if (W == 32) launch_hadamard<K, 32, true>(am, (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8), smem, st, ea);

@@ -661,6 +661,71 @@ class Rot_GeneralUnitary(BaseOperator):
         return ("rot_general_unitary", self.id, self.mat, self.dim, self._cond(), dag)
 
 
+def stateprep_unitary(target):
+    """Unitary U with U e0 = target / |target| (rot.cpp:481-519): a complex
+    Householder reflection I - 2 v v* / <v, v>, v = psi + phase(psi_0) e0, whose
+    first column is multiplied by -phase(psi_0). psi is the target scaled by
+    its largest component, then normalised."""
+    import numpy as np
+    t = np.asarray(target, dtype=np.complex128).reshape(-1)
+    if t.size == 0:
+        raise ValueError("Cannot prepare an empty vector.")
+    if not (np.all(np.isfinite(t.real)) and np.all(np.isfinite(t.imag))):
+        raise ValueError("State amplitudes must be finite.")
+    scale = max(float(np.max(np.abs(t.real))), float(np.max(np.abs(t.imag))))
+    if scale == 0:
+        raise ValueError("Cannot prepare the zero vector.")
+    v = t / scale
+    norm_sq = 0.0
+    for x in v:
+        norm_sq += x.real * x.real + x.imag * x.imag
+    v = v / math.sqrt(norm_sq)
+    first_abs = abs(v[0])
+    phase = complex(1.0, 0.0) if first_abs == 0 else v[0] / first_abs
+    v = v.copy()
+    v[0] += phase
+    vns = 0.0
+    for x in v:
+        vns += x.real * x.real + x.imag * x.imag
+    n = v.size
+    u = np.empty((n, n), dtype=np.complex128)
+    for i in range(n):
+        for j in range(n):
+            e = (1.0 if i == j else 0.0) - (2.0 / vns) * v[i] * v[j].conjugate()
+            if j == 0:
+                e *= -phase
+            u[i, j] = e
+    return u
+
+
+class Rot_GeneralStatePrep(Rot_GeneralUnitary):
+    """Prepare `vec` on a register from |0> (rot.cpp:528-564): the state-prep
+    unitary above applied with Rot_GeneralUnitary; dag applies its inverse."""
+
+    def __init__(self, reg, vec):
+        import numpy as np
+        dim = 1 << System.size_of(_R(reg))
+        if len(vec) != dim:
+            raise ValueError("Matrix size does not match the register's size.")
+        super().__init__(reg, stateprep_unitary(np.asarray(vec, dtype=np.complex128)))
+        self.vec = list(vec)
+
+
+class PlusOneAndOverflow(ElementwiseOperator):
+    """main = main + 1 mod 2^|main|, and on the wrap overflow = (overflow + 1) % 2;
+    dag subtracts (SparQ_Algorithm/src/BlockEncoding/block_encoding_tridiagonal.cpp:20-83)."""
+
+    opcode = "PLUS_ONE_OVERFLOW"
+
+    def __init__(self, main_reg, overflow_reg):
+        super().__init__()
+        self.main, self.overflow = _R(main_reg), _R(overflow_reg)
+
+    def _fill(self, ins, dag):
+        ins.reg[0] = self.main
+        ins.reg[1] = self.overflow
+
+
 class Hadamard_Partial(SelfAdjointOperator):
     """H on one bit position of a register (hadamard.cpp:470-712; the
     reference's active path is defined for a single position)."""
