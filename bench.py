@@ -338,6 +338,16 @@ def run_qda(args, ext) -> dict:
 
     counted, _, _ = walk(True)
     run, ms, wall = walk(False)
+    # per-kernel device time of the same steps
+    from sparqsim_gb300 import _native
+    _native.profile_reset()
+    _native.profile_enable(True)
+    walk(False)
+    _native.profile_enable(False)
+    prof = _native.profile_read()
+    tot = sum(v[1] for v in prof.values()) or 1.0
+    kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot, 4)}
+               for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]}
     return {
         "workload": (f"QDA walk, N=2^{n_bits}, tridiagonal block encoding of alpha I + beta (S + S^T) "
                      f"(alpha={alpha:.4f}, beta={beta}, kappa about 50), b uniform, schedule of a "
@@ -346,6 +356,8 @@ def run_qda(args, ext) -> dict:
         "updates": counted.updates, "value": counted.updates / (ms / 1e3), "unit": UNIT,
         "ms_per_walk_step": ms / sample, "wall_ms_per_walk_step": wall * 1e3 / sample,
         "projected_2000_step_walk_s": ms / sample * total_steps / 1e3,
+        "kernels": kernels,
+        "kernel_ms_per_walk_step": tot / sample,
     }
 
 

@@ -300,6 +300,12 @@ int sq_hadamard_partial(sq_state* st, uint32_t reg, const uint32_t* positions, u
  * (its CPU path sorts or uses std::map buckets, its GPU path sorts). */
 int sq_set_group_strategy(int strategy);
 int sq_get_group_strategy(int* strategy);
+/* Strategy 3 (the default) is autotuned: per shape class (operator kind,
+ * conditions, key words, log2 N; 4096 entries and more) the first split runs
+ * the sort grouping, the second the hash grouping, each timed around the
+ * whole operator, and later splits of the class use the faster. */
+int sq_autotune_reset(void);
+int sq_autotune_classes(uint64_t* classes, uint64_t* decided);
 /* How split operators size their output: 0 = automatic (one pass that
  * reserves each group's output range with an atomic, when the bound "every
  * group fully populated" fits in memory), 1 = exact count pass, scan, write

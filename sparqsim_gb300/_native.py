@@ -138,6 +138,8 @@ _SIGS = [
     ("sq_set_group_strategy", c_int, [c_int]),
     ("sq_get_group_strategy", c_int, [POINTER(c_int)]),
     ("sq_set_output_sizing", c_int, [c_int]),
+    ("sq_autotune_reset", c_int, []),
+    ("sq_autotune_classes", c_int, [POINTER(c_uint64), POINTER(c_uint64)]),
     ("sq_get_output_sizing", c_int, [POINTER(c_int)]),
     ("sq_set_fwht_arithmetic", c_int, [c_int]),
     ("sq_set_single_pass_limit", c_int, [c_uint64]),

@@ -147,15 +147,27 @@ class System:
 
 def set_group_strategy(strategy: str) -> None:
     """'auto', 'sort' (onesweep radix sort) or 'hash' (hash-table buckets):
-    how split/merge operators group entries. Results are identical."""
-    call("sq_set_group_strategy", {"auto": 0, "sort": 1, "hash": 2}[strategy])
+    how split/merge operators group entries ('autotune', the default, times
+    sort and hash per shape class and keeps the faster). Results are identical."""
+    call("sq_set_group_strategy", {"auto": 0, "sort": 1, "hash": 2, "autotune": 3}[strategy])
 
 
 def get_group_strategy() -> str:
     from ctypes import c_int
     v = c_int()
     call("sq_get_group_strategy", byref(v))
-    return ["auto", "sort", "hash"][v.value]
+    return ["auto", "sort", "hash", "autotune"][v.value]
+
+
+def autotune_reset() -> None:
+    call("sq_autotune_reset")
+
+
+def autotune_classes() -> tuple:
+    """(shape classes seen, classes whose choice is made)."""
+    c, d = ctypes.c_uint64(), ctypes.c_uint64()
+    call("sq_autotune_classes", byref(c), byref(d))
+    return c.value, d.value
 
 
 def set_output_sizing(mode: str) -> None:

@@ -769,6 +769,18 @@ int sq_get_group_strategy(int* strategy) {
     SQ_API_END
 }
 
+int sq_autotune_reset(void) {
+    SQ_API_BEGIN
+    autotune_reset();
+    SQ_API_END
+}
+int sq_autotune_classes(uint64_t* classes, uint64_t* decided) {
+    SQ_API_BEGIN
+    const uint64_t c = autotune_classes(decided);
+    if (classes) *classes = c;
+    SQ_API_END
+}
+
 int sq_set_output_sizing(int mode) {
     SQ_API_BEGIN
     set_output_sizing(mode);

@@ -21,8 +21,10 @@
 // a * 2^{-n/2} shortcut, the pair formulas), so results do not depend on the
 // order entries arrive in.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "lookback.cuh"
@@ -1302,12 +1304,14 @@ template <int K>
 __global__ void __launch_bounds__(256) hash_insert_kernel(ConstKeyPtrs keys, const uint64_t* __restrict__ gmask,
                                                           DCondSet cond, uint64_t n, HashWs h, unsigned gmax,
                                                           Field tgt, Field varw, unsigned max_digits, unsigned* err) {
+    __shared__ unsigned s_fail[32];
+    __shared__ unsigned s_fail_base;
     uint64_t gm[K];
 #pragma unroll
     for (int w = 0; w < K; ++w) gm[w] = gmask[w];
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x; b < n; b += stride) {  // warp-uniform trip count
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x; b < n; b += stride) {  // block-uniform trip count
         const uint64_t i = b + threadIdx.x;
         const bool valid = i < n;
         uint64_t k[K];
@@ -1328,10 +1332,26 @@ __global__ void __launch_bounds__(256) hash_insert_kernel(ConstKeyPtrs keys, con
                     kword_set<K>(k, tgt.word, kword<K>(k, tgt.word) & ~(wmask(nd) << tgt.shift));
                 }
             }
-            if (!pass) {
-                h.pass_list[warp_aggregated_add(&h.gcount[1])] = (unsigned)i;
-                h.gid[i] = ~0u;
+            if (!pass) h.gid[i] = ~0u;
+        }
+        {   // entries failing the conditions: one atomic per block and round
+            const bool fail = valid && !pass;
+            const unsigned fb = __ballot_sync(0xffffffffu, fail);
+            const unsigned warp = threadIdx.x >> 5;
+            if (lane == 0) s_fail[warp] = (unsigned)__popc(fb);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                unsigned run = 0;
+                for (unsigned w = 0; w < (blockDim.x >> 5); ++w) {
+                    const unsigned c = s_fail[w];
+                    s_fail[w] = run;
+                    run += c;
+                }
+                s_fail_base = run ? atomicAdd(&h.gcount[1], run) : 0u;
             }
+            __syncthreads();
+            if (fail) h.pass_list[s_fail_base + s_fail[warp] + __popc(fb & ((1u << lane) - 1u))] = (unsigned)i;
+            __syncthreads();
         }
         unsigned long long hv = 0x9e3779b97f4a7c15ull;
 #pragma unroll
@@ -1668,7 +1688,7 @@ __global__ void __launch_bounds__(kSelBlock) scan_seg_kernel(const unsigned* __r
 }  // namespace
 
 #ifndef SQ_GROUP_K
-static int g_strategy = 0;  // 0 auto, 1 sort, 2 hash
+static int g_strategy = 3;  // 0 heuristic (hash from 4096 entries), 1 sort, 2 hash, 3 autotuned
 static int g_sizing = 0;    // 0 auto (single pass when the output bound fits), 1 exact count-then-scan
 void set_output_sizing(int m) {
     if (m < 0 || m > 1) fail(SQ_ERR_INVALID, "output sizing must be 0 (auto) or 1 (count then scan)");
@@ -1683,10 +1703,47 @@ void set_fwht_arithmetic(int m) {
 }
 int get_fwht_arithmetic() { return g_arith; }
 void set_group_strategy(int s) {
-    if (s < 0 || s > 2) fail(SQ_ERR_INVALID, "group strategy must be 0 (auto), 1 (sort) or 2 (hash)");
+    if (s < 0 || s > 3)
+        fail(SQ_ERR_INVALID, "group strategy must be 0 (auto), 1 (sort), 2 (hash) or 3 (autotuned)");
     g_strategy = s;
 }
 int get_group_strategy() { return g_strategy; }
+
+// The autotuner of the grouping: per shape class (operator kind, conditions,
+// key words, log2 N) the first split of the class runs the sort grouping, the
+// second the hash grouping, each timed on the host around the whole operator
+// (both synchronise); later splits of the class use the faster. Results are
+// the same either way; only the order of the output entries differs.
+namespace {
+struct TuneEntry {
+    double ms[2] = {0.0, 0.0};
+    bool tried[2] = {false, false};
+};
+std::map<uint64_t, TuneEntry> g_tune;
+}  // namespace
+int autotune_pick(uint64_t key) {
+    TuneEntry& e = g_tune[key];
+    if (!e.tried[0]) return 1;
+    if (!e.tried[1]) return 2;
+    return e.ms[1] <= e.ms[0] ? 2 : 1;
+}
+void autotune_record(uint64_t key, int strategy, double ms) {
+    TuneEntry& e = g_tune[key];
+    const int i = strategy == 2 ? 1 : 0;
+    if (!e.tried[i]) {
+        e.tried[i] = true;
+        e.ms[i] = ms;
+    } else {
+        e.ms[i] = 0.75 * e.ms[i] + 0.25 * ms;  // keeps following the class
+    }
+}
+void autotune_reset() { g_tune.clear(); }
+uint64_t autotune_classes(uint64_t* decided) {
+    uint64_t d = 0;
+    for (const auto& kv : g_tune) d += (kv.second.tried[0] && kv.second.tried[1]) ? 1 : 0;
+    if (decided) *decided = d;
+    return g_tune.size();
+}
 static uint64_t g_hash_groups_hint = 1ull << 20;
 void set_hash_groups_hint(uint64_t g) { g_hash_groups_hint = g ? g : (1ull << 20); }
 uint64_t hash_groups_hint() { return g_hash_groups_hint; }
@@ -2098,8 +2155,27 @@ static void run_group(State& s, const GroupSpec& gs) {
 
     // the merge sums runs in order, so it keeps the (stable) sort; the
     // transforms are order-independent and default to the hash grouping
-    const bool use_hash = gs.varw.width ||
-                          (gs.mode != GM_MERGE && (get_group_strategy() == 2 || (get_group_strategy() == 0 && N >= 4096)));
+    int strat = get_group_strategy();
+    uint64_t tune_key = 0;
+    const bool tuned = strat == 3 && gs.mode != GM_MERGE && !gs.varw.width && N >= 4096;
+    if (tuned) {
+        tune_key = (uint64_t)gs.mode | ((uint64_t)gs.cond.n << 8) | ((uint64_t)K << 16) |
+                   ((uint64_t)(63 - __builtin_clzll(N)) << 24);
+        strat = autotune_pick(tune_key);
+    } else if (strat == 3) {
+        strat = 0;
+    }
+    const bool use_hash = gs.varw.width || (gs.mode != GM_MERGE && (strat == 2 || (strat == 0 && N >= 4096)));
+    struct TuneTimer {
+        bool on;
+        uint64_t key;
+        int strategy;
+        std::chrono::steady_clock::time_point t0;
+        ~TuneTimer() {
+            if (on) autotune_record(key, strategy,
+                                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+        }
+    } tune_timer{tuned, tune_key, strat, std::chrono::steady_clock::now()};
     // A Hadamard on the same bits as the split that produced this state (no
     // key change since, no conditions) takes that split's output ranges as
     // its groups: every member is still read and transformed, only the
@@ -2109,6 +2185,7 @@ static void run_group(State& s, const GroupSpec& gs) {
     const bool reuse = gc.valid && cache_out && gs.cond.n == 0 && same_field(gc.target, gs.target) &&
                        same_field(gc.varw, gs.varw) && std::equal(gmask, gmask + SQ_KMAX, gc.gmask);
     gc.valid = false;
+    if (reuse) tune_timer.on = false;  // no grouping to time
 
     // the size model: features before the operator, sizes after it
     const bool model_on = (predictor_enabled() || predictor_logging()) && N >= kModelMinEntries;

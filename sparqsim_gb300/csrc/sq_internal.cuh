@@ -322,6 +322,10 @@ void note_output_size(int mode, uint64_t n_in, uint64_t groups, uint64_t n_out);
 void note_single_pass_overflow();
 uint64_t single_pass_overflows();
 void set_single_pass_limit(uint64_t entries);
+int autotune_pick(uint64_t key);
+void autotune_record(uint64_t key, int strategy, double ms);
+void autotune_reset();
+uint64_t autotune_classes(uint64_t* decided);
 uint64_t single_pass_limit();
 // The learned size model (predictor.cu).
 bool predictor_enabled();

@@ -54,6 +54,8 @@ def fresh_system():
     ps.System.clear()
     O.clear()
     ps.set_fwht_arithmetic("reference")
+    ps.set_group_strategy("autotune")
+    ps.autotune_reset()
     yield
     ps.System.clear()
     O.clear()

@@ -1,0 +1,42 @@
+"""The grouping autotuner: per shape class the first split runs the sort
+grouping, the second the hash grouping, and later ones use the faster; the
+state after every split equals the oracle's whichever grouping ran."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import sparqsim_gb300 as ps
+from sparqsim_gb300 import _native
+
+pytestmark = pytest.mark.gpu
+
+U = ps.UnsignedInteger
+
+
+def test_autotuner_decides_and_matches_oracle(dual):
+    assert ps.get_group_strategy() == "autotune"
+    dual.reg("a", U, 6)
+    dual.reg("b", U, 16)
+    rng = np.random.default_rng(12)
+    half = 10000  # complete pairs in bit 2 of a: the rotation keeps the entry count (one shape class)
+    a0 = rng.integers(0, 64, half) & ~4
+    b = rng.permutation(1 << 16)[:half]
+    regs = np.concatenate([np.stack([a0, b], axis=1), np.stack([a0 | 4, b], axis=1)]).astype(np.uint64)
+    n = len(regs)
+    amps = rng.normal(size=n) + 1j * rng.normal(size=n)
+    dual.start(regs, amps / np.linalg.norm(amps))
+    ran = []
+    for i in range(4):
+        _native.profile_reset()
+        _native.profile_enable(True)
+        dual.apply(ps.Rot_Bool("a", 2, [0.6, 0.8, 0.8, -0.6]))
+        _native.profile_enable(False)
+        names = _native.profile_read()
+        ran.append("sort" if any(k.startswith("radix") or k == "group_heads" for k in names) else "hash")
+        dual.compare(exact_amp=True)
+        dual.apply(ps.Add_ConstUInt_InPlace("b", 1))  # key change: no cached ranges
+    assert ran[0] == "sort" and ran[1] == "hash"
+    assert ran[2] == ran[3]
+    classes, decided = ps.autotune_classes()
+    assert classes >= 1 and decided >= 1

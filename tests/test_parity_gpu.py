@@ -29,7 +29,7 @@ def strategy(request, dual):
         ps.set_fwht_arithmetic("exact-sum")
         dual.relaxed = True
     yield request.param
-    ps.set_group_strategy("auto")
+    ps.set_group_strategy("autotune")
     ps.set_output_sizing("auto")
 
 

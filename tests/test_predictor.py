@@ -130,6 +130,7 @@ def test_trained_model_gain():
         return prof, regs[order], amps[order]
 
     try:
+        ps.set_group_strategy("hash")
         P.set_single_pass_limit(1 << 16)   # the fully populated bound of the held-out merge exceeds this
         P.set_hash_groups_hint(1024)       # and its group count exceeds the table's default sizing
         # log sizes from a family of circuits, train, predict
@@ -168,3 +169,4 @@ def test_trained_model_gain():
         P.log(False)
         P.set_single_pass_limit(0)
         P.set_hash_groups_hint(0)
+        ps.set_group_strategy("autotune")
