@@ -1239,6 +1239,273 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
     }
 }
 
+// The 12-bit Hadamard in the exact-sum arithmetic, one CTA of 512 threads
+// per group, two CTAs per SM (32 warps). A thread holds 8 slots; the integer
+// stages run in registers in four phases, each with 3 slot bits in the
+// thread's index j: layout A (slot = j << 9 | tid: bits 9-11), P0 (tid << 3 | j:
+// bits 0-2), P1 (tid_hi << 6 | j << 3 | tid_lo: bits 3-5), P2 (tid_hi << 9 |
+// j << 6 | tid_lo: bits 6-8), then back to A for coalesced output. Integer sums
+// are exact, so the stage order does not change the result. Slots are stored
+// at s ^ ((s >> 3) & 7) (16-byte units): conflict-free in all four layouts.
+__device__ __forceinline__ void fwht8(longlong2 (&x)[8]) {
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (j & (1 << b)) continue;
+            const longlong2 x0 = x[j], x1 = x[j | (1 << b)];
+            x[j] = ladd(x0, x1);
+            x[j | (1 << b)] = lsub(x0, x1);
+        }
+    }
+}
+__device__ __forceinline__ unsigned swz8(unsigned q) { return q ^ ((q >> 3) & 7u); }
+
+template <int K, int MODE, int AM>
+__global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_constant__ EmitArgs a) {
+    extern __shared__ double2 sl[];  // 4096 slots
+    __shared__ unsigned s_cnt[8][16];
+    __shared__ unsigned long long s_base;
+    __shared__ uint64_t s_mt[64];
+    __shared__ double2 s_ma[64];
+    __shared__ unsigned s_emax[16];
+    __shared__ bool s_fits;
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const Field tg = a.target;
+    longlong2* ls = reinterpret_cast<longlong2*>(sl);
+    for (uint64_t g = blockIdx.x; g < a.groups; g += gridDim.x) {
+        unsigned s0, m;
+        group_range<AM>(a, g, s0, m);
+        if (m == 0) {  // an emptied cached range
+            if (tid == 0) {
+                if (MODE == EMIT_COUNT) a.cnt[g] = 0u;
+                else if (MODE == EMIT_ATOMIC && a.ocnt) {
+                    a.ostart[g] = 0ull;
+                    a.ocnt[g] = 0u;
+                }
+            }
+            continue;
+        }
+        uint64_t gk[K];
+        load_key<K>(a.in_keys, group_head<AM>(a, g, s0), gk);
+        if (a.mode == GM_HADAMARD_INT && m == 1) {
+            // singleton: a * 2^-6, sign (-1)^popcount(t & v) (hadamard.cpp:27-42)
+            uint64_t v0;
+            double2 a0;
+            member_at<AM>(a, s0, v0, a0);
+            const double2 base = cscale(a0, a.extra);
+            const bool keep = keep_amp(base, a.eps);
+            if (MODE == EMIT_COUNT) {
+                if (tid == 0) a.cnt[g] = keep ? 4096u : 0u;
+            } else if (MODE == EMIT_ATOMIC && !keep) {
+                if (tid == 0 && a.ocnt) {
+                    a.ostart[g] = 0ull;
+                    a.ocnt[g] = 0u;
+                }
+            } else if (keep) {
+                if (MODE == EMIT_ATOMIC) {
+                    if (tid == 0) {
+                        s_base = atomicAdd(a.cursor, 4096ull);
+                        if (a.ocnt) {
+                            a.ostart[g] = s_base;
+                            a.ocnt[g] = 4096u;
+                        }
+                    }
+                    __syncthreads();
+                }
+                const unsigned long long o = MODE == EMIT_WRITE ? a.off[g] : s_base;
+                const bool fits = MODE != EMIT_ATOMIC || o + 4096ull <= a.capacity;
+                for (unsigned c = tid; fits && c < 4096u; c += 512u) {
+                    uint64_t kk[K];
+#pragma unroll
+                    for (int w = 0; w < K; ++w) kk[w] = gk[w];
+                    fset<K>(kk, tg, (uint64_t)c);
+                    store_entry_sign<K>(a.out_keys, a.out_amp, o + c, kk, base, __popcll((uint64_t)c & v0) & 1);
+                }
+            }
+            __syncthreads();
+            continue;
+        }
+        double2 v[8];
+        unsigned rows = 0xffu;  // rows j that may hold a kept slot (warp-uniform)
+        if (a.mode == GM_HADAMARD_FULL && m <= 11u) {
+            // sparse bucket: direct product, members in ascending target order (hadamard.cpp:267-304)
+            for (unsigned j = tid; j < m; j += 512u) {
+                uint64_t tj;
+                double2 aj;
+                member_at<AM>(a, s0 + j, tj, aj);
+                s_mt[j] = tj;
+                s_ma[j] = aj;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                for (unsigned i = 1; i < m; ++i) {
+                    const uint64_t kt = s_mt[i];
+                    const double2 ka = s_ma[i];
+                    int j = (int)i - 1;
+                    while (j >= 0 && s_mt[j] > kt) {
+                        s_mt[j + 1] = s_mt[j];
+                        s_ma[j + 1] = s_ma[j];
+                        --j;
+                    }
+                    s_mt[j + 1] = kt;
+                    s_ma[j + 1] = ka;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const unsigned c = ((unsigned)j << 9) | tid;
+                double2 acc = make_double2(0.0, 0.0);
+                for (unsigned q = 0; q < m; ++q) {
+                    double2 term = cscale(s_ma[q], (__popcll((uint64_t)c & s_mt[q]) & 1) ? -1. : 1.);
+                    term = cscale(term, a.extra);
+                    acc = cadd(acc, term);
+                }
+                v[j] = acc;
+            }
+        } else {
+            const bool direct = AM == 2 && m == 4096u;  // a full cached range: member c has target c
+            int emax = 1;
+            if (direct) {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) v[j] = __ldcs(a.in_amp + s0 + (((unsigned)j << 9) | tid));
+#pragma unroll
+                for (int j = 0; j < 8; ++j) emax = max(emax, amp_exp(v[j]));
+            } else {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) sl[((unsigned)j << 9) | tid] = make_double2(0.0, 0.0);
+                __syncthreads();
+                for (unsigned j0 = 0; j0 < m; j0 += 8u * 512u) {
+                    uint64_t tq[8];
+                    double2 aq[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const unsigned j = j0 + (unsigned)q * 512u + tid;
+                        if (j < m) member_at<AM>(a, s0 + j, tq[q], aq[q]);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const unsigned j = j0 + (unsigned)q * 512u + tid;
+                        if (j < m) {
+                            sl[tq[q]] = aq[q];
+                            emax = max(emax, amp_exp(aq[q]));
+                        }
+                    }
+                }
+            }
+            emax = (int)__reduce_max_sync(0xffffffffu, (unsigned)emax);
+            if (lane == 0) s_emax[warp] = (unsigned)emax;
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < 16; ++i) emax = max(emax, (int)s_emax[i]);
+            longlong2 x[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const double2 d = direct ? v[j] : sl[((unsigned)j << 9) | tid];
+                x[j] = make_longlong2(to_fixed_right(d.x, emax, 50), to_fixed_right(d.y, emax, 50));
+            }
+            fwht8(x);  // layout A: slot bits 9-11
+            __syncthreads();  // every thread has read its slots as doubles
+#pragma unroll
+            for (int j = 0; j < 8; ++j) ls[swz8(((unsigned)j << 9) | tid)] = x[j];
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < 8; ++j) x[j] = ls[swz8((tid << 3) | (unsigned)j)];
+            fwht8(x);  // P0: bits 0-2
+#pragma unroll
+            for (int j = 0; j < 8; ++j) ls[swz8((tid << 3) | (unsigned)j)] = x[j];
+            __syncthreads();
+            const unsigned b1 = ((tid >> 3) << 6) | (tid & 7u);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) x[j] = ls[swz8(b1 | ((unsigned)j << 3))];
+            fwht8(x);  // P1: bits 3-5
+#pragma unroll
+            for (int j = 0; j < 8; ++j) ls[swz8(b1 | ((unsigned)j << 3))] = x[j];
+            __syncthreads();
+            const unsigned b2 = ((tid >> 6) << 9) | (tid & 63u);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) x[j] = ls[swz8(b2 | ((unsigned)j << 6))];
+            fwht8(x);  // P2: bits 6-8
+#pragma unroll
+            for (int j = 0; j < 8; ++j) ls[swz8(b2 | ((unsigned)j << 6))] = x[j];
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < 8; ++j) x[j] = ls[swz8(((unsigned)j << 9) | tid)];
+            const int e2 = fix_out_exp(emax, 12);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                // merges leave most slots exactly zero: skip the conversion and the prune test row by row
+                const bool nz = (x[j].x | x[j].y) != 0;
+                if (__any_sync(0xffffffffu, nz)) {
+                    v[j] = from_fixed2(x[j], e2, false, a.sqrt2inv);
+                } else {
+                    v[j] = make_double2(0.0, 0.0);
+                    rows &= ~(1u << j);
+                }
+            }
+        }
+        // kept slots in ascending slot order: row j (slot bits 9..11), then warp, then lane
+        unsigned ball[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            ball[j] = ((rows >> j) & 1u) ? __ballot_sync(0xffffffffu, keep_amp(v[j], a.eps)) : 0u;
+            if (lane == 0) s_cnt[j][warp] = __popc(ball[j]);
+        }
+        __syncthreads();
+        if (warp == 0) {
+            unsigned c4[4], sum = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const unsigned idx = lane * 4 + q;  // (row, warp) in row-major order
+                c4[q] = s_cnt[idx >> 4][idx & 15];
+                sum += c4[q];
+            }
+            unsigned inc = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= (unsigned)o) inc += t;
+            }
+            unsigned run = inc - sum;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const unsigned idx = lane * 4 + q;
+                s_cnt[idx >> 4][idx & 15] = run;
+                run += c4[q];
+            }
+            const unsigned total = __shfl_sync(0xffffffffu, inc, 31);
+            if (lane == 0) {
+                if (MODE == EMIT_COUNT) a.cnt[g] = total;
+                else if (MODE == EMIT_ATOMIC) {
+                    s_base = total ? atomicAdd(a.cursor, (unsigned long long)total) : 0ull;
+                    s_fits = s_base + total <= a.capacity;
+                    if (a.ocnt) {
+                        a.ostart[g] = s_base;
+                        a.ocnt[g] = total;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (MODE != EMIT_COUNT) {
+            const unsigned long long o = MODE == EMIT_WRITE ? a.off[g] : s_base;
+            const unsigned lt = (1u << lane) - 1u;
+            const bool fits = MODE != EMIT_ATOMIC || s_fits;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (!fits || !((ball[j] >> lane) & 1u)) continue;
+                uint64_t kk[K];
+#pragma unroll
+                for (int w = 0; w < K; ++w) kk[w] = gk[w];
+                fset<K>(kk, tg, (uint64_t)(((unsigned)j << 9) | tid));
+                store_entry<K>(a.out_keys, a.out_amp, o + s_cnt[j][warp] + __popc(ball[j] & lt), kk, v[j]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // Entries that fail the control conditions: copied through unchanged.
 template <int K>
 __global__ void passthrough_kernel(ConstKeyPtrs ik, const double2* __restrict__ ia, const unsigned* __restrict__ idx,
@@ -2093,8 +2360,13 @@ static void launch_h4096_arith(int am, unsigned grid, size_t sm, cudaStream_t st
 }
 template <int K, int MODE>
 static void launch_h4096(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
-    if (ea.fix) launch_h4096_arith<K, MODE, true>(am, grid, sm, st, ea);
-    else launch_h4096_arith<K, MODE, false>(am, grid, sm, st, ea);
+    if (ea.fix) {  // exact sums: 512 threads, 8 slots each
+        if (am == 2) emit_h4096x_kernel<K, MODE, 2><<<grid, 512, sm, st>>>(ea);
+        else if (am == 1) emit_h4096x_kernel<K, MODE, 1><<<grid, 512, sm, st>>>(ea);
+        else emit_h4096x_kernel<K, MODE, 0><<<grid, 512, sm, st>>>(ea);
+    } else {
+        launch_h4096_arith<K, MODE, false>(am, grid, sm, st, ea);
+    }
 }
 template <int K, int W, bool WRITE>
 static void launch_hadamard(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
@@ -2109,8 +2381,8 @@ static void set_emit_smem_limits() {
 #define SQ_SMEM(f, b) SQ_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, b))
 #define SQ_SMEM_H(m)                                                                                           \
     SQ_SMEM((emit_h4096_kernel<K, m, 0, false>), sm); SQ_SMEM((emit_h4096_kernel<K, m, 1, false>), sm);       \
-    SQ_SMEM((emit_h4096_kernel<K, m, 2, false>), sm); SQ_SMEM((emit_h4096_kernel<K, m, 0, true>), sm);        \
-    SQ_SMEM((emit_h4096_kernel<K, m, 1, true>), sm); SQ_SMEM((emit_h4096_kernel<K, m, 2, true>), sm);
+    SQ_SMEM((emit_h4096_kernel<K, m, 2, false>), sm); SQ_SMEM((emit_h4096x_kernel<K, m, 0>), sm);             \
+    SQ_SMEM((emit_h4096x_kernel<K, m, 1>), sm); SQ_SMEM((emit_h4096x_kernel<K, m, 2>), sm);
     SQ_SMEM_H(EMIT_COUNT)
     SQ_SMEM_H(EMIT_WRITE)
     SQ_SMEM_H(EMIT_ATOMIC)
