@@ -911,35 +911,20 @@ __device__ __forceinline__ double2 sel_neg(bool lower, double2 p, double2 v) {
                         __longlong_as_double((long long)(lower ? (unsigned long long)__double_as_longlong(p.y) : sy)));
 }
 
-// The 4-stage exact-sum FWHT of 16 values held by one thread (index bits
-// 0-3 of j), stages in ascending order.
-__device__ __forceinline__ void fwht16(longlong2 (&x)[16]) {
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            if (j & (1 << b)) continue;
-            const longlong2 x0 = x[j], x1 = x[j | (1 << b)];
-            x[j] = ladd(x0, x1);
-            x[j | (1 << b)] = lsub(x0, x1);
-        }
-    }
-}
 
 __device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
     return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
 }
 
-// FIX selects the exact-sum arithmetic at compile time: one arithmetic per
-// instantiation keeps the unrolled code within the instruction cache.
-template <int K, int MODE, int AM, bool FIX>
+// The reference FP64 arithmetic (the exact-sum arithmetic runs in
+// emit_h4096x_kernel below).
+template <int K, int MODE, int AM>
 __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constant__ EmitArgs a) {
     extern __shared__ double2 sl[];  // 4096 slots
     __shared__ unsigned s_cnt[16][8];
     __shared__ unsigned long long s_base;
     __shared__ uint64_t s_mt[64];
     __shared__ double2 s_ma[64];
-    __shared__ unsigned s_emax[8];
     __shared__ bool s_fits;
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const Field tg = a.target;
@@ -1040,16 +1025,13 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
             // has target c: the 16 slots of a thread load straight into
             // registers, 16 coalesced loads in flight, no scatter.
             const bool direct = AM == 2 && m == 4096u;
-            int emax = 1;
             if (direct) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) v[j] = __ldcs(a.in_amp + s0 + (((unsigned)j << 8) | tid));
-#pragma unroll
-                for (int j = 0; j < 16; ++j) emax = max(emax, amp_exp(v[j]));
             } else {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) sl[((unsigned)j << 8) | tid] = make_double2(0.0, 0.0);
-            __syncthreads();
+                for (int j = 0; j < 16; ++j) sl[((unsigned)j << 8) | tid] = make_double2(0.0, 0.0);
+                __syncthreads();
             }
             // members: 8 independent loads in flight per thread, then scatter
             for (unsigned j0 = 0; !direct && j0 < m; j0 += 8u * 256u) {
@@ -1063,69 +1045,10 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
                     const unsigned j = j0 + (unsigned)q * 256u + tid;
-                    if (j < m) {
-                        sl[tq[q]] = aq[q];
-                        emax = max(emax, amp_exp(aq[q]));
-                    }
+                    if (j < m) sl[tq[q]] = aq[q];
                 }
-            }
-            if (FIX) {
-                emax = (int)__reduce_max_sync(0xffffffffu, (unsigned)emax);
-                if (lane == 0) s_emax[warp] = (unsigned)emax;
             }
             __syncthreads();
-            if (FIX) {
-                // exact-sum arithmetic on the int64 grid, one rounding at the end.
-                // Every stage runs in registers: a thread holds 16 slots that
-                // differ in bits 0-3 (layout P: slot = tid << 4 | j), then bits
-                // 4-7 (layout Q: slot = tid_hi << 8 | j << 4 | tid_lo), then
-                // bits 8-11 (layout A); two shared-memory transposes in between.
-                // Slots are stored at s ^ ((s >> 4) & 7) (16-byte units), which
-                // keeps all three layouts free of bank conflicts.
-#pragma unroll
-                for (int i = 0; i < 8; ++i) emax = max(emax, (int)s_emax[i]);
-                longlong2* ls = reinterpret_cast<longlong2*>(sl);
-                longlong2 x[16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const double2 d = direct ? v[j] : sl[((unsigned)j << 8) | tid];
-                    x[j] = make_longlong2(to_fixed_right(d.x, emax, 50), to_fixed_right(d.y, emax, 50));
-                }
-                auto sw = [](unsigned q) { return q ^ ((q >> 4) & 7u); };
-                __syncthreads();  // every thread has read its slots as doubles
-#pragma unroll
-                for (int j = 0; j < 16; ++j) ls[sw(((unsigned)j << 8) | tid)] = x[j];
-                __syncthreads();
-#pragma unroll
-                for (int j = 0; j < 16; ++j) x[j] = ls[sw((tid << 4) | (unsigned)j)];
-                fwht16(x);  // stages 0-3
-#pragma unroll
-                for (int j = 0; j < 16; ++j) ls[sw((tid << 4) | (unsigned)j)] = x[j];
-                __syncthreads();
-                const unsigned qb = ((tid >> 4) << 8) | (tid & 15u);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) x[j] = ls[sw(qb | ((unsigned)j << 4))];
-                fwht16(x);  // stages 4-7
-#pragma unroll
-                for (int j = 0; j < 16; ++j) ls[sw(qb | ((unsigned)j << 4))] = x[j];
-                __syncthreads();
-#pragma unroll
-                for (int j = 0; j < 16; ++j) x[j] = ls[sw(((unsigned)j << 8) | tid)];
-                fwht16(x);  // stages 8-11
-                const int e2 = fix_out_exp(emax, 12);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    // merges leave most slots exactly zero: skip the conversion
-                    // and the prune test row by row
-                    const bool nz = (x[j].x | x[j].y) != 0;
-                    if (__any_sync(0xffffffffu, nz)) {
-                        v[j] = from_fixed2(x[j], e2, false, s2);
-                    } else {
-                        v[j] = make_double2(0.0, 0.0);
-                        rows &= ~(1u << j);
-                    }
-                }
-            } else {
 #pragma unroll
             for (int j = 0; !direct && j < 16; ++j) v[j] = sl[((unsigned)j << 8) | tid];
             // stages 0..4: partner lane = lane ^ h
@@ -1175,7 +1098,6 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
                     v[j | (1 << b)] = cscale(csub(x0, x1), s2);
                 }
             }
-            }  // FP64 butterflies
         }
         // kept slots in ascending slot order: row j (slot bits 8..11), then warp, then lane
         unsigned ball[16];
@@ -2352,11 +2274,11 @@ static void split_features(State& s, const GroupSpec& gs, uint64_t N, const uint
     for (int i = 0; i < 32; ++i) f[16 + i] = (float)h[i] / 32.f;
 }
 
-template <int K, int MODE, bool FIX>
-static void launch_h4096_arith(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
-    if (am == 2) emit_h4096_kernel<K, MODE, 2, FIX><<<grid, 256, sm, st>>>(ea);
-    else if (am == 1) emit_h4096_kernel<K, MODE, 1, FIX><<<grid, 256, sm, st>>>(ea);
-    else emit_h4096_kernel<K, MODE, 0, FIX><<<grid, 256, sm, st>>>(ea);
+template <int K, int MODE>
+static void launch_h4096_fp64(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
+    if (am == 2) emit_h4096_kernel<K, MODE, 2><<<grid, 256, sm, st>>>(ea);
+    else if (am == 1) emit_h4096_kernel<K, MODE, 1><<<grid, 256, sm, st>>>(ea);
+    else emit_h4096_kernel<K, MODE, 0><<<grid, 256, sm, st>>>(ea);
 }
 template <int K, int MODE>
 static void launch_h4096(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
@@ -2365,7 +2287,7 @@ static void launch_h4096(int am, unsigned grid, size_t sm, cudaStream_t st, cons
         else if (am == 1) emit_h4096x_kernel<K, MODE, 1><<<grid, 512, sm, st>>>(ea);
         else emit_h4096x_kernel<K, MODE, 0><<<grid, 512, sm, st>>>(ea);
     } else {
-        launch_h4096_arith<K, MODE, false>(am, grid, sm, st, ea);
+        launch_h4096_fp64<K, MODE>(am, grid, sm, st, ea);
     }
 }
 template <int K, int W, bool WRITE>
@@ -2380,8 +2302,8 @@ static void set_emit_smem_limits() {
     const int g = 96 * 1024;
 #define SQ_SMEM(f, b) SQ_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, b))
 #define SQ_SMEM_H(m)                                                                                           \
-    SQ_SMEM((emit_h4096_kernel<K, m, 0, false>), sm); SQ_SMEM((emit_h4096_kernel<K, m, 1, false>), sm);       \
-    SQ_SMEM((emit_h4096_kernel<K, m, 2, false>), sm); SQ_SMEM((emit_h4096x_kernel<K, m, 0>), sm);             \
+    SQ_SMEM((emit_h4096_kernel<K, m, 0>), sm); SQ_SMEM((emit_h4096_kernel<K, m, 1>), sm);                     \
+    SQ_SMEM((emit_h4096_kernel<K, m, 2>), sm); SQ_SMEM((emit_h4096x_kernel<K, m, 0>), sm);                     \
     SQ_SMEM((emit_h4096x_kernel<K, m, 1>), sm); SQ_SMEM((emit_h4096x_kernel<K, m, 2>), sm);
     SQ_SMEM_H(EMIT_COUNT)
     SQ_SMEM_H(EMIT_WRITE)
