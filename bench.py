@@ -206,6 +206,22 @@ def cpu_baseline_sample(h: int, table, thetas, layers_sample: int = 2):
     return upd, dt
 
 
+def replica_max(ms: float, device: str) -> float:
+    """The slowest replica's time: all-reduce MAX over the ranks, then a barrier
+    (independent circuits per GPU, no exchange on the data path)."""
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(tt.item())
+
+
+def replica_value(world: int, updates_per_step: int, steps: int, t_max_ms: float) -> float:
+    """Whole-job updates/s: every replica runs the same circuit, timed by the slowest."""
+    return world * updates_per_step * steps / (t_max_ms / 1e3)
+
+
 def run_trajectories(args, ext) -> dict:
     """Batched noisy trajectories (4096 instances, a/b/c 16-bit, per-instance
     Hadamard width h_t in [4, 8], Pauli X/Z at p = 1e-3 per bit per layer,
@@ -407,13 +423,9 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
 
     t_max = ms
     if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-        dist.barrier()
+        t_max = replica_max(ms, "cuda")
     ms_per_step = t_max / args.steps
-    value = world * updates * args.steps / (t_max / 1e3)
+    value = replica_value(world, updates, args.steps, t_max)
 
     # the same steps in the other butterfly arithmetic (same keys; amplitudes
     # bit-identical to the reference in 'reference', within 1e-12 in 'exact-sum')

@@ -347,10 +347,10 @@ int sq_state_upload_packed(sq_state* st, uint64_t n, const uint64_t* keys, const
     need(n == 0 || (keys != nullptr && amps != nullptr), "null pointer");
     const uint32_t k = regtable().k;
     ensure_buffers(s.live, std::max<uint64_t>(n, 1), k, 0);
-    for (uint32_t w = 0; w < k; ++w)
-        SQ_CUDA(cudaMemcpyAsync(s.live.keys[w], keys + (size_t)w * n, n * 8, cudaMemcpyHostToDevice, stream()));
-    SQ_CUDA(cudaMemcpyAsync(s.live.amp, amps, n * 16, cudaMemcpyHostToDevice, stream()));
-    SQ_CUDA(cudaStreamSynchronize(stream()));
+    std::vector<CopyJob> jobs;
+    for (uint32_t w = 0; w < k; ++w) jobs.push_back({s.live.keys[w], keys + (size_t)w * n, (size_t)n * 8});
+    jobs.push_back({s.live.amp, amps, (size_t)n * 16});
+    parallel_copy(jobs.data(), (int)jobs.size(), cudaMemcpyHostToDevice);
     s.n = n;
     SQ_API_END
 }
@@ -360,15 +360,14 @@ int sq_state_download_packed(const sq_state* st, uint64_t* keys, double* amps) {
     const State& s = S(st);
     const uint32_t k = regtable().k;
     const uint64_t n = s.n;
+    std::vector<CopyJob> jobs;
     for (uint32_t w = 0; w < k; ++w) {
         if (!keys) break;
-        if (w < s.live.kalloc)
-            SQ_CUDA(cudaMemcpyAsync(keys + (size_t)w * n, s.live.keys[w], n * 8, cudaMemcpyDeviceToHost, stream()));
-        else
-            memset(keys + (size_t)w * n, 0, n * 8);
+        if (w < s.live.kalloc) jobs.push_back({keys + (size_t)w * n, s.live.keys[w], (size_t)n * 8});
+        else memset(keys + (size_t)w * n, 0, n * 8);
     }
-    if (amps) SQ_CUDA(cudaMemcpyAsync(amps, s.live.amp, n * 16, cudaMemcpyDeviceToHost, stream()));
-    SQ_CUDA(cudaStreamSynchronize(stream()));
+    if (amps) jobs.push_back({amps, s.live.amp, (size_t)n * 16});
+    parallel_copy(jobs.data(), (int)jobs.size(), cudaMemcpyDeviceToHost);
     SQ_API_END
 }
 
@@ -394,23 +393,19 @@ int sq_qram_create(uint32_t address_size, uint32_t data_size, const uint64_t* me
     const uint64_t words = 1ull << address_size;
     need(memory != nullptr && n_words >= words, "QRAM memory must hold 2^address_size words");
     // the highest bit any word uses decides the stored width (and is checked
-    // against the data register at use); the narrowing runs on the GPU
-    uint64_t all = 0;
-    for (uint64_t i = 0; i < words; ++i) all |= memory[i];
-    const uint32_t eb = all <= 0xffffull ? 2 : (all <= 0xffffffffull ? 4 : 8);
+    // against the data register at use); found and narrowed on the GPU, the
+    // declared data size gives the first guess
     sq_qram* q = new sq_qram();
-    q->t.elem_bytes = eb;
     q->t.address_size = address_size;
     q->t.data_size = data_size;
     q->t.n_words = words;
-    q->t.max_word = all;
     try {
-        q->t.dev = dev_alloc((size_t)words * eb);
-        qram_pack(memory, words, eb, q->t.dev);
-        // the caller's buffer may be pinned: the copy completes before return
-        SQ_CUDA(cudaStreamSynchronize(stream()));
+        uint32_t eb = 8;
+        uint64_t all = 0;
+        q->t.dev = qram_upload(memory, words, data_size <= 16 ? 2 : data_size <= 32 ? 4 : 8, &eb, &all);
+        q->t.elem_bytes = eb;
+        q->t.max_word = all;
     } catch (...) {
-        dev_free(q->t.dev);
         delete q;
         throw;
     }

@@ -536,29 +536,56 @@ void run_program(State& s, const sq_instr* prog, uint32_t n) {
     }
 }
 
-// QRAM tables are stored at the narrowest width that holds every word.
-__global__ void qram_pack_kernel(const uint64_t* __restrict__ src, uint64_t n, uint32_t eb, void* __restrict__ dst) {
+// QRAM tables are stored at the narrowest width that holds every word. The
+// words are copied as they are, then narrowed on the GPU, which also ORs them
+// together (the highest bit any word uses).
+__global__ void qram_pack_kernel(const uint64_t* __restrict__ src, uint64_t n, uint32_t eb, void* __restrict__ dst,
+                                 unsigned long long* __restrict__ all) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    unsigned long long acc = 0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const uint64_t v = src[i];
+        acc |= v;
         if (eb == 2) ((unsigned short*)dst)[i] = (unsigned short)v;
-        else ((unsigned int*)dst)[i] = (unsigned int)v;
+        else if (eb == 4) ((unsigned int*)dst)[i] = (unsigned int)v;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc |= __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31u) == 0 && acc) atomicOr(all, acc);
 }
 
-void qram_pack(const uint64_t* host_words, uint64_t n, uint32_t eb, void* dst) {
+static uint32_t width_bytes(uint64_t all) { return all <= 0xffffull ? 2 : (all <= 0xffffffffull ? 4 : 8); }
+
+void* qram_upload(const uint64_t* host_words, uint64_t n, uint32_t eb_guess, uint32_t* eb_out, uint64_t* all_out) {
     cudaStream_t st = stream();
-    if (eb == 8) {
-        SQ_CUDA(cudaMemcpyAsync(dst, host_words, n * 8, cudaMemcpyHostToDevice, st));
-        return;
-    }
-    uint64_t* tmp = (uint64_t*)dev_alloc(n * 8);
-    SQ_CUDA(cudaMemcpyAsync(tmp, host_words, n * 8, cudaMemcpyHostToDevice, st));
+    uint64_t* raw = (uint64_t*)dev_alloc(n * 8);
+    unsigned long long* all = (unsigned long long*)dev_alloc(8);
+    void* dst = eb_guess == 8 ? (void*)raw : dev_alloc(n * eb_guess);
+    SQ_CUDA(cudaMemcpyAsync(raw, host_words, n * 8, cudaMemcpyHostToDevice, st));
+    SQ_CUDA(cudaMemsetAsync(all, 0, 8, st));
     prof_begin("qram_pack");
-    qram_pack_kernel<<<grid_for(n, 256), 256, 0, st>>>(tmp, n, eb, dst);
-    prof_end((double)n * (8 + eb));
+    qram_pack_kernel<<<grid_for(n, 256), 256, 0, st>>>(raw, n, eb_guess, dst, all);
+    prof_end((double)n * (8 + (eb_guess == 8 ? 0 : eb_guess)));
     SQ_CUDA(cudaGetLastError());
-    dev_free(tmp);
+    unsigned long long h = 0;
+    SQ_CUDA(cudaMemcpyAsync(&h, all, 8, cudaMemcpyDeviceToHost, st));
+    SQ_CUDA(cudaStreamSynchronize(st));  // the caller's buffer may be pinned: the copy is complete on return
+    const uint32_t eb = width_bytes(h);
+    if (eb != eb_guess) {  // the words need another width: narrow again from the raw copy
+        if (dst != raw) dev_free(dst);
+        dst = eb == 8 ? (void*)raw : dev_alloc(n * eb);
+        if (eb != 8) {
+            prof_begin("qram_pack");
+            qram_pack_kernel<<<grid_for(n, 256), 256, 0, st>>>(raw, n, eb, dst, all);
+            prof_end((double)n * (8 + eb));
+            SQ_CUDA(cudaGetLastError());
+        }
+    }
+    if (dst != raw) dev_free(raw);
+    dev_free(all);
+    *eb_out = eb;
+    *all_out = h;
+    return dst;
 }
 
 // Zero one register field in every entry (AddRegister on reused bits,

@@ -296,6 +296,51 @@ void free_buffers(Buffers& b) {
     b.kalloc = 0;
 }
 
+namespace {
+constexpr int kCopyStreams = 4;
+cudaStream_t g_copy[kCopyStreams] = {nullptr};
+cudaEvent_t g_copy_ev[kCopyStreams + 1] = {nullptr};
+}  // namespace
+
+void parallel_copy(const CopyJob* jobs, int n, cudaMemcpyKind kind) {
+    cudaStream_t st = stream();
+    if (!g_copy[0]) {
+        for (int i = 0; i < kCopyStreams; ++i) {
+            SQ_CUDA(cudaStreamCreateWithFlags(&g_copy[i], cudaStreamNonBlocking));
+            SQ_CUDA(cudaEventCreateWithFlags(&g_copy_ev[i], cudaEventDisableTiming));
+        }
+        SQ_CUDA(cudaEventCreateWithFlags(&g_copy_ev[kCopyStreams], cudaEventDisableTiming));
+    }
+    size_t total = 0;
+    for (int j = 0; j < n; ++j) total += jobs[j].bytes;
+    if (total < (8u << 20)) {  // small: one stream is as fast
+        for (int j = 0; j < n; ++j)
+            if (jobs[j].bytes) SQ_CUDA(cudaMemcpyAsync(jobs[j].dst, jobs[j].src, jobs[j].bytes, kind, st));
+        SQ_CUDA(cudaStreamSynchronize(st));
+        return;
+    }
+    // every copy stream starts after the library stream's queued work
+    SQ_CUDA(cudaEventRecord(g_copy_ev[kCopyStreams], st));
+    for (int i = 0; i < kCopyStreams; ++i) SQ_CUDA(cudaStreamWaitEvent(g_copy[i], g_copy_ev[kCopyStreams], 0));
+    // chunks of about total / (2 * streams) bytes, round-robin over the streams
+    const size_t chunk = std::max<size_t>((total / (2 * kCopyStreams) + 4095) & ~size_t(4095), 1u << 20);
+    int next = 0;
+    for (int j = 0; j < n; ++j) {
+        for (size_t off = 0; off < jobs[j].bytes; off += chunk) {
+            const size_t b = std::min(chunk, jobs[j].bytes - off);
+            SQ_CUDA(cudaMemcpyAsync((char*)jobs[j].dst + off, (const char*)jobs[j].src + off, b, kind,
+                                    g_copy[next]));
+            next = (next + 1) % kCopyStreams;
+        }
+    }
+    // the library stream waits for the copies too (later work may reuse the buffers)
+    for (int i = 0; i < kCopyStreams; ++i) {
+        SQ_CUDA(cudaEventRecord(g_copy_ev[i], g_copy[i]));
+        SQ_CUDA(cudaStreamWaitEvent(st, g_copy_ev[i], 0));
+    }
+    SQ_CUDA(cudaStreamSynchronize(st));
+}
+
 void free_group_cache(GroupCache& c) {
     for (int i = 0; i < 2; ++i) {
         dev_free(c.start[i]);

@@ -201,8 +201,19 @@ struct State {
 };
 inline void drop_groups(State& s) { s.groups.valid = false; }
 void free_group_cache(GroupCache& c);
-// Copy a host table of 64-bit words to `dst` on the device as eb-byte words.
-void qram_pack(const uint64_t* host_words, uint64_t n, uint32_t eb, void* dst);
+// Host <-> device copies of several arrays, split into chunks spread over a
+// few copy streams (one copy engine does not reach the host link's rate);
+// ordered after all work queued on the library stream, and complete on
+// return. `dirs` gives cudaMemcpyDeviceToHost or HostToDevice per copy.
+struct CopyJob {
+    void* dst;
+    const void* src;
+    size_t bytes;
+};
+void parallel_copy(const CopyJob* jobs, int n, cudaMemcpyKind kind);
+// Copy a host table of 64-bit words to the device at the narrowest width (2,
+// 4 or 8 bytes) that holds every word; eb_guess is tried first.
+void* qram_upload(const uint64_t* host_words, uint64_t n, uint32_t eb_guess, uint32_t* eb_out, uint64_t* all_out);
 
 struct KeyPtrs {
     uint64_t* w[SQ_KMAX];
