@@ -99,7 +99,7 @@ class Circuit:
 
 
 def sample_clocks_start(path: Path):
-    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
     try:
@@ -111,7 +111,22 @@ def sample_clocks_start(path: Path):
         return None, None
 
 
-def sample_clocks_stop(p, f, path: Path, device: int):
+def sample_clocks_wait(path: Path, timeout_s: float = 3.0) -> None:
+    """Wait until the sampler has written its first line (nvidia-smi start-up)."""
+    t0 = time.time()
+    while time.time() - t0 < timeout_s:
+        try:
+            if path.stat().st_size > 0:
+                return
+        except OSError:
+            pass
+        time.sleep(0.02)
+
+
+def sample_clocks_stop(p, f, path: Path, device: int, window=None):
+    """Median SM clock and the throttle reasons seen, over the samples taken
+    inside `window` = (start, end) host times (all samples when None)."""
+    import datetime
     if p is None:
         return None
     p.terminate()
@@ -124,19 +139,27 @@ def sample_clocks_stop(p, f, path: Path, device: int):
     names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
     for line in path.read_text().splitlines():
         parts = [x.strip() for x in line.split(",")]
-        if len(parts) < 9 or not parts[0].isdigit() or int(parts[0]) != device:
+        if len(parts) < 10 or not parts[1].isdigit() or int(parts[1]) != device:
             continue
+        if window is not None:
+            try:
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                continue
+            if not window[0] <= ts <= window[1]:
+                continue
         try:
-            sm.append(float(parts[1]))
-            mx = max(mx, float(parts[2]))
+            sm.append(float(parts[2]))
+            mx = max(mx, float(parts[3]))
         except ValueError:
             continue
-        for nm, v in zip(names, parts[5:9]):
+        for nm, v in zip(names, parts[6:10]):
             if v.lower() == "active":
                 reasons.add(nm)
     if not sm:
         return None
-    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm),
+            "window": "timed region" if window is not None else "whole run"}
 
 
 def measured_peak_hbm():
@@ -204,6 +227,191 @@ def cpu_baseline_sample(h: int, table, thetas, layers_sample: int = 2):
     dt = time.perf_counter() - t0
     O.clear()
     return upd, dt
+
+
+def replica_max(ms: float, device: str) -> float:
+    """The slowest replica's time: all-reduce MAX over the ranks, then a barrier
+    (independent circuits per GPU, no exchange on the data path)."""
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(tt.item())
+
+
+def replica_value(world: int, updates_per_step: int, steps: int, t_max_ms: float) -> float:
+    """Whole-job updates/s: every replica runs the same circuit, timed by the slowest."""
+    return world * updates_per_step * steps / (t_max_ms / 1e3)
+
+
+def run_trajectories(args, ext) -> dict:
+    """Batched noisy trajectories (4096 instances, a/b/c 16-bit, per-instance
+    Hadamard width h_t in [4, 8], Pauli X/Z at p = 1e-3 per bit per layer,
+    6 layers): the batched form, the plain GPU form (one state per instance)
+    on a sample of instances, and the oracle on a smaller sample."""
+    import numpy as np
+    import torch
+
+    import sparqsim_gb300 as ps
+    from sparqsim_gb300.workloads import NoisyTrajectories
+    wl = NoisyTrajectories(n_traj=args.trajectories, layers=6, p=1e-3, h_min=4, h_max=8, seed=SEED)
+    wl.build_batched()
+    st = ps.SparseState(capacity=1 << 20)
+    upd = wl.run_batched(st, count=True)
+    peak_hint = st.size()
+    for _ in range(2):
+        wl.run_batched(st)
+    steps = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(ext)
+    for _ in range(steps):
+        wl.run_batched(st)
+    e.record(ext)
+    e.synchronize()
+    batched_ms = s.elapsed_time(e) / steps
+    batched_wall = (time.perf_counter() - t0) / steps
+    # plain GPU form: instance by instance, on a sample of instances
+    n_sample = min(args.plain_sample, wl.n_traj)
+    wl.build_plain()
+    sp = ps.SparseState(capacity=1 << 17)
+    upd_p = sum(wl.run_plain(sp, t, count=True) for t in range(n_sample))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for t in range(n_sample):
+        wl.run_plain(sp, t)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    # the oracle, one thread, plain form, on a smaller sample
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.clear()
+        for rid in ps.System.active_ids():
+            O.add_register(int(ps.System.type_of(rid)), ps.System.size_of(rid))
+        _, qram, noise, mids, Hs = wl._built
+        O.register_qram(qram)
+        for nt in noise:
+            O.register_qram(nt.table)
+        n_cpu = min(args.cpu_sample, wl.n_traj)
+        upd_c = 0
+        t0 = time.perf_counter()
+        for t in range(n_cpu):
+            ost = O.OracleState()
+            ost.set(np.array([[t, 0, 0, 0]], dtype=np.uint64), np.ones(1, dtype=np.complex128))
+            H = Hs[int(wl.widths[t])]
+            for mid in mids:
+                n0 = ost.size()
+                O.apply(ost, H.spec())
+                n1 = ost.size()
+                O.apply(ost, mid.spec())
+                O.apply(ost, H.spec())
+                upd_c += max(n0, n1) + 4 * n1 + max(n1, ost.size())
+        cpu_s = time.perf_counter() - t0
+        O.clear()
+        cpu = {"value": upd_c / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"instances 0..{n_cpu - 1}, plain form, {upd_c} updates in {cpu_s:.1f} s, one thread"}
+    batched_ups = upd / (batched_ms / 1e3)
+    plain_ups = upd_p / plain_s
+    out = {
+        "workload": (f"{wl.n_traj} noisy instances of the register circuit (a/b/c 16-bit, 2^16-word uint16 table), "
+                     "Hadamard width h_t in [4,8] per instance, Pauli X/Z p=1e-3 per bit per layer, 6 layers, "
+                     "support 2^h..2^2h per instance"),
+        "updates_per_step": upd, "peak_entries": peak_hint,
+        "batched": {"value": batched_ups, "unit": UNIT, "ms_per_step": batched_ms,
+                    "wall_ms_per_step": batched_wall * 1e3},
+        "plain_gpu": {"value": plain_ups, "unit": UNIT,
+                      "sample": f"instances 0..{n_sample - 1}, {upd_p} updates in {plain_s:.2f} s (wall clock)"},
+        "batched_over_plain": batched_ups / plain_ups,
+        "fwht_arithmetic": ps.get_fwht_arithmetic(),
+    }
+    if cpu:
+        out["cpu"] = cpu
+        out["batched_over_cpu"] = batched_ups / cpu["value"]
+    return out
+
+
+def run_qda(args, ext) -> dict:
+    """The reference's QDA walk benchmark (PoiseuilleQDABench: the 1D Poisson
+    matrix A = tridiag(beta, alpha, beta) with alpha = 2.2666666666564934,
+    beta = -1, kappa = 16, b = ones / sqrt(n), p = 1.3, a step budget of
+    ceil(1.1 * 2305 * 16) = 40568, clearzero eps 1e-14) at n = 2^qda_bits:
+    `--qda-steps` walk steps of that schedule timed after 2 untimed ones, and
+    counted (sizes per operator) in a separate untimed pass."""
+    import torch
+
+    import sparqsim_gb300 as ps
+    from sparqsim_gb300 import qda
+    n_bits = args.qda_bits
+    alpha, beta, kappa, p = 2.2666666666564934, -1.0, 16.0, 1.3
+    total_steps, sample, warm = 40568, args.qda_steps, 2
+
+    class Counting(qda.Runner):
+        def __init__(self, state, count):
+            super().__init__(state)
+            self.count, self.updates = count, 0
+
+        def op(self, o, dag=False):
+            n0 = self.state.size() if self.count else 0
+            super().op(o, dag)
+            if self.count:
+                self.updates += max(n0, self.state.size())
+
+    def walk(count):
+        ps.System.clear()
+        run = Counting(ps.SparseState(capacity=1 << 22), False)
+        qda.declare_registers(run, n_bits)
+        run.op(ps.Hadamard_Int_Full("main_reg"))
+        enc_A = qda.BlockEncodingTridiagonal("main_reg", "anc_UA", alpha, beta)
+        enc_b = qda.StatePrepHadamard("main_reg")
+
+        def step(n):
+            qda.WalkS(enc_A, enc_b, *qda.REGS, n / total_steps, kappa, p).apply(run)
+            run.op(ps.ClearZero(1e-14))
+
+        for n in range(warm):
+            step(n)
+        run.count = count
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        s.record(ext)
+        for n in range(warm, warm + sample):
+            step(n)
+        e.record(ext)
+        e.synchronize()
+        return run, s.elapsed_time(e), time.perf_counter() - t0
+
+    counted, _, _ = walk(True)
+    run, ms, wall = walk(False)
+    # per-kernel device time of the same steps
+    from sparqsim_gb300 import _native
+    _native.profile_reset()
+    _native.profile_enable(True)
+    walk(False)
+    _native.profile_enable(False)
+    prof = _native.profile_read()
+    tot = sum(v[1] for v in prof.values()) or 1.0
+    kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot, 4)}
+               for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]}
+    ref_s_per_step = {16: 0.24, 20: 1.33}.get(n_bits)
+    out = {
+        "workload": (f"QDA walk of the reference's PoiseuilleQDABench: n=2^{n_bits}, A = tridiag(-1, "
+                     f"{alpha}, -1) (kappa 16), b uniform, p={p}, schedule of {total_steps} steps; "
+                     f"steps {warm}..{warm + sample - 1} timed"),
+        "steps_timed": sample, "entries": run.state.size(),
+        "updates": counted.updates, "value": counted.updates / (ms / 1e3), "unit": UNIT,
+        "ms_per_walk_step": ms / sample, "wall_ms_per_walk_step": wall * 1e3 / sample,
+        "projected_full_budget_s": ms / sample * total_steps / 1e3,
+        "kernels": kernels, "kernel_ms_per_walk_step": tot / sample,
+    }
+    if ref_s_per_step:
+        out["reference_published"] = {"s_per_walk_step": ref_s_per_step, "hardware": "1x A800-SXM4-80GB",
+                                      "source": "docs/verification/v1d-qda-linsolver-a800.md:48-52"}
+        out["speedup_vs_published"] = ref_s_per_step / (ms / sample / 1e3)
+    return out
 
 
 def replica_max(ms: float, device: str) -> float:
@@ -408,18 +616,22 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     clocks_path = ROOT / "gpurun_out" / f"clocks_rank{rank}.csv"
     clocks_path.parent.mkdir(exist_ok=True)
     cp, cf = sample_clocks_start(clocks_path) if rank == 0 else (None, None)
+    if cp is not None:
+        sample_clocks_wait(clocks_path)
     launches0 = ps.launch_count()
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    w0 = time.time()
     start.record(ext)
     for _ in range(args.steps):
         circ.run(st)
     end.record(ext)
     end.synchronize()
     torch.cuda.synchronize()
+    w1 = time.time()
     ms = start.elapsed_time(end)
     launches = ps.launch_count() - launches0
-    clocks = sample_clocks_stop(cp, cf, clocks_path, local_rank) if rank == 0 else None
+    clocks = sample_clocks_stop(cp, cf, clocks_path, local_rank, (w0, w1)) if rank == 0 else None
 
     t_max = ms
     if world > 1:
@@ -436,12 +648,13 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         circ.run(st)
         torch.cuda.synchronize()
         s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        other_steps = max(1, min(args.steps, 20))
         s2.record(ext)
-        for _ in range(args.steps):
+        for _ in range(other_steps):
             circ.run(st)
         e2.record(ext)
         e2.synchronize()
-        other_ms = s2.elapsed_time(e2) / args.steps
+        other_ms = s2.elapsed_time(e2) / other_steps
         ps.set_fwht_arithmetic(args.fwht_arithmetic)
 
     # end to end through the public API: host inputs in, final state out
@@ -620,7 +833,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=300)  # about 1 s of timed work: several clock samples
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--hadamard-bits", type=int, default=12)
@@ -632,7 +845,8 @@ def main():
                     help="instances in the batched noisy-trajectory leg (0 skips it)")
     ap.add_argument("--plain-sample", type=int, default=256, help="instances timed in the plain GPU form")
     ap.add_argument("--cpu-sample", type=int, default=16, help="instances timed in the oracle")
-    ap.add_argument("--qda-steps", type=int, default=20, help="QDA walk steps timed at N=2^16 (0 skips)")
+    ap.add_argument("--qda-steps", type=int, default=10, help="QDA walk steps timed (0 skips)")
+    ap.add_argument("--qda-bits", type=int, default=16, help="main register of the QDA walk (16 or 20)")
     ap.add_argument("--fwht-arithmetic", default="exact-sum", choices=["exact-sum", "reference"],
                     help="Hadamard butterfly arithmetic of the headline run (the other one is timed too)")
     args = ap.parse_args()

@@ -372,6 +372,16 @@ int sq_get_fwht_arithmetic(int* mode);
 /* clearzero_default_eps (system_operations.h:577), initially 1e-14. */
 int sq_set_clearzero_eps(double eps);
 int sq_get_clearzero_eps(double* eps);
+/* PartialTraceSelect (partial_trace.cpp:148-185): keep the entries whose
+ * registers regs[i] hold values[i] (all i), in order, and scale them by
+ * 1/sqrt(p), p their total probability; *result = that factor, +inf when
+ * nothing is left, 0 for n == 0 or an empty state. The registers keep their
+ * values. */
+int sq_partial_trace_select(sq_state* st, const uint32_t* regs, const uint64_t* values, uint32_t n,
+                            double* result);
+/* PartialTraceSelectRange (partial_trace.cpp:187-225): the same for
+ * lo <= value(reg) <= hi. */
+int sq_partial_trace_select_range(sq_state* st, uint32_t reg, uint64_t lo, uint64_t hi, double* result);
 /* ClearZero (system_operations.cpp:371-382): drop entries with |a|^2 < eps;
  * order of survivors is preserved. */
 int sq_clear_zero(sq_state* st, double eps);

@@ -50,6 +50,8 @@ def lib():
             "sqo_rot_general_unitary": (c_int, [c_void_p, c_uint32, POINTER(c_double), c_uint64, POINTER(SqCond), c_int]),
             "sqo_hadamard_partial": (c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_uint32, POINTER(SqCond)]),
             "sqo_normalize": (c_int, [c_void_p, POINTER(c_double)]),
+            "sqo_partial_trace_select": (c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_int, c_uint64, c_uint64,
+                                                 POINTER(c_double)]),
             "sqo_add_systems": (c_int, [c_void_p, c_void_p, c_double]),
             "sqo_add_register_sync": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_uint32)]),
             "sqo_remove_register_sync": (c_int, [c_void_p, c_uint32]),
@@ -219,6 +221,18 @@ def apply(state: OracleState, spec) -> None:
         _chk(L.sqo_clear_zero(h, spec[1]))
     elif kind == "normalize":
         _chk(L.sqo_normalize(h, None))
+    elif kind in ("partial_trace_select", "partial_trace_select_range"):
+        out = c_double()
+        if kind == "partial_trace_select":
+            regs = np.array(spec[1], dtype=np.uint32)
+            vals = np.array(spec[2], dtype=np.uint64)
+            _chk(L.sqo_partial_trace_select(h, regs.ctypes.data_as(c_void_p), vals.ctypes.data_as(c_void_p),
+                                            len(regs), 0, 0, 0, byref(out)))
+        else:
+            regs = np.array([spec[1]], dtype=np.uint32)
+            _chk(L.sqo_partial_trace_select(h, regs.ctypes.data_as(c_void_p), None, 1, 1, spec[2], spec[3],
+                                            byref(out)))
+        return out.value
     else:
         raise ValueError(kind)
 

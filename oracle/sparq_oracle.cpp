@@ -36,6 +36,7 @@
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <limits>
 #include <vector>
 
 #include "sparq_gb300.h"
@@ -483,6 +484,42 @@ struct LessExceptKey {
         return false;
     }
 };
+
+// ---------------------------------------------------------------- PartialTraceSelect
+// partial_trace.cpp:148-225: remove_if (order kept) with the probability
+// summed in order, then a *= 1/sqrt(p); returns that factor or +inf.
+static double partial_trace_select(State& st, const std::vector<uint32_t>& regs,
+                                   const std::vector<uint64_t>& values, bool range, uint64_t lo, uint64_t hi) {
+    if (!range && regs.empty()) return 0;
+    if (st.empty()) return 0;
+    double sum_prob = 0;
+    State kept;
+    kept.reserve(st.size());
+    for (const auto& s : st) {
+        bool keep = true;
+        if (range) {
+            const uint64_t v = get_as(s, regs[0]);
+            keep = v >= lo && v <= hi;
+        } else {
+            for (size_t i = 0; i < regs.size(); ++i)
+                if (values[i] != s.get(regs[i])) {
+                    keep = false;
+                    break;
+                }
+        }
+        if (keep) {
+            sum_prob += abs_sqr(s.amplitude);
+            kept.push_back(s);
+        }
+    }
+    st.swap(kept);
+    if (sum_prob != 0) {
+        sum_prob = 1.0 / std::sqrt(sum_prob);
+        for (auto& s : st) s.amplitude *= sum_prob;
+        return sum_prob;
+    }
+    return std::numeric_limits<double>::infinity();
+}
 
 // ---------------------------------------------------------------- Hadamard_Int
 // Hadamard_Int::operate (hadamard.cpp:18-132). Groups whose members disagree
@@ -1118,6 +1155,15 @@ int sqo_hadamard_partial(void* h, uint32_t reg, const uint32_t* positions, uint3
     })
 }
 int sqo_clear_zero(void* h, double eps) { SQO_TRY(clear_zero(*static_cast<State*>(h), eps)) }
+int sqo_partial_trace_select(void* h, const uint32_t* regs, const uint64_t* values, uint32_t n, int range,
+                             uint64_t lo, uint64_t hi, double* result) {
+    SQO_TRY({
+        std::vector<uint32_t> r(regs, regs + n);
+        std::vector<uint64_t> v;
+        if (values) v.assign(values, values + n);
+        *result = partial_trace_select(*static_cast<State*>(h), r, v, range != 0, lo, hi);
+    })
+}
 int sqo_normalize(void* h, double* norm_sq) {
     SQO_TRY({ double s = normalize(*static_cast<State*>(h)); if (norm_sq) *norm_sq = s; })
 }

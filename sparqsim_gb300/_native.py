@@ -138,6 +138,8 @@ _SIGS = [
     ("sq_set_group_strategy", c_int, [c_int]),
     ("sq_get_group_strategy", c_int, [POINTER(c_int)]),
     ("sq_set_output_sizing", c_int, [c_int]),
+    ("sq_partial_trace_select", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, POINTER(c_double)]),
+    ("sq_partial_trace_select_range", c_int, [c_void_p, c_uint32, c_uint64, c_uint64, POINTER(c_double)]),
     ("sq_autotune_reset", c_int, []),
     ("sq_autotune_classes", c_int, [POINTER(c_uint64), POINTER(c_uint64)]),
     ("sq_get_output_sizing", c_int, [POINTER(c_int)]),

@@ -831,6 +831,40 @@ int sq_clear_zero(sq_state* st, double eps) {
     SQ_API_END
 }
 
+int sq_partial_trace_select(sq_state* st, const uint32_t* regs, const uint64_t* values, uint32_t n,
+                            double* result) {
+    SQ_API_BEGIN
+    need(result != nullptr, "null pointer");
+    need(n <= SQ_MAX_CONDITIONS, "PartialTraceSelect: at most SQ_MAX_CONDITIONS registers");
+    need(n == 0 || (regs != nullptr && values != nullptr), "null pointer");
+    if (n == 0) {  // partial_trace.cpp:151-152
+        *result = 0.0;
+        return SQ_OK;
+    }
+    sq_cond c;
+    memset(&c, 0, sizeof(c));
+    c.count = n;
+    for (uint32_t i = 0; i < n; ++i) {
+        c.c[i].kind = SQ_COND_VALUE;
+        c.c[i].reg = regs[i];
+        c.c[i].param = values[i];
+    }
+    Field none{};
+    *result = select_entries(S(st), resolve_cond(&c), none, 0, 0);
+    SQ_API_END
+}
+
+int sq_partial_trace_select_range(sq_state* st, uint32_t reg, uint64_t lo, uint64_t hi, double* result) {
+    SQ_API_BEGIN
+    need(result != nullptr, "null pointer");
+    Field f = regtable().field(reg);
+    need(f.width > 0, "PartialTraceSelectRange: empty register");
+    DCondSet none;
+    memset(&none, 0, sizeof(none));
+    *result = select_entries(S(st), none, f, lo, hi);
+    SQ_API_END
+}
+
 int sq_normalize(sq_state* st, double* norm_sq_out) {
     SQ_API_BEGIN
     State& s = S(st);

@@ -5,7 +5,9 @@
 // once, and writes the survivors once: N*16 + N_out*(8K+16) bytes, the
 // algorithmic minimum. Tile offsets come from a decoupled look-back, so the
 // kernel is a single pass and keeps the reference's remove_if order.
+#include <cmath>
 #include <cstring>
+#include <limits>
 
 #include "lookback.cuh"
 #include "sq_internal.cuh"
@@ -34,11 +36,24 @@ static LookbackWs lookback_ws(long long ntiles) {
     return w;
 }
 
-template <int K>
+// Entries kept by a selection on key values (PartialTraceSelect[Range]): all
+// conditions of `sel` hold and, if rf has a width, lo <= value(rf) <= hi.
+double norm_sq(const State& s);
+void scale_amp(State& s, double k);
+
+struct KeySelect {
+    DCondSet sel;
+    Field rf;
+    uint64_t lo, hi;
+};
+
+// SEL = false: ClearZero (keep |a|^2 >= eps); SEL = true: keep the entries the
+// key selection accepts. Same single pass either way.
+template <int K, bool SEL>
 __global__ void __launch_bounds__(kCzBlock) clearzero_kernel(ConstKeyPtrs ik, const double2* __restrict__ ia,
                                                              KeyPtrs ok, double2* __restrict__ oa, uint64_t n,
                                                              double eps, LookbackWs lb, long long ntiles,
-                                                             unsigned* err) {
+                                                             unsigned* err, const __grid_constant__ KeySelect ks) {
     __shared__ unsigned s_tile;
     __shared__ unsigned s_cnt[kCzItems][kCzBlock / 32];
     __shared__ unsigned long long s_prefix;
@@ -55,7 +70,18 @@ __global__ void __launch_bounds__(kCzBlock) clearzero_kernel(ConstKeyPtrs ik, co
         bool keep = false;
         if (i < n) {
             a[j] = ia[i];
-            keep = sq_keep_amp(a[j].x, a[j].y, eps);
+            if (SEL) {
+                uint64_t k[K];
+#pragma unroll
+                for (int w = 0; w < K; ++w) k[w] = ik.w[w][i];
+                keep = cond_ok<K>(k, ks.sel);
+                if (ks.rf.width) {
+                    const uint64_t v = fget<K>(k, ks.rf);
+                    keep = keep && ks.lo <= v && v <= ks.hi;
+                }
+            } else {
+                keep = sq_keep_amp(a[j].x, a[j].y, eps);
+            }
         }
         ball[j] = __ballot_sync(0xffffffffu, keep);
         if (lane == 0) s_cnt[j][warp] = __popc(ball[j]);
@@ -95,17 +121,20 @@ __global__ void __launch_bounds__(kCzBlock) clearzero_kernel(ConstKeyPtrs ik, co
     }
 }
 
-template <int K>
-static void launch_cz(const Buffers& in, Buffers& out, uint64_t n, double eps, LookbackWs lb, long long nt) {
+template <int K, bool SEL = false>
+static void launch_cz(const Buffers& in, Buffers& out, uint64_t n, double eps, LookbackWs lb, long long nt,
+                      const KeySelect* ks = nullptr) {
     ConstKeyPtrs ik;
     KeyPtrs okp;
     for (int w = 0; w < SQ_KMAX; ++w) {
         ik.w[w] = in.keys[w];
         okp.w[w] = out.keys[w];
     }
-    prof_begin("clearzero");
-    clearzero_kernel<K><<<(unsigned)nt, kCzBlock, 0, stream()>>>(ik, in.amp, okp, out.amp, n, eps, lb, nt,
-                                                               device_error_word());
+    KeySelect none;
+    memset(&none, 0, sizeof(none));
+    prof_begin(SEL ? "select_entries" : "clearzero");
+    clearzero_kernel<K, SEL><<<(unsigned)nt, kCzBlock, 0, stream()>>>(ik, in.amp, okp, out.amp, n, eps, lb, nt,
+                                                                    device_error_word(), ks ? *ks : none);
     prof_end((double)n * 16);  // every amplitude read; survivors added below
     SQ_CUDA(cudaGetLastError());
 }
@@ -143,6 +172,49 @@ uint64_t compact_nonzero(const Buffers& in, Buffers& out, uint64_t n, double eps
     check_device_error();  // synchronizes
     prof_add_bytes_last((double)total * (16.0 * k + 16));  // survivors: keys read + keys and amp written
     return total;
+}
+
+// PartialTraceSelect / PartialTraceSelectRange (partial_trace.cpp:148-225):
+// keep the entries whose selected registers hold the selected values (or
+// whose register lies in [lo, hi]), in order; then scale them by 1/sqrt(p), p
+// their total probability. Returns that factor, or +inf when nothing is left.
+double select_entries(State& s, const DCondSet& sel, Field rf, uint64_t lo, uint64_t hi) {
+    drop_groups(s);
+    sync_words(s);
+    if (s.n == 0) return 0.0;
+    const uint32_t k = regtable().k;
+    ensure_buffers(s.spare, s.n, k, 0);
+    KeySelect ks;
+    memset(&ks, 0, sizeof(ks));
+    ks.sel = sel;
+    ks.rf = rf;
+    ks.lo = lo;
+    ks.hi = hi;
+    const uint64_t n = s.n;
+    const long long nt = (long long)((n + kCzTile - 1) / kCzTile);
+    LookbackWs lb = lookback_ws(nt);
+    switch (k) {
+        case 1: launch_cz<1, true>(s.live, s.spare, n, 0.0, lb, nt, &ks); break;
+        case 2: launch_cz<2, true>(s.live, s.spare, n, 0.0, lb, nt, &ks); break;
+        case 3: launch_cz<3, true>(s.live, s.spare, n, 0.0, lb, nt, &ks); break;
+        case 4: launch_cz<4, true>(s.live, s.spare, n, 0.0, lb, nt, &ks); break;
+        case 5: launch_cz<5, true>(s.live, s.spare, n, 0.0, lb, nt, &ks); break;
+        case 6: launch_cz<6, true>(s.live, s.spare, n, 0.0, lb, nt, &ks); break;
+        case 7: launch_cz<7, true>(s.live, s.spare, n, 0.0, lb, nt, &ks); break;
+        default: launch_cz<8, true>(s.live, s.spare, n, 0.0, lb, nt, &ks); break;
+    }
+    unsigned long long total = 0;
+    SQ_CUDA(cudaMemcpyAsync(&total, lb.total, 8, cudaMemcpyDeviceToHost, stream()));
+    check_device_error();  // synchronizes
+    prof_add_bytes_last((double)total * (16.0 * k + 16) - (double)n * 16 + (double)n * (8.0 * k + 16));
+    swap_live_spare(s);
+    s.n = total;
+    if (total == 0) return std::numeric_limits<double>::infinity();
+    const double p = norm_sq(s);
+    if (p == 0.0) return std::numeric_limits<double>::infinity();
+    const double f = 1.0 / std::sqrt(p);
+    scale_amp(s, f);
+    return f;
 }
 
 void clear_zero(State& s, double eps) {
@@ -257,8 +329,11 @@ static void launch_cz_noalloc(const uint64_t* const* keys_in, const double* amps
     lb.counter = (unsigned*)scratch;
     lb.total = scratch + 1;
     lb.status = scratch + kNoAllocHeaderWords;
-    clearzero_kernel<K><<<(unsigned)nt, kCzBlock, 0, s>>>(ik, (const double2*)amps_in, okp, (double2*)amps_out, n, eps,
-                                                          lb, nt, (unsigned*)(scratch + 2));
+    KeySelect none;
+    memset(&none, 0, sizeof(none));
+    clearzero_kernel<K, false><<<(unsigned)nt, kCzBlock, 0, s>>>(ik, (const double2*)amps_in, okp,
+                                                                 (double2*)amps_out, n, eps, lb, nt,
+                                                                 (unsigned*)(scratch + 2), none);
     count_launch();
 }
 

@@ -201,6 +201,7 @@ struct State {
 };
 inline void drop_groups(State& s) { s.groups.valid = false; }
 void free_group_cache(GroupCache& c);
+double select_entries(State& s, const DCondSet& sel, Field rf, uint64_t lo, uint64_t hi);
 // Host <-> device copies of several arrays, split into chunks spread over a
 // few copy streams (one copy engine does not reach the host link's rate);
 // ordered after all work queued on the library stream, and complete on

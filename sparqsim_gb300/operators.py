@@ -760,6 +760,48 @@ class Normalize(SelfAdjointOperator):
         return ("normalize",)
 
 
+class PartialTraceSelect:
+    """Keep the entries whose registers hold the selected values, scale them by
+    1/sqrt(p) and return that factor (+inf if none is left)
+    (partial_trace.cpp:148-185). Built from {reg: value} or (regs, values)."""
+
+    def __init__(self, regs, values=None):
+        if values is None:
+            items = list(dict(regs).items())
+        else:
+            items = list(zip(regs, values))
+        self.regs = [_R(r) for r, _ in items]
+        self.values = [int(v) & U64 for _, v in items]
+
+    def __call__(self, state: SparseState) -> float:
+        import numpy as np
+        r = np.array(self.regs, dtype=np.uint32)
+        v = np.array(self.values, dtype=np.uint64)
+        out = c_double()
+        call("sq_partial_trace_select", state._h, r.ctypes.data_as(ctypes.c_void_p),
+             v.ctypes.data_as(ctypes.c_void_p), len(self.regs), byref(out))
+        return out.value
+
+    def spec(self, dag=False):
+        return ("partial_trace_select", self.regs, self.values)
+
+
+class PartialTraceSelectRange:
+    """The same for lo <= value(reg) <= hi (partial_trace.cpp:187-225)."""
+
+    def __init__(self, reg, select_range):
+        self.reg = _R(reg)
+        self.lo, self.hi = int(select_range[0]), int(select_range[1])
+
+    def __call__(self, state: SparseState) -> float:
+        out = c_double()
+        call("sq_partial_trace_select_range", state._h, self.reg, self.lo, self.hi, byref(out))
+        return out.value
+
+    def spec(self, dag=False):
+        return ("partial_trace_select_range", self.reg, self.lo, self.hi)
+
+
 # ---------------------------------------------------------------------- register surgery
 class AddRegister:
     """New zero-valued register (system_operations.cpp:252-272); returns its id."""

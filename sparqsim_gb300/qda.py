@@ -242,14 +242,18 @@ def declare_registers(run, n_bits: int):
 
 def read_solution(state: SparseState, n_bits: int):
     """Amplitudes of the main register where anc_UA = anc_2 = anc_3 = anc_4 = 0
-    and anc_1 = 1, and the probability of that sector."""
-    ids = [System.resolve(r) for r in REGS]
-    regs, amps = state.download()
-    sel = (regs[:, ids[1]] == 0) & (regs[:, ids[3]] == 0) & (regs[:, ids[4]] == 0) & (regs[:, ids[5]] == 0) \
-        & (regs[:, ids[2]] == 1)
+    and anc_1 = 1, and the probability of that sector. The post-selection
+    runs on the GPU (PartialTraceSelect, which also renormalises the state);
+    only the selected entries are read back."""
+    from .operators import PartialTraceSelect
+    f = PartialTraceSelect({"anc_UA": 0, "anc_1": 1, "anc_2": 0, "anc_3": 0, "anc_4": 0})(state)
     x = np.zeros(1 << n_bits, dtype=np.complex128)
-    np.add.at(x, regs[sel, ids[0]].astype(np.int64), amps[sel])
-    return x, float(np.sum(np.abs(x) ** 2))
+    if not np.isfinite(f) or f == 0:
+        return x, 0.0
+    regs, amps = state.download()
+    main = System.resolve("main_reg")
+    np.add.at(x, regs[:, main].astype(np.int64), amps / f)
+    return x, float(1.0 / (f * f))
 
 
 def walk_sequence(run, n_bits: int, alpha: float, beta: float, kappa: float, p: float, steps: int,
