@@ -229,6 +229,67 @@ def cpu_baseline_sample(h: int, table, thetas, layers_sample: int = 2):
     return upd, dt
 
 
+def run_cks(args, ext) -> dict:
+    """The reference's CKS benchmark (CKSPoiseuilleBench: A = tridiag(-1,
+    2.2666666666564934, -1) quantised to 32 bits, b = ones / sqrt(n) with the
+    parity phase D, least-squares 1/x coefficients with J = 640, kappa 16) at
+    n = 2^cks_bits: FirstStep and one untimed LCU term, then `--cks-terms`
+    terms timed, each two walk steps and the add_systems merge into the
+    accumulator, device time with CUDA events."""
+    import torch
+
+    import sparqsim_gb300 as ps
+    from sparqsim_gb300 import _native, cks
+    n_bits, terms = args.cks_bits, args.cks_terms
+    n = 1 << n_bits
+    ps.System.clear()
+    mat, spec = cks.make_tridiagonal_matrix_spec(2.2666666666564934, -1.0, n, 32)
+    obj = cks.LCU_Container_NoiseFree_Tridiagonal(mat, spec, 16.0, 0.01)
+    obj.set_inverse_coefficients(cks.ChebyshevInverseCoefficients(*cks.walk_spectrum(spec), 640))
+    st = obj.step_state
+    ps.Hadamard_Int(obj.GetInputVecReg(), n_bits)(st)
+    cks.TridiagParityPhase(obj.GetInputVecReg())(st)
+    ps.ClearZero()(st)
+    t0 = time.perf_counter()
+    obj.quantum_walk_obj.FirstStep(obj.run)
+    torch.cuda.synchronize()
+    first_s = time.perf_counter() - t0
+    obj.Step()
+    obj.Step()
+    torch.cuda.synchronize()
+    _native.profile_reset()
+    _native.profile_enable(True)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    s.record(ext)
+    for _ in range(terms):
+        obj.Step()
+    e.record(ext)
+    e.synchronize()
+    wall = time.perf_counter() - t0
+    _native.profile_enable(False)
+    prof = _native.profile_read()
+    ms = s.elapsed_time(e)
+    tot = sum(v[1] for v in prof.values()) or 1.0
+    kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot, 4)}
+               for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:10]}
+    out = {
+        "workload": (f"CKS walk of the reference's CKSPoiseuilleBench: n=2^{n_bits}, tridiagonal 1D Poisson "
+                     f"matrix quantised to 32 bits, least-squares 1/x coefficients (J=640), kappa 16; LCU terms "
+                     f"2..{1 + terms} timed (two walk steps and one add_systems merge each)"),
+        "terms_timed": terms, "entries_walk_state": st.size(), "entries_accumulator": obj.current_state.size(),
+        "peak_walk_entries": obj.max_system_size, "first_step_s": first_s,
+        "s_per_term": ms / terms / 1e3, "wall_s_per_term": wall / terms,
+        "kernels": kernels, "kernel_s_per_term": tot / terms / 1e3,
+    }
+    if n_bits == 20:
+        out["reference_published"] = {"s_per_term": 4.2, "entries_after_first_step": 20971512,
+                                      "hardware": "1x A800-SXM4-80GB",
+                                      "source": "docs/verification/v1e-cks-direct-oracle-linsolver.md:116-118"}
+        out["speedup_vs_published"] = 4.2 / (ms / terms / 1e3)
+    return out
+
+
 def replica_max(ms: float, device: str) -> float:
     """The slowest replica's time: all-reduce MAX over the ranks, then a barrier
     (independent circuits per GPU, no exchange on the data path)."""
@@ -338,29 +399,37 @@ def run_qda(args, ext) -> dict:
     matrix A = tridiag(beta, alpha, beta) with alpha = 2.2666666666564934,
     beta = -1, kappa = 16, b = ones / sqrt(n), p = 1.3, a step budget of
     ceil(1.1 * 2305 * 16) = 40568, clearzero eps 1e-14) at n = 2^qda_bits:
-    `--qda-steps` walk steps of that schedule timed after 2 untimed ones, and
-    counted (sizes per operator) in a separate untimed pass."""
+    `--qda-steps` walk steps of that schedule timed after `--qda-warm` (at least
+    2) untimed ones, each followed by ClearZero and Normalize as there, and
+    counted (sizes per operator, peak entries) in a separate untimed pass."""
     import torch
 
     import sparqsim_gb300 as ps
-    from sparqsim_gb300 import qda
+    from sparqsim_gb300 import _native, qda
     n_bits = args.qda_bits
     alpha, beta, kappa, p = 2.2666666666564934, -1.0, 16.0, 1.3
-    total_steps, sample, warm = 40568, args.qda_steps, 2
+    total_steps, sample, warm = 40568, args.qda_steps, max(2, args.qda_warm)
 
     class Counting(qda.Runner):
+        """Counts entries read or written per operator (max of the sizes
+        before and after) and the peak entry count, the reference's
+        System::max_system_size."""
+
         def __init__(self, state, count):
             super().__init__(state)
-            self.count, self.updates = count, 0
+            self.count, self.updates, self.peak, self.sizes = count, 0, 0, []
 
         def op(self, o, dag=False):
             n0 = self.state.size() if self.count else 0
             super().op(o, dag)
             if self.count:
-                self.updates += max(n0, self.state.size())
+                n1 = self.state.size()
+                self.updates += max(n0, n1)
+                self.peak = max(self.peak, n0, n1)
 
-    def walk(count):
+    def walk(count, profile=False):
         ps.System.clear()
+        ps.set_clearzero_default_eps(1e-14)  # the walk's own ClearZero calls use the bench's threshold
         run = Counting(ps.SparseState(capacity=1 << 22), False)
         qda.declare_registers(run, n_bits)
         run.op(ps.Hadamard_Int_Full("main_reg"))
@@ -370,11 +439,18 @@ def run_qda(args, ext) -> dict:
         def step(n):
             qda.WalkS(enc_A, enc_b, *qda.REGS, n / total_steps, kappa, p).apply(run)
             run.op(ps.ClearZero(1e-14))
+            run.op(ps.Normalize())
+            if run.count:
+                run.sizes.append(run.state.size())
 
+        run.count = count
         for n in range(warm):
             step(n)
-        run.count = count
+        run.updates = 0  # the timed steps' updates only; peak and sizes cover the whole walk
         torch.cuda.synchronize()
+        if profile:
+            _native.profile_reset()
+            _native.profile_enable(True)
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
         s.record(ext)
@@ -382,16 +458,13 @@ def run_qda(args, ext) -> dict:
             step(n)
         e.record(ext)
         e.synchronize()
+        if profile:
+            _native.profile_enable(False)
         return run, s.elapsed_time(e), time.perf_counter() - t0
 
     counted, _, _ = walk(True)
     run, ms, wall = walk(False)
-    # per-kernel device time of the same steps
-    from sparqsim_gb300 import _native
-    _native.profile_reset()
-    _native.profile_enable(True)
-    walk(False)
-    _native.profile_enable(False)
+    walk(False, profile=True)  # per-kernel device time of the timed steps
     prof = _native.profile_read()
     tot = sum(v[1] for v in prof.values()) or 1.0
     kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot, 4)}
@@ -401,7 +474,8 @@ def run_qda(args, ext) -> dict:
         "workload": (f"QDA walk of the reference's PoiseuilleQDABench: n=2^{n_bits}, A = tridiag(-1, "
                      f"{alpha}, -1) (kappa 16), b uniform, p={p}, schedule of {total_steps} steps; "
                      f"steps {warm}..{warm + sample - 1} timed"),
-        "steps_timed": sample, "entries": run.state.size(),
+        "steps_timed": sample, "entries": run.state.size(), "peak_entries": counted.peak,
+        "entries_after_each_step": counted.sizes,
         "updates": counted.updates, "value": counted.updates / (ms / 1e3), "unit": UNIT,
         "ms_per_walk_step": ms / sample, "wall_ms_per_walk_step": wall * 1e3 / sample,
         "projected_full_budget_s": ms / sample * total_steps / 1e3,
@@ -516,73 +590,6 @@ def run_trajectories(args, ext) -> dict:
         out["cpu"] = cpu
         out["batched_over_cpu"] = batched_ups / cpu["value"]
     return out
-
-
-def run_qda(args, ext) -> dict:
-    """QDA walk steps at N = 2^16 (config 3's size) with the tridiagonal block
-    encoding: A = alpha I + beta (S + S^T) with kappa(A) about 50, b uniform,
-    on the schedule of a 2000-step walk. The first `--qda-steps` steps are run
-    once with size counting (untimed), then again from the start, timed."""
-    import torch
-
-    import sparqsim_gb300 as ps
-    from sparqsim_gb300 import qda
-    n_bits, beta = 16, 1.0
-    alpha = 2 * beta * 51 / 49  # eigenvalues alpha + 2 beta cos(k pi / (N+1)): kappa about 50
-    kappa, p, total_steps, sample = 50.0, 0.5, 2000, args.qda_steps
-
-    class Counting(qda.Runner):
-        def __init__(self, state, count):
-            super().__init__(state)
-            self.count, self.updates = count, 0
-
-        def op(self, o, dag=False):
-            n0 = self.state.size() if self.count else 0
-            super().op(o, dag)
-            if self.count:
-                self.updates += max(n0, self.state.size())
-
-    def walk(count):
-        ps.System.clear()
-        run = Counting(ps.SparseState(capacity=1 << 22), count)
-        qda.declare_registers(run, n_bits)
-        run.op(ps.Hadamard_Int_Full("main_reg"))
-        enc_A = qda.BlockEncodingTridiagonal("main_reg", "anc_UA", alpha, beta)
-        enc_b = qda.StatePrepHadamard("main_reg")
-        torch.cuda.synchronize()
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0 = time.perf_counter()
-        s.record(ext)
-        for n in range(sample):
-            qda.WalkS(enc_A, enc_b, *qda.REGS, n / total_steps, kappa, p).apply(run)
-            run.op(ps.ClearZero())
-        e.record(ext)
-        e.synchronize()
-        return run, s.elapsed_time(e), time.perf_counter() - t0
-
-    counted, _, _ = walk(True)
-    run, ms, wall = walk(False)
-    # per-kernel device time of the same steps
-    from sparqsim_gb300 import _native
-    _native.profile_reset()
-    _native.profile_enable(True)
-    walk(False)
-    _native.profile_enable(False)
-    prof = _native.profile_read()
-    tot = sum(v[1] for v in prof.values()) or 1.0
-    kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot, 4)}
-               for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]}
-    return {
-        "workload": (f"QDA walk, N=2^{n_bits}, tridiagonal block encoding of alpha I + beta (S + S^T) "
-                     f"(alpha={alpha:.4f}, beta={beta}, kappa about 50), b uniform, schedule of a "
-                     f"{total_steps}-step walk (p={p}); its first {sample} steps timed"),
-        "steps_timed": sample, "entries_after": run.state.size(),
-        "updates": counted.updates, "value": counted.updates / (ms / 1e3), "unit": UNIT,
-        "ms_per_walk_step": ms / sample, "wall_ms_per_walk_step": wall * 1e3 / sample,
-        "projected_2000_step_walk_s": ms / sample * total_steps / 1e3,
-        "kernels": kernels,
-        "kernel_ms_per_walk_step": tot / sample,
-    }
 
 
 def run_gb300(args, rank: int, world: int, local_rank: int):
@@ -724,6 +731,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         result["batched_trajectories"] = run_trajectories(args, ext)
     if args.qda_steps and rank == 0:
         result["qda_walk"] = run_qda(args, ext)
+    if args.cks_terms and rank == 0:
+        result["cks_walk"] = run_cks(args, ext)
     return result, (table, thetas)
 
 
@@ -847,6 +856,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=16, help="instances timed in the oracle")
     ap.add_argument("--qda-steps", type=int, default=10, help="QDA walk steps timed (0 skips)")
     ap.add_argument("--qda-bits", type=int, default=16, help="main register of the QDA walk (16 or 20)")
+    ap.add_argument("--qda-warm", type=int, default=2, help="untimed QDA walk steps before the timed ones")
+    ap.add_argument("--cks-terms", type=int, default=3, help="CKS LCU terms timed (0 skips)")
+    ap.add_argument("--cks-bits", type=int, default=20, help="main register of the CKS walk")
     ap.add_argument("--fwht-arithmetic", default="exact-sum", choices=["exact-sum", "reference"],
                     help="Hadamard butterfly arithmetic of the headline run (the other one is timed too)")
     args = ap.parse_args()

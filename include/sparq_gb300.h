@@ -131,7 +131,29 @@ typedef enum {
      * w[6t .. 6t+5] = (xa, xb, xc, za, zb, zc) read from `qram`:
      * reg1 ^= xa, reg2 ^= xb, reg3 ^= xc, then
      * amp *= (-1)^(popcount(reg1 & za) + popcount(reg2 & zb) + popcount(reg3 & zc)). */
-    SQ_OP_PAULI_NOISE = 71
+    SQ_OP_PAULI_NOISE = 71,
+    /* The CKS walk on a constant-diagonal tridiagonal matrix with 4-slot row
+     * windows (SparQ_Algorithm/include/hamiltonian_simulation_tridiagonal.h:
+     * 104-190). mem(idx) is the word of the combined [elements | columns]
+     * table at idx & (8n - 1); imm0 = n (a power of two >= 8), imm1 =
+     * alpha_enc | beta_enc << 32 (the quantised elements, < 2^32 each).
+     * TridiagOracle1 (hamiltonian_tridiagonal.cpp:16-33):
+     *   reg3 ^= mem(reg0 + 4 * reg1 + reg2)  (offset, row, slot, data). */
+    SQ_OP_TRIDIAG_ELEMENT = 72,
+    /* TridiagOracle2 (hamiltonian_tridiagonal.cpp:35-83) on offset reg0,
+     * row reg1, slot/column reg2 and tag reg3, imm2 = k_width; dag = 0 maps
+     * column -> slot, dag = 1 slot -> column. The tag is read modulo
+     * 2^k_width; the dagger stores it unmasked, so it wants a register wide
+     * enough for row addresses (64 bits) to keep every bit the reference
+     * keeps. */
+    SQ_OP_TRIDIAG_SLOT_COLUMN = 73,
+    /* reg1 ^= f(reg0), f from a table of sq_lookup_create (passed in `qram`);
+     * a value the table does not hold XORs 0 and is reported as
+     * SQ_ERR_INVALID at the next synchronising call. */
+    SQ_OP_LOOKUP_XOR = 74,
+    /* TridiagParityPhase (hamiltonian_tridiagonal.cpp:88-105): amp = -amp
+     * where reg0 is odd. */
+    SQ_OP_PARITY_PHASE = 75
 } sq_opcode;
 
 /* One elementwise instruction. Register ids in reg[], integer constants in
@@ -226,6 +248,20 @@ int sq_state_device_arrays(sq_state* st, uint64_t** key_words, uint32_t* k, doub
 int sq_qram_create(uint32_t address_size, uint32_t data_size, const uint64_t* memory, uint64_t n_words,
                    sq_qram** out);
 int sq_qram_destroy(sq_qram* q);
+/* A classical function table for SQ_OP_LOOKUP_XOR: f(v) = dense[v] for
+ * v < dense_len, words[i] for v == keys[i] (keys ascending, unique, each >=
+ * dense_len). Released with sq_qram_destroy. */
+int sq_lookup_create(const uint64_t* dense, uint64_t dense_len, const uint64_t* keys, const uint64_t* words,
+                     uint64_t n_sparse, sq_qram** out);
+/* The quantised walk angles of GetQWRotateAngle_Int_Int_Int
+ * (SparQ_Algorithm/src/hamiltonian_simulation.cpp:257-291) for the element
+ * values v[i]: ratio = v / (2^ds - 1) (positive_only) or
+ * |sext(v)| / (2^(ds-1) - 1), clamped to [0, 1]; out[i] = the Rational
+ * fixed point of acos(sqrt(ratio)) / (2 pi) at out_width bits (truncated).
+ * Computed on the host with the C library's acos, so that the angles a
+ * lookup table gives on the GPU are the CPU's bit for bit. */
+int sq_qw_rotate_angle_words(const uint64_t* v, uint64_t n, uint32_t data_size, int positive_only,
+                             uint32_t out_width, uint64_t* out);
 
 /* ------------------------------------------------------------------ */
 /* Elementwise operators                                               */
@@ -382,6 +418,21 @@ int sq_partial_trace_select(sq_state* st, const uint32_t* regs, const uint64_t* 
 /* PartialTraceSelectRange (partial_trace.cpp:187-225): the same for
  * lo <= value(reg) <= hi. */
 int sq_partial_trace_select_range(sq_state* st, uint32_t reg, uint64_t lo, uint64_t hi, double* result);
+/* GetOutput (SparQ_Algorithm qda_fundamental.cpp:123-166, the QDA read-out):
+ * every entry whose registers zero_regs[] all hold 0 is placed in a dense
+ * vector of 2^(sum of the widths of idx_regs) amplitudes at the index formed
+ * by concatenating its idx_regs values, the first register in the lowest bits
+ * (main + anc_1 * 2^n + anc_4 * 2^(n+1) for the QDA layout,
+ * qda_fundamental.h:640-645); other slots are 0. *prob = those entries' total
+ * probability; the vector is scaled by 1/sqrt(*prob) unless
+ * |*prob - 1| < 1e-14 or *prob == 0. out (host memory) receives 2 doubles
+ * (re, im) per slot, out_len slots, which must equal the vector length. The
+ * zero and index registers together must cover every active register (so
+ * that no two entries share a slot) and the index widths sum to at most 30;
+ * otherwise SQ_ERR_INVALID. The state is unchanged. */
+#define SQ_MAX_OUTPUT_FIELDS 8
+int sq_get_output(sq_state* st, const uint32_t* zero_regs, uint32_t n_zero, const uint32_t* idx_regs,
+                  uint32_t n_idx, double* out, uint64_t out_len, double* prob);
 /* ClearZero (system_operations.cpp:371-382): drop entries with |a|^2 < eps;
  * order of survivors is preserved. */
 int sq_clear_zero(sq_state* st, double eps);

@@ -52,6 +52,9 @@ def lib():
             "sqo_normalize": (c_int, [c_void_p, POINTER(c_double)]),
             "sqo_partial_trace_select": (c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_int, c_uint64, c_uint64,
                                                  POINTER(c_double)]),
+            "sqo_get_output": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_void_p, c_uint64,
+                                       POINTER(c_double)]),
+            "sqo_qw_rotate_angle": (c_int, [c_void_p, c_uint32, c_uint32, c_uint32, c_int, POINTER(SqCond)]),
             "sqo_add_systems": (c_int, [c_void_p, c_void_p, c_double]),
             "sqo_add_register_sync": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_uint32)]),
             "sqo_remove_register_sync": (c_int, [c_void_p, c_uint32]),
@@ -217,6 +220,8 @@ def apply(state: OracleState, spec) -> None:
     elif kind == "hadamard_partial":
         pos = (c_uint32 * len(spec[2]))(*spec[2])
         _chk(L.sqo_hadamard_partial(h, spec[1], pos, len(spec[2]), byref(spec[3])))
+    elif kind == "qw_rotate_angle":
+        _chk(L.sqo_qw_rotate_angle(h, spec[1], spec[2], spec[3], 1 if spec[4] else 0, byref(spec[5])))
     elif kind == "clear_zero":
         _chk(L.sqo_clear_zero(h, spec[1]))
     elif kind == "normalize":
@@ -235,6 +240,19 @@ def apply(state: OracleState, spec) -> None:
         return out.value
     else:
         raise ValueError(kind)
+
+
+def get_output(state: "OracleState", zero_regs, idx_regs, width_of):
+    """GetOutput (qda_fundamental.cpp:123-166): (dense amplitude vector,
+    post-selected probability); width_of(reg) gives a register's width."""
+    z = np.array(zero_regs, dtype=np.uint32)
+    ix = np.array(idx_regs, dtype=np.uint32)
+    n = 1 << sum(width_of(r) for r in idx_regs)
+    out = np.zeros(2 * n, dtype=np.float64)
+    prob = c_double()
+    _chk(lib().sqo_get_output(state.h, z.ctypes.data_as(c_void_p), len(z), ix.ctypes.data_as(c_void_p), len(ix),
+                              out.ctypes.data_as(c_void_p), n, byref(prob)))
+    return out.view(np.complex128), prob.value
 
 
 def add_systems(dst: OracleState, src: OracleState, coef: float):

@@ -147,6 +147,56 @@ struct Qram {
     std::vector<uint64_t> memory;
 };
 
+// ---------------------------------------------------------------- tridiagonal CKS oracles
+// TridiagonalSpec (SparQ_Algorithm/include/hamiltonian_simulation_tridiagonal.h:
+// 104-190): row j's 4-slot window starts at clamp(j - 1, 0, n - 4); the
+// combined table word at idx & (8n - 1) is the quantised element of (row,
+// slot) in the first half and the window column in the second.
+static uint64_t tri_window_base(uint64_t j, uint64_t n) {
+    uint64_t b = (j > 0) ? (j - 1) : 0;
+    uint64_t bmax = n - 4;
+    return b < bmax ? b : bmax;
+}
+static uint64_t tri_value_of(uint64_t j, uint64_t s, uint64_t n, uint64_t alpha_enc, uint64_t beta_enc) {
+    uint64_t c = tri_window_base(j, n) + s;
+    if (c == j) return alpha_enc;
+    if (c + 1 == j || c == j + 1) return beta_enc;
+    return 0;
+}
+static uint64_t tri_combined_mem(uint64_t idx, uint64_t n, uint64_t alpha_enc, uint64_t beta_enc) {
+    idx &= 8 * n - 1;
+    uint64_t half = n * 4;
+    if (idx < half) return tri_value_of(idx >> 2, idx & 3, n, alpha_enc, beta_enc);
+    uint64_t t = idx - half;
+    return tri_window_base(t >> 2, n) + (t & 3);
+}
+
+// GetQWRotateAngle_Int_Int_Int (SparQ_Algorithm/src/hamiltonian_simulation.cpp:
+// 257-291): the Rational fixed point of acos(sqrt(ratio)) / pi / 2, XORed
+// into the output register; get_rational truncates (value * 2^size).
+static uint64_t qw_rational(double x, size_t size) { return (uint64_t)(x * (double)pow2(size)); }
+static void qw_rotate_angle(State& st, uint32_t data, uint32_t out, uint32_t data_size, bool positive_only,
+                            const sq_cond* cond) {
+    for (auto& s : st) {
+        if (!condition_satisfied(s, cond)) continue;
+        uint64_t v = get_as(s, data);
+        double ratio;
+        if (positive_only) {
+            uint64_t amax = pow2(data_size) - 1;
+            v = v % (amax + 1);
+            ratio = v * 1.0 / amax;
+        } else {
+            uint64_t amax = pow2(data_size - 1) - 1;
+            v = v % pow2(data_size);
+            int64_t vr = get_complement(v, data_size);
+            ratio = std::abs(vr) * 1.0 / amax;
+        }
+        ratio = std::max(0.0, std::min(1.0, ratio));
+        double a = std::acos(std::sqrt(ratio)) / M_PI / 2;
+        s.get(out) ^= qw_rational(a, size_of(out));
+    }
+}
+
 // ---------------------------------------------------------------- elementwise
 static void apply_instr_entry(System& s, const sq_instr& in) {
     const uint32_t* r = in.reg;
@@ -424,6 +474,38 @@ static void apply_instr_entry(System& s, const sq_instr& in) {
             v ^= pow2(in.imm[0]);
             return;
         }
+        case SQ_OP_TRIDIAG_ELEMENT: {  // TridiagOracle1, hamiltonian_tridiagonal.cpp:16-33
+            uint64_t off = get_as(s, r[0]), j = get_as(s, r[1]), slot = get_as(s, r[2]);
+            s.get(r[3]) ^= tri_combined_mem(off + 4 * j + slot, in.imm[0], in.imm[1] & 0xffffffffull,
+                                            in.imm[1] >> 32);
+            return;
+        }
+        case SQ_OP_TRIDIAG_SLOT_COLUMN: {  // TridiagOracle2, hamiltonian_tridiagonal.cpp:35-83
+            const uint64_t n = in.imm[0], ae = in.imm[1] & 0xffffffffull, be = in.imm[1] >> 32;
+            const uint64_t kmask = in.imm[2] >= 64 ? ~uint64_t{0} : pow2(in.imm[2]) - 1;
+            uint64_t j = get_as(s, r[1]), off = get_as(s, r[0]), k = get_as(s, r[2]);
+            uint64_t sr = get_as(s, r[3]) & kmask;  // the tag register, read at k_width bits
+            uint64_t base = tri_window_base(j, n);
+            uint64_t row_addr = off + 4 * j;
+            if (!in.dag) {
+                bool hit = k >= base && k < base + 4;
+                uint64_t sr1 = sr ^ (hit ? row_addr + (k - base) : 0);
+                uint64_t k1 = k ^ tri_combined_mem(sr1, n, ae, be);
+                s.get(r[2]) = (sr1 - row_addr) & kmask;
+                s.get(r[3]) = k1 & kmask;
+            } else {
+                uint64_t k1 = (k + row_addr) & kmask;
+                uint64_t k2 = sr ^ tri_combined_mem(k1, n, ae, be);
+                bool hit = k2 >= base && k2 < base + 4;
+                s.get(r[2]) = k2;
+                s.get(r[3]) = k1 ^ (hit ? row_addr + (k2 - base) : 0);
+            }
+            return;
+        }
+        case SQ_OP_PARITY_PHASE: {  // TridiagParityPhase, hamiltonian_tridiagonal.cpp:88-105
+            if (get_as(s, r[0]) & 1) s.amplitude = -s.amplitude;
+            return;
+        }
         case SQ_OP_PAULI_NOISE: {  // per-trajectory X then Z masks (batched trajectories)
             const Qram* q = reinterpret_cast<const Qram*>(in.qram);
             uint64_t t = get_as(s, r[0]);
@@ -519,6 +601,42 @@ static double partial_trace_select(State& st, const std::vector<uint32_t>& regs,
         return sum_prob;
     }
     return std::numeric_limits<double>::infinity();
+}
+
+// ---------------------------------------------------------------- GetOutput
+// GetOutput::operator() (SparQ_Algorithm qda_fundamental.cpp:123-166): the
+// entries whose post-selected registers all hold 0 are written, in state
+// order, to a dense vector at the concatenation of their index registers (the
+// first in the lowest bits, qda_fundamental.h:640-645); sum = their total
+// probability; the vector is scaled by 1/sqrt(sum) unless |sum - 1| < epsilon
+// (a sum of 0 scales by 1).
+static double get_output(const State& st, const std::vector<uint32_t>& zero, const std::vector<uint32_t>& idx,
+                         std::vector<complex_t>& out) {
+    size_t bits = 0;
+    for (uint32_t r : idx) bits += size_of(r);
+    out.assign(pow2(bits), complex_t(0, 0));
+    double sum = 0.0;
+    for (const auto& s : st) {
+        bool is_zero = true;
+        for (uint32_t r : zero)
+            if (get_as(s, r) != 0) {
+                is_zero = false;
+                break;
+            }
+        if (!is_zero) continue;
+        uint64_t id = 0;
+        size_t off = 0;
+        for (uint32_t r : idx) {
+            id |= get_as(s, r) << off;
+            off += size_of(r);
+        }
+        out[id] = s.amplitude;
+        sum += abs_sqr(s.amplitude);
+    }
+    if (std::abs(sum - 1.0) < kEpsilon) return sum;
+    const double k = sum != 0 ? 1.0 / std::sqrt(sum) : 1.0;
+    for (auto& v : out) v *= k;
+    return sum;
 }
 
 // ---------------------------------------------------------------- Hadamard_Int
@@ -1163,6 +1281,23 @@ int sqo_partial_trace_select(void* h, const uint32_t* regs, const uint64_t* valu
         if (values) v.assign(values, values + n);
         *result = partial_trace_select(*static_cast<State*>(h), r, v, range != 0, lo, hi);
     })
+}
+int sqo_get_output(void* h, const uint32_t* zero, uint32_t n_zero, const uint32_t* idx, uint32_t n_idx,
+                   double* out, uint64_t out_len, double* prob) {
+    SQO_TRY({
+        std::vector<complex_t> v;
+        *prob = get_output(*static_cast<State*>(h), std::vector<uint32_t>(zero, zero + n_zero),
+                           std::vector<uint32_t>(idx, idx + n_idx), v);
+        if (v.size() != out_len) throw std::invalid_argument("out_len");
+        for (size_t i = 0; i < v.size(); ++i) {
+            out[2 * i] = v[i].real();
+            out[2 * i + 1] = v[i].imag();
+        }
+    })
+}
+int sqo_qw_rotate_angle(void* h, uint32_t data, uint32_t out, uint32_t data_size, int positive_only,
+                        const sq_cond* cond) {
+    SQO_TRY(qw_rotate_angle(*static_cast<State*>(h), data, out, data_size, positive_only != 0, cond))
 }
 int sqo_normalize(void* h, double* norm_sq) {
     SQO_TRY({ double s = normalize(*static_cast<State*>(h)); if (norm_sq) *norm_sq = s; })

@@ -27,6 +27,7 @@ from .operators import (Abs_SInt, Add_AnyInt_AnyInt_InPlace, Add_ConstUInt_InPla
                         RemoveRegister, Rot_Bool, RX_Bool, RY_Bool, S_Bool, Select_Bool_UInt_UInt,
                         SelfAdjointOperator, ShiftLeft_InPlace, ShiftRight_InPlace, SplitRegister,
                         Sqrt_UInt, Sub_UInt_UInt, Swap_Bool_Bool, Swap_General_General, T_Bool, X_Bool,
-                        Xor_UInt_UInt, Y_Bool, Z_Bool, ZeroConditionalPhaseFlip, add_systems, synchronize)
+                        Xor_UInt_UInt, Y_Bool, Z_Bool, ZeroConditionalPhaseFlip, add_systems, get_output,
+                        synchronize)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

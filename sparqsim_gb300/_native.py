@@ -34,7 +34,7 @@ OP = dict(
     ADD_ANYINT_INPLACE=28, ASSIGN=29, COMPARE_UINT_UINT=30, LESS_UINT_UINT=31, SWAP_GENERAL=32,
     GETMID_UINT_UINT=33, X_BOOL=34, INIT_UNSAFE=35, QRAM_LOAD=36, PLUS_ONE_OVERFLOW=37, PHASE_BOOL=64, GLOBAL_PHASE=65,
     Y_BOOL=66, REFLECTION_BOOL=67, ZERO_COND_PHASE_FLIP=68, ROT_DIAGONAL=69, ROT_OFF_DIAGONAL=70,
-    PAULI_NOISE=71,
+    PAULI_NOISE=71, TRIDIAG_ELEMENT=72, TRIDIAG_SLOT_COLUMN=73, LOOKUP_XOR=74, PARITY_PHASE=75,
 )
 
 
@@ -106,6 +106,8 @@ _SIGS = [
     ("sq_state_device_arrays", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_uint32), POINTER(c_void_p)]),
     ("sq_qram_create", c_int, [c_uint32, c_uint32, c_void_p, c_uint64, POINTER(c_void_p)]),
     ("sq_qram_destroy", c_int, [c_void_p]),
+    ("sq_lookup_create", c_int, [c_void_p, c_uint64, c_void_p, c_void_p, c_uint64, POINTER(c_void_p)]),
+    ("sq_qw_rotate_angle_words", c_int, [c_void_p, c_uint64, c_uint32, c_int, c_uint32, c_void_p]),
     ("sq_apply_program", c_int, [c_void_p, POINTER(SqInstr), c_uint32]),
     ("sq_add_uint_uint", c_int, [c_void_p, c_uint32, c_uint32, c_uint32, POINTER(SqCond)]),
     ("sq_add_uint_uint_inplace", c_int, [c_void_p, c_uint32, c_uint32, POINTER(SqCond), c_int]),
@@ -140,6 +142,8 @@ _SIGS = [
     ("sq_set_output_sizing", c_int, [c_int]),
     ("sq_partial_trace_select", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, POINTER(c_double)]),
     ("sq_partial_trace_select_range", c_int, [c_void_p, c_uint32, c_uint64, c_uint64, POINTER(c_double)]),
+    ("sq_get_output", c_int, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_void_p, c_uint64,
+                              POINTER(c_double)]),
     ("sq_autotune_reset", c_int, []),
     ("sq_autotune_classes", c_int, [POINTER(c_uint64), POINTER(c_uint64)]),
     ("sq_get_output_sizing", c_int, [POINTER(c_int)]),

@@ -3,6 +3,7 @@
 // register ids into packed fields and forwards to the device pipelines.
 // Exceptions never cross the boundary: every entry returns an sq_status and
 // records a message for sq_last_error().
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -421,6 +422,75 @@ int sq_qram_destroy(sq_qram* q) {
     SQ_API_END
 }
 
+int sq_lookup_create(const uint64_t* dense, uint64_t dense_len, const uint64_t* keys, const uint64_t* words,
+                     uint64_t n_sparse, sq_qram** out) {
+    SQ_API_BEGIN
+    need(out != nullptr, "null pointer");
+    need(dense_len == 0 || dense != nullptr, "null pointer");
+    need(n_sparse == 0 || (keys != nullptr && words != nullptr), "null pointer");
+    need(dense_len + n_sparse > 0, "lookup: empty table");
+    for (uint64_t i = 0; i < n_sparse; ++i) {
+        need(keys[i] >= dense_len, "lookup: a sparse key inside the dense range");
+        need(i == 0 || keys[i] > keys[i - 1], "lookup: sparse keys must ascend");
+    }
+    const uint64_t total = dense_len + 2 * n_sparse;
+    std::vector<uint64_t> h(total);
+    uint64_t all = 0;
+    for (uint64_t i = 0; i < dense_len; ++i) {
+        h[i] = dense[i];
+        all |= dense[i];
+    }
+    for (uint64_t i = 0; i < n_sparse; ++i) {
+        h[dense_len + i] = keys[i];
+        h[dense_len + n_sparse + i] = words[i];
+        all |= words[i];
+    }
+    sq_qram* q = new sq_qram();
+    q->t.lookup = true;
+    q->t.dense_len = dense_len;
+    q->t.n_sparse = n_sparse;
+    q->t.n_words = total;
+    q->t.elem_bytes = 8;
+    q->t.max_word = all;
+    try {
+        q->t.dev = dev_alloc(total * 8);
+        SQ_CUDA(cudaMemcpyAsync(q->t.dev, h.data(), total * 8, cudaMemcpyHostToDevice, stream()));
+        SQ_CUDA(cudaStreamSynchronize(stream()));  // the host copy goes out of scope
+    } catch (...) {
+        if (q->t.dev) dev_free(q->t.dev);
+        delete q;
+        throw;
+    }
+    *out = q;
+    SQ_API_END
+}
+
+int sq_qw_rotate_angle_words(const uint64_t* v, uint64_t n, uint32_t data_size, int positive_only,
+                             uint32_t out_width, uint64_t* out) {
+    SQ_API_BEGIN
+    need(n == 0 || (v != nullptr && out != nullptr), "null pointer");
+    need(data_size >= 2 && data_size <= 64, "GetQWRotateAngle: data_size out of range");
+    need(out_width >= 1 && out_width <= 63, "GetQWRotateAngle: output width out of range");
+    for (uint64_t i = 0; i < n; ++i) {
+        double ratio;
+        if (positive_only) {
+            const uint64_t amax = (data_size >= 64 ? ~0ull : (1ull << data_size)) - 1;
+            const uint64_t x = data_size >= 64 ? v[i] : v[i] % (amax + 1);
+            ratio = x * 1.0 / amax;
+        } else {
+            const uint64_t amax = (1ull << (data_size - 1)) - 1;
+            const uint64_t x = data_size >= 64 ? v[i] : v[i] % (1ull << data_size);
+            const int64_t s = data_size >= 64 ? (int64_t)x
+                                              : (int64_t)((x ^ (1ull << (data_size - 1))) - (1ull << (data_size - 1)));
+            ratio = std::fabs((double)s) * 1.0 / amax;
+        }
+        ratio = std::max(0.0, std::min(1.0, ratio));
+        const double a = std::acos(std::sqrt(ratio)) / M_PI / 2;
+        out[i] = (uint64_t)(a * (double)(1ull << out_width));
+    }
+    SQ_API_END
+}
+
 // ------------------------------------------------------------------ elementwise
 int sq_apply_program(sq_state* st, const sq_instr* prog, uint32_t n) {
     SQ_API_BEGIN
@@ -428,7 +498,8 @@ int sq_apply_program(sq_state* st, const sq_instr* prog, uint32_t n) {
     std::vector<sq_instr> p(prog, prog + n);
     for (auto& in : p) {
         // the ABI carries the opaque sq_qram*; the kernel wants its table record
-        if (in.op == SQ_OP_QRAM_LOAD && in.qram) in.qram = reinterpret_cast<const sq_qram*>(&in.qram->t);
+        if ((in.op == SQ_OP_QRAM_LOAD || in.op == SQ_OP_LOOKUP_XOR) && in.qram)
+            in.qram = reinterpret_cast<const sq_qram*>(&in.qram->t);
     }
     run_program(S(st), p.data(), n);
     SQ_API_END
@@ -862,6 +933,43 @@ int sq_partial_trace_select_range(sq_state* st, uint32_t reg, uint64_t lo, uint6
     DCondSet none;
     memset(&none, 0, sizeof(none));
     *result = select_entries(S(st), none, f, lo, hi);
+    SQ_API_END
+}
+
+int sq_get_output(sq_state* st, const uint32_t* zero_regs, uint32_t n_zero, const uint32_t* idx_regs,
+                  uint32_t n_idx, double* out, uint64_t out_len, double* prob) {
+    SQ_API_BEGIN
+    need(prob != nullptr && out != nullptr, "null pointer");
+    need(n_zero <= SQ_MAX_CONDITIONS, "GetOutput: at most SQ_MAX_CONDITIONS post-selected registers");
+    need(n_idx >= 1 && n_idx <= SQ_MAX_OUTPUT_FIELDS, "GetOutput: 1 to SQ_MAX_OUTPUT_FIELDS index registers");
+    need(n_zero == 0 || zero_regs != nullptr, "null pointer");
+    need(idx_regs != nullptr, "null pointer");
+    const RegTable& rt = regtable();
+    Field f[SQ_MAX_OUTPUT_FIELDS];
+    uint32_t bits = 0;
+    std::vector<uint32_t> used;
+    for (uint32_t j = 0; j < n_idx; ++j) {
+        f[j] = rt.field(idx_regs[j]);
+        bits += f[j].width;
+        used.push_back(idx_regs[j]);
+    }
+    need(bits <= 30, "GetOutput: the index registers exceed 30 bits");
+    need(out_len == (1ull << bits), "GetOutput: out_len must be 2^(sum of index widths)");
+    sq_cond c;
+    memset(&c, 0, sizeof(c));
+    c.count = n_zero;
+    for (uint32_t i = 0; i < n_zero; ++i) {
+        c.c[i].kind = SQ_COND_VALUE;
+        c.c[i].reg = zero_regs[i];
+        c.c[i].param = 0;
+        used.push_back(zero_regs[i]);
+    }
+    for (uint32_t r = 0; r < rt.regs.size(); ++r) {
+        if (!rt.regs[r].active || rt.regs[r].width == 0) continue;
+        need(std::find(used.begin(), used.end(), r) != used.end(),
+             "GetOutput: every active register must be post-selected or indexed");
+    }
+    *prob = get_output(S(st), resolve_cond(&c), f, n_idx, out);
     SQ_API_END
 }
 

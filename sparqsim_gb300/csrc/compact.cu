@@ -145,6 +145,7 @@ void check_device_error() {
     SQ_CUDA(cudaStreamSynchronize(stream()));
     if (v) {
         SQ_CUDA(cudaMemsetAsync(device_error_word(), 0, 4, stream()));
+        if (v & 8u) fail(SQ_ERR_INVALID, "lookup: a register value has no entry in the table");
         if (v & 4u) fail(SQ_ERR_INVALID, "batched Hadamard: an entry's digit count exceeds max_digits");
         if (v & 2u) fail(SQ_ERR_DEVICE_TIMEOUT, "hash grouping gave up (table full or a bounded wait expired)");
         fail(SQ_ERR_DEVICE_TIMEOUT, "a bounded device-side wait gave up (decoupled look-back)");
@@ -217,6 +218,118 @@ double select_entries(State& s, const DCondSet& sel, Field rf, uint64_t lo, uint
     return f;
 }
 
+// ------------------------------------------------------------------ GetOutput
+constexpr int kRedBlock = 256;
+__global__ void __launch_bounds__(kRedBlock) norm_final_kernel(const double* __restrict__ partial, int m,
+                                                               double* __restrict__ out);
+__global__ void scale_kernel(double2* __restrict__ a, uint64_t n, double k);
+
+// The dense index of a selected entry: its index fields concatenated, the
+// first field in the lowest bits.
+struct OutIndex {
+    uint32_t n;
+    uint32_t off[SQ_MAX_OUTPUT_FIELDS];
+    Field f[SQ_MAX_OUTPUT_FIELDS];
+};
+
+// Scatter + partial probability sums in one pass. Dense indices are distinct
+// because the selected registers and the index fields together cover every
+// active register (checked on the host) and keys are unique.
+template <int K>
+__global__ void __launch_bounds__(kRedBlock) get_output_kernel(ConstKeyPtrs ik, const double2* __restrict__ ia,
+                                                               uint64_t n, const __grid_constant__ DCondSet sel,
+                                                               const __grid_constant__ OutIndex ix,
+                                                               double2* __restrict__ out,
+                                                               double* __restrict__ partial) {
+    __shared__ double s[kRedBlock];
+    double acc = 0.0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint64_t k[K];
+#pragma unroll
+        for (int w = 0; w < K; ++w) k[w] = ik.w[w][i];
+        if (!cond_ok<K>(k, sel)) continue;
+        uint64_t id = 0;
+        for (uint32_t j = 0; j < ix.n; ++j) id |= fget<K>(k, ix.f[j]) << ix.off[j];
+        const double2 v = ia[i];
+        out[id] = v;
+        acc += v.x * v.x + v.y * v.y;
+    }
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = kRedBlock / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
+}
+
+template <int K>
+static void launch_get_output(const State& s, const DCondSet& sel, const OutIndex& ix, double2* out,
+                              double* part, int g) {
+    ConstKeyPtrs ik;
+    for (int w = 0; w < SQ_KMAX; ++w) ik.w[w] = s.live.keys[w];
+    get_output_kernel<K><<<g, kRedBlock, 0, stream()>>>(ik, s.live.amp, s.n, sel, ix, out, part);
+}
+
+// GetOutput (qda_fundamental.cpp:123-166): the entries whose `sel` registers
+// all hold 0 are placed in a dense vector of 2^(sum of index widths)
+// amplitudes, at the concatenation of their index fields (main + anc_1 * 2^n +
+// anc_4 * 2^(n+1) for the QDA read-out, qda_fundamental.h:640-645); every other
+// slot is 0. p = the placed entries' total probability; the vector is scaled
+// by 1/sqrt(p) unless |p - 1| < 1e-14 (the reference's epsilon) or p == 0.
+// The state is left as it is. Returns p; the vector is copied into `host_out`
+// (2 doubles per slot).
+double get_output(State& s, const DCondSet& sel, const Field* fields, uint32_t nf, double* host_out) {
+    sync_words(s);
+    OutIndex ix;
+    memset(&ix, 0, sizeof(ix));
+    ix.n = nf;
+    uint32_t bits = 0;
+    for (uint32_t j = 0; j < nf; ++j) {
+        ix.f[j] = fields[j];
+        ix.off[j] = bits;
+        bits += fields[j].width;
+    }
+    const uint64_t len = 1ull << bits;
+    double2* out = (double2*)ws().get(WS_OUTPUT, len * 16);
+    SQ_CUDA(cudaMemsetAsync(out, 0, len * 16, stream()));
+    const int g = num_sms() * 4;
+    double* part = (double*)ws().get(WS_REDUCE, (size_t)(g + 1) * 8);
+    if (s.n == 0) {
+        SQ_CUDA(cudaMemsetAsync(part + g, 0, 8, stream()));
+    } else {
+        const uint32_t k = regtable().k;
+        prof_begin("get_output");
+        switch (k) {
+            case 1: launch_get_output<1>(s, sel, ix, out, part, g); break;
+            case 2: launch_get_output<2>(s, sel, ix, out, part, g); break;
+            case 3: launch_get_output<3>(s, sel, ix, out, part, g); break;
+            case 4: launch_get_output<4>(s, sel, ix, out, part, g); break;
+            case 5: launch_get_output<5>(s, sel, ix, out, part, g); break;
+            case 6: launch_get_output<6>(s, sel, ix, out, part, g); break;
+            case 7: launch_get_output<7>(s, sel, ix, out, part, g); break;
+            default: launch_get_output<8>(s, sel, ix, out, part, g); break;
+        }
+        prof_end((double)s.n * (8.0 * k + 16));
+        SQ_CUDA(cudaGetLastError());
+        norm_final_kernel<<<1, kRedBlock, 0, stream()>>>(part, g, part + g);
+        SQ_CUDA(cudaGetLastError());
+    }
+    double p = 0.0;
+    SQ_CUDA(cudaMemcpyAsync(&p, part + g, 8, cudaMemcpyDeviceToHost, stream()));
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    if (!(std::fabs(p - 1.0) < 1e-14) && p != 0.0) {
+        prof_begin("scale");
+        scale_kernel<<<grid_for(len, 256), 256, 0, stream()>>>(out, len, 1.0 / std::sqrt(p));
+        prof_end((double)len * 32);
+        SQ_CUDA(cudaGetLastError());
+    }
+    SQ_CUDA(cudaMemcpyAsync(host_out, out, len * 16, cudaMemcpyDeviceToHost, stream()));
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    return p;
+}
+
 void clear_zero(State& s, double eps) {
     drop_groups(s);
     sync_words(s);
@@ -229,7 +342,6 @@ void clear_zero(State& s, double eps) {
 }
 
 // ------------------------------------------------------------------ norm
-constexpr int kRedBlock = 256;
 
 __global__ void __launch_bounds__(kRedBlock) norm_partial_kernel(const double2* __restrict__ a, uint64_t n,
                                                                  double* __restrict__ partial) {

@@ -33,6 +33,7 @@ struct DInstr {
 
 template <int MAXI>
 struct ProgramArgs {
+    unsigned* err;         // device error word (bit 3: a lookup value without a table entry)
     uint32_t n;
     uint32_t read_words;   // bit w: word w is read
     uint32_t write_words;  // bit w: word w is written
@@ -70,8 +71,29 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 __device__ __forceinline__ uint64_t shl(uint64_t v, unsigned s) { return s >= 64 ? 0 : v << s; }
 __device__ __forceinline__ uint64_t shr(uint64_t v, unsigned s) { return s >= 64 ? 0 : v >> s; }
 
+// The combined [elements | column indices] table of a constant-diagonal
+// tridiagonal matrix with 4-slot row windows, computed instead of stored
+// (hamiltonian_simulation_tridiagonal.h:104-190): row j's window starts at
+// clamp(j - 1, 0, n - 4); enc = alpha_enc | beta_enc << 32.
+__device__ __forceinline__ uint64_t tri_window_base(uint64_t j, uint64_t n) {
+    const uint64_t b = j > 0 ? j - 1 : 0, bmax = n - 4;
+    return b < bmax ? b : bmax;
+}
+__device__ __forceinline__ uint64_t tri_mem(uint64_t idx, uint64_t n, uint64_t enc) {
+    idx &= 8 * n - 1;
+    const uint64_t half = 4 * n;
+    if (idx < half) {
+        const uint64_t j = idx >> 2, c = tri_window_base(j, n) + (idx & 3);
+        if (c == j) return enc & 0xffffffffull;
+        if (c + 1 == j || c == j + 1) return enc >> 32;
+        return 0;
+    }
+    const uint64_t t = idx - half;
+    return tri_window_base(t >> 2, n) + (t & 3);
+}
+
 template <int K>
-__device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2& a) {
+__device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2& a, unsigned* err) {
     const Field* f = in.f;
     switch (in.op) {
         case SQ_OP_FLIP_BOOLS: fset<K>(k, f[0], ~fget<K>(k, f[0])); break;
@@ -226,6 +248,53 @@ __device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2
             fset<K>(k, f[1], fget<K>(k, f[1]) ^ word);
             break;
         }
+        case SQ_OP_TRIDIAG_ELEMENT: {
+            const uint64_t idx = fget<K>(k, f[0]) + 4 * fget<K>(k, f[1]) + fget<K>(k, f[2]);
+            fset<K>(k, f[3], fget<K>(k, f[3]) ^ tri_mem(idx, in.imm[0], in.imm[1]));
+            break;
+        }
+        case SQ_OP_TRIDIAG_SLOT_COLUMN: {
+            const uint64_t n = in.imm[0], kmask = wmask((unsigned)in.imm[2]);
+            const uint64_t j = fget<K>(k, f[1]), kv = fget<K>(k, f[2]), sr = fget<K>(k, f[3]) & kmask;
+            const uint64_t base = tri_window_base(j, n), row = fget<K>(k, f[0]) + 4 * j;
+            if (!in.dag) {  // column -> slot; out-of-window branches tagged into the tag register
+                const bool hit = kv >= base && kv < base + 4;
+                const uint64_t sr1 = sr ^ (hit ? row + (kv - base) : 0ull);
+                const uint64_t k1 = kv ^ tri_mem(sr1, n, in.imm[1]);
+                fset<K>(k, f[2], (sr1 - row) & kmask);
+                fset<K>(k, f[3], k1 & kmask);
+            } else {  // slot -> column
+                const uint64_t k1 = (kv + row) & kmask;
+                const uint64_t k2 = sr ^ tri_mem(k1, n, in.imm[1]);
+                const bool hit = k2 >= base && k2 < base + 4;
+                fset<K>(k, f[2], k2);
+                fset<K>(k, f[3], k1 ^ (hit ? row + (k2 - base) : 0ull));
+            }
+            break;
+        }
+        case SQ_OP_LOOKUP_XOR: {
+            const uint64_t v = fget<K>(k, f[0]);
+            const uint64_t* t = static_cast<const uint64_t*>(in.table);
+            const uint64_t nd = in.imm[0], ns = in.imm[1];
+            uint64_t w = 0;
+            if (v < nd) {
+                w = __ldg(t + v);
+            } else {
+                uint64_t lo = 0, hi = ns;
+                while (lo < hi) {
+                    const uint64_t mid = (lo + hi) >> 1;
+                    if (__ldg(t + nd + mid) < v) lo = mid + 1;
+                    else hi = mid;
+                }
+                if (lo < ns && __ldg(t + nd + lo) == v) w = __ldg(t + nd + ns + lo);
+                else atomicOr(err, 8u);
+            }
+            fset<K>(k, f[1], fget<K>(k, f[1]) ^ w);
+            break;
+        }
+        case SQ_OP_PARITY_PHASE:
+            if (fget<K>(k, f[0]) & 1ull) a = make_double2(-a.x, -a.y);
+            break;
         case SQ_OP_PHASE_BOOL:
             if ((fget<K>(k, f[0]) >> in.imm[0]) & 1ull) a = cmul(a, in.c[0]);
             break;
@@ -292,7 +361,7 @@ __global__ void __launch_bounds__(256) program_kernel(const __grid_constant__ Pr
         for (uint32_t j = 0; j < p.n; ++j) {
             const DInstr& in = p.ins[j];
             if (!cond_ok<K>(k, in.cond)) continue;
-            exec<K>(in, k, a);
+            exec<K>(in, k, a, p.err);
         }
 #pragma unroll
         for (int w = 0; w < K; ++w)
@@ -481,6 +550,33 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
             if (in.imm[0] >= d.f[0].width) fail(SQ_ERR_INVALID, "Rot_Bool: digit >= register size");
             am |= 3u;
             break;
+        case SQ_OP_TRIDIAG_ELEMENT:
+        case SQ_OP_TRIDIAG_SLOT_COLUMN: {
+            const bool el = in.op == SQ_OP_TRIDIAG_ELEMENT;
+            const char* what = el ? "TridiagOracle1" : "TridiagOracle2";
+            R(0); R(1);
+            if (el) { R(2); W(3); } else { W(2); W(3); }
+            for (int x = 0; x < 3; ++x)
+                for (int y = x + 1; y < 4; ++y)
+                    if (el ? y == 3 : y >= 2) distinct(in.reg[x], in.reg[y], what);
+            const uint64_t n = in.imm[0];
+            if (n < 8 || (n & (n - 1))) fail(SQ_ERR_INVALID, std::string(what) + ": n must be a power of two >= 8");
+            if (!el && (in.imm[2] == 0 || in.imm[2] > 64)) fail(SQ_ERR_INVALID, "TridiagOracle2: k_width out of range");
+            break;
+        }
+        case SQ_OP_LOOKUP_XOR: {
+            R(0); W(1);
+            distinct(in.reg[0], in.reg[1], "lookup");
+            const QramTable* q = reinterpret_cast<const QramTable*>(in.qram);
+            if (!q || !q->dev || !q->lookup) fail(SQ_ERR_INVALID, "lookup: not a table of sq_lookup_create");
+            if (d.f[1].width < 64 && q->max_word > wmask(d.f[1].width))
+                fail(SQ_ERR_INVALID, "lookup: table word wider than the output register");
+            d.table = q->dev;
+            d.imm[0] = q->dense_len;
+            d.imm[1] = q->n_sparse;
+            break;
+        }
+        case SQ_OP_PARITY_PHASE: R(0); am |= 3u; break;
         case SQ_OP_PAULI_NOISE: {
             R(0); W(1); W(2); W(3);
             const QramTable* q = reinterpret_cast<const QramTable*>(in.qram);
@@ -511,6 +607,7 @@ void run_program(State& s, const sq_instr* prog, uint32_t n) {
         ProgramArgs<4> a;
         memset(&a, 0, sizeof(a));
         for (uint32_t i = 0; i < n; ++i) translate(prog[i], a.ins[i], rw, ww, am);
+        a.err = device_error_word();
         a.n = n;
         a.read_words = rw;
         a.write_words = ww;
@@ -526,6 +623,7 @@ void run_program(State& s, const sq_instr* prog, uint32_t n) {
             delete a;
             throw;
         }
+        a->err = device_error_word();
         a->n = n;
         a->read_words = rw;
         a->write_words = ww;

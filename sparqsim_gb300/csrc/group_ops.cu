@@ -890,6 +890,183 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
     }
 }
 
+// Hadamard_Int, Hadamard_Int_Full and Rot_GeneralUnitary on targets of 1 to 3
+// bits: one thread per group, the group's 2^NB slots in registers. The
+// arithmetic and its order are those of emit_hadamard_kernel, so the results
+// are bit-identical; what changes is that millions of small groups no longer
+// run one after another on a warp (a chain of dependent loads per group, with
+// most lanes idle), and that in the single-pass mode the lanes of a warp
+// reserve their outputs with one atomic, in lane order.
+template <int K, int NB, bool WRITE, int AM, bool UNI>
+__global__ void __launch_bounds__(256) emit_small_kernel(const __grid_constant__ EmitArgs a) {
+    constexpr unsigned S = 1u << NB;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint64_t gb = (uint64_t)blockIdx.x * blockDim.x; gb < a.groups; gb += stride) {  // warp-uniform trips
+        const uint64_t g = gb + threadIdx.x;
+        const bool valid = g < a.groups;
+        double2 v[S];
+        uint64_t gk[K];
+        unsigned keepm = 0;  // bit c: output slot c survives the prune
+        bool single = false;
+        uint64_t v0 = 0;
+        double2 base = make_double2(0.0, 0.0);
+        unsigned s0 = 0, m = 0;
+        if (valid) group_range<AM>(a, g, s0, m);
+        if (m) {
+            load_key<K>(a.in_keys, group_head<AM>(a, g, s0), gk);
+            if (!UNI && a.mode == GM_HADAMARD_INT && m == 1) {
+                // singleton: a * 2^{-n/2}, sign (-1)^{popcount(t & v)} (hadamard.cpp:27-42)
+                double2 a0;
+                member_at<AM>(a, s0, v0, a0);
+                base = cscale(a0, a.extra);
+                single = true;
+                keepm = keep_amp(base, a.eps) ? (1u << S) - 1u : 0u;
+            } else if (!UNI && a.mode == GM_HADAMARD_FULL && m <= (unsigned)(NB - 1)) {
+                // Hadamard_Int_Full sparse bucket (hadamard.cpp:267-304): at most two
+                // members, summed in ascending target value
+                uint64_t t0 = 0, t1 = 0;
+                double2 a0 = make_double2(0.0, 0.0), a1 = make_double2(0.0, 0.0);
+                member_at<AM>(a, s0, t0, a0);
+                if (m == 2) {
+                    member_at<AM>(a, s0 + 1, t1, a1);
+                    if (t1 < t0) {
+                        const uint64_t tt = t0;
+                        t0 = t1;
+                        t1 = tt;
+                        const double2 ta = a0;
+                        a0 = a1;
+                        a1 = ta;
+                    }
+                }
+#pragma unroll
+                for (unsigned c = 0; c < S; ++c) {
+                    double2 acc = make_double2(0.0, 0.0);
+                    double2 term = cscale(a0, (__popcll((uint64_t)c & t0) & 1) ? -1. : 1.);
+                    acc = cadd(acc, cscale(term, a.extra));
+                    if (m == 2) {
+                        term = cscale(a1, (__popcll((uint64_t)c & t1) & 1) ? -1. : 1.);
+                        acc = cadd(acc, cscale(term, a.extra));
+                    }
+                    v[c] = acc;
+                }
+            } else {
+                // zero-filled slots, members scattered, then the FWHT or the unitary
+#pragma unroll
+                for (unsigned c = 0; c < S; ++c) v[c] = make_double2(0.0, 0.0);
+                int emax = 1;
+#pragma unroll
+                for (unsigned j = 0; j < S; ++j) {
+                    if (j < m) {
+                        uint64_t tj;
+                        double2 aj;
+                        member_at<AM>(a, s0 + j, tj, aj);
+#pragma unroll
+                        for (unsigned c = 0; c < S; ++c)
+                            if (c == (unsigned)(tj & (S - 1u))) v[c] = aj;
+                        emax = max(emax, amp_exp(aj));
+                    }
+                }
+                if (UNI) {
+                    // Rot_GeneralUnitary (rot.cpp:353-389): out[i] = sum_j M(i,j) * amp[j], j ascending
+                    double2 r[S];
+#pragma unroll
+                    for (unsigned c = 0; c < S; ++c) {
+                        double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
+                        for (unsigned j = 0; j < S; ++j) {
+                            const double2 mij = a.udag ? make_double2(a.umat[j * S + c].x, -a.umat[j * S + c].y)
+                                                       : a.umat[c * S + j];
+                            acc = cadd(acc, cmul2(mij, v[j]));
+                        }
+                        r[c] = acc;
+                    }
+#pragma unroll
+                    for (unsigned c = 0; c < S; ++c) v[c] = r[c];
+                } else if (a.fix) {
+                    // exact-sum arithmetic: integer grid, NB exact stages, one rounding
+                    longlong2 ls[S];
+#pragma unroll
+                    for (unsigned c = 0; c < S; ++c) ls[c] = to_fixed2(v[c], emax, 62 - NB);
+#pragma unroll
+                    for (int qn = 0; qn < NB; ++qn) {
+                        const unsigned h = 1u << qn;
+#pragma unroll
+                        for (unsigned p = 0; p < S / 2; ++p) {
+                            const unsigned i0 = ((p >> qn) << (qn + 1)) | (p & (h - 1u));
+                            const unsigned i1 = i0 + h;
+                            const longlong2 x0 = ls[i0], x1 = ls[i1];
+                            ls[i0] = ladd(x0, x1);
+                            ls[i1] = lsub(x0, x1);
+                        }
+                    }
+                    const int e2 = fix_out_exp(emax, NB);
+#pragma unroll
+                    for (unsigned c = 0; c < S; ++c) v[c] = from_fixed2(ls[c], e2, NB & 1, a.sqrt2inv);
+                } else {
+                    // stage-ascending butterflies (hadamard.cpp:44-59, 100-131)
+#pragma unroll
+                    for (int qn = 0; qn < NB; ++qn) {
+                        const unsigned h = 1u << qn;
+#pragma unroll
+                        for (unsigned p = 0; p < S / 2; ++p) {
+                            const unsigned i0 = ((p >> qn) << (qn + 1)) | (p & (h - 1u));
+                            const unsigned i1 = i0 + h;
+                            const double2 x0 = v[i0], x1 = v[i1];
+                            v[i0] = cscale(cadd(x0, x1), a.sqrt2inv);
+                            v[i1] = cscale(csub(x0, x1), a.sqrt2inv);
+                        }
+                    }
+                }
+            }
+            if (!single) {
+#pragma unroll
+                for (unsigned c = 0; c < S; ++c)
+                    if (keep_amp(v[c], a.eps)) keepm |= 1u << c;
+            }
+        }
+        const unsigned cnt = (unsigned)__popc(keepm);
+        if (!WRITE) {
+            if (valid) a.cnt[g] = cnt;
+            continue;
+        }
+        unsigned long long o = 0;
+        bool fits = true;
+        if (a.cursor) {
+            unsigned inc = cnt;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned t = __shfl_up_sync(0xffffffffu, inc, d);
+                if (lane >= (unsigned)d) inc += t;
+            }
+            const unsigned total = __shfl_sync(0xffffffffu, inc, 31);
+            unsigned long long wbase = 0;
+            if (lane == 31 && total) wbase = atomicAdd(a.cursor, (unsigned long long)total);
+            wbase = __shfl_sync(0xffffffffu, wbase, 31);
+            fits = wbase + total <= a.capacity;
+            o = wbase + (inc - cnt);
+            if (valid && a.ocnt) {  // this group's output range, for the next split
+                a.ostart[g] = o;
+                a.ocnt[g] = cnt;
+            }
+        } else if (valid) {
+            o = a.off[g];
+        }
+        if (!valid || !fits || !cnt) continue;
+#pragma unroll
+        for (unsigned c = 0; c < S; ++c) {
+            if (!((keepm >> c) & 1u)) continue;
+            uint64_t kk[K];
+#pragma unroll
+            for (int w = 0; w < K; ++w) kk[w] = gk[w];
+            fset<K>(kk, a.target, (uint64_t)c);
+            if (single) store_entry_sign<K>(a.out_keys, a.out_amp, o, kk, base, __popcll((uint64_t)c & v0) & 1);
+            else store_entry<K>(a.out_keys, a.out_amp, o, kk, v[c]);
+            ++o;
+        }
+    }
+}
+
 // Hadamard on 12 bits (4096 slots), one CTA of 256 threads per group. The
 // stage-ascending FWHT runs mostly in registers: each thread holds 16 slots.
 // Layout A: slot = j << 8 | warp << 5 | lane (j = 0..15); layout B:
@@ -2296,6 +2473,23 @@ static void launch_hadamard(int am, unsigned grid, size_t sm, cudaStream_t st, c
     else if (am == 1) emit_hadamard_kernel<K, W, WRITE, 1><<<grid, 256, sm, st>>>(ea);
     else emit_hadamard_kernel<K, W, WRITE, 0><<<grid, 256, sm, st>>>(ea);
 }
+template <int K, int NB, bool WRITE, bool UNI>
+static void launch_small_am(int am, unsigned grid, cudaStream_t st, const EmitArgs& ea) {
+    if (am == 2) emit_small_kernel<K, NB, WRITE, 2, UNI><<<grid, 256, 0, st>>>(ea);
+    else if (am == 1) emit_small_kernel<K, NB, WRITE, 1, UNI><<<grid, 256, 0, st>>>(ea);
+    else emit_small_kernel<K, NB, WRITE, 0, UNI><<<grid, 256, 0, st>>>(ea);
+}
+template <int K, int NB, bool WRITE>
+static void launch_small_nb(int am, unsigned grid, cudaStream_t st, const EmitArgs& ea) {
+    if (ea.mode == GM_UNITARY) launch_small_am<K, NB, WRITE, true>(am, grid, st, ea);
+    else launch_small_am<K, NB, WRITE, false>(am, grid, st, ea);
+}
+template <int K, bool WRITE>
+static void launch_small(int am, int nb, unsigned grid, cudaStream_t st, const EmitArgs& ea) {
+    if (nb == 1) launch_small_nb<K, 1, WRITE>(am, grid, st, ea);
+    else if (nb == 2) launch_small_nb<K, 2, WRITE>(am, grid, st, ea);
+    else launch_small_nb<K, 3, WRITE>(am, grid, st, ea);
+}
 template <int K>
 static void set_emit_smem_limits() {
     const int sm = 4096 * (int)sizeof(double2);
@@ -2468,6 +2662,8 @@ static void run_group(State& s, const GroupSpec& gs) {
         smem = (size_t)(W == 32 ? 8 : 1) * S * sizeof(double2);
     }
     const bool bk = gr.bucket;
+    // targets of 1 to 3 bits (not batched): one thread per group
+    const bool small = !pair && gs.mode != GM_MERGE && nb >= 1 && nb <= 3 && !gs.varw.width;
     uint64_t T = 0;
     // Hadamard on 12 bits: register FWHT kernel; single pass when the output
     // bound (every group fully populated) fits a modest multiple of the input
@@ -2484,10 +2680,11 @@ static void run_group(State& s, const GroupSpec& gs) {
     const uint64_t boundT = sizable ? G * (uint64_t)S : 0;
     const uint64_t policy = single_pass_limit() ? single_pass_limit() : std::max<uint64_t>(4 * N, 1ull << 27);
     uint64_t capT = 0;
-    // every group reserves its outputs with one atomic on one cursor; past
-    // about a million groups that serialisation costs more than a count pass
+    // a warp per group reserves its outputs with one atomic on one cursor;
+    // past about a million groups that serialisation costs more than a count
+    // pass (the one-thread-per-group kernels reserve once per 32 groups)
     const uint64_t max_single_groups = 1ull << 20;
-    if (sizable && get_output_sizing() == 0 && G > 0 && (pair || G <= max_single_groups)) {
+    if (sizable && get_output_sizing() == 0 && G > 0 && (pair || small || G <= max_single_groups)) {
         const uint64_t hint = take_output_size_hint();
         if (boundT <= policy) capT = boundT;
         else if (hint) capT = std::min<uint64_t>(hint, boundT);
@@ -2533,6 +2730,11 @@ static void run_group(State& s, const GroupSpec& gs) {
             else emit_pair_kernel<K, true, false><<<grid_for(G, 256), 256, 0, st>>>(ea);
             prof_end((double)P * E);
             SQ_CUDA(cudaGetLastError());
+        } else if (small) {
+            prof_begin("emit_small_single_pass");
+            launch_small<K, true>(am, nb, grid_for(G, 256), st, ea);
+            prof_end((double)P * E);
+            SQ_CUDA(cudaGetLastError());
         } else {
             prof_begin("emit_hadamard_single_pass");
             if (W == 32) launch_hadamard<K, 32, true>(am, (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8), smem, st, ea);
@@ -2570,9 +2772,14 @@ static void run_group(State& s, const GroupSpec& gs) {
             return;
         }
         if (G == 0) return;
-        prof_begin(write ? (pair ? "emit_pair_write" : gs.mode == GM_MERGE ? "emit_merge_write" : "emit_hadamard_write")
-                         : (pair ? "emit_pair_count" : gs.mode == GM_MERGE ? "emit_merge_count" : "emit_hadamard_count"));
-        if (pair) {
+        prof_begin(write ? (pair ? "emit_pair_write" : gs.mode == GM_MERGE ? "emit_merge_write"
+                                                    : small ? "emit_small_write" : "emit_hadamard_write")
+                         : (pair ? "emit_pair_count" : gs.mode == GM_MERGE ? "emit_merge_count"
+                                                    : small ? "emit_small_count" : "emit_hadamard_count"));
+        if (small) {
+            if (write) launch_small<K, true>(am, nb, grid_for(G, 256), st, ea);
+            else launch_small<K, false>(am, nb, grid_for(G, 256), st, ea);
+        } else if (pair) {
             const unsigned grid = grid_for(G, 256);
             if (write && bk) emit_pair_kernel<K, true, true><<<grid, 256, 0, st>>>(ea);
             else if (write) emit_pair_kernel<K, true, false><<<grid, 256, 0, st>>>(ea);

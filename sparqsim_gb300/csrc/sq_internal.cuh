@@ -165,6 +165,11 @@ struct QramTable {
     uint32_t data_size = 0;
     uint64_t n_words = 0;
     uint64_t max_word = 0;  // OR of every word: the highest bit any word uses
+    // a lookup table (SQ_OP_LOOKUP_XOR): u64 words [dense (dense_len) |
+    // sparse keys (n_sparse) | sparse words (n_sparse)]
+    bool lookup = false;
+    uint64_t dense_len = 0;
+    uint64_t n_sparse = 0;
 };
 
 // ------------------------------------------------------------------ state
@@ -202,6 +207,7 @@ struct State {
 inline void drop_groups(State& s) { s.groups.valid = false; }
 void free_group_cache(GroupCache& c);
 double select_entries(State& s, const DCondSet& sel, Field rf, uint64_t lo, uint64_t hi);
+double get_output(State& s, const DCondSet& sel, const Field* fields, uint32_t nf, double* host_out);
 // Host <-> device copies of several arrays, split into chunks spread over a
 // few copy streams (one copy engine does not reach the host link's rate);
 // ordered after all work queued on the library stream, and complete on
@@ -274,6 +280,7 @@ enum WsSlot {
     WS_MATRIX,
     WS_CURSOR,
     WS_SKETCH,
+    WS_OUTPUT,
     WS_COUNT_MAX
 };
 

@@ -851,6 +851,23 @@ class CombineRegister:
         return f
 
 
+def get_output(state: SparseState, zero_regs, idx_regs):
+    """Dense read-out of a post-selected block (GetOutput,
+    qda_fundamental.cpp:123-166): the entries whose `zero_regs` all hold 0
+    land at index concat(idx_regs) (first register lowest); returns (complex
+    vector of 2^(sum of index widths), their total probability p), the vector
+    scaled by 1/sqrt(p) unless |p - 1| < 1e-14. The state is unchanged."""
+    import numpy as np
+    z = np.array([_R(r) for r in zero_regs], dtype=np.uint32)
+    ix = np.array([_R(r) for r in idx_regs], dtype=np.uint32)
+    n = 1 << sum(System.size_of(int(r)) for r in ix)
+    out = np.zeros(2 * n, dtype=np.float64)
+    prob = c_double()
+    call("sq_get_output", state._h, z.ctypes.data_as(ctypes.c_void_p), len(z), ix.ctypes.data_as(ctypes.c_void_p),
+         len(ix), out.ctypes.data_as(ctypes.c_void_p), n, byref(prob))
+    return out.view(np.complex128), prob.value
+
+
 def add_systems(current: SparseState, new_state: SparseState, coef: float = 1.0) -> None:
     """current += coef * new_state, equal keys merged, |a|^2 < epsilon dropped
     (system_operations.h:157-175)."""

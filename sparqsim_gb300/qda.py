@@ -13,8 +13,10 @@ reference's:
   (SparQ_Algorithm/include/BlockEncoding/block_encoding_tridiagonal.h:33-108,
   src/BlockEncoding/block_encoding_tridiagonal.cpp:84-130): an LCU over
   {I, +1 shift, -1 shift, annihilation} prepared on two ancilla qubits;
-- the read-out of GetOutput (qda_fundamental.h:556-660): post-selection on
-  anc_UA = anc_2 = anc_3 = anc_4 = 0, solution in the anc_1 = 1 sector.
+- the read-out of GetOutput (qda_fundamental.h:556-660,
+  qda_fundamental.cpp:123-166): post-selection on anc_UA = anc_2 = anc_3 = 0,
+  a dense vector indexed main + anc_1 * n + anc_4 * 2n whose block
+  anc_1 = 1, anc_4 = 0 holds the solution.
 
 Conditions on a composite operator apply to every operator inside it (the
 reference partitions the state by the conditions, applies the inside, and
@@ -254,6 +256,23 @@ def read_solution(state: SparseState, n_bits: int):
     main = System.resolve("main_reg")
     np.add.at(x, regs[:, main].astype(np.int64), amps / f)
     return x, float(1.0 / (f * f))
+
+
+class GetOutput:
+    """The QDA read-out (qda_fundamental.h:556-660; qda_fundamental.cpp:123-166):
+    post-selects anc_UA = anc_3 = anc_2 = 0 and returns (the 4n amplitudes
+    indexed main + anc_1 * n + anc_4 * 2n, scaled to unit norm unless already
+    within 1e-14 of it; the post-selected probability). The state is left as
+    it is; the scatter and the probability sum run on the GPU. `is_PD` is
+    accepted and unused, as in the reference."""
+
+    def __init__(self, main_reg, anc_UA, anc_4, anc_3, anc_2, anc_1, is_PD: bool = False):
+        self.zero = [System.resolve(r) for r in (anc_UA, anc_3, anc_2)]
+        self.idx = [System.resolve(r) for r in (main_reg, anc_1, anc_4)]
+
+    def __call__(self, state: SparseState):
+        from .operators import get_output
+        return get_output(state, self.zero, self.idx)
 
 
 def walk_sequence(run, n_bits: int, alpha: float, beta: float, kappa: float, p: float, steps: int,

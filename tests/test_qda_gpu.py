@@ -139,3 +139,121 @@ def test_tridiagonal_solve_fidelity():
     assert steps > 1000
     assert prob > 0.99, prob
     assert fid > 0.999, fid
+
+
+# ------------------------------------------------------------------ GetOutput and the Poiseuille benchmark
+POISSON_ALPHA = 2.2666666666564934
+_BENCH_REGS = (("main", U, 3), ("anc_UA", U, 4), ("anc_4", ps.Boolean, 1), ("anc_3", ps.Boolean, 1),
+               ("anc_2", ps.Boolean, 1), ("anc_1", ps.Boolean, 1))
+
+
+def _oracle_output(dual, go):
+    from oracle import oracle as O
+    return O.get_output(dual.ora, go.zero, go.idx, ps.System.size_of)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("arith", ["reference", "exact-sum"])
+def test_get_output_along_a_walk(dual, arith):
+    """GetOutput on the GPU against the oracle's restatement of
+    qda_fundamental.cpp:123-166 after walk steps of the Poisson benchmark
+    (n = 8, a 24-step schedule), with ClearZero and Normalize after each step
+    as the benchmark driver does; the state is left unchanged by the read-out.
+    Vectors within 1e-12 of the largest amplitude, probabilities within
+    1e-12 relative. Normalize sums |a|^2 as a tree on the GPU and in order in
+    the oracle, so the states agree within 1e-12 rather than bit for bit."""
+    ps.set_fwht_arithmetic(arith)
+    dual.relaxed = True
+    for name, t, w in _BENCH_REGS:
+        dual.reg(name, t, w)
+    dual.start()
+    run = DualRunner(dual)
+    enc_b = qda.StatePrepHadamard("main")
+    enc_b.apply(run)
+    enc_A = qda.BlockEncodingTridiagonal("main", "anc_UA", POISSON_ALPHA, -1.0)
+    go = qda.GetOutput("main", "anc_UA", "anc_4", "anc_3", "anc_2", "anc_1")
+    steps = 24
+    for i in range(steps):
+        qda.WalkS(enc_A, enc_b, "main", "anc_UA", "anc_1", "anc_2", "anc_3", "anc_4", i / steps, 16.0,
+                  1.3).apply(run)
+        run.op(ps.ClearZero(1e-14))
+        run.op(ps.Normalize())
+        if i % 4 == 3:
+            g, gp = go(dual.gpu)
+            o, op_ = _oracle_output(dual, go)
+            assert g.shape == (32,)
+            assert gp == pytest.approx(op_, rel=1e-12, abs=1e-300)
+            assert np.max(np.abs(g - o)) <= 1e-12 * max(np.max(np.abs(o)), 1e-300)
+            dual.compare(exact_amp=True)
+
+
+@pytest.mark.gpu
+def test_get_output_edges(dual):
+    """An already normalised selection is returned as it is (|p - 1| < 1e-14),
+    a selection of nothing gives zeros and p = 0, and a register that is
+    neither post-selected nor indexed is rejected (two entries could share a
+    slot)."""
+    dual.reg("m", U, 3)
+    dual.reg("a", U, 2)
+    dual.reg("c", U, 2)
+    regs = np.array([[m, a, c] for m in range(8) for a in range(4) for c in range(4)], dtype=np.uint64)
+    rng = np.random.default_rng(11)
+    amps = rng.normal(size=len(regs)) + 1j * rng.normal(size=len(regs))
+    dual.start(regs, amps / np.linalg.norm(amps))
+    for zero, idx in ((["a"], ["m", "c"]), (["a", "c"], ["m"]), ([], ["m", "a", "c"]), (["m"], ["c", "a"])):
+        z = [ps.System.resolve(r) for r in zero]
+        ix = [ps.System.resolve(r) for r in idx]
+        g, gp = ps.get_output(dual.gpu, z, ix)
+        from oracle import oracle as O
+        o, op_ = O.get_output(dual.ora, z, ix, ps.System.size_of)
+        assert gp == pytest.approx(op_, rel=1e-13)
+        assert np.max(np.abs(g - o)) <= 1e-13
+    # everything selected: p = 1 within 1e-14, returned unscaled
+    g, gp = ps.get_output(dual.gpu, [], ["m", "a", "c"])
+    assert abs(gp - 1.0) < 1e-14
+    # nothing selected: keep c in [1, 3] first (both sides), then post-select c = 0
+    dual.apply(ps.PartialTraceSelectRange("c", (1, 3)))
+    dual.compare()
+    g, gp = ps.get_output(dual.gpu, ["c"], ["m", "a"])
+    assert gp == 0.0 and not np.any(g)
+    with pytest.raises(ps.SparQInvalid):
+        ps.get_output(dual.gpu, ["a"], ["m"])
+
+
+def _poiseuille(tmp_path, *argv):
+    import json
+
+    from sparqsim_gb300 import poiseuille
+    summary = poiseuille.run(poiseuille.parser().parse_args([*argv, "--outdir", str(tmp_path)]))
+    rows = np.loadtxt(tmp_path / "residual_curve.csv", delimiter=",", skiprows=1, ndmin=2)
+    assert json.loads((tmp_path / "qda_summary.json").read_text())["steps_executed"] == summary["steps_executed"]
+    return summary, rows
+
+
+@pytest.mark.gpu
+def test_poiseuille_compressed_schedule_2_16(tmp_path):
+    """n = 2^16, the schedule compressed to 40 steps, logged every 10 steps:
+    res_dir 2.071000e-02 at all four log points in the reference's runs
+    (docs/verification/v1d-qda-linsolver-a800.md:21,133-135), printed to 7
+    digits, so within 6e-9."""
+    summary, rows = _poiseuille(tmp_path, "--nqubit", "16", "--maxSteps", "40", "--logEvery", "10")
+    assert rows.shape == (4, 5)
+    assert list(rows[:, 0]) == [10, 20, 30, 40]
+    assert np.all(np.abs(rows[:, 1] - 2.071000e-02) <= 6e-9), rows[:, 1]
+    assert summary["step_budget"] == 40568 and summary["termination"] == "fixed_step_budget"
+
+
+@pytest.mark.gpu
+def test_poiseuille_dim256_rate_0_1(tmp_path):
+    """n = 256, rate 0.1 (3688 steps), kappa 16: final res_dir 3.135e-2,
+    fidelity 0.999438 and success probability 0.5969 in the reference's CUDA
+    run (docs/verification/v1d-qda-linsolver-a800.md:138-140), with about
+    17.5k entries at the peak (:50). res_dir is quoted truncated to four
+    digits; the others to the digits printed there."""
+    summary, rows = _poiseuille(tmp_path, "--nqubit", "8", "--steprate", "0.1", "--kappa", "16",
+                                "--logEvery", "922")
+    assert summary["steps_executed"] == 3688
+    assert 3.135e-2 <= summary["final_res_dir"] < 3.136e-2, summary
+    assert abs(summary["final_fidelity_vs_classical"] - 0.999438) <= 5e-7, summary
+    assert abs(summary["final_success_prob"] - 0.5969) <= 5e-5, summary
+    assert 17_400 <= summary["max_system_size"] <= 17_600, summary
