@@ -236,6 +236,14 @@ int sq_state_download(const sq_state* st, uint64_t* regs, uint32_t nregs, double
  * move_to_gpu / copy_to_cpu, cuda/basic_components.cu:49-106). */
 int sq_state_upload_packed(sq_state* st, uint64_t n, const uint64_t* keys, const double* amps);
 int sq_state_download_packed(const sq_state* st, uint64_t* keys, double* amps);
+/* The same download, enqueued behind the work already queued on the library
+ * stream and returned from at once, so that it overlaps later work on other
+ * states. The host buffers must stay valid until sq_state_wait(st) (or
+ * sq_synchronize) returns; a later call that writes or frees this state
+ * waits for the copy on the device first. */
+int sq_state_download_packed_async(sq_state* st, uint64_t* keys, double* amps);
+/* Blocks until the state's last asynchronous download has finished. */
+int sq_state_wait(sq_state* st);
 /* Device pointers of the live arrays (valid until the next call that resizes). */
 int sq_state_device_arrays(sq_state* st, uint64_t** key_words, uint32_t* k, double** amps);
 

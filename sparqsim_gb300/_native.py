@@ -103,6 +103,8 @@ _SIGS = [
     ("sq_state_download", c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
     ("sq_state_upload_packed", c_int, [c_void_p, c_uint64, c_void_p, c_void_p]),
     ("sq_state_download_packed", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("sq_state_download_packed_async", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("sq_state_wait", c_int, [c_void_p]),
     ("sq_state_device_arrays", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_uint32), POINTER(c_void_p)]),
     ("sq_qram_create", c_int, [c_uint32, c_uint32, c_void_p, c_uint64, POINTER(c_void_p)]),
     ("sq_qram_destroy", c_int, [c_void_p]),

@@ -270,6 +270,18 @@ class SparseState:
                  amps.ctypes.data_as(c_void_p))
         return regs[:, :nregs], amps
 
+    def download_packed_async(self, keys_ptr: int, amps_ptr: int) -> None:
+        """Start copying the packed key words (K x n uint64, word-major) and
+        the amplitudes (n complex128) into host memory at the given addresses
+        (pinned memory for full speed) and return at once; `wait()` blocks
+        until the copy is done. Later operations on this state wait for it on
+        the device."""
+        call("sq_state_download_packed_async", self._h, c_void_p(keys_ptr), c_void_p(amps_ptr))
+
+    def wait(self) -> None:
+        """Block until this state's last asynchronous download has finished."""
+        call("sq_state_wait", self._h)
+
     def to_dict(self) -> dict:
         """{tuple(values of the active registers in id order): amplitude}."""
         regs, amps = self.download()

@@ -53,9 +53,17 @@ void set_last_error(const std::string& msg) { t_err = msg; }
 static void need(bool ok, const char* msg) {
     if (!ok) fail(SQ_ERR_INVALID, msg);
 }
+// Every entry point that may write or free a state's buffers gets it here:
+// the library stream first waits for an asynchronous download still reading
+// them.
 static State& S(sq_state* st) {
     need(st != nullptr, "null state");
-    return st->s;
+    State& s = st->s;
+    if (s.d2h_pending) {
+        SQ_CUDA(cudaStreamWaitEvent(stream(), s.d2h_done, 0));
+        s.d2h_pending = false;
+    }
+    return s;
 }
 static const State& S(const sq_state* st) {
     need(st != nullptr, "null state");
@@ -89,6 +97,7 @@ int sq_init(int device) {
 int sq_synchronize(void) {
     SQ_API_BEGIN
     SQ_CUDA(cudaStreamSynchronize(stream()));
+    sync_async_copies();
     check_device_error();
     SQ_API_END
 }
@@ -225,6 +234,10 @@ int sq_state_create(uint64_t capacity, sq_state** out) {
 int sq_state_destroy(sq_state* st) {
     SQ_API_BEGIN
     if (!st) return SQ_OK;
+    if (st->s.d2h_done) {  // an asynchronous download may still read the buffers
+        SQ_CUDA(cudaEventSynchronize(st->s.d2h_done));
+        SQ_CUDA(cudaEventDestroy(st->s.d2h_done));
+    }
     free_buffers(st->s.live);
     free_buffers(st->s.spare);
     free_group_cache(st->s.groups);
@@ -369,6 +382,31 @@ int sq_state_download_packed(const sq_state* st, uint64_t* keys, double* amps) {
     }
     if (amps) jobs.push_back({amps, s.live.amp, (size_t)n * 16});
     parallel_copy(jobs.data(), (int)jobs.size(), cudaMemcpyDeviceToHost);
+    SQ_API_END
+}
+
+int sq_state_download_packed_async(sq_state* st, uint64_t* keys, double* amps) {
+    SQ_API_BEGIN
+    State& s = S(st);
+    const uint32_t k = regtable().k;
+    const uint64_t n = s.n;
+    std::vector<CopyJob> jobs;
+    for (uint32_t w = 0; w < k; ++w) {
+        if (!keys) break;
+        if (w < s.live.kalloc) jobs.push_back({keys + (size_t)w * n, s.live.keys[w], (size_t)n * 8});
+        else memset(keys + (size_t)w * n, 0, n * 8);
+    }
+    if (amps) jobs.push_back({amps, s.live.amp, (size_t)n * 16});
+    if (!s.d2h_done) SQ_CUDA(cudaEventCreateWithFlags(&s.d2h_done, cudaEventDisableTiming));
+    async_copy_d2h(jobs.data(), (int)jobs.size(), s.d2h_done);
+    s.d2h_pending = true;
+    SQ_API_END
+}
+
+int sq_state_wait(sq_state* st) {
+    SQ_API_BEGIN
+    need(st != nullptr, "null state");
+    if (st->s.d2h_done) SQ_CUDA(cudaEventSynchronize(st->s.d2h_done));
     SQ_API_END
 }
 

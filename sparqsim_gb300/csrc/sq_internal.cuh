@@ -203,6 +203,8 @@ struct State {
     Buffers spare;
     uint64_t n = 0;
     GroupCache groups;
+    cudaEvent_t d2h_done = nullptr;  // recorded when the last asynchronous download finished reading
+    bool d2h_pending = false;        // the library stream has not been made to wait for it yet
 };
 inline void drop_groups(State& s) { s.groups.valid = false; }
 void free_group_cache(GroupCache& c);
@@ -218,6 +220,12 @@ struct CopyJob {
     size_t bytes;
 };
 void parallel_copy(const CopyJob* jobs, int n, cudaMemcpyKind kind);
+// The same device-to-host copies on their own streams, returning at once;
+// `done` is recorded when every copy has finished. The host memory must stay
+// valid, and the device memory unwritten, until then.
+void async_copy_d2h(const CopyJob* jobs, int n, cudaEvent_t done);
+// Blocks until every asynchronous download has finished.
+void sync_async_copies();
 // Copy a host table of 64-bit words to the device at the narrowest width (2,
 // 4 or 8 bytes) that holds every word; eb_guess is tried first.
 void* qram_upload(const uint64_t* host_words, uint64_t n, uint32_t eb_guess, uint32_t* eb_out, uint64_t* all_out);
