@@ -334,6 +334,24 @@ def run_trajectories(args, ext) -> dict:
     e.synchronize()
     batched_ms = s.elapsed_time(e) / steps
     batched_wall = (time.perf_counter() - t0) / steps
+    eager_n, eager_norm = st.size(), st.norm_sq()
+    # the same batched circuit replayed as one CUDA graph per run (one
+    # recording pass, one capture; each run is the upload and one launch)
+    init = wl.initial_batched()
+    graph = ps.Graph(st, apply=lambda: wl.run_batched(st, upload=False), prepare=lambda: st.upload(*init))
+    graph.replay()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.record(ext)
+    for _ in range(steps):
+        graph.replay()
+    e.record(ext)
+    e.synchronize()
+    ps.synchronize()  # reports a replay whose sizes differed from the recording
+    graph_ms = s.elapsed_time(e) / steps
+    graph_wall = (time.perf_counter() - t0) / steps
+    graph_same = st.size() == eager_n and abs(st.norm_sq() - eager_norm) <= 1e-12 * eager_norm
+    del graph
     # plain GPU form: instance by instance, on a sample of instances
     n_sample = min(args.plain_sample, wl.n_traj)
     wl.build_plain()
@@ -383,6 +401,10 @@ def run_trajectories(args, ext) -> dict:
         "updates_per_step": upd, "peak_entries": peak_hint,
         "batched": {"value": batched_ups, "unit": UNIT, "ms_per_step": batched_ms,
                     "wall_ms_per_step": batched_wall * 1e3},
+        "batched_graph": {"value": upd / (graph_ms / 1e3), "unit": UNIT, "ms_per_step": graph_ms,
+                          "wall_ms_per_step": graph_wall * 1e3, "same_size_and_norm_as_eager": graph_same,
+                          "note": "the batched circuit recorded once and replayed as one CUDA graph launch per run; "
+                                  "each run uploads the initial state first"},
         "plain_gpu": {"value": plain_ups, "unit": UNIT,
                       "sample": f"instances 0..{n_sample - 1}, {upd_p} updates in {plain_s:.2f} s (wall clock)"},
         "batched_over_plain": batched_ups / plain_ups,
@@ -485,110 +507,6 @@ def run_qda(args, ext) -> dict:
         out["reference_published"] = {"s_per_walk_step": ref_s_per_step, "hardware": "1x A800-SXM4-80GB",
                                       "source": "docs/verification/v1d-qda-linsolver-a800.md:48-52"}
         out["speedup_vs_published"] = ref_s_per_step / (ms / sample / 1e3)
-    return out
-
-
-def replica_max(ms: float, device: str) -> float:
-    """The slowest replica's time: all-reduce MAX over the ranks, then a barrier
-    (independent circuits per GPU, no exchange on the data path)."""
-    import torch
-    import torch.distributed as dist
-    tt = torch.tensor([ms], device=device, dtype=torch.float64)
-    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-    dist.barrier()
-    return float(tt.item())
-
-
-def replica_value(world: int, updates_per_step: int, steps: int, t_max_ms: float) -> float:
-    """Whole-job updates/s: every replica runs the same circuit, timed by the slowest."""
-    return world * updates_per_step * steps / (t_max_ms / 1e3)
-
-
-def run_trajectories(args, ext) -> dict:
-    """Batched noisy trajectories (4096 instances, a/b/c 16-bit, per-instance
-    Hadamard width h_t in [4, 8], Pauli X/Z at p = 1e-3 per bit per layer,
-    6 layers): the batched form, the plain GPU form (one state per instance)
-    on a sample of instances, and the oracle on a smaller sample."""
-    import numpy as np
-    import torch
-
-    import sparqsim_gb300 as ps
-    from sparqsim_gb300.workloads import NoisyTrajectories
-    wl = NoisyTrajectories(n_traj=args.trajectories, layers=6, p=1e-3, h_min=4, h_max=8, seed=SEED)
-    wl.build_batched()
-    st = ps.SparseState(capacity=1 << 20)
-    upd = wl.run_batched(st, count=True)
-    peak_hint = st.size()
-    for _ in range(2):
-        wl.run_batched(st)
-    steps = max(2, min(args.steps, 5))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s.record(ext)
-    for _ in range(steps):
-        wl.run_batched(st)
-    e.record(ext)
-    e.synchronize()
-    batched_ms = s.elapsed_time(e) / steps
-    batched_wall = (time.perf_counter() - t0) / steps
-    # plain GPU form: instance by instance, on a sample of instances
-    n_sample = min(args.plain_sample, wl.n_traj)
-    wl.build_plain()
-    sp = ps.SparseState(capacity=1 << 17)
-    upd_p = sum(wl.run_plain(sp, t, count=True) for t in range(n_sample))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for t in range(n_sample):
-        wl.run_plain(sp, t)
-    torch.cuda.synchronize()
-    plain_s = time.perf_counter() - t0
-    # the oracle, one thread, plain form, on a smaller sample
-    cpu = None
-    if not args.no_cpu_baseline:
-        from oracle import oracle as O
-        O.clear()
-        for rid in ps.System.active_ids():
-            O.add_register(int(ps.System.type_of(rid)), ps.System.size_of(rid))
-        _, qram, noise, mids, Hs = wl._built
-        O.register_qram(qram)
-        for nt in noise:
-            O.register_qram(nt.table)
-        n_cpu = min(args.cpu_sample, wl.n_traj)
-        upd_c = 0
-        t0 = time.perf_counter()
-        for t in range(n_cpu):
-            ost = O.OracleState()
-            ost.set(np.array([[t, 0, 0, 0]], dtype=np.uint64), np.ones(1, dtype=np.complex128))
-            H = Hs[int(wl.widths[t])]
-            for mid in mids:
-                n0 = ost.size()
-                O.apply(ost, H.spec())
-                n1 = ost.size()
-                O.apply(ost, mid.spec())
-                O.apply(ost, H.spec())
-                upd_c += max(n0, n1) + 4 * n1 + max(n1, ost.size())
-        cpu_s = time.perf_counter() - t0
-        O.clear()
-        cpu = {"value": upd_c / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"instances 0..{n_cpu - 1}, plain form, {upd_c} updates in {cpu_s:.1f} s, one thread"}
-    batched_ups = upd / (batched_ms / 1e3)
-    plain_ups = upd_p / plain_s
-    out = {
-        "workload": (f"{wl.n_traj} noisy instances of the register circuit (a/b/c 16-bit, 2^16-word uint16 table), "
-                     "Hadamard width h_t in [4,8] per instance, Pauli X/Z p=1e-3 per bit per layer, 6 layers, "
-                     "support 2^h..2^2h per instance"),
-        "updates_per_step": upd, "peak_entries": peak_hint,
-        "batched": {"value": batched_ups, "unit": UNIT, "ms_per_step": batched_ms,
-                    "wall_ms_per_step": batched_wall * 1e3},
-        "plain_gpu": {"value": plain_ups, "unit": UNIT,
-                      "sample": f"instances 0..{n_sample - 1}, {upd_p} updates in {plain_s:.2f} s (wall clock)"},
-        "batched_over_plain": batched_ups / plain_ups,
-        "fwht_arithmetic": ps.get_fwht_arithmetic(),
-    }
-    if cpu:
-        out["cpu"] = cpu
-        out["batched_over_cpu"] = batched_ups / cpu["value"]
     return out
 
 

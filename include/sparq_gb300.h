@@ -244,6 +244,32 @@ int sq_state_download_packed(const sq_state* st, uint64_t* keys, double* amps);
 int sq_state_download_packed_async(sq_state* st, uint64_t* keys, double* amps);
 /* Blocks until the state's last asynchronous download has finished. */
 int sq_state_wait(sq_state* st);
+
+/* ------------------------------------------------------------------ */
+/* Graphs: a sequence of operators replayed as one CUDA graph launch    */
+/* ------------------------------------------------------------------ */
+/* 1. sq_graph_record_begin(st); apply the operators to the state (they run
+ *    eagerly; every count the host reads back is logged); sq_graph_record_end().
+ *    The sequence must leave the state's double buffers in their roles (an
+ *    even number of splits), so that every replay starts as the last ended. 
+ * 2. Bring the state back to the same input (the same size, e.g. upload it
+ *    again), then sq_graph_capture_begin(st); apply the same operators (they
+ *    are captured, not run, and take the logged counts); sq_graph_capture_end.
+ * 3. For every replay: bring the state to the same input and call
+ *    sq_graph_launch (asynchronous). Each logged count is checked on the
+ *    device; a replay whose counts differ from the recorded ones is reported
+ *    as SQ_ERR_INVALID at the next synchronising call and leaves the state
+ *    invalid. A launch is refused when the state's size or buffers, or the
+ *    library's workspace, differ from those captured. Tables used by the
+ *    operators (QRAM, lookup, noise) must outlive the graph. Allocation is
+ *    refused while capturing: the record pass grows every buffer. */
+typedef struct sq_graph sq_graph;
+int sq_graph_record_begin(sq_state* st);
+int sq_graph_record_end(void);
+int sq_graph_capture_begin(sq_state* st);
+int sq_graph_capture_end(sq_graph** out);
+int sq_graph_launch(sq_graph* g);
+int sq_graph_destroy(sq_graph* g);
 /* Device pointers of the live arrays (valid until the next call that resizes). */
 int sq_state_device_arrays(sq_state* st, uint64_t** key_words, uint32_t* k, double** amps);
 

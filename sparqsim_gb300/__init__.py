@@ -6,7 +6,7 @@ lives in GPU memory and every operator runs as hand-written sm_103a kernels
 behind the C ABI in include/sparq_gb300.h. There is no CPU fallback.
 """
 from ._native import SparQError, SparQInvalid, launch_count
-from .core import (Boolean, General, QRAMCircuit_qutrit, Rational, SignedInteger, SparseState,
+from .core import (Boolean, General, Graph, QRAMCircuit_qutrit, Rational, SignedInteger, SparseState,
                    StateStorageType, System, UnsignedInteger, get_clearzero_default_eps,
                    autotune_classes, autotune_reset, get_fwht_arithmetic, get_group_strategy,
                    set_clearzero_default_eps,

@@ -105,6 +105,12 @@ _SIGS = [
     ("sq_state_download_packed", c_int, [c_void_p, c_void_p, c_void_p]),
     ("sq_state_download_packed_async", c_int, [c_void_p, c_void_p, c_void_p]),
     ("sq_state_wait", c_int, [c_void_p]),
+    ("sq_graph_record_begin", c_int, [c_void_p]),
+    ("sq_graph_record_end", c_int, []),
+    ("sq_graph_capture_begin", c_int, [c_void_p]),
+    ("sq_graph_capture_end", c_int, [POINTER(c_void_p)]),
+    ("sq_graph_launch", c_int, [c_void_p]),
+    ("sq_graph_destroy", c_int, [c_void_p]),
     ("sq_state_device_arrays", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_uint32), POINTER(c_void_p)]),
     ("sq_qram_create", c_int, [c_uint32, c_uint32, c_void_p, c_uint64, POINTER(c_void_p)]),
     ("sq_qram_destroy", c_int, [c_void_p]),

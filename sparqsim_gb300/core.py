@@ -408,3 +408,56 @@ class Controllable:
             c.c[i].reg = r
             c.c[i].param = p & 0xFFFFFFFFFFFFFFFF
         return c
+
+
+class Graph:
+    """A sequence of operators on one state, replayed as one CUDA graph
+    launch (sq_graph_*). `prepare()` brings the state to its input (for
+    example uploads it) and `apply()` applies the operators. Construction
+    runs them once eagerly (recording every count the host reads back), then
+    once under capture; `replay()` prepares the state and launches the graph,
+    which runs every kernel again with no host round trip in between. The
+    counts a replay produces are checked on the device against the recorded
+    ones: a replay on an input whose split sizes differ is reported at the
+    next synchronising call (SparQInvalid) and leaves the state invalid. The
+    operators must leave the state's double buffers in their roles (an even
+    number of splits), so that each replay starts as the last one ended."""
+
+    def __init__(self, state: "SparseState", apply, prepare):
+        self.state, self._apply, self._prepare = state, apply, prepare
+        self._h = c_void_p()
+        prepare()
+        call("sq_graph_record_begin", state._h)
+        try:
+            apply()
+        finally:
+            call("sq_graph_record_end")
+        prepare()
+        call("sq_graph_capture_begin", state._h)
+        try:
+            apply()
+        except BaseException:
+            try:
+                call("sq_graph_capture_end", byref(self._h))  # closes the capture
+            except Exception:
+                pass
+            raise
+        call("sq_graph_capture_end", byref(self._h))
+
+    def launch(self) -> None:
+        """Launch on the state as it is (asynchronous)."""
+        call("sq_graph_launch", self._h)
+
+    def replay(self) -> None:
+        self._prepare()
+        self.launch()
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                call("sq_graph_destroy", h)
+            except Exception:
+                pass
+            self._h = None
+

@@ -53,11 +53,14 @@ void set_last_error(const std::string& msg) { t_err = msg; }
 static void need(bool ok, const char* msg) {
     if (!ok) fail(SQ_ERR_INVALID, msg);
 }
+static sq_state* g_capture_state = nullptr;  // the state a capture runs on
+
 // Every entry point that may write or free a state's buffers gets it here:
 // the library stream first waits for an asynchronous download still reading
-// them.
+// them. While a capture runs, only its state may be used.
 static State& S(sq_state* st) {
     need(st != nullptr, "null state");
+    if (capturing() && st != g_capture_state) fail(SQ_ERR_INVALID, "capture: operators on another state");
     State& s = st->s;
     if (s.d2h_pending) {
         SQ_CUDA(cudaStreamWaitEvent(stream(), s.d2h_done, 0));
@@ -407,6 +410,143 @@ int sq_state_wait(sq_state* st) {
     SQ_API_BEGIN
     need(st != nullptr, "null state");
     if (st->s.d2h_done) SQ_CUDA(cudaEventSynchronize(st->s.d2h_done));
+    SQ_API_END
+}
+
+// ------------------------------------------------------------------ graphs
+struct sq_graph {
+    cudaGraphExec_t exec = nullptr;
+    sq_state* st = nullptr;
+    State pre, post;  // the state's host-side fields before and after the captured operators
+    void* ws_p[16] = {nullptr};
+    uint64_t launches = 0;
+};
+
+static State g_capture_pre;
+static void* g_capture_ws[16];
+static uint64_t g_capture_launch0 = 0;
+
+static bool same_buffers(const Buffers& a, const Buffers& b) {
+    if (a.amp != b.amp || a.cap != b.cap || a.kalloc != b.kalloc) return false;
+    for (int w = 0; w < SQ_KMAX; ++w)
+        if (a.keys[w] != b.keys[w]) return false;
+    return true;
+}
+static bool same_layout(const State& a, const State& b) {
+    if (!same_buffers(a.live, b.live) || !same_buffers(a.spare, b.spare)) return false;
+    const GroupCache &x = a.groups, &y = b.groups;
+    for (int i = 0; i < 2; ++i)
+        if (x.start[i] != y.start[i] || x.cnt[i] != y.cnt[i] || x.cap[i] != y.cap[i]) return false;
+    return x.valid == y.valid && x.cur == y.cur && a.n == b.n;
+}
+
+static sq_state* g_record_state = nullptr;
+static uint64_t g_record_swaps = 0;
+static int g_record_cur = 0;
+
+int sq_graph_record_begin(sq_state* st) {
+    SQ_API_BEGIN
+    need(replay().mode == RP_OFF, "graph: a record or capture is already open");
+    const State& s = S(st);
+    g_record_state = st;
+    g_record_swaps = s.swaps;
+    g_record_cur = s.groups.cur;
+    replay().log.clear();
+    replay().pos = 0;
+    replay().mode = RP_RECORD;
+    SQ_API_END
+}
+
+int sq_graph_record_end(void) {
+    SQ_API_BEGIN
+    need(replay().mode == RP_RECORD, "graph: no record is open");
+    replay().mode = RP_OFF;
+    const State& s = g_record_state->s;
+    g_record_state = nullptr;
+    // a replay starts where the previous one ended: the buffers must be back in their roles
+    need((s.swaps - g_record_swaps) % 2 == 0 && s.groups.cur == g_record_cur,
+         "graph: the operators leave the state's buffers in other roles (an odd number of splits)");
+    SQ_API_END
+}
+
+int sq_graph_capture_begin(sq_state* st) {
+    SQ_API_BEGIN
+    need(replay().mode == RP_OFF, "graph: a record or capture is already open");
+    State& s = S(st);
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    g_capture_pre = s;
+    for (int i = 0; i < 16; ++i) g_capture_ws[i] = ws().p[i];
+    g_capture_launch0 = launches();
+    g_capture_state = st;
+    replay().pos = 0;
+    SQ_CUDA(cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal));
+    replay().mode = RP_CAPTURE;
+    SQ_API_END
+}
+
+int sq_graph_capture_end(sq_graph** out) {
+    SQ_API_BEGIN
+    need(replay().mode == RP_CAPTURE, "graph: no capture is open");
+    replay().mode = RP_OFF;
+    sq_state* st = g_capture_state;
+    g_capture_state = nullptr;
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(stream(), &g);
+    // nothing ran: the state is as it was, and the captured launches are not counted
+    State post = st->s;
+    const cudaEvent_t ev = st->s.d2h_done;
+    st->s = g_capture_pre;
+    st->s.d2h_done = ev;
+    const uint64_t captured = launches() - g_capture_launch0;
+    count_launch(-(int)captured);
+    if (ce != cudaSuccess || !g) {
+        (void)cudaGetLastError();
+        if (g) cudaGraphDestroy(g);
+        fail(SQ_ERR_CUDA, std::string("graph: capture failed: ") + cudaGetErrorString(ce));
+    }
+    bool ws_same = true;
+    for (int i = 0; i < 16; ++i) ws_same = ws_same && ws().p[i] == g_capture_ws[i];
+    if (replay().pos != replay().log.size() || !ws_same) {
+        cudaGraphDestroy(g);
+        fail(SQ_ERR_INVALID, "graph: the captured operators differ from the recorded ones");
+    }
+    sq_graph* gr = new sq_graph();
+    const cudaError_t ie = cudaGraphInstantiate(&gr->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        delete gr;
+        fail(SQ_ERR_CUDA, std::string("graph: instantiate failed: ") + cudaGetErrorString(ie));
+    }
+    gr->st = st;
+    gr->pre = g_capture_pre;
+    gr->post = post;
+    for (int i = 0; i < 16; ++i) gr->ws_p[i] = g_capture_ws[i];
+    gr->launches = captured;
+    *out = gr;
+    SQ_API_END
+}
+
+int sq_graph_launch(sq_graph* g) {
+    SQ_API_BEGIN
+    need(g != nullptr && g->exec != nullptr, "null graph");
+    need(replay().mode == RP_OFF, "graph: a record or capture is open");
+    State& s = S(g->st);
+    need(same_layout(s, g->pre), "graph: the state's size or buffers differ from the captured ones");
+    for (int i = 0; i < 16; ++i) need(ws().p[i] == g->ws_p[i], "graph: the library's workspace has been reallocated");
+    SQ_CUDA(cudaGraphLaunch(g->exec, stream()));
+    const cudaEvent_t ev = s.d2h_done;
+    s = g->post;
+    s.d2h_done = ev;
+    s.d2h_pending = false;
+    count_launch((int)g->launches);
+    SQ_API_END
+}
+
+int sq_graph_destroy(sq_graph* g) {
+    SQ_API_BEGIN
+    if (!g) return SQ_OK;
+    if (g->exec) SQ_CUDA(cudaGraphExecDestroy(g->exec));
+    delete g;
     SQ_API_END
 }
 

@@ -139,12 +139,17 @@ static void launch_cz(const Buffers& in, Buffers& out, uint64_t n, double eps, L
     SQ_CUDA(cudaGetLastError());
 }
 
+// Reads (and clears) the device error word. Not logged for replay: under
+// capture it is skipped, and the flags raised by a replayed graph are read at
+// the next synchronising call.
 void check_device_error() {
+    if (capturing()) return;
     unsigned v = 0;
     SQ_CUDA(cudaMemcpyAsync(&v, device_error_word(), 4, cudaMemcpyDeviceToHost, stream()));
     SQ_CUDA(cudaStreamSynchronize(stream()));
     if (v) {
         SQ_CUDA(cudaMemsetAsync(device_error_word(), 0, 4, stream()));
+        if (v & 32u) fail(SQ_ERR_INVALID, "a replayed graph saw other sizes than were recorded; the state is not valid");
         if (v & 8u) fail(SQ_ERR_INVALID, "lookup: a register value has no entry in the table");
         if (v & 4u) fail(SQ_ERR_INVALID, "batched Hadamard: an entry's digit count exceeds max_digits");
         if (v & 2u) fail(SQ_ERR_DEVICE_TIMEOUT, "hash grouping gave up (table full or a bounded wait expired)");
@@ -169,7 +174,7 @@ uint64_t compact_nonzero(const Buffers& in, Buffers& out, uint64_t n, double eps
         default: launch_cz<8>(in, out, n, eps, lb, nt); break;
     }
     unsigned long long total = 0;
-    SQ_CUDA(cudaMemcpyAsync(&total, lb.total, 8, cudaMemcpyDeviceToHost, stream()));
+    host_read(&total, lb.total, 8);
     check_device_error();  // synchronizes
     prof_add_bytes_last((double)total * (16.0 * k + 16));  // survivors: keys read + keys and amp written
     return total;
@@ -205,7 +210,7 @@ double select_entries(State& s, const DCondSet& sel, Field rf, uint64_t lo, uint
         default: launch_cz<8, true>(s.live, s.spare, n, 0.0, lb, nt, &ks); break;
     }
     unsigned long long total = 0;
-    SQ_CUDA(cudaMemcpyAsync(&total, lb.total, 8, cudaMemcpyDeviceToHost, stream()));
+    host_read(&total, lb.total, 8);
     check_device_error();  // synchronizes
     prof_add_bytes_last((double)total * (16.0 * k + 16) - (double)n * 16 + (double)n * (8.0 * k + 16));
     swap_live_spare(s);
@@ -317,16 +322,14 @@ double get_output(State& s, const DCondSet& sel, const Field* fields, uint32_t n
         SQ_CUDA(cudaGetLastError());
     }
     double p = 0.0;
-    SQ_CUDA(cudaMemcpyAsync(&p, part + g, 8, cudaMemcpyDeviceToHost, stream()));
-    SQ_CUDA(cudaStreamSynchronize(stream()));
+    host_read(&p, part + g, 8);
     if (!(std::fabs(p - 1.0) < 1e-14) && p != 0.0) {
         prof_begin("scale");
         scale_kernel<<<grid_for(len, 256), 256, 0, stream()>>>(out, len, 1.0 / std::sqrt(p));
         prof_end((double)len * 32);
         SQ_CUDA(cudaGetLastError());
     }
-    SQ_CUDA(cudaMemcpyAsync(host_out, out, len * 16, cudaMemcpyDeviceToHost, stream()));
-    SQ_CUDA(cudaStreamSynchronize(stream()));
+    host_read(host_out, out, len * 16);
     return p;
 }
 
@@ -387,8 +390,7 @@ double norm_sq(const State& s) {
     prof_end((double)g * 8);
     SQ_CUDA(cudaGetLastError());
     double r = 0;
-    SQ_CUDA(cudaMemcpyAsync(&r, part + g, 8, cudaMemcpyDeviceToHost, stream()));
-    SQ_CUDA(cudaStreamSynchronize(stream()));
+    host_read(&r, part + g, 8);
     return r;
 }
 

@@ -955,6 +955,7 @@ __global__ void __launch_bounds__(256) emit_small_kernel(const __grid_constant__
 #pragma unroll
                 for (unsigned c = 0; c < S; ++c) v[c] = make_double2(0.0, 0.0);
                 int emax = 1;
+                unsigned filled = 0;  // bit c: slot c holds a member
 #pragma unroll
                 for (unsigned j = 0; j < S; ++j) {
                     if (j < m) {
@@ -964,22 +965,27 @@ __global__ void __launch_bounds__(256) emit_small_kernel(const __grid_constant__
 #pragma unroll
                         for (unsigned c = 0; c < S; ++c)
                             if (c == (unsigned)(tj & (S - 1u))) v[c] = aj;
+                        filled |= 1u << (unsigned)(tj & (S - 1u));
                         emax = max(emax, amp_exp(aj));
                     }
                 }
                 if (UNI) {
-                    // Rot_GeneralUnitary (rot.cpp:353-389): out[i] = sum_j M(i,j) * amp[j], j ascending
+                    // Rot_GeneralUnitary (rot.cpp:353-389): out[i] = sum_j M(i,j) * amp[j], j ascending.
+                    // An empty slot's terms are +-0 and leave every nonzero sum as it is (an all-zero
+                    // output is pruned), so column j is skipped when no lane of the warp holds slot j:
+                    // FP64 is the limit of this kernel, and partly filled groups are common.
                     double2 r[S];
 #pragma unroll
-                    for (unsigned c = 0; c < S; ++c) {
-                        double2 acc = make_double2(0.0, 0.0);
+                    for (unsigned c = 0; c < S; ++c) r[c] = make_double2(0.0, 0.0);
 #pragma unroll
-                        for (unsigned j = 0; j < S; ++j) {
+                    for (unsigned j = 0; j < S; ++j) {
+                        if (!__any_sync(__activemask(), (filled >> j) & 1u)) continue;
+#pragma unroll
+                        for (unsigned c = 0; c < S; ++c) {
                             const double2 mij = a.udag ? make_double2(a.umat[j * S + c].x, -a.umat[j * S + c].y)
                                                        : a.umat[c * S + j];
-                            acc = cadd(acc, cmul2(mij, v[j]));
+                            r[c] = cadd(r[c], cmul2(mij, v[j]));
                         }
-                        r[c] = acc;
                     }
 #pragma unroll
                     for (unsigned c = 0; c < S; ++c) v[c] = r[c];
@@ -2089,11 +2095,12 @@ std::map<uint64_t, TuneEntry> g_tune;
 }  // namespace
 int autotune_pick(uint64_t key) {
     TuneEntry& e = g_tune[key];
-    if (!e.tried[0]) return 1;
-    if (!e.tried[1]) return 2;
-    return e.ms[1] <= e.ms[0] ? 2 : 1;
+    int pick = !e.tried[0] ? 1 : !e.tried[1] ? 2 : (e.ms[1] <= e.ms[0] ? 2 : 1);
+    host_decision(&pick, sizeof(pick));  // a capture repeats the recorded choice
+    return pick;
 }
 void autotune_record(uint64_t key, int strategy, double ms) {
+    if (capturing()) return;  // nothing ran: no time to learn from
     TuneEntry& e = g_tune[key];
     const int i = strategy == 2 ? 1 : 0;
     if (!e.tried[i]) {
@@ -2151,14 +2158,13 @@ static Grouping group_by_sort(State& s, const GroupSpec& gs, const uint64_t* gma
     unsigned long long* stats = (unsigned long long*)(dg + 16);
     std::vector<unsigned long long> init(2 * K + 1, 0);
     for (int w = 0; w < K; ++w) init[K + w] = ~0ull;
-    SQ_CUDA(cudaMemcpyAsync(stats, init.data(), init.size() * 8, cudaMemcpyHostToDevice, st));
+    h2d_small(stats, init.data(), init.size() * 8);
     prof_begin("group_stats");
     stats_kernel<K><<<grid_for(N, 256, 4), 256, 0, st>>>(ik, N, gs.cond, dg, stats);
     prof_end((double)N * 8 * K);
     SQ_CUDA(cudaGetLastError());
     std::vector<unsigned long long> res(2 * K + 1);
-    SQ_CUDA(cudaMemcpyAsync(res.data(), stats, res.size() * 8, cudaMemcpyDeviceToHost, st));
-    SQ_CUDA(cudaStreamSynchronize(st));
+    host_read(res.data(), stats, res.size() * 8);
     const uint64_t F = res[2 * K];
     const uint64_t P = N - F;
 
@@ -2276,7 +2282,7 @@ static Grouping group_by_sort(State& s, const GroupSpec& gs, const uint64_t* gma
     if (P > 0) {
         if (total_bits == 0 || V == 0) {
             unsigned hh[2] = {0u, (unsigned)P};
-            SQ_CUDA(cudaMemcpyAsync(seg, hh, 8, cudaMemcpyHostToDevice, st));
+            h2d_small(seg, hh, 8);
             out.G = 1;
         } else {
             const long long nt = (long long)((P + kSelTile - 1) / kSelTile);
@@ -2292,12 +2298,12 @@ static Grouping group_by_sort(State& s, const GroupSpec& gs, const uint64_t* gma
             prof_end((double)P * (key_bytes ? key_bytes : 4 + 8 * K));
             SQ_CUDA(cudaGetLastError());
             unsigned long long g = 0;
-            SQ_CUDA(cudaMemcpyAsync(&g, lb.total, 8, cudaMemcpyDeviceToHost, st));
+            host_read(&g, lb.total, 8);
             check_device_error();
             out.G = g;
             prof_add_bytes_last((double)out.G * 4);
             unsigned endv = (unsigned)P;
-            SQ_CUDA(cudaMemcpyAsync(seg + out.G, &endv, 4, cudaMemcpyHostToDevice, st));
+            h2d_small(seg + out.G, &endv, 4);
         }
     }
     return out;
@@ -2330,7 +2336,7 @@ static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg, uint6
         prof_end((double)N * (8.0 * K + 16) * 2);
         SQ_CUDA(cudaGetLastError());
         unsigned gc[2] = {0, 0};
-        SQ_CUDA(cudaMemcpyAsync(gc, base, 8, cudaMemcpyDeviceToHost, st));
+        host_read(gc, base, 8);
         check_device_error();  // synchronizes
         Grouping out;
         out.G = gc[0];
@@ -2377,15 +2383,14 @@ static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg, uint6
         prof_end((double)N * (8.0 * K + 4));
         SQ_CUDA(cudaGetLastError());
         unsigned gc[3] = {0, 0, 0};
-        SQ_CUDA(cudaMemcpyAsync(gc, h.gcount, 12, cudaMemcpyDeviceToHost, st));
+        host_read(gc, h.gcount, 12);
         check_device_error();
         if (!gc[2]) break;
         if (attempt == 1) fail(SQ_ERR_DEVICE_TIMEOUT, "hash grouping overflowed a table sized for every entry");
         want = N;
     }
     unsigned gc[2] = {0, 0};
-    SQ_CUDA(cudaMemcpyAsync(gc, h.gcount, 8, cudaMemcpyDeviceToHost, st));
-    SQ_CUDA(cudaStreamSynchronize(st));
+    host_read(gc, h.gcount, 8);
     Grouping out;
     out.G = gc[0];
     out.F = gc[1];
@@ -2403,7 +2408,7 @@ static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg, uint6
         prof_end((double)out.G * 8);
         SQ_CUDA(cudaGetLastError());
         unsigned endv = (unsigned)P;
-        SQ_CUDA(cudaMemcpyAsync(seg + out.G, &endv, 4, cudaMemcpyHostToDevice, st));
+        h2d_small(seg + out.G, &endv, 4);
         unsigned* btgt = (unsigned*)(base + off_btgt);
         double2* bamp = (double2*)(base + off_bamp);
         prof_begin("bucket_members");
@@ -2446,8 +2451,7 @@ static void split_features(State& s, const GroupSpec& gs, uint64_t N, const uint
     prof_end((double)samples * 8 * K);
     SQ_CUDA(cudaGetLastError());
     unsigned h[32];
-    SQ_CUDA(cudaMemcpyAsync(h, regs, sizeof(h), cudaMemcpyDeviceToHost, st));
-    SQ_CUDA(cudaStreamSynchronize(st));
+    host_read(h, regs, sizeof(h));
     for (int i = 0; i < 32; ++i) f[16 + i] = (float)h[i] / 32.f;
 }
 
@@ -2539,7 +2543,7 @@ static void run_group(State& s, const GroupSpec& gs) {
     // width: the hash kernel clears each entry's own low n bits
     if (gs.target.width && !gs.varw.width) gmask[gs.target.word] &= ~(wmask(gs.target.width) << gs.target.shift);
     uint64_t* dg = (uint64_t*)ws().get(WS_REDUCE, 64 * 8);
-    SQ_CUDA(cudaMemcpyAsync(dg, gmask, SQ_KMAX * 8, cudaMemcpyHostToDevice, st));
+    h2d_small(dg, gmask, SQ_KMAX * 8);
 
     // the merge sums runs in order, so it keeps the (stable) sort; the
     // transforms are order-independent and default to the hash grouping
@@ -2690,6 +2694,7 @@ static void run_group(State& s, const GroupSpec& gs) {
         else if (hint) capT = std::min<uint64_t>(hint, boundT);
         else if (have_pred) capT = std::min<uint64_t>((uint64_t)(t_pred * 1.25) + 4096, boundT);
     }
+    host_decision(&capT, sizeof(capT));  // a capture sizes the outputs as the recorded pass did
     const bool single_pass = capT > 0;
     {
         static bool limits_set = false;
@@ -2743,8 +2748,7 @@ static void run_group(State& s, const GroupSpec& gs) {
             SQ_CUDA(cudaGetLastError());
         }
         unsigned long long t = 0;
-        SQ_CUDA(cudaMemcpyAsync(&t, cur, 8, cudaMemcpyDeviceToHost, st));
-        SQ_CUDA(cudaStreamSynchronize(st));
+        host_read(&t, cur, 8);
         ea.cursor = nullptr;
         ea.capacity = 0;
         note_output_size(gs.mode, N, G, t);
@@ -2809,7 +2813,7 @@ static void run_group(State& s, const GroupSpec& gs) {
         prof_end((double)G * 12);
         SQ_CUDA(cudaGetLastError());
         unsigned long long t = 0;
-        SQ_CUDA(cudaMemcpyAsync(&t, lb.total, 8, cudaMemcpyDeviceToHost, st));
+        host_read(&t, lb.total, 8);
         check_device_error();
         T = t;
     }

@@ -251,15 +251,18 @@ bool predictor_logging() { return g_logging; }
 
 bool predictor_predict(const float* x, float* y) {
     if (!predictor_enabled()) return false;
-    ensure_rows(1);
-    cudaStream_t st = stream();
-    SQ_CUDA(cudaMemcpyAsync(g_net.x, x, kIn * 4, cudaMemcpyHostToDevice, st));
-    prof_begin("predictor_forward");
-    fwd_kernel<<<1, kHid, 0, st>>>(g_net.p, g_net.x, 1, nullptr, nullptr, nullptr, nullptr, g_net.y);
-    prof_end(0.0);
-    SQ_CUDA(cudaGetLastError());
-    SQ_CUDA(cudaMemcpyAsync(y, g_net.y, kOut * 4, cudaMemcpyDeviceToHost, st));
-    SQ_CUDA(cudaStreamSynchronize(st));
+    if (!capturing()) {  // a capture repeats the recorded prediction
+        ensure_rows(1);
+        cudaStream_t st = stream();
+        SQ_CUDA(cudaMemcpyAsync(g_net.x, x, kIn * 4, cudaMemcpyHostToDevice, st));
+        prof_begin("predictor_forward");
+        fwd_kernel<<<1, kHid, 0, st>>>(g_net.p, g_net.x, 1, nullptr, nullptr, nullptr, nullptr, g_net.y);
+        prof_end(0.0);
+        SQ_CUDA(cudaGetLastError());
+        SQ_CUDA(cudaMemcpyAsync(y, g_net.y, kOut * 4, cudaMemcpyDeviceToHost, st));
+        SQ_CUDA(cudaStreamSynchronize(st));
+    }
+    host_decision(y, kOut * 4);
     ++g_predictions;
     return true;
 }
@@ -301,8 +304,7 @@ int sq_predictor_get_params(float* out, uint64_t n) {
     SQP_BEGIN
     if (!out || n != (uint64_t)kParams) fail(SQ_ERR_INVALID, "predictor: need SQ_PRED_PARAMS floats");
     ensure_net();
-    SQ_CUDA(cudaMemcpyAsync(out, g_net.p, kParams * 4, cudaMemcpyDeviceToHost, stream()));
-    SQ_CUDA(cudaStreamSynchronize(stream()));
+    host_read(out, g_net.p, kParams * 4);
     SQP_END
 }
 
@@ -331,8 +333,7 @@ int sq_predictor_gradient(const float* x, const float* t, uint64_t n, float* gra
     SQ_CUDA(cudaGetLastError());
     SQ_CUDA(cudaMemcpyAsync(grad, g_net.g, kParams * 4, cudaMemcpyDeviceToHost, st));
     float l = 0.f;
-    SQ_CUDA(cudaMemcpyAsync(&l, g_net.loss, 4, cudaMemcpyDeviceToHost, st));
-    SQ_CUDA(cudaStreamSynchronize(st));
+    host_read(&l, g_net.loss, 4);
     if (loss) *loss = l;
     SQP_END
 }
@@ -347,8 +348,7 @@ int sq_predictor_predict(const float* x, uint64_t n, float* y) {
     fwd_kernel<<<(unsigned)n, kHid, 0, st>>>(g_net.p, g_net.x, (int)n, nullptr, nullptr, nullptr, nullptr, g_net.y);
     count_launch();
     SQ_CUDA(cudaGetLastError());
-    SQ_CUDA(cudaMemcpyAsync(y, g_net.y, n * kOut * 4, cudaMemcpyDeviceToHost, st));
-    SQ_CUDA(cudaStreamSynchronize(st));
+    host_read(y, g_net.y, n * kOut * 4);
     SQP_END
 }
 
@@ -399,8 +399,7 @@ int sq_predictor_train(const float* x, const float* t, uint64_t n, uint32_t epoc
             SQ_CUDA(cudaStreamSynchronize(st));  // the permutation buffer is rewritten next epoch
         }
         float l = 0.f;
-        SQ_CUDA(cudaMemcpyAsync(&l, g_net.loss, 4, cudaMemcpyDeviceToHost, st));
-        SQ_CUDA(cudaStreamSynchronize(st));
+        host_read(&l, g_net.loss, 4);
         if (final_loss) *final_loss = l;
     } catch (...) {
         if (exec) cudaGraphExecDestroy(exec);

@@ -177,8 +177,7 @@ int radix_sort_pairs(KeyT* k[2], unsigned* v[2], uint64_t n, int bits) {
     prof_end((double)n * sizeof(KeyT));
     SQ_CUDA(cudaGetLastError());
     std::vector<unsigned> h((size_t)passes * kRadix);
-    SQ_CUDA(cudaMemcpyAsync(h.data(), hist, h.size() * 4, cudaMemcpyDeviceToHost, stream()));
-    SQ_CUDA(cudaStreamSynchronize(stream()));
+    host_read(h.data(), hist, h.size() * 4);
     std::vector<int> live;
     std::vector<unsigned> bases((size_t)passes * kRadix);
     for (int p = 0; p < passes; ++p) {
@@ -194,7 +193,7 @@ int radix_sort_pairs(KeyT* k[2], unsigned* v[2], uint64_t n, int bits) {
     }
     if (live.empty()) return 0;
     unsigned* dbase = hist + (size_t)8 * kRadix;
-    SQ_CUDA(cudaMemcpyAsync(dbase, bases.data(), bases.size() * 4, cudaMemcpyHostToDevice, stream()));
+    h2d_small(dbase, bases.data(), bases.size() * 4);
     const unsigned ntiles = (unsigned)((n + kRsTile - 1) / kRsTile);
     const size_t per_pass = (size_t)ntiles * kRadix + 64;  // status + counter
     unsigned* lb = (unsigned*)ws().get(WS_LOOKBACK, per_pass * live.size() * 4);

@@ -215,8 +215,90 @@ static cudaEvent_t take_event() {
     return e;
 }
 
+// ------------------------------------------------------------------ record / replay
+// A sequence of operators is turned into a CUDA graph in two passes. The
+// record pass runs it eagerly and logs every value the host reads back (group
+// and output counts, histograms, flags). The capture pass issues the same
+// calls under stream capture: each read returns the logged value instead of
+// waiting for the device, and a one-block check compares it on the device with
+// what the replayed kernels actually produced (error bit 5: the replay is
+// invalid). Allocation, freeing and synchronisation are refused or skipped
+// while capturing; the record pass has grown every buffer the sequence needs.
+static ReplayState g_replay;
+ReplayState& replay() { return g_replay; }
+bool capturing() { return g_replay.mode == RP_CAPTURE; }
+
+struct ReplayBytes {
+    unsigned n;
+    unsigned char b[kReplayReadMax];
+};
+__global__ void replay_check_kernel(const unsigned char* __restrict__ src, const __grid_constant__ ReplayBytes want,
+                                    unsigned* err) {
+    for (unsigned i = threadIdx.x; i < want.n; i += blockDim.x)
+        if (src[i] != want.b[i]) atomicOr(err, 32u);
+}
+
+void host_read(void* dst, const void* src, size_t bytes) {
+    ReplayState& r = g_replay;
+    if (r.mode == RP_CAPTURE) {
+        if (bytes > kReplayReadMax) fail(SQ_ERR_UNSUPPORTED, "capture: a read-back larger than a replay check holds");
+        if (r.pos + bytes > r.log.size()) fail(SQ_ERR_INVALID, "capture: the operators differ from the recorded ones");
+        memcpy(dst, r.log.data() + r.pos, bytes);
+        r.pos += bytes;
+        ReplayBytes w;
+        w.n = (unsigned)bytes;
+        memcpy(w.b, dst, bytes);
+        replay_check_kernel<<<1, 128, 0, stream()>>>(static_cast<const unsigned char*>(src), w, device_error_word());
+        SQ_CUDA(cudaGetLastError());
+        count_launch();
+        return;
+    }
+    SQ_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream()));
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+    if (r.mode == RP_RECORD) {
+        const unsigned char* b = static_cast<const unsigned char*>(dst);
+        r.log.insert(r.log.end(), b, b + bytes);
+    }
+}
+
+void host_decision(void* v, size_t bytes) {
+    ReplayState& r = g_replay;
+    if (r.mode == RP_CAPTURE) {
+        if (r.pos + bytes > r.log.size()) fail(SQ_ERR_INVALID, "capture: the operators differ from the recorded ones");
+        memcpy(v, r.log.data() + r.pos, bytes);
+        r.pos += bytes;
+    } else if (r.mode == RP_RECORD) {
+        const unsigned char* b = static_cast<const unsigned char*>(v);
+        r.log.insert(r.log.end(), b, b + bytes);
+    }
+}
+
+__global__ void param_copy_kernel(unsigned char* __restrict__ dst, const __grid_constant__ ReplayBytes src) {
+    for (unsigned i = threadIdx.x; i < src.n; i += blockDim.x) dst[i] = src.b[i];
+}
+
+void h2d_small(void* dst, const void* src, size_t bytes) {
+    if (!capturing()) {
+        SQ_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream()));
+        return;
+    }
+    // a captured copy from host memory would read it at every replay: the
+    // bytes travel as a kernel parameter instead, baked into the graph
+    if (bytes > kReplayReadMax) fail(SQ_ERR_UNSUPPORTED, "capture: a host-to-device copy larger than a parameter block");
+    ReplayBytes b;
+    b.n = (unsigned)bytes;
+    memcpy(b.b, src, bytes);
+    param_copy_kernel<<<1, 128, 0, stream()>>>(static_cast<unsigned char*>(dst), b);
+    SQ_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+void sync_library_stream() {
+    if (!capturing()) SQ_CUDA(cudaStreamSynchronize(stream()));
+}
+
 void prof_begin(const char* name) {
-    if (!g_prof) return;
+    if (!g_prof || capturing()) return;
     g_open_name = name;
     g_open_event = take_event();
     SQ_CUDA(cudaEventRecord(g_open_event, stream()));
@@ -224,7 +306,7 @@ void prof_begin(const char* name) {
 
 void prof_end(double alg_bytes) {
     count_launch();
-    if (!g_prof || !g_open_event) return;
+    if (!g_prof || !g_open_event || capturing()) return;
     cudaEvent_t b = take_event();
     SQ_CUDA(cudaEventRecord(b, stream()));
     g_pending.push_back(ProfRec{g_open_name, g_open_event, b, alg_bytes});
@@ -270,6 +352,7 @@ double prof_ms(size_t i) { return g_stats[i].second.ms; }
 double prof_bytes(size_t i) { return g_stats[i].second.bytes; }
 
 void* dev_alloc(size_t bytes) {
+    if (capturing()) fail(SQ_ERR_UNSUPPORTED, "capture: a buffer would grow; the record pass must run the same operators");
     if (bytes == 0) bytes = 16;
     void* p = nullptr;
     cudaError_t e = cudaMallocAsync(&p, bytes, stream());
@@ -281,6 +364,7 @@ void* dev_alloc(size_t bytes) {
 }
 
 void dev_free(void* p) {
+    if (p && capturing()) fail(SQ_ERR_UNSUPPORTED, "capture: a buffer would be freed");
     if (p) SQ_CUDA(cudaFreeAsync(p, stream()));
 }
 
@@ -468,7 +552,10 @@ void sync_words(State& s) {
     if (s.live.kalloc < k) ensure_buffers(s.live, s.live.cap, k, s.n);
 }
 
-void swap_live_spare(State& s) { std::swap(s.live, s.spare); }
+void swap_live_spare(State& s) {
+    std::swap(s.live, s.spare);
+    ++s.swaps;
+}
 
 // ------------------------------------------------------------------ workspace
 static Workspace g_ws;

@@ -203,6 +203,7 @@ struct State {
     Buffers spare;
     uint64_t n = 0;
     GroupCache groups;
+    uint64_t swaps = 0;              // live/spare exchanges so far (graphs need an even number per sequence)
     cudaEvent_t d2h_done = nullptr;  // recorded when the last asynchronous download finished reading
     bool d2h_pending = false;        // the library stream has not been made to wait for it yet
 };
@@ -243,6 +244,29 @@ void count_launch(int n = 1);
 // Bracket one kernel launch: prof_begin(name); kernel<<<...>>>(...); prof_end(bytes);
 // prof_end() also counts the launch; `bytes` is the launch's algorithmic
 // (compulsory) HBM traffic, used for the roofline.
+// Record / replay of host decisions (graph capture of operator sequences).
+enum ReplayMode { RP_OFF = 0, RP_RECORD = 1, RP_CAPTURE = 2 };
+constexpr size_t kReplayReadMax = 8192;
+struct ReplayState {
+    int mode = RP_OFF;
+    std::vector<unsigned char> log;
+    size_t pos = 0;
+};
+ReplayState& replay();
+bool capturing();
+// `bytes` device bytes into host memory, after the work queued before them:
+// a read-back (logged when recording); under capture the logged bytes, with a
+// device-side check that the replay produces the same.
+void host_read(void* dst, const void* src, size_t bytes);
+// A host-side choice (autotuning, timing-dependent paths): logged when
+// recording, taken from the log under capture.
+void host_decision(void* v, size_t bytes);
+// A small host-to-device copy (parameters, counters' initial values) on the
+// library stream; under capture the bytes go into the graph as a kernel
+// parameter (at most kReplayReadMax bytes).
+void h2d_small(void* dst, const void* src, size_t bytes);
+// cudaStreamSynchronize on the library stream; nothing under capture.
+void sync_library_stream();
 void prof_begin(const char* name);
 void prof_end(double alg_bytes = 0.0);
 void prof_add_bytes_last(double alg_bytes);
