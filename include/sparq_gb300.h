@@ -256,13 +256,16 @@ int sq_state_wait(sq_state* st);
  *    again), then sq_graph_capture_begin(st); apply the same operators (they
  *    are captured, not run, and take the logged counts); sq_graph_capture_end.
  * 3. For every replay: bring the state to the same input and call
- *    sq_graph_launch (asynchronous). Each logged count is checked on the
- *    device; a replay whose counts differ from the recorded ones is reported
- *    as SQ_ERR_INVALID at the next synchronising call and leaves the state
- *    invalid. A launch is refused when the state's size or buffers, or the
- *    library's workspace, differ from those captured. Tables used by the
- *    operators (QRAM, lookup, noise) must outlive the graph. Allocation is
- *    refused while capturing: the record pass grows every buffer. */
+ *    sq_graph_launch. Every count, offset and size in the graph was recorded
+ *    for one input, so a launch is refused (SQ_ERR_INVALID, before anything
+ *    runs) unless the state's entries and the content of every table the
+ *    operators read (QRAM, lookup, noise) have the checksums they had when
+ *    recorded, and the state's buffers and the library's workspace are those
+ *    captured; the checksums cost one reduction and one synchronisation. The
+ *    logged counts are also checked on the device (a mismatch is reported as
+ *    SQ_ERR_INVALID at the next synchronising call). Tables must outlive the
+ *    graph. Allocation is refused while capturing: the record pass grows
+ *    every buffer. */
 typedef struct sq_graph sq_graph;
 int sq_graph_record_begin(sq_state* st);
 int sq_graph_record_end(void);
@@ -270,6 +273,11 @@ int sq_graph_capture_begin(sq_state* st);
 int sq_graph_capture_end(sq_graph** out);
 int sq_graph_launch(sq_graph* g);
 int sq_graph_destroy(sq_graph* g);
+/* Diagnostics: the captured graph as a DOT file with every node's parameters
+ * (cudaGraphDebugDotPrint, verbose), and a text listing of a state's buffers,
+ * group-range sets and the library's workspace slots. */
+int sq_graph_debug_dot(const sq_graph* g, const char* path);
+int sq_state_debug_layout(const sq_state* st, char* buf, uint64_t len);
 /* Device pointers of the live arrays (valid until the next call that resizes). */
 int sq_state_device_arrays(sq_state* st, uint64_t** key_words, uint32_t* k, double** amps);
 
@@ -281,6 +289,12 @@ int sq_state_device_arrays(sq_state* st, uint64_t** key_words, uint32_t* k, doub
  * of u16/u32/u64 that holds every word. */
 int sq_qram_create(uint32_t address_size, uint32_t data_size, const uint64_t* memory, uint64_t n_words,
                    sq_qram** out);
+/* New words for an existing table (2^address_size of them), written in place
+ * on the library stream: launches queued or captured earlier keep reading the
+ * same device table. The words must fit the width the table was stored at
+ * (that of the words it was created with); otherwise SQ_ERR_INVALID and the
+ * table's content is unspecified. */
+int sq_qram_write(sq_qram* q, const uint64_t* memory, uint64_t n_words);
 int sq_qram_destroy(sq_qram* q);
 /* A classical function table for SQ_OP_LOOKUP_XOR: f(v) = dense[v] for
  * v < dense_len, words[i] for v == keys[i] (keys ascending, unique, each >=

@@ -6,7 +6,7 @@ device is visible, calls raise instead of computing anything on the host.
 from __future__ import annotations
 
 import ctypes
-from ctypes import POINTER, c_double, c_float, c_int, c_uint32, c_uint64, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_uint32, c_uint64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().with_name("libsparq_gb300.so")
@@ -111,8 +111,11 @@ _SIGS = [
     ("sq_graph_capture_end", c_int, [POINTER(c_void_p)]),
     ("sq_graph_launch", c_int, [c_void_p]),
     ("sq_graph_destroy", c_int, [c_void_p]),
+    ("sq_graph_debug_dot", c_int, [c_void_p, c_char_p]),
+    ("sq_state_debug_layout", c_int, [c_void_p, c_char_p, c_uint64]),
     ("sq_state_device_arrays", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_uint32), POINTER(c_void_p)]),
     ("sq_qram_create", c_int, [c_uint32, c_uint32, c_void_p, c_uint64, POINTER(c_void_p)]),
+    ("sq_qram_write", c_int, [c_void_p, c_void_p, c_uint64]),
     ("sq_qram_destroy", c_int, [c_void_p]),
     ("sq_lookup_create", c_int, [c_void_p, c_uint64, c_void_p, c_void_p, c_uint64, POINTER(c_void_p)]),
     ("sq_qw_rotate_angle_words", c_int, [c_void_p, c_uint64, c_uint32, c_int, c_uint32, c_void_p]),

@@ -323,6 +323,18 @@ class QRAMCircuit_qutrit:
         call("sq_qram_create", self.address_size, self.data_size, mem.ctypes.data_as(c_void_p), mem.size, byref(h))
         self._h = h
 
+    def write(self, memory) -> None:
+        """New table words, written in place (launches queued or captured earlier
+        keep reading the same device table); they must fit the table's stored
+        width. `memory` may be a NumPy array or the address of 2^address_size
+        uint64 words (pinned memory for full speed)."""
+        if isinstance(memory, int):
+            call("sq_qram_write", self._h, c_void_p(memory), 1 << self.address_size)
+            return
+        mem = np.ascontiguousarray(np.asarray(memory, dtype=np.uint64))
+        call("sq_qram_write", self._h, mem.ctypes.data_as(c_void_p), mem.size)
+        self.memory = mem
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:

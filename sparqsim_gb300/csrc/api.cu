@@ -415,7 +415,10 @@ int sq_state_wait(sq_state* st) {
 
 // ------------------------------------------------------------------ graphs
 struct sq_graph {
+    cudaGraph_t graph = nullptr;  // kept for inspection (sq_graph_debug_dot)
     cudaGraphExec_t exec = nullptr;
+    uint64_t input_sum = 0, table_sum = 0;  // the recorded input state and tables
+    std::vector<std::pair<const void*, size_t>> tables;
     sq_state* st = nullptr;
     State pre, post;  // the state's host-side fields before and after the captured operators
     void* ws_p[16] = {nullptr};
@@ -443,6 +446,18 @@ static bool same_layout(const State& a, const State& b) {
 static sq_state* g_record_state = nullptr;
 static uint64_t g_record_swaps = 0;
 static int g_record_cur = 0;
+static uint64_t g_record_input_sum = 0;   // the state the recording started from
+static uint64_t g_record_table_sum = 0;   // the tables its operators read
+static std::vector<std::pair<const void*, size_t>> g_record_tables;
+
+// Checksum of a state's entries (key words and amplitudes): a replay runs only
+// on the input it was recorded with, so that every recorded count holds.
+static uint64_t state_checksum(const State& s) {
+    std::vector<std::pair<const void*, size_t>> spans;
+    for (uint32_t w = 0; w < s.live.kalloc; ++w) spans.emplace_back(s.live.keys[w], (size_t)s.n * 8);
+    spans.emplace_back(s.live.amp, (size_t)s.n * 16);
+    return device_checksum(spans);
+}
 
 int sq_graph_record_begin(sq_state* st) {
     SQ_API_BEGIN
@@ -451,7 +466,9 @@ int sq_graph_record_begin(sq_state* st) {
     g_record_state = st;
     g_record_swaps = s.swaps;
     g_record_cur = s.groups.cur;
+    g_record_input_sum = state_checksum(s);
     replay().log.clear();
+    replay().inputs.clear();
     replay().pos = 0;
     replay().mode = RP_RECORD;
     SQ_API_END
@@ -466,6 +483,8 @@ int sq_graph_record_end(void) {
     // a replay starts where the previous one ended: the buffers must be back in their roles
     need((s.swaps - g_record_swaps) % 2 == 0 && s.groups.cur == g_record_cur,
          "graph: the operators leave the state's buffers in other roles (an odd number of splits)");
+    g_record_tables = replay().inputs;
+    g_record_table_sum = device_checksum(g_record_tables);
     SQ_API_END
 }
 
@@ -474,6 +493,7 @@ int sq_graph_capture_begin(sq_state* st) {
     need(replay().mode == RP_OFF, "graph: a record or capture is already open");
     State& s = S(st);
     SQ_CUDA(cudaStreamSynchronize(stream()));
+    need(state_checksum(s) == g_record_input_sum, "graph: the capture does not start from the recorded input");
     g_capture_pre = s;
     for (int i = 0; i < 16; ++i) g_capture_ws[i] = ws().p[i];
     g_capture_launch0 = launches();
@@ -512,12 +532,16 @@ int sq_graph_capture_end(sq_graph** out) {
     }
     sq_graph* gr = new sq_graph();
     const cudaError_t ie = cudaGraphInstantiate(&gr->exec, g, 0);
-    cudaGraphDestroy(g);
+    gr->graph = g;
     if (ie != cudaSuccess) {
+        cudaGraphDestroy(g);
         delete gr;
         fail(SQ_ERR_CUDA, std::string("graph: instantiate failed: ") + cudaGetErrorString(ie));
     }
     gr->st = st;
+    gr->input_sum = g_record_input_sum;
+    gr->table_sum = g_record_table_sum;
+    gr->tables = g_record_tables;
     gr->pre = g_capture_pre;
     gr->post = post;
     for (int i = 0; i < 16; ++i) gr->ws_p[i] = g_capture_ws[i];
@@ -533,6 +557,11 @@ int sq_graph_launch(sq_graph* g) {
     State& s = S(g->st);
     need(same_layout(s, g->pre), "graph: the state's size or buffers differ from the captured ones");
     for (int i = 0; i < 16; ++i) need(ws().p[i] == g->ws_p[i], "graph: the library's workspace has been reallocated");
+    // every count and offset in the graph was recorded for one input: other
+    // data could take other sizes, so it is refused before anything runs
+    need(state_checksum(s) == g->input_sum, "graph: the state differs from the input the graph was recorded with");
+    need(device_checksum(g->tables) == g->table_sum,
+         "graph: a table the operators read differs from the one the graph was recorded with");
     SQ_CUDA(cudaGraphLaunch(g->exec, stream()));
     const cudaEvent_t ev = s.d2h_done;
     s = g->post;
@@ -546,7 +575,51 @@ int sq_graph_destroy(sq_graph* g) {
     SQ_API_BEGIN
     if (!g) return SQ_OK;
     if (g->exec) SQ_CUDA(cudaGraphExecDestroy(g->exec));
+    if (g->graph) SQ_CUDA(cudaGraphDestroy(g->graph));
     delete g;
+    SQ_API_END
+}
+
+int sq_graph_debug_dot(const sq_graph* g, const char* path) {
+    SQ_API_BEGIN
+    need(g != nullptr && g->graph != nullptr && path != nullptr, "null pointer");
+    SQ_CUDA(cudaGraphDebugDotPrint(g->graph, path, cudaGraphDebugDotFlagsVerbose));
+    SQ_API_END
+}
+
+int sq_state_debug_layout(const sq_state* st, char* buf, uint64_t len) {
+    SQ_API_BEGIN
+    need(buf != nullptr && len > 0, "null pointer");
+    const State& s = S(st);
+    std::string o;
+    char line[256];
+    auto bufs = [&](const char* name, const Buffers& b) {
+        snprintf(line, sizeof(line), "%s cap=%llu kalloc=%u amp=%p", name, (unsigned long long)b.cap, b.kalloc,
+                 (void*)b.amp);
+        o += line;
+        for (uint32_t w = 0; w < b.kalloc; ++w) {
+            snprintf(line, sizeof(line), " k%u=%p", w, (void*)b.keys[w]);
+            o += line;
+        }
+        o += "\n";
+    };
+    snprintf(line, sizeof(line), "n=%llu swaps=%llu\n", (unsigned long long)s.n, (unsigned long long)s.swaps);
+    o += line;
+    bufs("live", s.live);
+    bufs("spare", s.spare);
+    const GroupCache& c = s.groups;
+    for (int i = 0; i < 2; ++i) {
+        snprintf(line, sizeof(line), "cache%d start=%p cnt=%p cap=%llu\n", i, (void*)c.start[i], (void*)c.cnt[i],
+                 (unsigned long long)c.cap[i]);
+        o += line;
+    }
+    snprintf(line, sizeof(line), "cache valid=%d cur=%d G=%llu\n", (int)c.valid, c.cur, (unsigned long long)c.G);
+    o += line;
+    for (int i = 0; i < 16; ++i) {
+        snprintf(line, sizeof(line), "ws%d=%p size=%zu\n", i, ws().p[i], ws().sz[i]);
+        o += line;
+    }
+    snprintf(buf, len, "%s", o.c_str());
     SQ_API_END
 }
 
@@ -589,6 +662,17 @@ int sq_qram_create(uint32_t address_size, uint32_t data_size, const uint64_t* me
         throw;
     }
     *out = q;
+    SQ_API_END
+}
+
+int sq_qram_write(sq_qram* q, const uint64_t* memory, uint64_t n_words) {
+    SQ_API_BEGIN
+    need(q != nullptr && !q->t.lookup, "not a QRAM table");
+    need(memory != nullptr && n_words >= q->t.n_words, "QRAM memory must hold 2^address_size words");
+    const uint64_t all = qram_rewrite(q->t, memory);
+    const uint64_t fits = q->t.elem_bytes == 2 ? 0xffffull : q->t.elem_bytes == 4 ? 0xffffffffull : ~0ull;
+    if (all & ~fits) fail(SQ_ERR_INVALID, "QRAM write: a word wider than the table's stored width");
+    q->t.max_word = all;
     SQ_API_END
 }
 

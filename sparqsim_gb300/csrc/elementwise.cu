@@ -518,6 +518,7 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
             if (d.f[1].width < 64 && q->max_word > wmask(d.f[1].width))
                 fail(SQ_ERR_INVALID, "QRAMLoad: table word wider than the data register");
             d.table = q->dev;
+            replay_note_input(q->dev, q->n_words * q->elem_bytes);
             d.elem_bytes = q->elem_bytes;
             d.addr_bits = q->address_size;
             break;
@@ -574,6 +575,7 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
             d.table = q->dev;
             d.imm[0] = q->dense_len;
             d.imm[1] = q->n_sparse;
+            replay_note_input(q->dev, q->n_words * 8);
             break;
         }
         case SQ_OP_PARITY_PHASE: R(0); am |= 3u; break;
@@ -583,6 +585,7 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
             if (!q || !q->dev) fail(SQ_ERR_INVALID, "Pauli noise: null mask table");
             if (q->n_words < 6 * in.imm[0]) fail(SQ_ERR_INVALID, "Pauli noise: table smaller than 6 words per trajectory");
             d.table = q->dev;
+            replay_note_input(q->dev, q->n_words * q->elem_bytes);
             d.elem_bytes = q->elem_bytes;
             am |= 3u;
             break;
@@ -653,6 +656,28 @@ __global__ void qram_pack_kernel(const uint64_t* __restrict__ src, uint64_t n, u
 }
 
 static uint32_t width_bytes(uint64_t all) { return all <= 0xffffull ? 2 : (all <= 0xffffffffull ? 4 : 8); }
+
+// New words for an existing table, in place and at its stored width: its
+// device address (held by queued or captured launches) does not change.
+// Returns the OR of the new words.
+uint64_t qram_rewrite(QramTable& t, const uint64_t* host_words) {
+    cudaStream_t st = stream();
+    const uint64_t n = t.n_words;
+    uint64_t* raw = t.elem_bytes == 8 ? static_cast<uint64_t*>(t.dev) : (uint64_t*)dev_alloc(n * 8);
+    unsigned long long* all = (unsigned long long*)dev_alloc(8);
+    SQ_CUDA(cudaMemcpyAsync(raw, host_words, n * 8, cudaMemcpyHostToDevice, st));
+    SQ_CUDA(cudaMemsetAsync(all, 0, 8, st));
+    prof_begin("qram_pack");
+    qram_pack_kernel<<<grid_for(n, 256), 256, 0, st>>>(raw, n, t.elem_bytes, t.dev, all);
+    prof_end((double)n * (8 + (t.elem_bytes == 8 ? 0 : t.elem_bytes)));
+    SQ_CUDA(cudaGetLastError());
+    unsigned long long h = 0;
+    SQ_CUDA(cudaMemcpyAsync(&h, all, 8, cudaMemcpyDeviceToHost, st));
+    SQ_CUDA(cudaStreamSynchronize(st));  // the caller's buffer may go out of scope
+    if (raw != t.dev) dev_free(raw);
+    dev_free(all);
+    return h;
+}
 
 void* qram_upload(const uint64_t* host_words, uint64_t n, uint32_t eb_guess, uint32_t* eb_out, uint64_t* all_out) {
     cudaStream_t st = stream();

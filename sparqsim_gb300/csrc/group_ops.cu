@@ -439,6 +439,22 @@ __device__ __forceinline__ void store_entry(const KeyPtrs& kp, double2* amp, uns
     amp[o] = a;
 }
 
+// An output entry of a split or merge. Outputs past a.capacity are not
+// written: in a consistent run that never happens (the single pass reserves
+// within its capacity, the exact path's offsets sum to its total); a replayed
+// graph fed other data than it recorded could compute offsets past the
+// buffer, and is reported invalid by its count checks.
+template <int K>
+__device__ __forceinline__ void store_out(const EmitArgs& a, unsigned long long o, const uint64_t (&k)[K],
+                                          double2 v) {
+    if (o < a.capacity) store_entry<K>(a.out_keys, a.out_amp, o, k, v);
+}
+template <int K>
+__device__ __forceinline__ void store_out_sign(const EmitArgs& a, unsigned long long o, const uint64_t (&k)[K],
+                                               double2 v, bool negate) {
+    if (o < a.capacity) store_entry_sign<K>(a.out_keys, a.out_amp, o, k, v, negate);
+}
+
 __device__ __forceinline__ double as_rational(uint64_t v, unsigned w) {
     if (w >= 64) return v * 1.0 / 2 / 9223372036854775808.0;
     return 1.0 * v / (double)(1ull << w);
@@ -587,11 +603,11 @@ __global__ void __launch_bounds__(256) emit_pair_kernel(const __grid_constant__ 
         for (int w = 0; w < K; ++w) kk[w] = k0[w];
         if (kz) {
             fset<K>(kk, a.target, 0);
-            store_entry<K>(a.out_keys, a.out_amp, o++, kk, rz);
+            store_out<K>(a, o++, kk, rz);
         }
         if (ko) {
             fset<K>(kk, a.target, 1);
-            store_entry<K>(a.out_keys, a.out_amp, o, kk, ro);
+            store_out<K>(a, o, kk, ro);
         }
     }
 }
@@ -613,7 +629,7 @@ __global__ void __launch_bounds__(256) emit_merge_kernel(const __grid_constant__
         } else if (keep) {
             uint64_t k0[K];
             load_key<K>(a.in_keys, e0, k0);
-            store_entry<K>(a.out_keys, a.out_amp, a.off[g], k0, acc);
+            store_out<K>(a, a.off[g], k0, acc);
         }
     }
 }
@@ -742,7 +758,7 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
 #pragma unroll
                     for (int w = 0; w < K; ++w) kk[w] = gk[w];
                     fset<K>(kk, tg, (uint64_t)c);
-                    store_entry_sign<K>(a.out_keys, a.out_amp, o + c, kk, base, __popcll((uint64_t)c & v0) & 1);
+                    store_out_sign<K>(a, o + c, kk, base, __popcll((uint64_t)c & v0) & 1);
                 }
             }
             worker_sync<W>();
@@ -881,7 +897,7 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
 #pragma unroll
                 for (int w = 0; w < K; ++w) kk[w] = gk[w];
                 fset<K>(kk, tg, (uint64_t)c);
-                store_entry<K>(a.out_keys, a.out_amp, o + kept + rank, kk, slots[c]);
+                store_out<K>(a, o + kept + rank, kk, slots[c]);
             }
             kept += tot;
         }
@@ -1066,8 +1082,8 @@ __global__ void __launch_bounds__(256) emit_small_kernel(const __grid_constant__
 #pragma unroll
             for (int w = 0; w < K; ++w) kk[w] = gk[w];
             fset<K>(kk, a.target, (uint64_t)c);
-            if (single) store_entry_sign<K>(a.out_keys, a.out_amp, o, kk, base, __popcll((uint64_t)c & v0) & 1);
-            else store_entry<K>(a.out_keys, a.out_amp, o, kk, v[c]);
+            if (single) store_out_sign<K>(a, o, kk, base, __popcll((uint64_t)c & v0) & 1);
+            else store_out<K>(a, o, kk, v[c]);
             ++o;
         }
     }
@@ -1158,7 +1174,7 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
 #pragma unroll
                     for (int w = 0; w < K; ++w) kk[w] = gk[w];
                     fset<K>(kk, tg, (uint64_t)c);
-                    store_entry_sign<K>(a.out_keys, a.out_amp, o + c, kk, base, __popcll((uint64_t)c & v0) & 1);
+                    store_out_sign<K>(a, o + c, kk, base, __popcll((uint64_t)c & v0) & 1);
                 }
             }
             __syncthreads();
@@ -1337,7 +1353,7 @@ __global__ void __launch_bounds__(256, 2) emit_h4096_kernel(const __grid_constan
 #pragma unroll
                 for (int w = 0; w < K; ++w) kk[w] = gk[w];
                 fset<K>(kk, tg, (uint64_t)(((unsigned)j << 8) | tid));
-                store_entry<K>(a.out_keys, a.out_amp, o + s_cnt[j][warp] + __popc(ball[j] & lt), kk, v[j]);
+                store_out<K>(a, o + s_cnt[j][warp] + __popc(ball[j] & lt), kk, v[j]);
             }
         }
         __syncthreads();
@@ -1425,7 +1441,7 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
 #pragma unroll
                     for (int w = 0; w < K; ++w) kk[w] = gk[w];
                     fset<K>(kk, tg, (uint64_t)c);
-                    store_entry_sign<K>(a.out_keys, a.out_amp, o + c, kk, base, __popcll((uint64_t)c & v0) & 1);
+                    store_out_sign<K>(a, o + c, kk, base, __popcll((uint64_t)c & v0) & 1);
                 }
             }
             __syncthreads();
@@ -1604,7 +1620,7 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
 #pragma unroll
                 for (int w = 0; w < K; ++w) kk[w] = gk[w];
                 fset<K>(kk, tg, (uint64_t)(((unsigned)j << 9) | tid));
-                store_entry<K>(a.out_keys, a.out_amp, o + s_cnt[j][warp] + __popc(ball[j] & lt), kk, v[j]);
+                store_out<K>(a, o + s_cnt[j][warp] + __popc(ball[j] & lt), kk, v[j]);
             }
         }
         __syncthreads();
@@ -2823,6 +2839,7 @@ static void run_group(State& s, const GroupSpec& gs) {
     ensure_buffers(s.spare, std::max<uint64_t>(out_n, 1), regtable().k, 0);
     for (int w = 0; w < SQ_KMAX; ++w) ea.out_keys.w[w] = s.spare.keys[w];
     ea.out_amp = s.spare.amp;
+    ea.capacity = T;
     launch_emit(true);
     if (F) {
         prof_begin("passthrough");

@@ -158,8 +158,15 @@ __global__ void __launch_bounds__(kRsBlock) rs_onesweep_kernel(const KeyT* __res
         const KeyT k = s_k[p];
         const unsigned dd = (unsigned)(k >> shift) & 0xffu;
         const uint64_t o = (uint64_t)s_gbase[dd] + (p - s_tstart[dd]);
-        kout[o] = k;
-        vout[o] = s_v[p];
+        // digit bases computed on the host from this sort's histogram: a
+        // replayed graph whose keys differ from the recorded ones could point
+        // past the end (its replay is reported invalid; nothing is written there)
+        if (o < n) {
+            kout[o] = k;
+            vout[o] = s_v[p];
+        } else {
+            atomicOr(err, 32u);
+        }
     }
 }
 

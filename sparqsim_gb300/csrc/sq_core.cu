@@ -293,6 +293,56 @@ void h2d_small(void* dst, const void* src, size_t bytes) {
     count_launch();
 }
 
+void replay_note_input(const void* p, size_t bytes) {
+    ReplayState& r = g_replay;
+    if (r.mode == RP_OFF || !p || !bytes) return;
+    for (const auto& s : r.inputs)
+        if (s.first == p) return;
+    r.inputs.emplace_back(p, bytes);
+}
+
+__device__ __forceinline__ unsigned long long cs_mix(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+// Sum over the span's 8-byte words (and its tail bytes) of a mix of the word,
+// its position and the span's salt: independent of the summation order.
+__global__ void checksum_kernel(const unsigned char* __restrict__ p, uint64_t bytes, unsigned long long salt,
+                                unsigned long long* acc) {
+    const uint64_t n8 = bytes / 8;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    unsigned long long local = 0;
+    const unsigned long long* w = reinterpret_cast<const unsigned long long*>(p);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += stride)
+        local += cs_mix(w[i] ^ (i * 0x9e3779b97f4a7c15ull) ^ salt);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        for (uint64_t b = n8 * 8; b < bytes; ++b) local += cs_mix((unsigned long long)p[b] ^ (b << 8) ^ ~salt);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31u) == 0 && local) atomicAdd(acc, local);
+}
+
+uint64_t device_checksum(const std::vector<std::pair<const void*, size_t>>& spans) {
+    cudaStream_t st = stream();
+    unsigned long long* acc = (unsigned long long*)dev_alloc(8);
+    SQ_CUDA(cudaMemsetAsync(acc, 0, 8, st));
+    unsigned long long salt = 0x2545f4914f6cdd1dull;
+    for (const auto& s : spans) {
+        salt = salt * 6364136223846793005ull + 1442695040888963407ull;
+        if (!s.first || !s.second) continue;
+        if (reinterpret_cast<uintptr_t>(s.first) & 7) fail(SQ_ERR_INVALID, "checksum: unaligned span");
+        checksum_kernel<<<grid_for(s.second / 8 + 1, 256), 256, 0, st>>>(static_cast<const unsigned char*>(s.first),
+                                                                        s.second, salt, acc);
+        SQ_CUDA(cudaGetLastError());
+    }
+    unsigned long long h = 0;
+    SQ_CUDA(cudaMemcpyAsync(&h, acc, 8, cudaMemcpyDeviceToHost, st));
+    SQ_CUDA(cudaStreamSynchronize(st));
+    dev_free(acc);
+    return h;
+}
+
 void sync_library_stream() {
     if (!capturing()) SQ_CUDA(cudaStreamSynchronize(stream()));
 }

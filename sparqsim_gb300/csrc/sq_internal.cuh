@@ -12,6 +12,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "sparq_gb300.h"
@@ -230,6 +231,9 @@ void sync_async_copies();
 // Copy a host table of 64-bit words to the device at the narrowest width (2,
 // 4 or 8 bytes) that holds every word; eb_guess is tried first.
 void* qram_upload(const uint64_t* host_words, uint64_t n, uint32_t eb_guess, uint32_t* eb_out, uint64_t* all_out);
+// New words for an existing table (same size), written in place at its stored
+// width; returns the OR of the new words.
+uint64_t qram_rewrite(QramTable& t, const uint64_t* host_words);
 
 struct KeyPtrs {
     uint64_t* w[SQ_KMAX];
@@ -251,6 +255,7 @@ struct ReplayState {
     int mode = RP_OFF;
     std::vector<unsigned char> log;
     size_t pos = 0;
+    std::vector<std::pair<const void*, size_t>> inputs;  // device tables the recorded operators read
 };
 ReplayState& replay();
 bool capturing();
@@ -265,6 +270,11 @@ void host_decision(void* v, size_t bytes);
 // library stream; under capture the bytes go into the graph as a kernel
 // parameter (at most kReplayReadMax bytes).
 void h2d_small(void* dst, const void* src, size_t bytes);
+// Notes a device table read by an operator being recorded or captured (a
+// replay is only allowed when its content is unchanged).
+void replay_note_input(const void* p, size_t bytes);
+// Order-independent 64-bit checksum of device byte spans (synchronises).
+uint64_t device_checksum(const std::vector<std::pair<const void*, size_t>>& spans);
 // cudaStreamSynchronize on the library stream; nothing under capture.
 void sync_library_stream();
 void prof_begin(const char* name);

@@ -1,8 +1,7 @@
 """Operator sequences replayed as CUDA graphs (sq_graph_*): a replay gives
 the eager run's state bit for bit (batched noisy trajectories and the
-register circuit), replays repeat, a replay whose split sizes differ from
-the recorded ones is reported, and a launch on a state of another size is
-refused."""
+register circuit), replays repeat, and a replay on another input, on a
+changed table or on a state of another size is refused before it runs."""
 from __future__ import annotations
 
 import numpy as np
@@ -71,10 +70,11 @@ def test_register_circuit_graph_replay_and_launch_count():
     assert np.array_equal(got_k, want_k) and np.array_equal(got_a, want_a)
 
 
-def test_replay_on_other_split_sizes_is_reported():
-    """Recorded on four entries that form one Hadamard group, replayed on four
-    entries that form four groups: the device check reports it. (Two
-    Hadamards: a graph needs an even number of splits; one is refused.)"""
+def test_replay_on_other_input_is_refused():
+    """Recorded on four entries that form one Hadamard group; a replay on four
+    entries that form four groups (same size, other data) is refused before
+    anything runs, as is a launch on a state of another size. (Two Hadamards:
+    a graph needs an even number of splits; one is refused.)"""
     ps.System.clear()
     a = ps.System.add_register("a", ps.UnsignedInteger, 2)
     b = ps.System.add_register("b", ps.UnsignedInteger, 4)
@@ -94,8 +94,46 @@ def test_replay_on_other_split_sizes_is_reported():
     inp["regs"] = four_groups
     with pytest.raises(ps.SparQInvalid):
         g.replay()
-        ps.synchronize()
-    # a launch on a state of another size is refused before it runs
+    inp["regs"] = one_group
+    g.replay()  # the recorded input again: allowed
+    ps.synchronize()
+    assert st.size() == 4
     st.upload(np.zeros((3, 2), dtype=np.uint64) + np.arange(3, dtype=np.uint64)[:, None], np.ones(3) / np.sqrt(3))
     with pytest.raises(ps.SparQInvalid):
         g.launch()
+
+
+def test_qram_write_in_place_and_replay_guard():
+    """A captured graph reads the QRAM table where it is and only runs on the
+    table content it was recorded with: after new words are written the
+    replay is refused; writing the recorded words back (in place) makes it
+    valid again, equal to an eager run; a word wider than the stored width is
+    refused."""
+    ps.System.clear()
+    a = ps.System.add_register("a", ps.UnsignedInteger, 6)
+    b = ps.System.add_register("b", ps.UnsignedInteger, 16)
+    rng = np.random.default_rng(3)
+    t1 = rng.integers(0, 1 << 16, 64, dtype=np.uint64)
+    t2 = rng.integers(0, 1 << 16, 64, dtype=np.uint64)
+    q = ps.QRAMCircuit_qutrit(6, 16, t1)
+    ops = [ps.Hadamard_Int(a, 6), ps.QRAMLoad(q, a, b), ps.Phase_Bool(b, 3, 0.5), ps.Hadamard_Int(a, 6)]
+    st = ps.SparseState()
+
+    def apply():
+        for o in ops:
+            o(st)
+
+    g = ps.Graph(st, apply, st.reset)
+    st.reset()
+    apply()
+    want_k, want_a = _canon(st)
+    q.write(t2)
+    with pytest.raises(ps.SparQInvalid):
+        g.replay()
+    q.write(t1)
+    g.replay()
+    ps.synchronize()
+    got_k, got_a = _canon(st)
+    assert np.array_equal(got_k, want_k) and np.array_equal(got_a, want_a)
+    with pytest.raises(ps.SparQInvalid):
+        q.write(np.full(64, 1 << 20, dtype=np.uint64))
