@@ -619,18 +619,26 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     graphs = [ps.Graph(st, apply=lambda: circ.run(st, reset=False), prepare=st.reset),
               ps.Graph(s2, apply=lambda: circ.run(s2, reset=False), prepare=s2.reset)]
     e2e_steps = max(2, min(args.steps, 20))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for i in range(e2e_steps):
-        s_i = states[i % 2]
-        circ.qram.write(host_table.data_ptr())  # the step's table, in place (the graphs read it there)
-        _native.call("sq_state_upload_packed", s_i._h, 1, init_keys.data_ptr(), init_amp.data_ptr())
-        graphs[i % 2].launch()
-        s_i.download_packed_async(host_keys[i % 2].data_ptr(), host_amps[i % 2].data_ptr())
-    for s_i in states:
-        s_i.wait()
-    ps.synchronize()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+
+    def e2e_loop(engine):
+        ps.set_download_engine(engine)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(e2e_steps):
+            s_i = states[i % 2]
+            circ.qram.write(host_table.data_ptr())  # the step's table, in place (the graphs read it there)
+            _native.call("sq_state_upload_packed", s_i._h, 1, init_keys.data_ptr(), init_amp.data_ptr())
+            graphs[i % 2].launch()
+            s_i.download_packed_async(host_keys[i % 2].data_ptr(), host_amps[i % 2].data_ptr())
+        for s_i in states:
+            s_i.wait()
+        ps.synchronize()
+        ps.set_download_engine("sm")
+        return (time.perf_counter() - t0) / e2e_steps
+
+    other_engine = "sm" if args.download_engine == "copy" else "copy"
+    e2e_other_s = e2e_loop(other_engine)
+    e2e_s = e2e_loop(args.download_engine)
     del graphs
     # the downloaded result is the state the circuit produced
     gk = host_keys[(e2e_steps - 1) % 2].view(k, final_n)
@@ -670,7 +678,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         f"{other}_arithmetic": ({"value": world * updates / (other_ms / 1e3), "unit": UNIT, "ms_per_step": other_ms}
                                 if other_ms else None),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps,
+                "steps": e2e_steps, "download_engine": args.download_engine,
+                f"{other_engine}_download_engine": {"value": world * updates / e2e_other_s, "unit": UNIT},
                 "note": "public API: QRAM table written in place and initial state uploaded from pinned host "
                         "memory, the circuit launched as one CUDA graph, final packed state downloaded into pinned "
                         "host memory, each step; two states alternate so that a step's download overlaps the next "
@@ -804,6 +813,8 @@ def main():
     ap.add_argument("--hadamard-bits", type=int, default=12)
     ap.add_argument("--layers", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--download-engine", default="copy", choices=["copy", "sm"],
+                    help="how the end-to-end loop's downloads into pinned memory are moved")
     ap.add_argument("--skip-other-arithmetic", action="store_true",
                     help="do not also time the other Hadamard butterfly arithmetic")
     ap.add_argument("--trajectories", type=int, default=4096,

@@ -9,7 +9,7 @@ from ._native import SparQError, SparQInvalid, launch_count
 from .core import (Boolean, General, Graph, QRAMCircuit_qutrit, Rational, SignedInteger, SparseState,
                    StateStorageType, System, UnsignedInteger, get_clearzero_default_eps,
                    autotune_classes, autotune_reset, get_fwht_arithmetic, get_group_strategy,
-                   set_clearzero_default_eps,
+                   set_clearzero_default_eps, set_download_engine,
                    set_fwht_arithmetic, set_group_strategy, set_output_sizing)
 from .operators import *  # noqa: F401,F403
 from .operators import (Abs_SInt, Add_AnyInt_AnyInt_InPlace, Add_ConstUInt_InPlace,

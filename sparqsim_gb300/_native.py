@@ -105,6 +105,7 @@ _SIGS = [
     ("sq_state_download_packed", c_int, [c_void_p, c_void_p, c_void_p]),
     ("sq_state_download_packed_async", c_int, [c_void_p, c_void_p, c_void_p]),
     ("sq_state_wait", c_int, [c_void_p]),
+    ("sq_set_download_engine", c_int, [c_int]),
     ("sq_graph_record_begin", c_int, [c_void_p]),
     ("sq_graph_record_end", c_int, []),
     ("sq_graph_capture_begin", c_int, [c_void_p]),

@@ -190,6 +190,18 @@ def get_fwht_arithmetic() -> str:
     return ["reference", "exact-sum"][v.value]
 
 
+def set_download_engine(engine: str) -> None:
+    """How `SparseState.download_packed_async` moves data into pinned host
+    memory: "sm" (default: a few low-priority blocks store over the host link,
+    leaving the copy engine to the small count reads of eager operators) or
+    "copy" (the copy engine: no SM resources taken from the work it overlaps,
+    the better choice behind graph replays)."""
+    modes = {"sm": 0, "copy": 1}
+    if engine not in modes:
+        raise ValueError(f"download engine must be one of {sorted(modes)}")
+    call("sq_set_download_engine", modes[engine])
+
+
 def set_clearzero_default_eps(eps: float) -> None:
     """clearzero_default_eps (system_operations.h:577)."""
     call("sq_set_clearzero_eps", float(eps))

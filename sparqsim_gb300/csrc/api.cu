@@ -406,6 +406,12 @@ int sq_state_download_packed_async(sq_state* st, uint64_t* keys, double* amps) {
     SQ_API_END
 }
 
+int sq_set_download_engine(int engine) {
+    SQ_API_BEGIN
+    set_d2h_engine(engine);
+    SQ_API_END
+}
+
 int sq_state_wait(sq_state* st) {
     SQ_API_BEGIN
     need(st != nullptr, "null state");

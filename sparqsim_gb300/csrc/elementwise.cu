@@ -671,9 +671,7 @@ uint64_t qram_rewrite(QramTable& t, const uint64_t* host_words) {
     qram_pack_kernel<<<grid_for(n, 256), 256, 0, st>>>(raw, n, t.elem_bytes, t.dev, all);
     prof_end((double)n * (8 + (t.elem_bytes == 8 ? 0 : t.elem_bytes)));
     SQ_CUDA(cudaGetLastError());
-    unsigned long long h = 0;
-    SQ_CUDA(cudaMemcpyAsync(&h, all, 8, cudaMemcpyDeviceToHost, st));
-    SQ_CUDA(cudaStreamSynchronize(st));  // the caller's buffer may go out of scope
+    const uint64_t h = read_word_mapped(all);  // synchronises: the caller's buffer may go out of scope
     if (raw != t.dev) dev_free(raw);
     dev_free(all);
     return h;

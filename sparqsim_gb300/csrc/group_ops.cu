@@ -424,7 +424,39 @@ struct EmitArgs {
     unsigned long long capacity;  // single-pass mode: output entries available; a group whose
                                   // reservation ends past it writes nothing (the host reruns exactly)
     int fix;                   // FWHT arithmetic: 0 the reference's FP64 butterflies, 1 exact sums
+    unsigned long long* ticket;  // dynamic group order: next group, CTAs finished (zero between launches)
 };
+
+// Dynamic group order for the persistent emit kernels. A grid of two CTAs
+// per SM fills the register file; when another stream's blocks hold part of
+// an SM (an overlapped download), a CTA may become resident only when they
+// finish. With groups handed out by a counter such a CTA finds the work done
+// instead of holding back the launch with a fixed share. Thread 0 fetches
+// the next group while the CTA works on the current one (two shared slots,
+// alternating per iteration, each rewritten only after a barrier that
+// follows its last read); the last CTA to finish zeroes the counters.
+__device__ __forceinline__ uint64_t ticket_first(unsigned long long* t, unsigned long long (&s_g)[2]) {
+    if (threadIdx.x == 0) s_g[0] = atomicAdd(&t[0], 1ull);
+    __syncthreads();
+    return s_g[0];
+}
+__device__ __forceinline__ void ticket_prefetch(unsigned long long* t, unsigned long long (&s_g)[2], unsigned it) {
+    if (threadIdx.x == 0) s_g[(it + 1) & 1] = atomicAdd(&t[0], 1ull);
+}
+__device__ __forceinline__ uint64_t ticket_next(unsigned long long (&s_g)[2], unsigned& it) {
+    __syncthreads();
+    ++it;
+    return s_g[it & 1];
+}
+__device__ __forceinline__ void ticket_exit(unsigned long long* t) {
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&t[1], 1ull) == (unsigned long long)gridDim.x - 1ull) {
+            atomicExch(&t[0], 0ull);
+            atomicExch(&t[1], 0ull);
+        }
+    }
+}
 
 template <int K>
 __device__ __forceinline__ void load_key(const ConstKeyPtrs& kp, unsigned e, uint64_t (&k)[K]) {
@@ -1391,10 +1423,13 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
     __shared__ double2 s_ma[64];
     __shared__ unsigned s_emax[16];
     __shared__ bool s_fits;
+    __shared__ unsigned long long s_g[2];
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const Field tg = a.target;
     longlong2* ls = reinterpret_cast<longlong2*>(sl);
-    for (uint64_t g = blockIdx.x; g < a.groups; g += gridDim.x) {
+    unsigned it = 0;
+    for (uint64_t g = ticket_first(a.ticket, s_g); g < a.groups; g = ticket_next(s_g, it)) {
+        ticket_prefetch(a.ticket, s_g, it);
         unsigned s0, m;
         group_range<AM>(a, g, s0, m);
         if (m == 0) {  // an emptied cached range
@@ -1625,6 +1660,7 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
         }
         __syncthreads();
     }
+    ticket_exit(a.ticket);
 }
 
 // Entries that fail the control conditions: copied through unchanged.
@@ -2471,6 +2507,16 @@ static void split_features(State& s, const GroupSpec& gs, uint64_t N, const uint
     for (int i = 0; i < 32; ++i) f[16 + i] = (float)h[i] / 32.f;
 }
 
+// The counters of the dynamic group order (two words, zero between launches).
+static unsigned long long* group_ticket(cudaStream_t st) {
+    static unsigned long long* p = nullptr;
+    if (!p) {
+        p = (unsigned long long*)dev_alloc(16);
+        SQ_CUDA(cudaMemsetAsync(p, 0, 16, st));
+    }
+    return p;
+}
+
 template <int K, int MODE>
 static void launch_h4096_fp64(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
     if (am == 2) emit_h4096_kernel<K, MODE, 2><<<grid, 256, sm, st>>>(ea);
@@ -2727,6 +2773,7 @@ static void run_group(State& s, const GroupSpec& gs) {
     const double E = 8.0 * K + 16.0;
     auto launch_h4096_mode = [&](int mode) {
         const unsigned grid = (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2);
+        ea.ticket = group_ticket(st);
         const size_t sm = 4096 * sizeof(double2);
         prof_begin(mode == EMIT_COUNT ? "emit_h4096_count" : mode == EMIT_WRITE ? "emit_h4096_write" : "emit_h4096_single_pass");
         if (mode == EMIT_COUNT) launch_h4096<K, EMIT_COUNT>(am, grid, sm, st, ea);

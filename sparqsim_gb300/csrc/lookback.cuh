@@ -91,4 +91,15 @@ __device__ __forceinline__ unsigned lb32_load(unsigned* p) {
     return a.load(cuda::memory_order_acquire);
 }
 
+// Relaxed forms for status words that carry their own payload (flag and
+// count in one word): nothing else is published through them.
+__device__ __forceinline__ void lb32_store_relaxed(unsigned* p, unsigned v) {
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> a(*p);
+    a.store(v, cuda::memory_order_relaxed);
+}
+__device__ __forceinline__ unsigned lb32_load_relaxed(unsigned* p) {
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> a(*p);
+    return a.load(cuda::memory_order_relaxed);
+}
+
 }  // namespace sq

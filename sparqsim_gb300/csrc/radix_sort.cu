@@ -2,13 +2,14 @@
 //
 // One histogram kernel reads the keys once and counts every 8-bit digit of
 // every pass; passes whose digit is constant over all keys are skipped. Each
-// remaining pass is one kernel: a tile of 2048 keys is ranked per digit with
-// warp match (stable, in index order), each tile publishes its 256 digit
-// counts and resolves its global offsets by a per-digit decoupled look-back,
-// then the tile is staged in shared memory in digit order so that the global
-// scatter is written as contiguous runs. Per pass the HBM traffic is one read
-// and one write of (key, index).
+// remaining pass is one kernel: a tile of 2048 or 4096 keys is ranked per
+// digit with warp match (stable, in index order), each tile publishes its 256
+// digit counts and resolves its global offsets by a per-digit decoupled
+// look-back (16 predecessors per read), then the tile is staged in shared
+// memory in digit order so that the global scatter is written as contiguous
+// runs. Per pass the HBM traffic is one read and one write of (key, index).
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -19,8 +20,6 @@ namespace sq {
 
 constexpr int kRsBlock = 256;
 constexpr int kRsWarps = kRsBlock / 32;
-constexpr int kRsItems = 8;
-constexpr int kRsTile = kRsBlock * kRsItems;
 constexpr int kRadix = 256;
 
 template <typename KeyT>
@@ -41,49 +40,120 @@ __global__ void __launch_bounds__(kRsBlock) rs_histogram_kernel(const KeyT* __re
     }
 }
 
-template <typename KeyT>
+// Exclusive prefix of digit d over the tiles before `tile`: the tile's count
+// is published first (flag 1), then the predecessors are read kRsWindow at a
+// time (independent loads, so one window costs one L2 round trip) and their
+// counts summed back to the first inclusive prefix (flag 2), which ends the
+// walk; the tile then publishes its own inclusive prefix. A status word holds
+// flag and count together, so relaxed loads and stores suffice.
+constexpr int kRsWindow = 16;
+__device__ __forceinline__ unsigned rs_lookback(unsigned* status, unsigned tile, unsigned d, unsigned cnt,
+                                                unsigned* err) {
+    if (tile == 0) {
+        lb32_store_relaxed(&status[d], kFlag32Pre | cnt);
+        return 0;
+    }
+    lb32_store_relaxed(&status[(size_t)tile * kRadix + d], kFlag32Agg | cnt);
+    unsigned excl = 0, spins = 0;
+    long long t = (long long)tile - 1;  // next predecessor to read
+    while (true) {
+        unsigned s[kRsWindow];
+#pragma unroll
+        for (int q = 0; q < kRsWindow; ++q)
+            s[q] = t - q >= 0 ? lb32_load_relaxed(&status[(size_t)(t - q) * kRadix + d]) : kFlag32Pre;
+        bool stop = false, found = false;
+        int take = 0;
+#pragma unroll
+        for (int q = 0; q < kRsWindow; ++q) {
+            if (stop) continue;
+            const unsigned flag = s[q] >> 30;
+            if (flag == 0u) {
+                stop = true;  // not published yet: read it again
+            } else {
+                excl += s[q] & kVal32Mask;
+                ++take;
+                if (flag == 2u) stop = found = true;
+            }
+        }
+        if (found) break;
+        t -= take;
+        if (take == kRsWindow) {
+            spins = 0;
+            continue;
+        }
+        if (++spins > kSpinLimit) {  // count the missing predecessors as zero
+            atomicOr(err, 1u);
+            break;
+        }
+        __nanosleep(32);
+    }
+    lb32_store_relaxed(&status[(size_t)tile * kRadix + d], kFlag32Pre | (excl + cnt));
+    return excl;
+}
+
+// Peer masks of a warp's equal digits: MATCH_ANY = __match_any_sync (the
+// default); MATCH_OR = each lane ORs its bit into a per-warp shared word of
+// its digit and reads the word back (the leader, its lowest lane, clears it),
+// 7 % slower over a QDA walk step's sorts; SPARQ_RADIX_RANK=1 selects it.
+enum { RANK_MATCH_ANY = 0, RANK_MATCH_OR = 1 };
+
+template <typename KeyT, int ITEMS, int RANK>
 __global__ void __launch_bounds__(kRsBlock) rs_onesweep_kernel(const KeyT* __restrict__ kin,
                                                                const unsigned* __restrict__ vin,
                                                                KeyT* __restrict__ kout, unsigned* __restrict__ vout,
                                                                uint64_t n, int shift,
                                                                const unsigned* __restrict__ digit_base,
                                                                unsigned* status, unsigned* counter, unsigned* err) {
+    constexpr int kTile = kRsBlock * ITEMS;
+    extern __shared__ __align__(16) unsigned char rs_smem[];
+    KeyT* s_k = reinterpret_cast<KeyT*>(rs_smem);                       // kTile keys
+    unsigned* s_v = reinterpret_cast<unsigned*>(rs_smem + sizeof(KeyT) * kTile);  // kTile indices
     __shared__ unsigned s_tile;
     __shared__ unsigned s_whist[kRsWarps][kRadix];
     __shared__ unsigned s_tstart[kRadix];
     __shared__ unsigned s_gbase[kRadix];
     __shared__ unsigned s_wsum[kRsWarps];
-    __shared__ KeyT s_k[kRsTile];
-    __shared__ unsigned s_v[kRsTile];
+    __shared__ unsigned s_match[RANK == RANK_MATCH_OR ? kRsWarps : 1][kRadix];
 
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     if (tid == 0) s_tile = atomicAdd(counter, 1u);
     for (int i = tid; i < kRsWarps * kRadix; i += kRsBlock) (&s_whist[0][0])[i] = 0;
+    if (RANK == RANK_MATCH_OR)
+        for (int i = tid; i < kRsWarps * kRadix; i += kRsBlock) (&s_match[0][0])[i] = 0;
     __syncthreads();
     const unsigned tile = s_tile;
-    const uint64_t base = (uint64_t)tile * kRsTile;
+    const uint64_t base = (uint64_t)tile * kTile;
 
-    KeyT key[kRsItems];
-    unsigned val[kRsItems], rank[kRsItems], dg[kRsItems];
+    // a warp owns 32 * ITEMS consecutive keys; item j of lane l is key j * 32 + l
+    KeyT key[ITEMS];
+    unsigned val[ITEMS], rank[ITEMS];
     const unsigned lt = (1u << lane) - 1u;
+    const uint64_t wbase = base + (uint64_t)warp * (32 * ITEMS) + lane;
 #pragma unroll
-    for (int j = 0; j < kRsItems; ++j) {
-        const uint64_t i = base + (uint64_t)warp * (32 * kRsItems) + (uint64_t)j * 32 + lane;
-        const bool valid = i < n;
-        key[j] = valid ? kin[i] : (KeyT)0;
-        val[j] = valid ? vin[i] : 0u;
-        dg[j] = valid ? ((unsigned)(key[j] >> shift) & 0xffu) : 0xffffffffu;
+    for (int j = 0; j < ITEMS; ++j) {
+        const uint64_t i = wbase + (uint64_t)j * 32;
+        key[j] = i < n ? kin[i] : (KeyT)0;
+        val[j] = i < n ? vin[i] : 0u;
     }
 #pragma unroll
-    for (int j = 0; j < kRsItems; ++j) {
-        const bool valid = dg[j] != 0xffffffffu;
-        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-        const unsigned peers = __match_any_sync(0xffffffffu, dg[j]) & vmask;
+    for (int j = 0; j < ITEMS; ++j) {
+        const bool valid = wbase + (uint64_t)j * 32 < n;
+        const unsigned dg = valid ? ((unsigned)(key[j] >> shift) & 0xffu) : 0xffffffffu;
+        unsigned peers;
+        if (RANK == RANK_MATCH_OR) {
+            if (valid) atomicOr(&s_match[warp][dg], 1u << lane);
+            __syncwarp();
+            peers = valid ? s_match[warp][dg] : 0u;
+            __syncwarp();
+        } else {
+            peers = __match_any_sync(0xffffffffu, dg) & __ballot_sync(0xffffffffu, valid);
+        }
         const int leader = valid ? (__ffs(peers) - 1) : (int)lane;
         unsigned b = 0;
         if (valid && (int)lane == leader) {
-            b = s_whist[warp][dg[j]];
-            s_whist[warp][dg[j]] = b + __popc(peers);
+            b = s_whist[warp][dg];
+            s_whist[warp][dg] = b + __popc(peers);
+            if (RANK == RANK_MATCH_OR) s_match[warp][dg] = 0u;
         }
         b = __shfl_sync(0xffffffffu, b, leader);
         rank[j] = b + __popc(peers & lt);
@@ -101,31 +171,7 @@ __global__ void __launch_bounds__(kRsBlock) rs_onesweep_kernel(const KeyT* __res
         run += t;
     }
     const unsigned cnt = run;
-    unsigned excl = 0;
-    if (tile == 0) {
-        lb32_store(&status[d], kFlag32Pre | cnt);
-    } else {
-        lb32_store(&status[(size_t)tile * kRadix + d], kFlag32Agg | cnt);
-        long long t = (long long)tile - 1;
-        unsigned spins = 0;
-        while (t >= 0) {
-            const unsigned s = lb32_load(&status[(size_t)t * kRadix + d]);
-            const unsigned flag = s >> 30;
-            if (flag == 0u) {
-                if (++spins > kSpinLimit) {
-                    atomicOr(err, 1u);
-                    break;
-                }
-                __nanosleep(32);
-                continue;
-            }
-            excl += s & kVal32Mask;
-            if (flag == 2u) break;
-            --t;
-            spins = 0;
-        }
-        lb32_store(&status[(size_t)tile * kRadix + d], kFlag32Pre | (excl + cnt));
-    }
+    const unsigned excl = rs_lookback(status, tile, d, cnt, err);
     // block exclusive scan of cnt over digits -> tile-local digit start
     unsigned inc = cnt;
 #pragma unroll
@@ -145,15 +191,16 @@ __global__ void __launch_bounds__(kRsBlock) rs_onesweep_kernel(const KeyT* __res
     __syncthreads();
 
 #pragma unroll
-    for (int j = 0; j < kRsItems; ++j) {
-        if (dg[j] == 0xffffffffu) continue;
-        const unsigned pos = s_tstart[dg[j]] + s_whist[warp][dg[j]] + rank[j];
+    for (int j = 0; j < ITEMS; ++j) {
+        if (wbase + (uint64_t)j * 32 >= n) continue;
+        const unsigned dg = (unsigned)(key[j] >> shift) & 0xffu;
+        const unsigned pos = s_tstart[dg] + s_whist[warp][dg] + rank[j];
         s_k[pos] = key[j];
         s_v[pos] = val[j];
     }
     __syncthreads();
     const uint64_t rem = n - base;
-    const unsigned tile_n = rem < (uint64_t)kRsTile ? (unsigned)rem : (unsigned)kRsTile;
+    const unsigned tile_n = rem < (uint64_t)kTile ? (unsigned)rem : (unsigned)kTile;
     for (unsigned p = tid; p < tile_n; p += kRsBlock) {
         const KeyT k = s_k[p];
         const unsigned dd = (unsigned)(k >> shift) & 0xffu;
@@ -170,12 +217,51 @@ __global__ void __launch_bounds__(kRsBlock) rs_onesweep_kernel(const KeyT* __res
     }
 }
 
+// Keys per thread of a onesweep tile: 8 (2048-key tiles, four CTAs of 64
+// registers per SM). The 16-key form (4096-key tiles, half the look-back
+// chains, 128 registers and two CTAs per SM) measured 7 % slower over the
+// sorts of a QDA walk step at 2^20 (4M entries); SPARQ_RADIX_ITEMS=16 selects it.
+static int radix_rank_mode() {
+    static int mode = -1;
+    if (mode < 0) {
+        const char* e = getenv("SPARQ_RADIX_RANK");
+        mode = e && atoi(e) == 1 ? RANK_MATCH_OR : RANK_MATCH_ANY;
+    }
+    return mode;
+}
+
+static int radix_tile_items(uint64_t n) {
+    static int forced = -1;
+    if (forced < 0) {
+        const char* e = getenv("SPARQ_RADIX_ITEMS");
+        forced = e && (atoi(e) == 8 || atoi(e) == 16) ? atoi(e) : 0;
+    }
+    (void)n;
+    return forced ? forced : 8;
+}
+
+template <typename KeyT>
+static void radix_set_smem() {
+    static bool done = false;
+    if (done) return;
+    SQ_CUDA(cudaFuncSetAttribute(rs_onesweep_kernel<KeyT, 8, RANK_MATCH_ANY>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kRsBlock * 8 * (int)(sizeof(KeyT) + 4)));
+    SQ_CUDA(cudaFuncSetAttribute(rs_onesweep_kernel<KeyT, 16, RANK_MATCH_ANY>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kRsBlock * 16 * (int)(sizeof(KeyT) + 4)));
+    SQ_CUDA(cudaFuncSetAttribute(rs_onesweep_kernel<KeyT, 8, RANK_MATCH_OR>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kRsBlock * 8 * (int)(sizeof(KeyT) + 4)));
+    SQ_CUDA(cudaFuncSetAttribute(rs_onesweep_kernel<KeyT, 16, RANK_MATCH_OR>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kRsBlock * 16 * (int)(sizeof(KeyT) + 4)));
+    done = true;
+}
+
 // Sorts (k[0], v[0]) by the low `bits` bits of the key; returns 0 or 1: the
 // buffer pair holding the result. Buffers k[1], v[1] are scratch.
 template <typename KeyT>
 int radix_sort_pairs(KeyT* k[2], unsigned* v[2], uint64_t n, int bits) {
     if (n >= (1ull << 30)) fail(SQ_ERR_CAPACITY, "radix sort limited to < 2^30 keys");
     if (n <= 1 || bits <= 0) return 0;
+    radix_set_smem<KeyT>();
     const int passes = (bits + 7) / 8;
     unsigned* hist = (unsigned*)ws().get(WS_HIST, (size_t)2 * 8 * kRadix * 4);
     SQ_CUDA(cudaMemsetAsync(hist, 0, (size_t)passes * kRadix * 4, stream()));
@@ -201,19 +287,24 @@ int radix_sort_pairs(KeyT* k[2], unsigned* v[2], uint64_t n, int bits) {
     if (live.empty()) return 0;
     unsigned* dbase = hist + (size_t)8 * kRadix;
     h2d_small(dbase, bases.data(), bases.size() * 4);
-    const unsigned ntiles = (unsigned)((n + kRsTile - 1) / kRsTile);
+    const int items = radix_tile_items(n);
+    const unsigned tile = (unsigned)(kRsBlock * items);
+    const unsigned ntiles = (unsigned)((n + tile - 1) / tile);
     const size_t per_pass = (size_t)ntiles * kRadix + 64;  // status + counter
     unsigned* lb = (unsigned*)ws().get(WS_LOOKBACK, per_pass * live.size() * 4);
     SQ_CUDA(cudaMemsetAsync(lb, 0, per_pass * live.size() * 4, stream()));
+    const size_t smem = (size_t)tile * (sizeof(KeyT) + 4);
     int cur = 0;
     for (size_t q = 0; q < live.size(); ++q) {
         const int p = live[q];
         unsigned* st = lb + q * per_pass;
         unsigned* counter = st + (size_t)ntiles * kRadix;
         prof_begin(sizeof(KeyT) == 8 ? "radix_onesweep_u64" : "radix_onesweep_u32");
-        rs_onesweep_kernel<KeyT><<<ntiles, kRsBlock, 0, stream()>>>(k[cur], v[cur], k[cur ^ 1], v[cur ^ 1], n, 8 * p,
-                                                                   dbase + (size_t)p * kRadix, st, counter,
-                                                                   device_error_word());
+        auto kern = radix_rank_mode() == RANK_MATCH_OR
+                        ? (items == 16 ? rs_onesweep_kernel<KeyT, 16, RANK_MATCH_OR> : rs_onesweep_kernel<KeyT, 8, RANK_MATCH_OR>)
+                        : (items == 16 ? rs_onesweep_kernel<KeyT, 16, RANK_MATCH_ANY> : rs_onesweep_kernel<KeyT, 8, RANK_MATCH_ANY>);
+        kern<<<ntiles, kRsBlock, smem, stream()>>>(k[cur], v[cur], k[cur ^ 1], v[cur ^ 1], n, 8 * p,
+                                                   dbase + (size_t)p * kRadix, st, counter, device_error_word());
         prof_end(2.0 * n * (sizeof(KeyT) + 4));  // one read and one write of (key, index)
         SQ_CUDA(cudaGetLastError());
         cur ^= 1;

@@ -3,6 +3,7 @@
 // grow-only workspace.
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <stdexcept>
 
@@ -323,6 +324,30 @@ __global__ void checksum_kernel(const unsigned char* __restrict__ p, uint64_t by
     if ((threadIdx.x & 31u) == 0 && local) atomicAdd(acc, local);
 }
 
+// One device word read back through a mapped pinned word that a single
+// thread stores, not by a device-to-host copy: a copy would wait in the copy
+// engine's queue behind a bulk download of another state in flight (these
+// reads come before every graph launch and table write, while the previous
+// step's result is being downloaded). Synchronises the library stream.
+__global__ void store_word_kernel(const unsigned long long* __restrict__ src, unsigned long long* dst) {
+    *reinterpret_cast<volatile unsigned long long*>(dst) = *src;
+}
+
+uint64_t read_word_mapped(const unsigned long long* dev_word) {
+    static unsigned long long* word_host = nullptr;
+    static unsigned long long* word_dev = nullptr;
+    if (capturing()) fail(SQ_ERR_UNSUPPORTED, "capture: a value would be read back");
+    if (!word_host) {
+        SQ_CUDA(cudaHostAlloc((void**)&word_host, 64, cudaHostAllocMapped));
+        SQ_CUDA(cudaHostGetDevicePointer((void**)&word_dev, word_host, 0));
+    }
+    cudaStream_t st = stream();
+    store_word_kernel<<<1, 1, 0, st>>>(dev_word, word_dev);
+    SQ_CUDA(cudaGetLastError());
+    SQ_CUDA(cudaStreamSynchronize(st));
+    return *reinterpret_cast<volatile unsigned long long*>(word_host);
+}
+
 uint64_t device_checksum(const std::vector<std::pair<const void*, size_t>>& spans) {
     cudaStream_t st = stream();
     unsigned long long* acc = (unsigned long long*)dev_alloc(8);
@@ -336,9 +361,7 @@ uint64_t device_checksum(const std::vector<std::pair<const void*, size_t>>& span
                                                                         s.second, salt, acc);
         SQ_CUDA(cudaGetLastError());
     }
-    unsigned long long h = 0;
-    SQ_CUDA(cudaMemcpyAsync(&h, acc, 8, cudaMemcpyDeviceToHost, st));
-    SQ_CUDA(cudaStreamSynchronize(st));
+    const uint64_t h = read_word_mapped(acc);
     dev_free(acc);
     return h;
 }
@@ -509,48 +532,84 @@ __global__ void __launch_bounds__(512) d2h_store_kernel(const __grid_constant__ 
     }
 }
 
-cudaStream_t g_async = nullptr;
-cudaEvent_t g_async_start = nullptr;
+// Low-priority download streams: copy-engine downloads are cut into chunks
+// spread over these, so that several copy engines share a large transfer.
+constexpr int kAsyncStreams = 4;
+static cudaStream_t g_async[kAsyncStreams] = {nullptr};
+static cudaEvent_t g_async_ev[kAsyncStreams + 1] = {nullptr};
+static int g_d2h_engine = SQ_DOWNLOAD_SM_STORES;
+
+void set_d2h_engine(int engine) {
+    if (engine != SQ_DOWNLOAD_SM_STORES && engine != SQ_DOWNLOAD_COPY_ENGINE)
+        fail(SQ_ERR_INVALID, "download engine must be SQ_DOWNLOAD_SM_STORES or SQ_DOWNLOAD_COPY_ENGINE");
+    g_d2h_engine = engine;
+}
+
+static int env_int(const char* name, int lo, int hi, int dflt) {
+    const char* e = getenv(name);
+    const int v = e ? atoi(e) : 0;
+    return e && v >= lo && v <= hi ? v : dflt;
+}
 
 void async_copy_d2h(const CopyJob* jobs, int n, cudaEvent_t done) {
     cudaStream_t st = stream();
-    if (!g_async) {
+    static const int nstreams = env_int("SPARQ_D2H_STREAMS", 1, kAsyncStreams, 1);
+    static const int blocks = env_int("SPARQ_D2H_BLOCKS", 1, 1024, kD2HBlocks);
+    if (!g_async[0]) {
         int least = 0, greatest = 0;
         SQ_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-        SQ_CUDA(cudaStreamCreateWithPriority(&g_async, cudaStreamNonBlocking, least));
-        SQ_CUDA(cudaEventCreateWithFlags(&g_async_start, cudaEventDisableTiming));
+        for (int i = 0; i < kAsyncStreams; ++i)
+            SQ_CUDA(cudaStreamCreateWithPriority(&g_async[i], cudaStreamNonBlocking, least));
+        for (int i = 0; i <= kAsyncStreams; ++i)
+            SQ_CUDA(cudaEventCreateWithFlags(&g_async_ev[i], cudaEventDisableTiming));
     }
     if (n > kD2HSegs) fail(SQ_ERR_INVALID, "asynchronous download: too many arrays");
     // after the library stream's queued work (the state's last writer)
-    SQ_CUDA(cudaEventRecord(g_async_start, st));
-    SQ_CUDA(cudaStreamWaitEvent(g_async, g_async_start, 0));
+    SQ_CUDA(cudaEventRecord(g_async_ev[kAsyncStreams], st));
+    for (int i = 0; i < nstreams; ++i) SQ_CUDA(cudaStreamWaitEvent(g_async[i], g_async_ev[kAsyncStreams], 0));
     D2HJobs kj;
     memset(&kj, 0, sizeof(kj));
+    size_t total = 0;
+    for (int i = 0; i < n; ++i) total += jobs[i].bytes;
+    const size_t chunk = std::max<size_t>((total / (2 * nstreams) + 4095) & ~size_t(4095), 1u << 20);
+    int next = 0;
     for (int i = 0; i < n; ++i) {
         if (jobs[i].bytes == 0) continue;
         cudaPointerAttributes at;
         const cudaError_t pe = cudaPointerGetAttributes(&at, jobs[i].dst);
         if (pe != cudaSuccess) (void)cudaGetLastError();  // that query's own error only
-        const bool mapped = pe == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer != nullptr &&
+        const bool mapped = g_d2h_engine == SQ_DOWNLOAD_SM_STORES && pe == cudaSuccess &&
+                            at.type == cudaMemoryTypeHost && at.devicePointer != nullptr &&
                             (reinterpret_cast<uintptr_t>(jobs[i].dst) & 7) == 0 && jobs[i].bytes % 8 == 0;
         if (mapped) {
             kj.src[kj.n] = static_cast<const uint2*>(jobs[i].src);
             kj.dst[kj.n] = static_cast<uint2*>(at.devicePointer);
             kj.n8[kj.n] = jobs[i].bytes / 8;
             ++kj.n;
-        } else {
-            SQ_CUDA(cudaMemcpyAsync(jobs[i].dst, jobs[i].src, jobs[i].bytes, cudaMemcpyDeviceToHost, g_async));
+            continue;
+        }
+        for (size_t off = 0; off < jobs[i].bytes; off += chunk) {
+            const size_t b = std::min(chunk, jobs[i].bytes - off);
+            SQ_CUDA(cudaMemcpyAsync((char*)jobs[i].dst + off, (const char*)jobs[i].src + off, b,
+                                    cudaMemcpyDeviceToHost, g_async[next]));
+            next = (next + 1) % nstreams;
         }
     }
     if (kj.n) {
-        d2h_store_kernel<<<kD2HBlocks, 512, 0, g_async>>>(kj);
+        d2h_store_kernel<<<blocks, 512, 0, g_async[0]>>>(kj);
         SQ_CUDA(cudaGetLastError());
     }
-    SQ_CUDA(cudaEventRecord(done, g_async));
+    // join the chunks' streams into the first, whose event marks the end
+    for (int i = 1; i < nstreams; ++i) {
+        SQ_CUDA(cudaEventRecord(g_async_ev[i], g_async[i]));
+        SQ_CUDA(cudaStreamWaitEvent(g_async[0], g_async_ev[i], 0));
+    }
+    SQ_CUDA(cudaEventRecord(done, g_async[0]));
 }
 
 void sync_async_copies() {
-    if (g_async) SQ_CUDA(cudaStreamSynchronize(g_async));
+    for (int i = 0; i < kAsyncStreams; ++i)
+        if (g_async[i]) SQ_CUDA(cudaStreamSynchronize(g_async[i]));
 }
 
 void free_group_cache(GroupCache& c) {

@@ -228,6 +228,8 @@ void parallel_copy(const CopyJob* jobs, int n, cudaMemcpyKind kind);
 void async_copy_d2h(const CopyJob* jobs, int n, cudaEvent_t done);
 // Blocks until every asynchronous download has finished.
 void sync_async_copies();
+uint64_t read_word_mapped(const unsigned long long* dev_word);
+void set_d2h_engine(int engine);
 // Copy a host table of 64-bit words to the device at the narrowest width (2,
 // 4 or 8 bytes) that holds every word; eb_guess is tried first.
 void* qram_upload(const uint64_t* host_words, uint64_t n, uint32_t eb_guess, uint32_t* eb_out, uint64_t* all_out);

@@ -25,8 +25,17 @@ def _buffers(kind, k, n):
     return (keys, amps), keys.ctypes.data, amps.ctypes.data, lambda: (keys, amps)
 
 
+@pytest.fixture(params=["sm", "copy"])
+def engine(request):
+    """Pinned destinations stored into by the download kernel, or copied by
+    the copy engine."""
+    ps.set_download_engine(request.param)
+    yield request.param
+    ps.set_download_engine("sm")
+
+
 @pytest.mark.parametrize("kind", ["pinned", "pageable"])
-def test_async_download_is_ordered_before_later_writes(kind):
+def test_async_download_is_ordered_before_later_writes(kind, engine):
     ps.System.clear()
     a = ps.System.add_register("a", ps.UnsignedInteger, 20)
     b = ps.System.add_register("b", ps.Boolean, 1)
@@ -49,7 +58,7 @@ def test_async_download_is_ordered_before_later_writes(kind):
     assert np.all(regs[:, b] == 1)
 
 
-def test_two_states_alternate():
+def test_two_states_alternate(engine):
     """Downloads of two states in flight while both are rewritten."""
     ps.System.clear()
     a = ps.System.add_register("a", ps.UnsignedInteger, 16)
@@ -70,3 +79,10 @@ def test_two_states_alternate():
         assert np.array_equal(np.sort(keys & 0xFFFF), np.arange(1 << 16, dtype=np.uint64))
         assert np.allclose(amps[0::2], 1 / 256) and np.all(amps[1::2] == 0)
     assert [s.size() for s in sts] == [1, 1]
+
+
+def test_download_engine_names():
+    with pytest.raises(ValueError):
+        ps.set_download_engine("dma")
+    with pytest.raises(ps.SparQInvalid):
+        ps._native.call("sq_set_download_engine", 7)
