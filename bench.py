@@ -813,7 +813,7 @@ def main():
     ap.add_argument("--hadamard-bits", type=int, default=12)
     ap.add_argument("--layers", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--download-engine", default="copy", choices=["copy", "sm"],
+    ap.add_argument("--download-engine", default="sm", choices=["sm", "copy"],
                     help="how the end-to-end loop's downloads into pinned memory are moved")
     ap.add_argument("--skip-other-arithmetic", action="store_true",
                     help="do not also time the other Hadamard butterfly arithmetic")

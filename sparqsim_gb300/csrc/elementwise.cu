@@ -665,7 +665,7 @@ uint64_t qram_rewrite(QramTable& t, const uint64_t* host_words) {
     const uint64_t n = t.n_words;
     uint64_t* raw = t.elem_bytes == 8 ? static_cast<uint64_t*>(t.dev) : (uint64_t*)dev_alloc(n * 8);
     unsigned long long* all = (unsigned long long*)dev_alloc(8);
-    SQ_CUDA(cudaMemcpyAsync(raw, host_words, n * 8, cudaMemcpyHostToDevice, st));
+    copy_h2d_async(raw, host_words, n * 8);
     SQ_CUDA(cudaMemsetAsync(all, 0, 8, st));
     prof_begin("qram_pack");
     qram_pack_kernel<<<grid_for(n, 256), 256, 0, st>>>(raw, n, t.elem_bytes, t.dev, all);

@@ -425,6 +425,7 @@ struct EmitArgs {
                                   // reservation ends past it writes nothing (the host reruns exactly)
     int fix;                   // FWHT arithmetic: 0 the reference's FP64 butterflies, 1 exact sums
     unsigned long long* ticket;  // dynamic group order: next group, CTAs finished (zero between launches)
+    unsigned* err;               // device error word
 };
 
 // Dynamic group order for the persistent emit kernels. A grid of two CTAs
@@ -1414,8 +1415,15 @@ __device__ __forceinline__ void fwht8(longlong2 (&x)[8]) {
 }
 __device__ __forceinline__ unsigned swz8(unsigned q) { return q ^ ((q >> 3) & 7u); }
 
-template <int K, int MODE, int AM>
+// SHAPE narrows the kernel to the groups the host knows it has, so that only
+// that path is compiled in and the other paths' registers do not count
+// against it: H_FULL, every group a cached range of 4096 members (the state
+// holds exactly 4096 entries per range); H_SINGLE, every group one entry of
+// an integer Hadamard (as many groups as entries); H_ANY, any groups.
+enum { H_ANY = 0, H_FULL = 1, H_SINGLE = 2 };
+template <int K, int MODE, int AM, int SHAPE>
 __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_constant__ EmitArgs a) {
+    constexpr bool FULL = SHAPE == H_FULL;
     extern __shared__ double2 sl[];  // 4096 slots
     __shared__ unsigned s_cnt[8][16];
     __shared__ unsigned long long s_base;
@@ -1424,6 +1432,7 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
     __shared__ unsigned s_emax[16];
     __shared__ bool s_fits;
     __shared__ unsigned long long s_g[2];
+    __shared__ unsigned s_ball[8][16];  // keep masks per (row, warp): not held in registers
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const Field tg = a.target;
     longlong2* ls = reinterpret_cast<longlong2*>(sl);
@@ -1432,7 +1441,13 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
         ticket_prefetch(a.ticket, s_g, it);
         unsigned s0, m;
         group_range<AM>(a, g, s0, m);
-        if (m == 0) {  // an emptied cached range
+        if ((FULL && m != 4096u) || (SHAPE == H_SINGLE && m != 1u)) {
+            // cannot happen for the sizes the host checked; a replayed graph
+            // whose groups differ from the recorded ones is reported instead
+            if (tid == 0) atomicOr(a.err, 32u);
+            continue;
+        }
+        if (!FULL && m == 0) {  // an emptied cached range
             if (tid == 0) {
                 if (MODE == EMIT_COUNT) a.cnt[g] = 0u;
                 else if (MODE == EMIT_ATOMIC && a.ocnt) {
@@ -1442,9 +1457,9 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
             }
             continue;
         }
-        uint64_t gk[K];
-        load_key<K>(a.in_keys, group_head<AM>(a, g, s0), gk);
-        if (a.mode == GM_HADAMARD_INT && m == 1) {
+        if (SHAPE == H_SINGLE || (!FULL && a.mode == GM_HADAMARD_INT && m == 1)) {
+            uint64_t gk[K];
+            load_key<K>(a.in_keys, group_head<AM>(a, g, s0), gk);
             // singleton: a * 2^-6, sign (-1)^popcount(t & v) (hadamard.cpp:27-42)
             uint64_t v0;
             double2 a0;
@@ -1482,9 +1497,10 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
             __syncthreads();
             continue;
         }
+        if (SHAPE == H_SINGLE) continue;  // not reached: every group took the path above
         double2 v[8];
         unsigned rows = 0xffu;  // rows j that may hold a kept slot (warp-uniform)
-        if (a.mode == GM_HADAMARD_FULL && m <= 11u) {
+        if (!FULL && a.mode == GM_HADAMARD_FULL && m <= 11u) {
             // sparse bucket: direct product, members in ascending target order (hadamard.cpp:267-304)
             for (unsigned j = tid; j < m; j += 512u) {
                 uint64_t tj;
@@ -1521,7 +1537,7 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
                 v[j] = acc;
             }
         } else {
-            const bool direct = AM == 2 && m == 4096u;  // a full cached range: member c has target c
+            const bool direct = FULL || (AM == 2 && m == 4096u);  // a full cached range: member c has target c
             int emax = 1;
             if (direct) {
 #pragma unroll
@@ -1602,11 +1618,13 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
             }
         }
         // kept slots in ascending slot order: row j (slot bits 9..11), then warp, then lane
-        unsigned ball[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            ball[j] = ((rows >> j) & 1u) ? __ballot_sync(0xffffffffu, keep_amp(v[j], a.eps)) : 0u;
-            if (lane == 0) s_cnt[j][warp] = __popc(ball[j]);
+            const unsigned ball = ((rows >> j) & 1u) ? __ballot_sync(0xffffffffu, keep_amp(v[j], a.eps)) : 0u;
+            if (lane == 0) {
+                s_cnt[j][warp] = __popc(ball);
+                s_ball[j][warp] = ball;
+            }
         }
         __syncthreads();
         if (warp == 0) {
@@ -1644,18 +1662,20 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
             }
         }
         __syncthreads();
-        if (MODE != EMIT_COUNT) {
+        if (MODE != EMIT_COUNT && (MODE != EMIT_ATOMIC || s_fits)) {
             const unsigned long long o = MODE == EMIT_WRITE ? a.off[g] : s_base;
             const unsigned lt = (1u << lane) - 1u;
-            const bool fits = MODE != EMIT_ATOMIC || s_fits;
+            uint64_t gk[K];  // the group's key, read here rather than held through the transform
+            load_key<K>(a.in_keys, group_head<AM>(a, g, s0), gk);
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                if (!fits || !((ball[j] >> lane) & 1u)) continue;
+                const unsigned ball = s_ball[j][warp];
+                if (!((ball >> lane) & 1u)) continue;
                 uint64_t kk[K];
 #pragma unroll
                 for (int w = 0; w < K; ++w) kk[w] = gk[w];
                 fset<K>(kk, tg, (uint64_t)(((unsigned)j << 9) | tid));
-                store_out<K>(a, o + s_cnt[j][warp] + __popc(ball[j] & lt), kk, v[j]);
+                store_out<K>(a, o + s_cnt[j][warp] + __popc(ball & lt), kk, v[j]);
             }
         }
         __syncthreads();
@@ -2526,11 +2546,15 @@ static void launch_h4096_fp64(int am, unsigned grid, size_t sm, cudaStream_t st,
 template <int K, int MODE>
 static void launch_h4096(int am, unsigned grid, size_t sm, cudaStream_t st, const EmitArgs& ea) {
     if (ea.fix) {  // exact sums: 512 threads, 8 slots each
-        if (am == 2) emit_h4096x_kernel<K, MODE, 2><<<grid, 512, sm, st>>>(ea);
-        else if (am == 1) emit_h4096x_kernel<K, MODE, 1><<<grid, 512, sm, st>>>(ea);
-        else emit_h4096x_kernel<K, MODE, 0><<<grid, 512, sm, st>>>(ea);
+        // am: 0-2 access mode; 3 full cached ranges; 4 / 5 singletons (access mode 0 / 1)
+        if (am == 3) emit_h4096x_kernel<K, MODE, 2, H_FULL><<<grid, 512, sm, st>>>(ea);
+        else if (am == 4) emit_h4096x_kernel<K, MODE, 0, H_SINGLE><<<grid, 512, sm, st>>>(ea);
+        else if (am == 5) emit_h4096x_kernel<K, MODE, 1, H_SINGLE><<<grid, 512, sm, st>>>(ea);
+        else if (am == 2) emit_h4096x_kernel<K, MODE, 2, H_ANY><<<grid, 512, sm, st>>>(ea);
+        else if (am == 1) emit_h4096x_kernel<K, MODE, 1, H_ANY><<<grid, 512, sm, st>>>(ea);
+        else emit_h4096x_kernel<K, MODE, 0, H_ANY><<<grid, 512, sm, st>>>(ea);
     } else {
-        launch_h4096_fp64<K, MODE>(am, grid, sm, st, ea);
+        launch_h4096_fp64<K, MODE>(am == 3 ? 2 : am == 4 ? 0 : am == 5 ? 1 : am, grid, sm, st, ea);
     }
 }
 template <int K, int W, bool WRITE>
@@ -2563,8 +2587,10 @@ static void set_emit_smem_limits() {
 #define SQ_SMEM(f, b) SQ_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, b))
 #define SQ_SMEM_H(m)                                                                                           \
     SQ_SMEM((emit_h4096_kernel<K, m, 0>), sm); SQ_SMEM((emit_h4096_kernel<K, m, 1>), sm);                     \
-    SQ_SMEM((emit_h4096_kernel<K, m, 2>), sm); SQ_SMEM((emit_h4096x_kernel<K, m, 0>), sm);                     \
-    SQ_SMEM((emit_h4096x_kernel<K, m, 1>), sm); SQ_SMEM((emit_h4096x_kernel<K, m, 2>), sm);
+    SQ_SMEM((emit_h4096_kernel<K, m, 2>), sm); SQ_SMEM((emit_h4096x_kernel<K, m, 0, H_ANY>), sm);              \
+    SQ_SMEM((emit_h4096x_kernel<K, m, 1, H_ANY>), sm); SQ_SMEM((emit_h4096x_kernel<K, m, 2, H_ANY>), sm);     \
+    SQ_SMEM((emit_h4096x_kernel<K, m, 2, H_FULL>), sm); SQ_SMEM((emit_h4096x_kernel<K, m, 0, H_SINGLE>), sm); \
+    SQ_SMEM((emit_h4096x_kernel<K, m, 1, H_SINGLE>), sm);
     SQ_SMEM_H(EMIT_COUNT)
     SQ_SMEM_H(EMIT_WRITE)
     SQ_SMEM_H(EMIT_ATOMIC)
@@ -2774,11 +2800,17 @@ static void run_group(State& s, const GroupSpec& gs) {
     auto launch_h4096_mode = [&](int mode) {
         const unsigned grid = (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2);
         ea.ticket = group_ticket(st);
+        ea.err = device_error_word();
+        // cached ranges holding N = 4096 G entries are all full (none holds
+        // more); G = P groups of an integer Hadamard are all singletons
+        const int amx = am == 2 && F == 0 && N == G * 4096ull                  ? 3
+                        : am < 2 && gs.mode == GM_HADAMARD_INT && G == P && !gs.varw.width ? 4 + am
+                                                                                          : am;
         const size_t sm = 4096 * sizeof(double2);
         prof_begin(mode == EMIT_COUNT ? "emit_h4096_count" : mode == EMIT_WRITE ? "emit_h4096_write" : "emit_h4096_single_pass");
-        if (mode == EMIT_COUNT) launch_h4096<K, EMIT_COUNT>(am, grid, sm, st, ea);
-        else if (mode == EMIT_WRITE) launch_h4096<K, EMIT_WRITE>(am, grid, sm, st, ea);
-        else launch_h4096<K, EMIT_ATOMIC>(am, grid, sm, st, ea);
+        if (mode == EMIT_COUNT) launch_h4096<K, EMIT_COUNT>(amx, grid, sm, st, ea);
+        else if (mode == EMIT_WRITE) launch_h4096<K, EMIT_WRITE>(amx, grid, sm, st, ea);
+        else launch_h4096<K, EMIT_ATOMIC>(amx, grid, sm, st, ea);
         prof_end(mode == EMIT_COUNT ? (double)P * E : (double)(P + T) * E);
         SQ_CUDA(cudaGetLastError());
     };

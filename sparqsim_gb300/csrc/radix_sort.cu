@@ -91,13 +91,88 @@ __device__ __forceinline__ unsigned rs_lookback(unsigned* status, unsigned tile,
     return excl;
 }
 
+// Reduce-then-scan form of a pass (no chain between tiles): the upsweep
+// counts each tile's digits, counts[d * ntiles + tile]; rs_scan_kernel turns
+// them into each tile's first output position per digit; the rank-and-scatter
+// kernel (rs_onesweep_kernel, CHAINED = false) reads those. Tiles are the
+// same 256 * ITEMS consecutive keys in all three.
+template <typename KeyT, int ITEMS>
+__global__ void __launch_bounds__(kRsBlock) rs_upsweep_kernel(const KeyT* __restrict__ kin, uint64_t n, int shift,
+                                                              unsigned* __restrict__ counts) {
+    __shared__ unsigned s_h[kRadix];
+    const unsigned tid = threadIdx.x, lane = tid & 31u;
+    s_h[tid] = 0;
+    __syncthreads();
+    const uint64_t base = (uint64_t)blockIdx.x * (kRsBlock * ITEMS);
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        const uint64_t i = base + (uint64_t)j * kRsBlock + tid;
+        const bool valid = i < n;
+        const unsigned dg = valid ? ((unsigned)(kin[i] >> shift) & 0xffu) : 0xffffffffu;
+        // one shared atomic per distinct digit in the warp: sorted or skewed
+        // keys would otherwise serialise 32 lanes on one counter
+        const unsigned peers = __match_any_sync(0xffffffffu, dg);
+        if (valid && (int)lane == __ffs(peers) - 1) atomicAdd(&s_h[dg], (unsigned)__popc(peers));
+    }
+    __syncthreads();
+    counts[(size_t)tid * gridDim.x + blockIdx.x] = s_h[tid];
+}
+
+// One CTA per digit d: offs[d * ntiles + t] = digit_base[d] + the digit's
+// count over tiles 0..t-1 (an exclusive scan along the digit's row, 1024
+// tiles per step with a running carry). `offs` may alias `counts`.
+__global__ void __launch_bounds__(kRsBlock) rs_scan_kernel(const unsigned* counts, unsigned ntiles,
+                                                           const unsigned* __restrict__ digit_base, unsigned* offs) {
+    __shared__ unsigned s_w[kRsWarps];
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, d = blockIdx.x;
+    const unsigned* row = counts + (size_t)d * ntiles;
+    unsigned* orow = offs + (size_t)d * ntiles;
+    unsigned carry = digit_base[d];
+    for (unsigned t0 = 0; t0 < ntiles; t0 += 4 * kRsBlock) {
+        unsigned v[4], sum = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const unsigned t = t0 + tid * 4 + q;
+            v[q] = t < ntiles ? row[t] : 0u;
+            sum += v[q];
+        }
+        unsigned inc = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned x = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= (unsigned)o) inc += x;
+        }
+        if (lane == 31) s_w[warp] = inc;
+        __syncthreads();
+        unsigned wpre = 0, total = 0;
+#pragma unroll
+        for (int w = 0; w < kRsWarps; ++w) {
+            if ((unsigned)w < warp) wpre += s_w[w];
+            total += s_w[w];
+        }
+        unsigned run = carry + wpre + inc - sum;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const unsigned t = t0 + tid * 4 + q;
+            if (t < ntiles) orow[t] = run;
+            run += v[q];
+        }
+        carry += total;
+        __syncthreads();  // s_w is rewritten by the next step
+    }
+}
+
 // Peer masks of a warp's equal digits: MATCH_ANY = __match_any_sync (the
 // default); MATCH_OR = each lane ORs its bit into a per-warp shared word of
 // its digit and reads the word back (the leader, its lowest lane, clears it),
 // 7 % slower over a QDA walk step's sorts; SPARQ_RADIX_RANK=1 selects it.
 enum { RANK_MATCH_ANY = 0, RANK_MATCH_OR = 1 };
 
-template <typename KeyT, int ITEMS, int RANK>
+// CHAINED: the tile's digit offsets come from the look-back (status words,
+// tile order from `counter`). Otherwise tile = blockIdx.x and its offsets are
+// read from `status` laid out digit-major, offs[d * ntiles + tile], as written
+// by rs_scan_kernel (`digit_base` and `counter` unused).
+template <typename KeyT, int ITEMS, int RANK, bool CHAINED>
 __global__ void __launch_bounds__(kRsBlock) rs_onesweep_kernel(const KeyT* __restrict__ kin,
                                                                const unsigned* __restrict__ vin,
                                                                KeyT* __restrict__ kout, unsigned* __restrict__ vout,
@@ -116,12 +191,12 @@ __global__ void __launch_bounds__(kRsBlock) rs_onesweep_kernel(const KeyT* __res
     __shared__ unsigned s_match[RANK == RANK_MATCH_OR ? kRsWarps : 1][kRadix];
 
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    if (tid == 0) s_tile = atomicAdd(counter, 1u);
+    if (CHAINED && tid == 0) s_tile = atomicAdd(counter, 1u);
     for (int i = tid; i < kRsWarps * kRadix; i += kRsBlock) (&s_whist[0][0])[i] = 0;
     if (RANK == RANK_MATCH_OR)
         for (int i = tid; i < kRsWarps * kRadix; i += kRsBlock) (&s_match[0][0])[i] = 0;
     __syncthreads();
-    const unsigned tile = s_tile;
+    const unsigned tile = CHAINED ? s_tile : blockIdx.x;
     const uint64_t base = (uint64_t)tile * kTile;
 
     // a warp owns 32 * ITEMS consecutive keys; item j of lane l is key j * 32 + l
@@ -171,7 +246,8 @@ __global__ void __launch_bounds__(kRsBlock) rs_onesweep_kernel(const KeyT* __res
         run += t;
     }
     const unsigned cnt = run;
-    const unsigned excl = rs_lookback(status, tile, d, cnt, err);
+    const unsigned gbase = CHAINED ? digit_base[d] + rs_lookback(status, tile, d, cnt, err)
+                                   : status[(size_t)d * gridDim.x + tile];
     // block exclusive scan of cnt over digits -> tile-local digit start
     unsigned inc = cnt;
 #pragma unroll
@@ -187,7 +263,7 @@ __global__ void __launch_bounds__(kRsBlock) rs_onesweep_kernel(const KeyT* __res
         if ((unsigned)w < warp) wpre += s_wsum[w];
     const unsigned tstart = wpre + inc - cnt;
     s_tstart[d] = tstart;
-    s_gbase[d] = digit_base[d] + excl;
+    s_gbase[d] = gbase;
     __syncthreads();
 
 #pragma unroll
@@ -240,18 +316,39 @@ static int radix_tile_items(uint64_t n) {
     return forced ? forced : 8;
 }
 
+// How a pass finds each tile's output offsets: 0 (default) the chained
+// onesweep, one launch with a per-digit look-back; 1 reduce-then-scan, three
+// launches with no dependence between tiles. Over the sorts of a QDA walk
+// step at 2^20 (4M entries, 46 passes) the chained form took 2.48 ms and the
+// three-launch form 3.3 ms (its rank-and-scatter alone 1.89 ms, the upsweep
+// 1.08 ms): the ranking inside a tile, not the look-back, dominates a pass.
+// SPARQ_RADIX_MODE=1 selects the three-launch form.
+static int radix_mode() {
+    static int mode = -1;
+    if (mode < 0) {
+        const char* e = getenv("SPARQ_RADIX_MODE");
+        mode = e && atoi(e) == 1 ? 1 : 0;
+    }
+    return mode;
+}
+
+template <typename KeyT, bool CH>
+static auto rs_pick(int items, int rank) {
+    if (rank == RANK_MATCH_OR)
+        return items == 16 ? rs_onesweep_kernel<KeyT, 16, RANK_MATCH_OR, CH> : rs_onesweep_kernel<KeyT, 8, RANK_MATCH_OR, CH>;
+    return items == 16 ? rs_onesweep_kernel<KeyT, 16, RANK_MATCH_ANY, CH> : rs_onesweep_kernel<KeyT, 8, RANK_MATCH_ANY, CH>;
+}
+
 template <typename KeyT>
 static void radix_set_smem() {
     static bool done = false;
     if (done) return;
-    SQ_CUDA(cudaFuncSetAttribute(rs_onesweep_kernel<KeyT, 8, RANK_MATCH_ANY>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kRsBlock * 8 * (int)(sizeof(KeyT) + 4)));
-    SQ_CUDA(cudaFuncSetAttribute(rs_onesweep_kernel<KeyT, 16, RANK_MATCH_ANY>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kRsBlock * 16 * (int)(sizeof(KeyT) + 4)));
-    SQ_CUDA(cudaFuncSetAttribute(rs_onesweep_kernel<KeyT, 8, RANK_MATCH_OR>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kRsBlock * 8 * (int)(sizeof(KeyT) + 4)));
-    SQ_CUDA(cudaFuncSetAttribute(rs_onesweep_kernel<KeyT, 16, RANK_MATCH_OR>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kRsBlock * 16 * (int)(sizeof(KeyT) + 4)));
+    for (int items : {8, 16})
+        for (int rank : {RANK_MATCH_ANY, RANK_MATCH_OR}) {
+            const int bytes = kRsBlock * items * (int)(sizeof(KeyT) + 4);
+            SQ_CUDA(cudaFuncSetAttribute(rs_pick<KeyT, true>(items, rank), cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            SQ_CUDA(cudaFuncSetAttribute(rs_pick<KeyT, false>(items, rank), cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        }
     done = true;
 }
 
@@ -288,24 +385,48 @@ int radix_sort_pairs(KeyT* k[2], unsigned* v[2], uint64_t n, int bits) {
     unsigned* dbase = hist + (size_t)8 * kRadix;
     h2d_small(dbase, bases.data(), bases.size() * 4);
     const int items = radix_tile_items(n);
+    const int rank = radix_rank_mode();
+    const bool chained = radix_mode() == 0;
     const unsigned tile = (unsigned)(kRsBlock * items);
     const unsigned ntiles = (unsigned)((n + tile - 1) / tile);
-    const size_t per_pass = (size_t)ntiles * kRadix + 64;  // status + counter
-    unsigned* lb = (unsigned*)ws().get(WS_LOOKBACK, per_pass * live.size() * 4);
-    SQ_CUDA(cudaMemsetAsync(lb, 0, per_pass * live.size() * 4, stream()));
     const size_t smem = (size_t)tile * (sizeof(KeyT) + 4);
+    cudaStream_t st = stream();
     int cur = 0;
+    if (chained) {
+        const size_t per_pass = (size_t)ntiles * kRadix + 64;  // status + counter
+        unsigned* lb = (unsigned*)ws().get(WS_LOOKBACK, per_pass * live.size() * 4);
+        SQ_CUDA(cudaMemsetAsync(lb, 0, per_pass * live.size() * 4, st));
+        for (size_t q = 0; q < live.size(); ++q) {
+            const int p = live[q];
+            unsigned* status = lb + q * per_pass;
+            unsigned* counter = status + (size_t)ntiles * kRadix;
+            prof_begin(sizeof(KeyT) == 8 ? "radix_onesweep_u64" : "radix_onesweep_u32");
+            rs_pick<KeyT, true>(items, rank)<<<ntiles, kRsBlock, smem, st>>>(
+                k[cur], v[cur], k[cur ^ 1], v[cur ^ 1], n, 8 * p, dbase + (size_t)p * kRadix, status, counter,
+                device_error_word());
+            prof_end(2.0 * n * (sizeof(KeyT) + 4));  // one read and one write of (key, index)
+            SQ_CUDA(cudaGetLastError());
+            cur ^= 1;
+        }
+        return cur;
+    }
+    // reduce-then-scan: per-tile digit counts, turned in place into offsets
+    unsigned* offs = (unsigned*)ws().get(WS_LOOKBACK, (size_t)ntiles * kRadix * 4);
     for (size_t q = 0; q < live.size(); ++q) {
         const int p = live[q];
-        unsigned* st = lb + q * per_pass;
-        unsigned* counter = st + (size_t)ntiles * kRadix;
-        prof_begin(sizeof(KeyT) == 8 ? "radix_onesweep_u64" : "radix_onesweep_u32");
-        auto kern = radix_rank_mode() == RANK_MATCH_OR
-                        ? (items == 16 ? rs_onesweep_kernel<KeyT, 16, RANK_MATCH_OR> : rs_onesweep_kernel<KeyT, 8, RANK_MATCH_OR>)
-                        : (items == 16 ? rs_onesweep_kernel<KeyT, 16, RANK_MATCH_ANY> : rs_onesweep_kernel<KeyT, 8, RANK_MATCH_ANY>);
-        kern<<<ntiles, kRsBlock, smem, stream()>>>(k[cur], v[cur], k[cur ^ 1], v[cur ^ 1], n, 8 * p,
-                                                   dbase + (size_t)p * kRadix, st, counter, device_error_word());
-        prof_end(2.0 * n * (sizeof(KeyT) + 4));  // one read and one write of (key, index)
+        prof_begin("radix_upsweep");
+        (items == 16 ? rs_upsweep_kernel<KeyT, 16> : rs_upsweep_kernel<KeyT, 8>)<<<ntiles, kRsBlock, 0, st>>>(
+            k[cur], n, 8 * p, offs);
+        prof_end((double)n * sizeof(KeyT));
+        SQ_CUDA(cudaGetLastError());
+        prof_begin("radix_tile_scan");
+        rs_scan_kernel<<<kRadix, kRsBlock, 0, st>>>(offs, ntiles, dbase + (size_t)p * kRadix, offs);
+        prof_end(2.0 * ntiles * kRadix * 4);
+        SQ_CUDA(cudaGetLastError());
+        prof_begin(sizeof(KeyT) == 8 ? "radix_scatter_u64" : "radix_scatter_u32");
+        rs_pick<KeyT, false>(items, rank)<<<ntiles, kRsBlock, smem, st>>>(
+            k[cur], v[cur], k[cur ^ 1], v[cur ^ 1], n, 8 * p, nullptr, offs, nullptr, device_error_word());
+        prof_end(2.0 * n * (sizeof(KeyT) + 4));
         SQ_CUDA(cudaGetLastError());
         cur ^= 1;
     }

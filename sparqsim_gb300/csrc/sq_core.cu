@@ -453,6 +453,76 @@ void free_buffers(Buffers& b) {
     b.kalloc = 0;
 }
 
+// Copies by the SMs over the host link, between device memory and mapped
+// pinned host memory (either side): a few blocks storing into host memory
+// (asynchronous downloads) or a full grid loading from it (uploads). A bulk
+// copy-engine transfer delays every small device-to-host read queued after it
+// (the count reads of the split operators wait behind it: 155 us instead of
+// 20 us each), and on some systems an upload waits behind a download in
+// flight; so downloads into pinned memory default to 12 blocks storing (about
+// 150 GB/s of the link's 190, leaving the SMs and the small reads to the work
+// they overlap), and uploads from pinned memory are loaded by the SMs, which
+// leaves the copy engine to a download that overlaps later work.
+constexpr int kD2HSegs = SQ_KMAX + 2;
+constexpr int kD2HBlocks = 12;
+struct D2HJobs {
+    const uint2* src[kD2HSegs];
+    uint2* dst[kD2HSegs];
+    uint64_t n8[kD2HSegs];  // 8-byte units
+    int n;
+};
+
+__global__ void __launch_bounds__(512) link_copy_kernel(const __grid_constant__ D2HJobs j) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (int s = 0; s < j.n; ++s) {
+        const uint64_t n8 = j.n8[s];
+        const bool v16 = ((reinterpret_cast<uintptr_t>(j.src[s]) | reinterpret_cast<uintptr_t>(j.dst[s])) & 15) == 0;
+        if (v16) {
+            const uint4* src = reinterpret_cast<const uint4*>(j.src[s]);
+            uint4* dst = reinterpret_cast<uint4*>(j.dst[s]);
+            const uint64_t n16 = n8 >> 1;
+            for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) dst[i] = src[i];
+            if ((n8 & 1) && blockIdx.x == 0 && threadIdx.x == 0) j.dst[s][n8 - 1] = j.src[s][n8 - 1];
+        } else {
+            for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += stride)
+                j.dst[s][i] = j.src[s][i];
+        }
+    }
+}
+
+// The device alias of mapped pinned host memory (8-byte aligned start and
+// size), or null for any other memory.
+static void* mapped_alias(const void* host, size_t bytes) {
+    cudaPointerAttributes at;
+    const cudaError_t pe = cudaPointerGetAttributes(&at, host);
+    if (pe != cudaSuccess) {
+        (void)cudaGetLastError();  // that query's own error only
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr) return nullptr;
+    if ((reinterpret_cast<uintptr_t>(host) & 7) != 0 || bytes % 8 != 0) return nullptr;
+    return at.devicePointer;
+}
+
+void copy_h2d_async(void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return;
+    cudaStream_t st = stream();
+    const void* alias = (reinterpret_cast<uintptr_t>(dst) & 7) == 0 ? mapped_alias(src, bytes) : nullptr;
+    if (!alias) {
+        SQ_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+        return;
+    }
+    D2HJobs j;
+    memset(&j, 0, sizeof(j));
+    j.src[0] = static_cast<const uint2*>(alias);
+    j.dst[0] = static_cast<uint2*>(dst);
+    j.n8[0] = bytes / 8;
+    j.n = 1;
+    const uint64_t blocks = std::min<uint64_t>((bytes / 16 + 511) / 512, (uint64_t)num_sms() * 2);
+    link_copy_kernel<<<(unsigned)std::max<uint64_t>(blocks, 1), 512, 0, st>>>(j);
+    SQ_CUDA(cudaGetLastError());
+}
+
 namespace {
 constexpr int kCopyStreams = 4;
 cudaStream_t g_copy[kCopyStreams] = {nullptr};
@@ -467,6 +537,18 @@ void parallel_copy(const CopyJob* jobs, int n, cudaMemcpyKind kind) {
             SQ_CUDA(cudaEventCreateWithFlags(&g_copy_ev[i], cudaEventDisableTiming));
         }
         SQ_CUDA(cudaEventCreateWithFlags(&g_copy_ev[kCopyStreams], cudaEventDisableTiming));
+    }
+    std::vector<CopyJob> rest;
+    if (kind == cudaMemcpyHostToDevice) {  // uploads from mapped pinned memory: by the SMs
+        for (int j = 0; j < n; ++j) {
+            if (jobs[j].bytes && mapped_alias(jobs[j].src, jobs[j].bytes) &&
+                (reinterpret_cast<uintptr_t>(jobs[j].dst) & 7) == 0)
+                copy_h2d_async(jobs[j].dst, jobs[j].src, jobs[j].bytes);
+            else
+                rest.push_back(jobs[j]);
+        }
+        jobs = rest.data();
+        n = (int)rest.size();
     }
     size_t total = 0;
     for (int j = 0; j < n; ++j) total += jobs[j].bytes;
@@ -496,40 +578,6 @@ void parallel_copy(const CopyJob* jobs, int n, cudaMemcpyKind kind) {
         SQ_CUDA(cudaStreamWaitEvent(st, g_copy_ev[i], 0));
     }
     SQ_CUDA(cudaStreamSynchronize(st));
-}
-
-// Asynchronous downloads. A bulk copy-engine transfer delays every small
-// device-to-host read queued after it (the count reads of the split
-// operators wait behind it: 155 us instead of 20 us each), so a download into
-// pinned host memory is done by a few blocks storing over the host link, on a
-// lowest-priority stream: 12 blocks move about 150 GB/s of the link's 190 and
-// leave the small reads and the SMs to the work that overlaps them. Other
-// host memory is copied by the copy engine.
-constexpr int kD2HSegs = SQ_KMAX + 2;
-constexpr int kD2HBlocks = 12;
-struct D2HJobs {
-    const uint2* src[kD2HSegs];
-    uint2* dst[kD2HSegs];
-    uint64_t n8[kD2HSegs];  // 8-byte units
-    int n;
-};
-
-__global__ void __launch_bounds__(512) d2h_store_kernel(const __grid_constant__ D2HJobs j) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (int s = 0; s < j.n; ++s) {
-        const uint64_t n8 = j.n8[s];
-        const bool v16 = ((reinterpret_cast<uintptr_t>(j.src[s]) | reinterpret_cast<uintptr_t>(j.dst[s])) & 15) == 0;
-        if (v16) {
-            const uint4* src = reinterpret_cast<const uint4*>(j.src[s]);
-            uint4* dst = reinterpret_cast<uint4*>(j.dst[s]);
-            const uint64_t n16 = n8 >> 1;
-            for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) dst[i] = src[i];
-            if ((n8 & 1) && blockIdx.x == 0 && threadIdx.x == 0) j.dst[s][n8 - 1] = j.src[s][n8 - 1];
-        } else {
-            for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += stride)
-                j.dst[s][i] = j.src[s][i];
-        }
-    }
 }
 
 // Low-priority download streams: copy-engine downloads are cut into chunks
@@ -575,15 +623,10 @@ void async_copy_d2h(const CopyJob* jobs, int n, cudaEvent_t done) {
     int next = 0;
     for (int i = 0; i < n; ++i) {
         if (jobs[i].bytes == 0) continue;
-        cudaPointerAttributes at;
-        const cudaError_t pe = cudaPointerGetAttributes(&at, jobs[i].dst);
-        if (pe != cudaSuccess) (void)cudaGetLastError();  // that query's own error only
-        const bool mapped = g_d2h_engine == SQ_DOWNLOAD_SM_STORES && pe == cudaSuccess &&
-                            at.type == cudaMemoryTypeHost && at.devicePointer != nullptr &&
-                            (reinterpret_cast<uintptr_t>(jobs[i].dst) & 7) == 0 && jobs[i].bytes % 8 == 0;
-        if (mapped) {
+        void* alias = g_d2h_engine == SQ_DOWNLOAD_SM_STORES ? mapped_alias(jobs[i].dst, jobs[i].bytes) : nullptr;
+        if (alias) {
             kj.src[kj.n] = static_cast<const uint2*>(jobs[i].src);
-            kj.dst[kj.n] = static_cast<uint2*>(at.devicePointer);
+            kj.dst[kj.n] = static_cast<uint2*>(alias);
             kj.n8[kj.n] = jobs[i].bytes / 8;
             ++kj.n;
             continue;
@@ -596,7 +639,7 @@ void async_copy_d2h(const CopyJob* jobs, int n, cudaEvent_t done) {
         }
     }
     if (kj.n) {
-        d2h_store_kernel<<<blocks, 512, 0, g_async[0]>>>(kj);
+        link_copy_kernel<<<blocks, 512, 0, g_async[0]>>>(kj);
         SQ_CUDA(cudaGetLastError());
     }
     // join the chunks' streams into the first, whose event marks the end

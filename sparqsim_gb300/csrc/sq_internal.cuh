@@ -229,6 +229,9 @@ void async_copy_d2h(const CopyJob* jobs, int n, cudaEvent_t done);
 // Blocks until every asynchronous download has finished.
 void sync_async_copies();
 uint64_t read_word_mapped(const unsigned long long* dev_word);
+// Host-to-device copy on the library stream, by the SMs from mapped pinned
+// memory, else by the copy engine.
+void copy_h2d_async(void* dst, const void* src, size_t bytes);
 void set_d2h_engine(int engine);
 // Copy a host table of 64-bit words to the device at the narrowest width (2,
 // 4 or 8 bytes) that holds every word; eb_guess is tried first.

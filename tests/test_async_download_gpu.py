@@ -86,3 +86,29 @@ def test_download_engine_names():
         ps.set_download_engine("dma")
     with pytest.raises(ps.SparQInvalid):
         ps._native.call("sq_set_download_engine", 7)
+
+
+def test_upload_packed_from_pinned_memory():
+    """Uploads from pinned memory are loaded by the SMs (mapped memory), other
+    host memory goes by the copy engine: both give the same state."""
+    import torch
+    ps.System.clear()
+    ps.System.add_register("a", ps.UnsignedInteger, 40)
+    ps.System.add_register("b", ps.UnsignedInteger, 40)
+    k = ps.System.key_words()
+    n = 300_001  # odd: the 8-byte tail of a 16-byte vector copy
+    rng = np.random.default_rng(3)
+    keys = rng.integers(0, 2 ** 63, k * n, dtype=np.int64)
+    amps = rng.normal(size=2 * n)
+    kt = torch.from_numpy(keys).pin_memory()
+    at = torch.from_numpy(amps).pin_memory()
+    outs = []
+    for kp, ap in ((kt.data_ptr(), at.data_ptr()), (keys.ctypes.data, amps.ctypes.data)):
+        st = ps.SparseState()
+        ps._native.call("sq_state_upload_packed", st._h, n, kp, ap)
+        rk = np.zeros(k * n, dtype=np.uint64)
+        ra = np.zeros(2 * n, dtype=np.float64)
+        ps._native.call("sq_state_download_packed", st._h, rk.ctypes.data, ra.ctypes.data)
+        outs.append((rk, ra))
+    assert np.array_equal(outs[0][0], keys.view(np.uint64)) and np.array_equal(outs[0][1], amps)
+    assert np.array_equal(outs[1][0], outs[0][0]) and np.array_equal(outs[1][1], outs[0][1])

@@ -1,8 +1,9 @@
 """Sort grouping at sizes where the onesweep radix sort runs hundreds of
 2048-key tiles, against the oracle: 32-bit and 64-bit sort keys, every digit
 pass live, ragged last tiles, and keys concentrated in a few digits (long
-equal-digit runs inside a tile). SPARQ_RADIX_ITEMS=16 and SPARQ_RADIX_RANK=1
-run the same cases on the 4096-key tiles and the atomic-OR ranking."""
+equal-digit runs inside a tile). SPARQ_RADIX_ITEMS=16, SPARQ_RADIX_RANK=1 and
+SPARQ_RADIX_MODE=1 run the same cases on the 4096-key tiles, the atomic-OR
+ranking and the reduce-then-scan passes."""
 from __future__ import annotations
 
 import numpy as np
