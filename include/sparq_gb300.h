@@ -254,6 +254,9 @@ int sq_state_wait(sq_state* st);
  * different systems. Other host memory always goes by the copy engine. */
 #define SQ_DOWNLOAD_SM_STORES 0
 #define SQ_DOWNLOAD_COPY_ENGINE 1
+/* Both at once: the first half of each pinned destination by SM stores, the
+ * second by the copy engine. */
+#define SQ_DOWNLOAD_SPLIT 2
 int sq_set_download_engine(int engine);
 
 /* ------------------------------------------------------------------ */

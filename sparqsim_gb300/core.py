@@ -196,8 +196,9 @@ def set_download_engine(engine: str) -> None:
     about 150 GB/s on every system measured, leaving the copy engine to the
     small count reads of eager operators) or "copy" (the copy engine: no SM
     resources taken from the work it overlaps, but its rate into pinned memory
-    varied from 84 to over 170 GB/s between systems)."""
-    modes = {"sm": 0, "copy": 1}
+    varied from 84 to over 170 GB/s between systems) or "split" (half of each
+    destination each way, at once)."""
+    modes = {"sm": 0, "copy": 1, "split": 2}
     if engine not in modes:
         raise ValueError(f"download engine must be one of {sorted(modes)}")
     call("sq_set_download_engine", modes[engine])

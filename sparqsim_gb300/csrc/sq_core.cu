@@ -588,8 +588,8 @@ static cudaEvent_t g_async_ev[kAsyncStreams + 1] = {nullptr};
 static int g_d2h_engine = SQ_DOWNLOAD_SM_STORES;
 
 void set_d2h_engine(int engine) {
-    if (engine != SQ_DOWNLOAD_SM_STORES && engine != SQ_DOWNLOAD_COPY_ENGINE)
-        fail(SQ_ERR_INVALID, "download engine must be SQ_DOWNLOAD_SM_STORES or SQ_DOWNLOAD_COPY_ENGINE");
+    if (engine != SQ_DOWNLOAD_SM_STORES && engine != SQ_DOWNLOAD_COPY_ENGINE && engine != SQ_DOWNLOAD_SPLIT)
+        fail(SQ_ERR_INVALID, "download engine must be SQ_DOWNLOAD_SM_STORES, SQ_DOWNLOAD_COPY_ENGINE or SQ_DOWNLOAD_SPLIT");
     g_d2h_engine = engine;
 }
 
@@ -601,7 +601,7 @@ static int env_int(const char* name, int lo, int hi, int dflt) {
 
 void async_copy_d2h(const CopyJob* jobs, int n, cudaEvent_t done) {
     cudaStream_t st = stream();
-    static const int nstreams = env_int("SPARQ_D2H_STREAMS", 1, kAsyncStreams, 1);
+    static const int nstreams = env_int("SPARQ_D2H_STREAMS", 1, kAsyncStreams - 1, 1);
     static const int blocks = env_int("SPARQ_D2H_BLOCKS", 1, 1024, kD2HBlocks);
     if (!g_async[0]) {
         int least = 0, greatest = 0;
@@ -612,38 +612,47 @@ void async_copy_d2h(const CopyJob* jobs, int n, cudaEvent_t done) {
             SQ_CUDA(cudaEventCreateWithFlags(&g_async_ev[i], cudaEventDisableTiming));
     }
     if (n > kD2HSegs) fail(SQ_ERR_INVALID, "asynchronous download: too many arrays");
+    // stream 0 runs the store kernel, streams 1..nstreams the copy-engine chunks
+    const int used = 1 + nstreams;
     // after the library stream's queued work (the state's last writer)
     SQ_CUDA(cudaEventRecord(g_async_ev[kAsyncStreams], st));
-    for (int i = 0; i < nstreams; ++i) SQ_CUDA(cudaStreamWaitEvent(g_async[i], g_async_ev[kAsyncStreams], 0));
+    for (int i = 0; i < used; ++i) SQ_CUDA(cudaStreamWaitEvent(g_async[i], g_async_ev[kAsyncStreams], 0));
     D2HJobs kj;
     memset(&kj, 0, sizeof(kj));
     size_t total = 0;
     for (int i = 0; i < n; ++i) total += jobs[i].bytes;
     const size_t chunk = std::max<size_t>((total / (2 * nstreams) + 4095) & ~size_t(4095), 1u << 20);
     int next = 0;
-    for (int i = 0; i < n; ++i) {
-        if (jobs[i].bytes == 0) continue;
-        void* alias = g_d2h_engine == SQ_DOWNLOAD_SM_STORES ? mapped_alias(jobs[i].dst, jobs[i].bytes) : nullptr;
-        if (alias) {
-            kj.src[kj.n] = static_cast<const uint2*>(jobs[i].src);
-            kj.dst[kj.n] = static_cast<uint2*>(alias);
-            kj.n8[kj.n] = jobs[i].bytes / 8;
-            ++kj.n;
-            continue;
-        }
-        for (size_t off = 0; off < jobs[i].bytes; off += chunk) {
-            const size_t b = std::min(chunk, jobs[i].bytes - off);
-            SQ_CUDA(cudaMemcpyAsync((char*)jobs[i].dst + off, (const char*)jobs[i].src + off, b,
-                                    cudaMemcpyDeviceToHost, g_async[next]));
+    auto by_copy_engine = [&](char* dst, const char* src, size_t bytes) {
+        for (size_t off = 0; off < bytes; off += chunk) {
+            const size_t b = std::min(chunk, bytes - off);
+            SQ_CUDA(cudaMemcpyAsync(dst + off, src + off, b, cudaMemcpyDeviceToHost, g_async[1 + next]));
             next = (next + 1) % nstreams;
         }
+    };
+    for (int i = 0; i < n; ++i) {
+        if (jobs[i].bytes == 0) continue;
+        void* alias = g_d2h_engine != SQ_DOWNLOAD_COPY_ENGINE ? mapped_alias(jobs[i].dst, jobs[i].bytes) : nullptr;
+        // split mode: the first half (a multiple of 16 bytes) by the SMs, the rest by the copy engine
+        const size_t sm_bytes = !alias ? 0
+                                : g_d2h_engine == SQ_DOWNLOAD_SPLIT ? (jobs[i].bytes / 2) & ~size_t(15)
+                                                                    : jobs[i].bytes;
+        if (sm_bytes) {
+            kj.src[kj.n] = static_cast<const uint2*>(jobs[i].src);
+            kj.dst[kj.n] = static_cast<uint2*>(alias);
+            kj.n8[kj.n] = sm_bytes / 8;
+            ++kj.n;
+        }
+        if (sm_bytes < jobs[i].bytes)
+            by_copy_engine((char*)jobs[i].dst + sm_bytes, (const char*)jobs[i].src + sm_bytes,
+                           jobs[i].bytes - sm_bytes);
     }
     if (kj.n) {
         link_copy_kernel<<<blocks, 512, 0, g_async[0]>>>(kj);
         SQ_CUDA(cudaGetLastError());
     }
-    // join the chunks' streams into the first, whose event marks the end
-    for (int i = 1; i < nstreams; ++i) {
+    // join the copy streams into the first, whose event marks the end
+    for (int i = 1; i < used; ++i) {
         SQ_CUDA(cudaEventRecord(g_async_ev[i], g_async[i]));
         SQ_CUDA(cudaStreamWaitEvent(g_async[0], g_async_ev[i], 0));
     }

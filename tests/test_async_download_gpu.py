@@ -25,7 +25,7 @@ def _buffers(kind, k, n):
     return (keys, amps), keys.ctypes.data, amps.ctypes.data, lambda: (keys, amps)
 
 
-@pytest.fixture(params=["sm", "copy"])
+@pytest.fixture(params=["sm", "copy", "split"])
 def engine(request):
     """Pinned destinations stored into by the download kernel, or copied by
     the copy engine."""
