@@ -520,6 +520,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     torch.cuda.set_device(local_rank)
     _native.call("sq_init", local_rank)
     ps.set_fwht_arithmetic(args.fwht_arithmetic)
+    ps.set_group_strategy(args.group_strategy)
     h, L = args.hadamard_bits, args.layers
     table, thetas = circuit_inputs(h, L)
     circ = Circuit(ps, h, L, table, thetas)
@@ -834,6 +835,8 @@ def main():
     ap.add_argument("--cks-bits", type=int, default=20, help="main register of the CKS walk")
     ap.add_argument("--fwht-arithmetic", default="exact-sum", choices=["exact-sum", "reference"],
                     help="Hadamard butterfly arithmetic of the headline run (the other one is timed too)")
+    ap.add_argument("--group-strategy", default="autotune", choices=["autotune", "hash", "sort"],
+                    help="how split operators group entries (autotune: timed per shape class)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 

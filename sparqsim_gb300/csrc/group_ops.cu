@@ -1922,8 +1922,10 @@ __device__ __forceinline__ void group_key(const ConstKeyPtrs& keys, unsigned e, 
 }
 
 template <int K>
-__global__ void __launch_bounds__(1024) group_small_kernel(ConstKeyPtrs keys, const uint64_t* __restrict__ gmask,
-                                                           DCondSet cond, const double2* __restrict__ amp,
+__global__ void __launch_bounds__(1024) group_small_kernel(const __grid_constant__ ConstKeyPtrs keys,
+                                                           const uint64_t* __restrict__ gmask,
+                                                           const __grid_constant__ DCondSet cond,
+                                                           const double2* __restrict__ amp,
                                                            unsigned n, unsigned cap, Field tgt, Field varw,
                                                            unsigned max_digits, unsigned* __restrict__ counts,
                                                            unsigned* __restrict__ seg, unsigned* __restrict__ ghead,
