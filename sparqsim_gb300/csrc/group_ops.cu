@@ -21,6 +21,7 @@
 // a * 2^{-n/2} shortcut, the pair formulas), so results do not depend on the
 // order entries arrive in.
 #include <algorithm>
+#include <cstdlib>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -2389,7 +2390,13 @@ static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg, uint6
     cudaStream_t st = stream();
     ConstKeyPtrs ik;
     for (int w = 0; w < SQ_KMAX; ++w) ik.w[w] = s.live.keys[w];
-    if (N <= kSmallGroupMax) {
+    // states up to this many entries are grouped by one CTA (SPARQ_SMALL_GROUP_MAX lowers it)
+    static const uint64_t small_max = [] {
+        const char* e = getenv("SPARQ_SMALL_GROUP_MAX");
+        const long v = e ? atol(e) : -1;
+        return v >= 0 && v <= (long)kSmallGroupMax ? (uint64_t)v : (uint64_t)kSmallGroupMax;
+    }();
+    if (N <= small_max) {
         unsigned cap = 1024;
         while (cap < 2 * N) cap <<= 1;
         // one allocation: counts | seg | head | pass | bucket target | bucket amp
