@@ -261,11 +261,15 @@ def run_cks(args, ext) -> dict:
     _native.profile_enable(True)
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
+    if args.cuda_profiler_range == "cks":
+        torch.cuda.profiler.start()
     s.record(ext)
     for _ in range(terms):
         obj.Step()
     e.record(ext)
     e.synchronize()
+    if args.cuda_profiler_range == "cks":
+        torch.cuda.profiler.stop()
     wall = time.perf_counter() - t0
     _native.profile_enable(False)
     prof = _native.profile_read()
@@ -449,7 +453,7 @@ def run_qda(args, ext) -> dict:
                 self.updates += max(n0, n1)
                 self.peak = max(self.peak, n0, n1)
 
-    def walk(count, profile=False):
+    def walk(count, profile=False, bracket=False):
         ps.System.clear()
         ps.set_clearzero_default_eps(1e-14)  # the walk's own ClearZero calls use the bench's threshold
         run = Counting(ps.SparseState(capacity=1 << 22), False)
@@ -475,17 +479,21 @@ def run_qda(args, ext) -> dict:
             _native.profile_enable(True)
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
+        if bracket:
+            torch.cuda.profiler.start()
         s.record(ext)
         for n in range(warm, warm + sample):
             step(n)
         e.record(ext)
         e.synchronize()
+        if bracket:
+            torch.cuda.profiler.stop()
         if profile:
             _native.profile_enable(False)
         return run, s.elapsed_time(e), time.perf_counter() - t0
 
     counted, _, _ = walk(True)
-    run, ms, wall = walk(False)
+    run, ms, wall = walk(False, bracket=args.cuda_profiler_range == "qda")
     walk(False, profile=True)  # per-kernel device time of the timed steps
     prof = _native.profile_read()
     tot = sum(v[1] for v in prof.values()) or 1.0
@@ -835,6 +843,9 @@ def main():
     ap.add_argument("--cks-bits", type=int, default=20, help="main register of the CKS walk")
     ap.add_argument("--fwht-arithmetic", default="exact-sum", choices=["exact-sum", "reference"],
                     help="Hadamard butterfly arithmetic of the headline run (the other one is timed too)")
+    ap.add_argument("--cuda-profiler-range", default="none", choices=["none", "qda", "cks"],
+                    help="bracket the timed QDA steps or CKS terms with cudaProfilerStart/Stop "
+                         "(for ncu --profile-from-start off)")
     ap.add_argument("--group-strategy", default="autotune", choices=["autotune", "hash", "sort"],
                     help="how split operators group entries (autotune: timed per shape class)")
     args = ap.parse_args()
