@@ -338,6 +338,17 @@ def run_trajectories(args, ext) -> dict:
     e.synchronize()
     batched_ms = s.elapsed_time(e) / steps
     batched_wall = (time.perf_counter() - t0) / steps
+    # per-kernel device time of one more batched run (CUDA events on the library stream)
+    from sparqsim_gb300 import _native
+    _native.profile_reset()
+    _native.profile_enable(True)
+    wl.run_batched(st)
+    _native.profile_enable(False)
+    tprof = _native.profile_read()
+    ttot = sum(v[1] for v in tprof.values()) or 1.0
+    traj_kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / ttot, 4),
+                        "alg_GBps": round(v[2] / (v[1] / 1e3) / 1e9, 1) if v[1] > 0 else 0}
+                    for k, v in sorted(tprof.items(), key=lambda kv: -kv[1][1])[:8]}
     eager_n, eager_norm = st.size(), st.norm_sq()
     # the same batched circuit replayed as one CUDA graph per run (one
     # recording pass, one capture; each run is the upload and one launch)
@@ -411,6 +422,7 @@ def run_trajectories(args, ext) -> dict:
                                   "each run uploads the initial state first"},
         "plain_gpu": {"value": plain_ups, "unit": UNIT,
                       "sample": f"instances 0..{n_sample - 1}, {upd_p} updates in {plain_s:.2f} s (wall clock)"},
+        "kernels": traj_kernels,
         "batched_over_plain": batched_ups / plain_ups,
         "fwht_arithmetic": ps.get_fwht_arithmetic(),
     }
