@@ -744,6 +744,72 @@ __device__ __forceinline__ unsigned worker_rank(bool f, unsigned* s_tmp, unsigne
     return pre + in_warp;
 }
 
+// Single-pass integer Hadamard of up to 8 bits (or a batched width) whose
+// groups are all singletons (a fresh grouping with as many groups as
+// condition-passing entries):
+// a warp per group fans the entry out to its 2^n outputs. A group's data is
+// a chain of dependent reads (range, member, key), so each warp reads the
+// next group's while it writes the current one; groups are taken in a fixed
+// grid-stride order. Arithmetic and output order are those of the singleton
+// case of emit_hadamard_kernel.
+template <int K, int AM>
+__global__ void __launch_bounds__(256) emit_fanout_kernel(const __grid_constant__ EmitArgs a) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warps = (uint64_t)gridDim.x * 8u;
+    struct One {
+        unsigned s0 = 0, m = 0;
+        uint64_t v0 = 0;
+        double2 a0 = make_double2(0.0, 0.0);
+        uint64_t gk[K] = {};
+    };
+    auto fetch = [&](uint64_t gg, One& d) {
+        group_range<AM>(a, gg, d.s0, d.m);
+        if (d.m == 1u) {
+            member_at<AM>(a, d.s0, d.v0, d.a0);
+            load_key<K>(a.in_keys, group_head<AM>(a, gg, d.s0), d.gk);
+        }
+    };
+    uint64_t g = (uint64_t)blockIdx.x * 8u + (threadIdx.x >> 5);
+    One cur;
+    if (g < a.groups) fetch(g, cur);
+    for (; g < a.groups; g += warps) {
+        One nxt;
+        if (g + warps < a.groups) fetch(g + warps, nxt);
+        // a group that is not a singleton only arises in a graph replayed on
+        // other data: nothing is written for it and the replay is reported
+        const bool one = cur.m == 1u;
+        const int nbits = a.varw.width ? (int)fget<K>(cur.gk, a.varw) : a.nbits;
+        const unsigned S = 1u << nbits;
+        const double extra = a.varw.width ? 1.0 / sqrt((double)S) : a.extra;
+        Field tg = a.target;
+        tg.width = (uint8_t)nbits;
+        // singleton: a * 2^{-n/2}, sign (-1)^{popcount(t & v)} (hadamard.cpp:27-42)
+        const double2 base = cscale(cur.a0, extra);
+        // batched width 0: the entry is left as it is, never pruned
+        const bool keep = one && ((a.varw.width && nbits == 0) || keep_amp(base, a.eps));
+        unsigned long long o = 0;
+        if (lane == 0) {
+            if (!one) atomicOr(a.err, 32u);
+            o = keep ? atomicAdd(a.cursor, (unsigned long long)S) : 0ull;
+            if (a.ocnt) {
+                a.ostart[g] = o;
+                a.ocnt[g] = keep ? S : 0u;
+            }
+        }
+        o = __shfl_sync(0xffffffffu, o, 0);
+        if (keep && o + S <= a.capacity) {
+            for (unsigned c = lane; c < S; c += 32u) {
+                uint64_t kk[K];
+#pragma unroll
+                for (int w = 0; w < K; ++w) kk[w] = cur.gk[w];
+                fset<K>(kk, tg, (uint64_t)c);
+                store_out_sign<K>(a, o + c, kk, base, __popcll((uint64_t)c & cur.v0) & 1);
+            }
+        }
+        cur = nxt;
+    }
+}
+
 template <int K, int W, bool WRITE, int AM>
 __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constant__ EmitArgs a) {
     extern __shared__ double2 s_slots[];
@@ -2846,7 +2912,13 @@ static void run_group(State& s, const GroupSpec& gs) {
             SQ_CUDA(cudaGetLastError());
         } else {
             prof_begin("emit_hadamard_single_pass");
-            if (W == 32) launch_hadamard<K, 32, true>(am, (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8), smem, st, ea);
+            const unsigned fgrid = (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8);
+            // a fresh grouping (no empty groups) with as many groups as entries: all singletons
+            if (W == 32 && gs.mode == GM_HADAMARD_INT && am < 2 && G == P) {
+                ea.err = device_error_word();
+                if (am == 1) emit_fanout_kernel<K, 1><<<fgrid, 256, 0, st>>>(ea);
+                else emit_fanout_kernel<K, 0><<<fgrid, 256, 0, st>>>(ea);
+            } else if (W == 32) launch_hadamard<K, 32, true>(am, fgrid, smem, st, ea);
             else launch_hadamard<K, 256, true>(am, (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2), smem, st, ea);
             prof_end((double)P * E);
             SQ_CUDA(cudaGetLastError());
