@@ -25,6 +25,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -559,8 +560,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         import torch.distributed as dist
         dist.barrier()
 
-    clocks_path = ROOT / "gpurun_out" / f"clocks_rank{rank}.csv"
-    clocks_path.parent.mkdir(exist_ok=True)
+    # raw samples in a scratch file; their summary goes into the JSON line
+    clocks_path = Path(tempfile.gettempdir()) / f"sparqsim_clocks_rank{rank}_{os.getpid()}.csv"
     cp, cf = sample_clocks_start(clocks_path) if rank == 0 else (None, None)
     if cp is not None:
         sample_clocks_wait(clocks_path)
