@@ -61,44 +61,6 @@ def circuit_inputs(h: int, layers: int):
 
 
 # ---------------------------------------------------------------------- GB300 arm
-class Circuit:
-    def __init__(self, ps, h: int, layers: int, table, thetas):
-        self.ps, self.h, self.layers = ps, h, layers
-        ps.System.clear()
-        for name, w in (("a", A_BITS), ("b", B_BITS), ("c", C_BITS), ("t", T_BITS)):
-            ps.System.add_register(name, ps.UnsignedInteger, w)
-        self.table = table
-        self.qram = ps.QRAMCircuit_qutrit(TABLE_BITS, 32, table)
-        self.H = ps.Hadamard_Int("a", h)
-        self.mid = [ps.Fused([ps.QRAMLoad(self.qram, "a", "b"), ps.Mul_UInt_UInt("a", "b", "t"),
-                              ps.Add_UInt_UInt_InPlace("t", "c"), ps.Mul_UInt_UInt("a", "b", "t"),
-                              ps.Phase_Bool("c", 0, float(th))]) for th in thetas]
-
-    def run(self, st, count=False, qram=None, reset=True):
-        """One step from |0>. Returns the update count when count=True."""
-        ps = self.ps
-        if reset:
-            st.reset()
-        upd = 0
-        mids = self.mid if qram is None else [self._mid_with(qram, m) for m in self.mid]
-        for layer in range(self.layers):
-            n0 = st.size() if count else 0
-            self.H(st)
-            n1 = st.size() if count else 0
-            mids[layer](st)
-            self.H(st)
-            if count:
-                n2 = st.size()
-                upd += max(n0, n1) + 5 * n1 + max(n1, n2)
-        return upd
-
-    def _mid_with(self, qram, m):
-        ps = self.ps
-        ops = list(m.ops)
-        ops[0] = ps.QRAMLoad(qram, "a", "b")
-        return ps.Fused(ops)
-
-
 def sample_clocks_start(path: Path):
     q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -185,49 +147,63 @@ def ncu_traffic(kernel: str):
         return None
 
 
-def cpu_baseline_sample(h: int, table, thetas, layers_sample: int = 2):
-    """The CPU restatement of the reference path, single thread, on the first
-    `layers_sample` layers of the same full-size circuit."""
+def _canonical_rows(regs, amps):
+    """Entries sorted by (a, b, c, t): two 64-bit sort words, a << 32 | b and
+    c << 32 | t (a has 20 bits)."""
+    import numpy as np
+    k0 = (regs[:, 0] << np.uint64(32)) | regs[:, 1]
+    k1 = (regs[:, 2] << np.uint64(32)) | regs[:, 3]
+    order = np.lexsort((k1, k0))
+    return k0[order], k1[order], amps[order]
+
+
+def cpu_baseline_and_parity(ps, circ, layers_sample: int = 2):
+    """The oracle (the CPU restatement of the reference path), one thread, on
+    the first `layers_sample` layers of the same full-size circuit, timed;
+    then the GPU engine over the same layers from |0>, in the headline
+    (exact-sum) and in the reference butterfly arithmetic, compared with the
+    oracle's state: keys bit-exact, amplitudes relative to the largest."""
+    import numpy as np
     from oracle import oracle as O
-    from sparqsim_gb300._native import OP, SqInstr
-    import ctypes
     O.clear()
-    a, b, c, t = (O.add_register(1, w) for w in (A_BITS, B_BITS, C_BITS, T_BITS))
-    q = O.Qram(TABLE_BITS, 32, table)
-    st = O.OracleState()
-    from sparqsim_gb300.core import SqCond
-    nocond = SqCond()
-
-    def ins(op, regs, imm=(), cc=()):
-        x = SqInstr()
-        x.op = OP[op]
-        for i, r in enumerate(regs):
-            x.reg[i] = r
-        for i, v in enumerate(imm):
-            x.imm[i] = v
-        for i, v in enumerate(cc):
-            x.c[i] = v
-        return x
-
+    for rid in ps.System.active_ids():
+        O.add_register(int(ps.System.type_of(rid)), ps.System.size_of(rid))
+    O.register_qram(circ.qram)
+    ost = O.OracleState()
     t0 = time.perf_counter()
     upd = 0
     for layer in range(layers_sample):
-        th = float(thetas[layer])
-        n0 = st.size()
-        O._chk(O.lib().sqo_hadamard_int(st.h, a, h, ctypes.byref(nocond)))
-        n1 = st.size()
-        qi = ins("QRAM_LOAD", [a, b])
-        qi.qram = q.h
-        prog = [qi, ins("MUL_UINT_UINT", [a, b, t]), ins("ADD_UINT_UINT_INPLACE", [t, c]),
-                ins("MUL_UINT_UINT", [a, b, t]), ins("PHASE_BOOL", [c], [0], [math.cos(th), math.sin(th)])]
-        arr = (SqInstr * len(prog))(*prog)
-        O._chk(O.lib().sqo_apply(st.h, arr, len(prog)))
-        O._chk(O.lib().sqo_hadamard_int(st.h, a, h, ctypes.byref(nocond)))
-        n2 = st.size()
+        n0 = ost.size()
+        O.apply(ost, circ.H.spec())
+        n1 = ost.size()
+        O.apply(ost, circ.mid[layer].spec())
+        O.apply(ost, circ.H.spec())
+        n2 = ost.size()
         upd += max(n0, n1) + 5 * n1 + max(n1, n2)
     dt = time.perf_counter() - t0
+    ok0, ok1, oa = _canonical_rows(*ost.get())
+    del ost
     O.clear()
-    return upd, dt
+    parity = {"layers": layers_sample, "entries": int(len(oa)), "oracle": "CPU restatement of the reference path"}
+    scale = float(np.max(np.abs(oa))) if len(oa) else 1.0
+    arith0 = ps.get_fwht_arithmetic()
+    for arith in ("exact-sum", "reference"):
+        ps.set_fwht_arithmetic(arith)
+        st = ps.SparseState(capacity=max(len(oa), 1))
+        circ.run(st, layers=layers_sample)
+        gk0, gk1, ga = _canonical_rows(*st.download())
+        del st
+        same = len(ga) == len(oa) and bool(np.array_equal(gk0, ok0) and np.array_equal(gk1, ok1))
+        err = float(np.max(np.abs(ga - oa))) / scale if same and len(oa) else None
+        if arith == "exact-sum":
+            parity.update(keys_equal=same, max_rel_amp_err=err, fwht_arithmetic=arith, tolerance=1e-12,
+                          ok=bool(same and err is not None and err <= 1e-12))
+        else:
+            parity["reference_arithmetic"] = {
+                "keys_equal": same,
+                "amps_bit_exact": bool(same and np.array_equal(ga.view(np.float64), oa.view(np.float64)))}
+    ps.set_fwht_arithmetic(arith0)
+    return upd, dt, parity
 
 
 def run_cks(args, ext) -> dict:
@@ -285,7 +261,7 @@ def run_cks(args, ext) -> dict:
         "terms_timed": terms, "entries_walk_state": st.size(), "entries_accumulator": obj.current_state.size(),
         "peak_walk_entries": obj.max_system_size, "first_step_s": first_s,
         "s_per_term": ms / terms / 1e3, "wall_s_per_term": wall / terms,
-        "kernels": kernels, "kernel_s_per_term": tot / terms / 1e3,
+        "kernels": kernels, "kernel_s_per_term": tot / terms / 1e3, "roofline": leg_roofline(prof),
     }
     if n_bits == 20:
         out["reference_published"] = {"s_per_term": 4.2, "entries_after_first_step": 20971512,
@@ -293,6 +269,19 @@ def run_cks(args, ext) -> dict:
                                       "source": "docs/verification/v1e-cks-direct-oracle-linsolver.md:116-118"}
         out["speedup_vs_published"] = 4.2 / (ms / terms / 1e3)
     return out
+
+
+def leg_roofline(prof: dict) -> dict:
+    """The kernel with the largest device time in a leg's profile: its
+    algorithmic bytes per launch over its event-timed duration, against the
+    measured HBM copy peak."""
+    dom = max(prof, key=lambda k_: prof[k_][1])
+    n_l, d_ms, d_bytes = prof[dom]
+    peak, kind = measured_peak_hbm()
+    achieved = d_bytes / (d_ms / 1e3) / 1e9 if d_ms > 0 else 0.0
+    return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": kind, "traffic": ncu_traffic(dom),
+            "alg_bytes_per_launch": d_bytes / max(n_l, 1), "avg_launch_ms": d_ms / max(n_l, 1)}
 
 
 def replica_max(ms: float, device: str) -> float:
@@ -324,10 +313,13 @@ def run_trajectories(args, ext) -> dict:
     wl = NoisyTrajectories(n_traj=args.trajectories, layers=6, p=1e-3, h_min=4, h_max=8, seed=SEED)
     wl.build_batched()
     st = ps.SparseState(capacity=1 << 20)
+    from sparqsim_gb300 import predictor as P
+    P.log(True)  # untimed runs: their split sizes join the size model's training log
     upd = wl.run_batched(st, count=True)
     peak_hint = st.size()
     for _ in range(2):
         wl.run_batched(st)
+    P.log(False)
     steps = max(2, min(args.steps, 5))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -351,6 +343,33 @@ def run_trajectories(args, ext) -> dict:
                         "alg_GBps": round(v[2] / (v[1] / 1e3) / 1e9, 1) if v[1] > 0 else 0}
                     for k, v in sorted(tprof.items(), key=lambda kv: -kv[1][1])[:8]}
     eager_n, eager_norm = st.size(), st.norm_sq()
+    # batched + learned: the size model, trained on the split sizes logged so
+    # far in this run (register circuit and these trajectories), sizes the
+    # hash tables and single passes of the same batched runs
+    learned = None
+    x_log, t_log = P.read_log()
+    if x_log.shape[0] >= 16:
+        P.reset(seed=11)
+        loss = P.train(x_log, t_log, epochs=200, batch=64, lr=2e-3, seed=12)
+        P.enable(True)
+        pred0, over0 = P.stats()["predictions"], P.stats()["single_pass_overflows"]
+        wl.run_batched(st)
+        torch.cuda.synchronize()
+        s.record(ext)
+        for _ in range(steps):
+            wl.run_batched(st)
+        e.record(ext)
+        e.synchronize()
+        learned_ms = s.elapsed_time(e) / steps
+        same = st.size() == eager_n and abs(st.norm_sq() - eager_norm) <= 1e-12 * eager_norm
+        st_ = P.stats()
+        P.enable(False)
+        learned = {"value": upd / (learned_ms / 1e3), "unit": UNIT, "ms_per_step": learned_ms,
+                   "training_rows": int(x_log.shape[0]), "final_loss": loss,
+                   "predictions": st_["predictions"] - pred0, "overflows": st_["single_pass_overflows"] - over0,
+                   "same_size_and_norm_as_without": same,
+                   "note": "the size model trained on the split sizes logged earlier in this run, enabled for "
+                           "the same batched runs; results are identical with it on or off"}
     # the same batched circuit replayed as one CUDA graph per run (one
     # recording pass, one capture; each run is the upload and one launch)
     init = wl.initial_batched()
@@ -375,10 +394,13 @@ def run_trajectories(args, ext) -> dict:
     upd_p = sum(wl.run_plain(sp, t, count=True) for t in range(n_sample))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    s.record(ext)
     for t in range(n_sample):
         wl.run_plain(sp, t)
-    torch.cuda.synchronize()
+    e.record(ext)
+    e.synchronize()
     plain_s = time.perf_counter() - t0
+    plain_ev_s = s.elapsed_time(e) / 1e3
     # the oracle, one thread, plain form, on a smaller sample
     cpu = None
     if not args.no_cpu_baseline:
@@ -409,7 +431,7 @@ def run_trajectories(args, ext) -> dict:
         cpu = {"value": upd_c / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": f"instances 0..{n_cpu - 1}, plain form, {upd_c} updates in {cpu_s:.1f} s, one thread"}
     batched_ups = upd / (batched_ms / 1e3)
-    plain_ups = upd_p / plain_s
+    plain_ups = upd_p / plain_ev_s
     out = {
         "workload": (f"{wl.n_traj} noisy instances of the register circuit (a/b/c 16-bit, 2^16-word uint16 table), "
                      "Hadamard width h_t in [4,8] per instance, Pauli X/Z p=1e-3 per bit per layer, 6 layers, "
@@ -421,15 +443,23 @@ def run_trajectories(args, ext) -> dict:
                           "wall_ms_per_step": graph_wall * 1e3, "same_size_and_norm_as_eager": graph_same,
                           "note": "the batched circuit recorded once and replayed as one CUDA graph launch per run; "
                                   "each run uploads the initial state first"},
-        "plain_gpu": {"value": plain_ups, "unit": UNIT,
-                      "sample": f"instances 0..{n_sample - 1}, {upd_p} updates in {plain_s:.2f} s (wall clock)"},
+        "plain_gpu": {"value": plain_ups, "unit": UNIT, "wall_value": upd_p / plain_s,
+                      "sample": f"instances 0..{n_sample - 1}, {upd_p} updates in {plain_ev_s:.3f} s between CUDA "
+                                f"events on the library stream ({plain_s:.3f} s wall clock); one state per instance, "
+                                f"so each split's count read-back sits between the launches, as in any unbatched driver"},
         "kernels": traj_kernels,
         "batched_over_plain": batched_ups / plain_ups,
         "fwht_arithmetic": ps.get_fwht_arithmetic(),
     }
+    if learned:
+        out["batched_learned"] = learned
     if cpu:
         out["cpu"] = cpu
         out["batched_over_cpu"] = batched_ups / cpu["value"]
+    best = max(batched_ups, learned["value"] if learned else 0.0)
+    out["target"] = {"batched_learned_over_plain": best / plain_ups,
+                     "batched_learned_over_cpu": best / cpu["value"] if cpu else None,
+                     "goal": ">= 5x plain GPU, >= 20x the stated-core CPU"}
     return out
 
 
@@ -522,12 +552,175 @@ def run_qda(args, ext) -> dict:
         "updates": counted.updates, "value": counted.updates / (ms / 1e3), "unit": UNIT,
         "ms_per_walk_step": ms / sample, "wall_ms_per_walk_step": wall * 1e3 / sample,
         "projected_full_budget_s": ms / sample * total_steps / 1e3,
-        "kernels": kernels, "kernel_ms_per_walk_step": tot / sample,
+        "kernels": kernels, "kernel_ms_per_walk_step": tot / sample, "roofline": leg_roofline(prof),
     }
     if ref_s_per_step:
         out["reference_published"] = {"s_per_walk_step": ref_s_per_step, "hardware": "1x A800-SXM4-80GB",
                                       "source": "docs/verification/v1d-qda-linsolver-a800.md:48-52"}
         out["speedup_vs_published"] = ref_s_per_step / (ms / sample / 1e3)
+    return out
+
+
+def run_qda_config3(args, ext) -> dict:
+    """The QDA solve of the banded system through the QRAM encodings: A =
+    N x N symmetric, half bandwidth 4 (bandwidth 8), off-diagonals uniform in
+    [-1, 1], the diagonal set for lambda_max / lambda_min = 50; b standard
+    normal, normalised; A through Block_Encoding_via_QRAM (U_L, U_R on its
+    quantised column tree), b through State_Prep_via_QRAM; a schedule of 2000
+    walk steps. Timed: `--qda3-steps` steps at n = `--qda3-bits` after two
+    untimed ones (device time, CUDA events), projected to the 2000-step
+    solve; solved: all 2000 steps at n = `--qda3-solve-bits`, fidelity
+    against the FP64 solve. The oracle times one walk step at the solved
+    size on one host core."""
+    import numpy as np
+    import torch
+
+    import sparqsim_gb300 as ps
+    from sparqsim_gb300 import _native
+    from sparqsim_gb300 import qram_encoding as Q
+    from sparqsim_gb300.qda import Runner
+    total = 2000
+
+    class Counting(Runner):
+        def __init__(self, state):
+            super().__init__(state)
+            self.count, self.updates, self.peak, self.ops = False, 0, 0, 0
+
+        def op(self, o, dag=False):
+            n0 = self.state.size() if self.count else 0
+            super().op(o, dag)
+            self.ops += 1
+            if self.count:
+                n1 = self.state.size()
+                self.updates += max(n0, n1)
+                self.peak = max(self.peak, n0, n1)
+
+    def problem(n_bits):
+        rng = np.random.default_rng(SEED + n_bits)
+        A = Q.banded_spd(1 << n_bits, 4, 50.0, seed=SEED + n_bits)
+        return Q.QDAviaQRAM(A, rng.normal(size=1 << n_bits))
+
+    # timed steps at the larger size
+    n = args.qda3_bits
+    solver = problem(n)
+    ps.System.clear()
+    st = ps.SparseState(capacity=1 << 22)
+    run = Counting(st)
+    solver.start(run)
+    for i in range(2):
+        solver.step(run, i, total)
+    run.count = True
+    k = args.qda3_steps
+    for i in range(2, 2 + k):  # counted pass (sizes), untimed
+        solver.step(run, i, total)
+    ups, peak = run.updates, run.peak
+    run.count = False
+    ps.System.clear()
+    st = ps.SparseState(capacity=1 << 22)
+    run = Counting(st)
+    solver.start(run)
+    for i in range(2):
+        solver.step(run, i, total)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    _native.profile_reset()
+    _native.profile_enable(True)
+    t0 = time.perf_counter()
+    s.record(ext)
+    ops0 = run.ops
+    for i in range(2, 2 + k):
+        solver.step(run, i, total)
+    e.record(ext)
+    e.synchronize()
+    wall = time.perf_counter() - t0
+    _native.profile_enable(False)
+    prof = _native.profile_read()
+    ms = s.elapsed_time(e) / k
+    tot = sum(v[1] for v in prof.values()) or 1.0
+    kernels = {kk: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot, 4)}
+               for kk, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:10]}
+    out = {
+        "workload": (f"QDA via QRAM: N=2^{n} banded SPD (half bandwidth 4, off-diagonals U[-1,1], kappa(A) 50), "
+                     "b ~ N(0,1); A by Block_Encoding_via_QRAM, b by State_Prep_via_QRAM (exponent 20, data 50 "
+                     f"bits, rational 51 bits); walk steps 2..{1 + k} of a 2000-step schedule timed"),
+        "n_bits": n, "kappa_matrix": solver.kappa_matrix, "kappa_walk": solver.kappa,
+        "ms_per_walk_step": ms, "wall_ms_per_walk_step": wall * 1e3 / k, "operators_per_walk_step": (run.ops - ops0) / k,
+        "projected_solve_s": ms * total / 1e3, "updates": ups, "value": ups / (ms * k / 1e3), "unit": UNIT,
+        "peak_entries": peak, "entries": st.size(), "kernels": kernels, "roofline": leg_roofline(prof),
+    }
+    # the whole 2000-step solve at the smaller size: fidelity
+    ns = args.qda3_solve_bits
+    solver = problem(ns)
+    ps.System.clear()
+    st = ps.SparseState()
+    run = Runner(st)
+    solver.start(run)
+    torch.cuda.synchronize()
+    s.record(ext)
+    t0 = time.perf_counter()
+    for i in range(total):
+        solver.step(run, i, total)
+    e.record(ext)
+    e.synchronize()
+    solve_wall = time.perf_counter() - t0
+    x, prob, fid = solver.read_out(st)
+    out["solve"] = {"n_bits": ns, "steps": total, "s": s.elapsed_time(e) / 1e3, "wall_s": solve_wall,
+                    "fidelity_vs_fp64_solve": fid, "success_probability": prob, "kappa_walk": solver.kappa,
+                    "kappa_matrix": solver.kappa_matrix}
+    # the oracle: one walk step at the solved size (the GPU runs beside it to
+    # keep the register table; only the oracle's calls are timed)
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        class OracleTimed(Runner):
+            def __init__(self, state, ost):
+                super().__init__(state)
+                self.ost, self.t, self.updates = ost, 0.0, 0
+
+            def op(self, o, dag=False):
+                (o.dag if dag else o)(self.state)
+                n0 = self.ost.size()
+                t0 = time.perf_counter()
+                O.apply(self.ost, o.spec(dag and not o.self_adjoint))
+                self.t += time.perf_counter() - t0
+                self.updates += max(n0, self.ost.size())
+
+            def split(self, first, name, size):
+                rid = super().split(first, name, size)
+                f = ps.System.resolve(first)
+                assert O.split_register(self.ost, f, size) == rid
+                return rid
+
+            def combine(self, first, second):
+                f, s2 = ps.System.resolve(first), ps.System.resolve(second)
+                super().combine(first, second)
+                O.combine_register(self.ost, f, s2)
+
+            def add_register(self, name, type_, size):
+                rid = super().add_register(name, type_, size)
+                assert O.add_register_sync(self.ost, int(type_), size) == rid
+                return rid
+
+            def remove_register(self, reg):
+                rid = ps.System.resolve(reg)
+                super().remove_register(reg)
+                O.remove_register_sync(self.ost, rid)
+
+        solver = problem(ns)
+        ps.System.clear()
+        O.clear()
+        O.register_qram(solver.tree_A.qram)
+        O.register_qram(solver.tree_b.qram)
+        st = ps.SparseState()
+        run = OracleTimed(st, O.OracleState())
+        solver.start(run)
+        for i in range(3):
+            solver.step(run, i, total)
+        run.t, run.updates = 0.0, 0
+        solver.step(run, 3, total)
+        out["cpu_baseline"] = {"value": run.updates / run.t, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"walk step 3 at n={ns} ({run.updates} updates in {run.t:.2f} s), one thread"}
+        O.clear()
     return out
 
 
@@ -543,18 +736,24 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     ps.set_fwht_arithmetic(args.fwht_arithmetic)
     ps.set_group_strategy(args.group_strategy)
     h, L = args.hadamard_bits, args.layers
-    table, thetas = circuit_inputs(h, L)
-    circ = Circuit(ps, h, L, table, thetas)
+    from sparqsim_gb300.workloads import RegisterCircuit
+    circ = RegisterCircuit(h, L, seed=SEED).build()
+    table = circ.table
     st = ps.SparseState(capacity=1 << (2 * h))
     sp = ctypes_void_p()
     _native.call("sq_get_stream", __import__("ctypes").byref(sp))
     ext = torch.cuda.ExternalStream(sp.value)
 
+    # the split sizes of every leg are logged for the size model (host memory)
+    from sparqsim_gb300 import predictor as P
+    P.clear_log()
+    P.log(True)
     # untimed: count updates (deterministic), warm up
     updates = circ.run(st, count=True)
     final_n = st.size()
     for _ in range(max(args.warmup - 1, 0)):
         circ.run(st)
+    P.log(False)  # logging computes key sketches: never inside a timed region
     torch.cuda.synchronize()
     if world > 1:
         import torch.distributed as dist
@@ -719,13 +918,24 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     }
     if clocks:
         result["clocks"] = clocks
+    # the oracle on the first two layers of the same circuit: the CPU baseline
+    # (timed on this host, one thread) and the parity of this kernel
+    # configuration (K = 2 key words, 2^24 entries, both butterfly arithmetics)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        upd, dt, parity = cpu_baseline_and_parity(ps, circ)
+        result["cpu_baseline"] = {"value": upd / dt, "unit": UNIT, "cores": 1, "kind": "port",
+                                  "sample": f"first 2 of {args.layers} layers of the same full-size circuit, "
+                                            f"{upd} updates in {dt:.1f} s, one thread"}
+        result["parity"] = parity
     if args.trajectories and rank == 0:
         result["batched_trajectories"] = run_trajectories(args, ext)
     if args.qda_steps and rank == 0:
         result["qda_walk"] = run_qda(args, ext)
     if args.cks_terms and rank == 0:
         result["cks_walk"] = run_cks(args, ext)
-    return result, (table, thetas)
+    if args.qda3_steps and rank == 0:
+        result["qda_config3"] = run_qda_config3(args, ext)
+    return result
 
 
 def ctypes_void_p():
@@ -851,8 +1061,13 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=16, help="instances timed in the oracle")
     ap.add_argument("--qda-steps", type=int, default=10, help="QDA walk steps timed (0 skips)")
     ap.add_argument("--qda-bits", type=int, default=16, help="main register of the QDA walk (16 or 20)")
-    ap.add_argument("--qda-warm", type=int, default=2, help="untimed QDA walk steps before the timed ones")
+    ap.add_argument("--qda-warm", type=int, default=200,
+                    help="untimed QDA walk steps before the timed ones (200: the state has grown to the size the "
+                         "reference's published per-step times are quoted at)")
     ap.add_argument("--cks-terms", type=int, default=3, help="CKS LCU terms timed (0 skips)")
+    ap.add_argument("--qda3-steps", type=int, default=3, help="QDA-via-QRAM walk steps timed (0 skips)")
+    ap.add_argument("--qda3-bits", type=int, default=8, help="N = 2^bits of the timed QDA-via-QRAM walk")
+    ap.add_argument("--qda3-solve-bits", type=int, default=4, help="N = 2^bits of the 2000-step QDA-via-QRAM solve")
     ap.add_argument("--cks-bits", type=int, default=20, help="main register of the CKS walk")
     ap.add_argument("--fwht-arithmetic", default="exact-sum", choices=["exact-sum", "reference"],
                     help="Hadamard butterfly arithmetic of the headline run (the other one is timed too)")
@@ -878,13 +1093,8 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
-    result, (table, thetas) = run_gb300(args, rank, world, local_rank)
+    result = run_gb300(args, rank, world, local_rank)
     if rank == 0:
-        if not args.no_cpu_baseline and world == 1:
-            upd, dt = cpu_baseline_sample(args.hadamard_bits, table, thetas)
-            result["cpu_baseline"] = {"value": upd / dt, "unit": UNIT, "cores": 1, "kind": "port",
-                                      "sample": f"first 2 of {args.layers} layers of the same full-size circuit, "
-                                                f"{upd} updates in {dt:.1f} s, one thread"}
         print(json.dumps(result))
     if world > 1:
         import torch.distributed as dist

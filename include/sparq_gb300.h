@@ -117,6 +117,13 @@ typedef enum {
     SQ_OP_QRAM_LOAD = 36,            /* qram.cpp:15-35  reg1 ^= table[reg0 mod 2^addr_size] */
     SQ_OP_PLUS_ONE_OVERFLOW = 37,    /* SparQ_Algorithm/src/BlockEncoding/block_encoding_tridiagonal.cpp:20-83
                                         reg0 = reg0 +/- 1 mod 2^width; on the wrap reg1 = (reg1 + 1) % 2 */
+    /* A bit permutation of one register (no single reference operator; the
+     * index map of Hadamard_Partial, map_position / from_map_position,
+     * hadamard.cpp:443-466): imm0 = a set of bit positions (a mask below the
+     * register's width); dag = 0 moves those bits, in ascending order, to
+     * the lowest bits and the other bits, in order, above them; dag = 1
+     * moves them back. */
+    SQ_OP_BIT_GATHER = 38,
     /* amplitude-only or key+amplitude elementwise ops */
     SQ_OP_PHASE_BOOL = 64,           /* basic_gates.cpp:11-54  amp *= c0 if bit imm0 of reg0 */
     SQ_OP_GLOBAL_PHASE = 65,         /* parallel_phase_operations.cpp:72-107  amp *= c0 */
@@ -153,7 +160,14 @@ typedef enum {
     SQ_OP_LOOKUP_XOR = 74,
     /* TridiagParityPhase (hamiltonian_tridiagonal.cpp:88-105): amp = -amp
      * where reg0 is odd. */
-    SQ_OP_PARITY_PHASE = 75
+    SQ_OP_PARITY_PHASE = 75,
+    /* reg2 ^= angle(reg0, reg1), the rational angle word of imm0's operator
+     * (SQ_ANGLE_*) looked up in a table of sq_angle_table_create (passed in
+     * `qram`): Div_Sqrt_Arccos_UInt_UInt (quantum_arithmetic.cpp:413-432) or
+     * GetRotateAngle_Int_Int (quantum_arithmetic.cpp:458-487). A pair the
+     * table does not hold XORs 0 and is reported as SQ_ERR_INVALID at the
+     * next synchronising call. */
+    SQ_OP_ANGLE_XOR = 76
 } sq_opcode;
 
 /* One elementwise instruction. Register ids in reg[], integer constants in
@@ -182,6 +196,26 @@ int sq_init(int device);
 /* Block until all work on the library stream is done; reports device-side
  * error flags raised by bounded waits (SQ_ERR_DEVICE_TIMEOUT). */
 int sq_synchronize(void);
+/* The number of polls after which every bounded device-side wait gives up
+ * (decoupled look-backs of ClearZero, group starts, count scans and the radix
+ * sort's per-digit look-back; the hash grouping's wait on a locked slot): the
+ * waiting block raises the device error word, finishes without waiting
+ * further, and the next synchronising call returns SQ_ERR_DEVICE_TIMEOUT.
+ * 0 restores the default, 2^22 polls. Stream-ordered: launches already
+ * queued keep the limit they were queued with. No counterpart in the
+ * reference, whose kernels have no waits between blocks. */
+int sq_set_wait_limit(uint32_t polls);
+int sq_get_wait_limit(uint32_t* polls);
+/* Exercises that failure path: one ClearZero look-back (two tiles of zero
+ * amplitudes in library scratch, one block) whose predecessor tile is never
+ * published, with a limit of `polls` (1..2^20). Returns SQ_ERR_DEVICE_TIMEOUT
+ * when the wait gave up and was reported as it must be, and leaves the
+ * library usable; SQ_OK would mean the wait did not end as specified. */
+int sq_selftest_wait_timeout(uint32_t polls);
+/* Number of device allocations (cudaMalloc, cudaMallocAsync) this library
+ * has made since load; callers that must not see the library allocate can
+ * check that a call left it unchanged. */
+int sq_device_allocation_count(uint64_t* count);
 /* Number of kernels this library has launched since load. */
 int sq_launch_count(uint64_t* count);
 /* The library's CUDA stream (cudaStream_t), for callers that order their own work after it. */
@@ -277,9 +311,10 @@ int sq_set_download_engine(int engine);
  *    recorded, and the state's buffers and the library's workspace are those
  *    captured; the checksums cost one reduction and one synchronisation. The
  *    logged counts are also checked on the device (a mismatch is reported as
- *    SQ_ERR_INVALID at the next synchronising call). Tables must outlive the
- *    graph. Allocation is refused while capturing: the record pass grows
- *    every buffer. */
+ *    SQ_ERR_INVALID at the next synchronising call). A launch after the state
+ *    or a table the operators read was destroyed is refused on the host
+ *    (SQ_ERR_INVALID) before any device work. Allocation is refused while
+ *    capturing: the record pass grows every buffer. */
 typedef struct sq_graph sq_graph;
 int sq_graph_record_begin(sq_state* st);
 int sq_graph_record_end(void);
@@ -307,7 +342,8 @@ int sq_qram_create(uint32_t address_size, uint32_t data_size, const uint64_t* me
  * on the library stream: launches queued or captured earlier keep reading the
  * same device table. The words must fit the width the table was stored at
  * (that of the words it was created with); otherwise SQ_ERR_INVALID and the
- * table's content is unspecified. */
+ * table keeps its previous content (the words are checked before any is
+ * written). */
 int sq_qram_write(sq_qram* q, const uint64_t* memory, uint64_t n_words);
 int sq_qram_destroy(sq_qram* q);
 /* A classical function table for SQ_OP_LOOKUP_XOR: f(v) = dense[v] for
@@ -324,6 +360,31 @@ int sq_lookup_create(const uint64_t* dense, uint64_t dense_len, const uint64_t* 
  * lookup table gives on the GPU are the CPU's bit for bit. */
 int sq_qw_rotate_angle_words(const uint64_t* v, uint64_t n, uint32_t data_size, int positive_only,
                              uint32_t out_width, uint64_t* out);
+
+/* Angle tables for SQ_OP_ANGLE_XOR. The reference computes these angles per
+ * entry with the C library (acos, sqrt, atan2) and truncates them to a
+ * Rational register (get_rational); a last-place difference in the device's
+ * math functions would move a bit of the key, so the angles of the (lhs, rhs)
+ * register pairs an operator can meet are computed here on the host with the
+ * C library, exactly as the reference's CPU loop does, and looked up on the
+ * GPU (an open-addressing hash, probes bounded by the longest insertion):
+ *   SQ_ANGLE_DIV_SQRT_ARCCOS: acos(sqrt(lhs / rhs)) / (2 pi), unsigned values
+ *     (Div_Sqrt_Arccos_UInt_UInt, quantum_arithmetic.h:1066);
+ *   SQ_ANGLE_ROTATE: atan2(rhs, lhs) / (2 pi) in [0, 1) of the
+ *     two's-complement values, 0.25 / 0.75 for lhs = 0 (GetRotateAngle_Int_Int,
+ *     quantum_arithmetic.h:1266).
+ * The word is the angle times 2^out_width, truncated; a NaN angle (0 / 0, or
+ * lhs > rhs) gives 0 (the reference converts NaN to an integer, which C++
+ * leaves undefined). Widths 1..63; pairs are taken modulo their widths and
+ * repeats collapse. Released with sq_qram_destroy. */
+#define SQ_ANGLE_DIV_SQRT_ARCCOS 0
+#define SQ_ANGLE_ROTATE 1
+int sq_angle_table_create(int kind, uint32_t lhs_width, uint32_t rhs_width, uint32_t out_width, const uint64_t* lhs,
+                          const uint64_t* rhs, uint64_t n, sq_qram** out);
+/* The word sq_angle_table_create stores for one pair (the host computation
+ * itself, for callers that build their own tables). */
+int sq_angle_word(int kind, uint32_t lhs_width, uint32_t rhs_width, uint32_t out_width, uint64_t lhs, uint64_t rhs,
+                  uint64_t* word);
 
 /* ------------------------------------------------------------------ */
 /* Elementwise operators                                               */
@@ -377,6 +438,11 @@ int sq_hadamard_bool(sq_state* st, uint32_t reg, const sq_cond* cond);
 int sq_rot_bool(sq_state* st, uint32_t reg, uint32_t digit, const double* mat8, const sq_cond* cond, int dag);
 /* CondRot_Rational_Bool (condrot.cpp:12-152): angle 2*pi*in/2^width(in) on the 1-bit out. */
 int sq_condrot_rational_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, int dag);
+/* The same applied to the entries that satisfy `cond` only, the others left as
+ * they are: what the reference's composite operators (SPLIT_BY_CONDITIONS /
+ * MERGE_BY_CONDITIONS, system_operations.h:109-129, around U_L and U_R in
+ * block_encoding_via_QRAM.h:408-478) do to the CondRot inside them. */
+int sq_condrot_rational_bool_cond(sq_state* st, uint32_t reg_in, uint32_t reg_out, int dag, const sq_cond* cond);
 /* CondRot_General_Bool_Fast<F> (condrot.h:149-300): 2x2 unitary func(in) on
  * the 1-bit out register. The callable becomes a table: table[8*v .. 8*v+7]
  * = {m00, m01, m10, m11} as (re, im) for every v < 2^width(in) = n_values. */
@@ -384,8 +450,14 @@ int sq_condrot_general_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, con
 /* Rot_GeneralUnitary (rot.cpp:353-477): dense dim x dim unitary (dim = 2^width(reg),
  * width <= 8) on the whole register, row-major (re, im) pairs; dag applies M^dagger. */
 int sq_rot_general_unitary(sq_state* st, uint32_t reg, const double* mat, uint64_t dim, const sq_cond* cond, int dag);
-/* Hadamard_Partial (hadamard.cpp:470-712): H on a set of bit positions of reg.
- * The reference's active (hash) path is defined for one position; so is this. */
+/* Hadamard_Partial (hadamard.cpp:470-712): H on a set of bit positions of reg
+ * (repeats collapse, as in the reference's std::set). One position: the
+ * reference's active path (pairs of entries equal except that bit,
+ * a*sqrt2inv +- b*sqrt2inv). Several: H on each bit of the set, as
+ * Hadamard_Partial::operate over groups equal outside the set (hadamard.cpp:
+ * 468-570), with the one-member sign (-1)^popcount(i & v) of the Hadamard
+ * transform. Conditions are tested per entry (the reference's active path
+ * ignores them). */
 int sq_hadamard_partial(sq_state* st, uint32_t reg, const uint32_t* positions, uint32_t n_positions, const sq_cond* cond);
 
 /* ------------------------------------------------------------------ */
@@ -510,7 +582,9 @@ int sq_clear_zero(sq_state* st, double eps);
  * on `stream` (NULL = the default stream) and the call waits for it. The
  * first call on each device looks up that array's device address with the
  * device current; make that first call before capturing any stream. All calls
- * share the array: calls that overlap on the GPU race. */
+ * share the array: calls that overlap on the GPU race. No output array may
+ * overlap an input array (blocks write outputs while others still read
+ * inputs): overlapping arrays return SQ_ERR_INVALID. */
 #define SQ_NOALLOC_MAX_ENTRIES (1ull << 26)
 int sq_clear_zero_noalloc(const uint64_t* const* keys_in, const double* amps_in, uint32_t k, uint64_t n, double eps,
                           uint64_t* const* keys_out, double* amps_out, uint64_t* n_out, void* stream);

@@ -44,7 +44,7 @@ def lib():
             "sqo_hadamard_int_full": (c_int, [c_void_p, c_uint32, POINTER(SqCond)]),
             "sqo_hadamard_bool": (c_int, [c_void_p, c_uint32, POINTER(SqCond)]),
             "sqo_rot_bool": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), POINTER(SqCond), c_int]),
-            "sqo_condrot": (c_int, [c_void_p, c_uint32, c_uint32, c_int]),
+            "sqo_condrot": (c_int, [c_void_p, c_uint32, c_uint32, c_int, POINTER(SqCond)]),
             "sqo_clear_zero": (c_int, [c_void_p, c_double]),
             "sqo_condrot_general": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), c_uint64]),
             "sqo_rot_general_unitary": (c_int, [c_void_p, c_uint32, POINTER(c_double), c_uint64, POINTER(SqCond), c_int]),
@@ -209,7 +209,7 @@ def apply(state: OracleState, spec) -> None:
         m = (c_double * 8)(*spec[3])
         _chk(L.sqo_rot_bool(h, spec[1], spec[2], m, byref(spec[4]), 0))
     elif kind == "condrot":
-        _chk(L.sqo_condrot(h, spec[1], spec[2], 1 if spec[3] else 0))
+        _chk(L.sqo_condrot(h, spec[1], spec[2], 1 if spec[3] else 0, byref(spec[4])))
     elif kind == "condrot_general":
         tab = spec[3]
         _chk(L.sqo_condrot_general(h, spec[1], spec[2], tab.ctypes.data_as(POINTER(c_double)), tab.size // 8))

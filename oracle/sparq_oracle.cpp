@@ -33,6 +33,7 @@
 #include <cstdint>
 #include <cstring>
 #include <map>
+#include <set>
 #include <numeric>
 #include <stdexcept>
 #include <string>
@@ -500,6 +501,46 @@ static void apply_instr_entry(System& s, const sq_instr& in) {
                 s.get(r[2]) = k2;
                 s.get(r[3]) = k1 ^ (hit ? row_addr + (k2 - base) : 0);
             }
+            return;
+        }
+        case SQ_OP_ANGLE_XOR: {
+            // imm0 = 0: Div_Sqrt_Arccos_UInt_UInt (quantum_arithmetic.cpp:413-432)
+            //   out = acos(sqrt(1.0 * lhs / rhs)) / pi / 2 of the unsigned values;
+            // imm0 = 1: GetRotateAngle_Int_Int (:458-487) of the two's-complement
+            //   values: 0.25 / 0.75 for lhs = 0, else atan2(rhs, lhs) / pi / 2 in [0, 1).
+            // regout ^= get_rational(out, size): truncation (a NaN angle gives 0;
+            // the reference's conversion of NaN is undefined in C++).
+            double out;
+            if (in.imm[0] == 0) {
+                uint64_t lv = get_as(s, r[0]), rv = get_as(s, r[1]);
+                out = std::acos(std::sqrt(1.0 * lv / rv)) / kPi / 2;
+            } else {
+                int64_t l = get_complement(get_as(s, r[0]), size_of(r[0]));
+                int64_t rr = get_complement(get_as(s, r[1]), size_of(r[1]));
+                if (l == 0 && rr >= 0) out = 0.25;
+                else if (l == 0 && rr < 0) out = 0.75;
+                else {
+                    out = std::atan2((double)rr, (double)l) / kPi / 2;
+                    if (out < 0) out += 1;
+                }
+            }
+            uint64_t word = std::isnan(out) ? 0 : (uint64_t)(out * (double)pow2(size_of(r[2])));
+            s.get(r[2]) ^= word & width_mask(size_of(r[2]));
+            return;
+        }
+        case SQ_OP_BIT_GATHER: {  // Hadamard_Partial's index map (hadamard.cpp:443-466)
+            uint64_t& v = s.get(r[0]);
+            const size_t w = size_of(r[0]);
+            const uint64_t set = in.imm[0] & width_mask(w);
+            std::vector<size_t> lo, hi;
+            for (size_t b = 0; b < w; ++b) ((set >> b) & 1 ? lo : hi).push_back(b);
+            lo.insert(lo.end(), hi.begin(), hi.end());  // new position k takes old bit lo[k]
+            uint64_t out = 0;
+            for (size_t k = 0; k < lo.size(); ++k) {
+                if (in.dag) out |= ((v >> k) & 1ull) << lo[k];
+                else out |= ((v >> lo[k]) & 1ull) << k;
+            }
+            v = out;
             return;
         }
         case SQ_OP_PARITY_PHASE: {  // TridiagParityPhase, hamiltonian_tridiagonal.cpp:88-105
@@ -1040,9 +1081,15 @@ static void rot_general_unitary(State& st, size_t id, const complex_t* mat, bool
     clear_zero(st, g_clearzero_eps);
 }
 
-// ---------------------------------------------------------------- Hadamard_Partial (one position)
-// hadamard.cpp:619-711 (use_hash path): buckets equal except the chosen bit
-static void hadamard_partial1(State& st, size_t id, size_t pos) {
+// ---------------------------------------------------------------- Hadamard_Partial
+// One position: the reference's active path, Hadamard_Partial::operator()
+// with use_hash (hadamard.cpp:619-711): buckets of entries equal except the
+// chosen bit, pairs combined as a*sqrt2inv +- b*sqrt2inv, lone entries given
+// their partner. That path never tests the operator's conditions; this
+// restatement leaves the entries that fail them untouched (every other
+// controllable split operator of the reference does so), which is the same
+// result wherever no condition is set.
+static void hadamard_partial1(State& st, size_t id, size_t pos, const sq_cond* cond) {
     if (st.empty()) return;
     uint64_t bit = pow2(pos);
     struct Less {
@@ -1067,6 +1114,7 @@ static void hadamard_partial1(State& st, size_t id, size_t pos) {
     };
     size_t current_size = st.size();
     for (size_t i = 0; i < current_size; ++i) {
+        if (!condition_satisfied(st[i], cond)) continue;
         auto iter = buckets.find(st[i]);
         if (iter == buckets.end()) { buckets.insert({st[i], i}); continue; }
         if (st[iter->second].get(id) & bit) op_pair(i, iter->second);
@@ -1086,6 +1134,118 @@ static void hadamard_partial1(State& st, size_t id, size_t pos) {
             st.back().get(id) |= bit;
             st[k].amplitude = cscale(st[k].amplitude, kSqrt2Inv);
             st.back().amplitude = cscale(st.back().amplitude, kSqrt2Inv);
+        }
+    }
+    clear_zero(st, g_clearzero_eps);
+}
+
+// Several positions: H on each bit of the set, Hadamard_Partial::operate
+// (hadamard.cpp:468-570) over the groups of SortExceptKeyHadamard
+// (sort_state.cpp:133-170; equal on every other register and on the
+// register's bits outside the set, members in ascending value). Member
+// index i of a group is the set's bits of its value gathered in ascending
+// position order (from_map_position, hadamard.cpp:457-466); the group's
+// fan-out writes index i back at those positions (map_position, :443-452).
+// The three cases (one member, a full group, the rest) and their butterfly
+// order are the reference's. The one-member sign is (-1)^popcount(i & v):
+// the reference's expression there, bitcount(i & v & 1), reads only bit 0
+// of i & v, which is the same for one position and not the Hadamard
+// transform for more (that code path is compiled but not the one the
+// operator runs; the reference's QASM front end merges runs of single-qubit
+// h gates into one Hadamard_Partial, which needs the transform).
+static uint64_t hp_map_position(uint64_t i, const std::vector<size_t>& pos) {
+    uint64_t v = 0;
+    for (size_t k = 0; k < pos.size(); ++k) v |= ((i >> k) & 1ull) << pos[k];
+    return v;
+}
+static uint64_t hp_from_map_position(uint64_t v, const std::vector<size_t>& pos) {
+    uint64_t i = 0;
+    for (size_t k = 0; k < pos.size(); ++k) i |= ((v >> pos[k]) & 1ull) << k;
+    return i;
+}
+static void hadamard_partial_operate(size_t l, size_t r, State& st, size_t id, const std::vector<size_t>& pos,
+                                     uint64_t mask, const sq_cond* cond) {
+    size_t n = r - l;
+    size_t full_size = (size_t)pow2(pos.size());
+    size_t original_size = st.size();
+    double extra_amplitude = 1.0 / std::sqrt((double)full_size);
+    if (n == 0) return;
+    if (!condition_satisfied(st[l], cond)) return;
+    if (n == 1) {
+        uint64_t v = hp_from_map_position(st[l].get(id), pos);
+        st[l].amplitude = cscale(st[l].amplitude, extra_amplitude);
+        System base = st[l];
+        st.insert(st.end(), full_size, base);
+        for (size_t i = 0; i < full_size; ++i) {
+            size_t p = original_size + i;
+            st[p].get(id) = (st[p].get(id) & mask) + hp_map_position(i, pos);
+            if (bitcount(i & v) & 1) st[p].amplitude = complex_t(st[p].amplitude.real() * -1, st[p].amplitude.imag() * -1);
+        }
+        st[l].amplitude = 0;
+    } else if (n == full_size) {
+        for (size_t qn = 0; qn < pos.size(); ++qn)
+            for (size_t i = 0; i < full_size; ++i)
+                if ((i >> qn) & 1) {
+                    complex_t a0 = st[i + l - pow2(qn)].amplitude, a1 = st[i + l].amplitude;
+                    st[i + l - pow2(qn)].amplitude = cscale(a0 + a1, kSqrt2Inv);
+                    st[i + l].amplitude = cscale(a0 - a1, kSqrt2Inv);
+                }
+    } else {
+        System base = st[l];
+        st.insert(st.end(), full_size, base);
+        uint64_t value_mask = st[l].get(id) & mask;
+        for (size_t i = 0; i < full_size; ++i) {
+            st[i + original_size].amplitude = 0;
+            st[i + original_size].get(id) = value_mask + hp_map_position(i, pos);
+        }
+        for (size_t i = l; i < r; ++i) {
+            st[hp_from_map_position(st[i].get(id), pos) + original_size].amplitude = st[i].amplitude;
+            st[i].amplitude = 0;
+        }
+        for (size_t qn = 0; qn < pos.size(); ++qn)
+            for (size_t i = 0; i < full_size; ++i)
+                if ((i >> qn) & 1) {
+                    complex_t a0 = st[i + original_size - pow2(qn)].amplitude, a1 = st[i + original_size].amplitude;
+                    st[i + original_size - pow2(qn)].amplitude = cscale(a0 + a1, kSqrt2Inv);
+                    st[i + original_size].amplitude = cscale(a0 - a1, kSqrt2Inv);
+                }
+    }
+}
+static void hadamard_partial_multi(State& st, size_t id, std::vector<size_t> pos, const sq_cond* cond) {
+    if (st.empty()) return;
+    uint64_t setbits = 0;
+    for (size_t p : pos) setbits |= pow2(p);
+    const uint64_t mask = ~setbits;  // make_mask: every bit outside the set
+    auto pred = [&](const System& a, const System& b) {
+        for (size_t i = 0; i < g_regs.size(); ++i) {
+            if (!status_of(i)) continue;
+            uint64_t x = a.get(i), y = b.get(i);
+            if (i == id) { x &= mask; y &= mask; }
+            if (x < y) return true;
+            if (x > y) return false;
+        }
+        return a.get(id) < b.get(id);
+    };
+    auto same = [&](const System& a, const System& b) {  // compare_equal_hadamard
+        for (size_t i = 0; i < g_regs.size(); ++i) {
+            if (!status_of(i)) continue;
+            uint64_t x = a.get(i), y = b.get(i);
+            if (i == id) { x &= mask; y &= mask; }
+            if (x != y) return false;
+        }
+        return true;
+    };
+    std::sort(st.begin(), st.end(), pred);
+    size_t current_size = st.size();
+    size_t l = 0, r = 1;
+    while (true) {
+        if (r == current_size) { hadamard_partial_operate(l, r, st, id, pos, mask, cond); break; }
+        if (!same(st[l], st[r])) {
+            hadamard_partial_operate(l, r, st, id, pos, mask, cond);
+            l = r;
+            r = l + 1;
+        } else {
+            r++;
         }
     }
     clear_zero(st, g_clearzero_eps);
@@ -1246,8 +1406,23 @@ int sqo_rot_bool(void* h, uint32_t reg, uint32_t digit, const double* m8, const 
         rot_bool(*static_cast<State*>(h), reg, digit, m, cond);
     })
 }
-int sqo_condrot(void* h, uint32_t reg_in, uint32_t reg_out, int dag) {
-    SQO_TRY(condrot(*static_cast<State*>(h), reg_in, reg_out, dag != 0))
+// With conditions: SPLIT_BY_CONDITIONS / MERGE_BY_CONDITIONS
+// (system_operations.h:109-129) around the operator, as the reference's
+// composite operators apply it: the entries failing the conditions are set
+// aside, the operator (and its ClearZero) runs on the rest, they come back.
+int sqo_condrot(void* h, uint32_t reg_in, uint32_t reg_out, int dag, const sq_cond* cond) {
+    SQO_TRY({
+        State& st = *static_cast<State*>(h);
+        if (!cond || cond->count == 0) {
+            condrot(st, reg_in, reg_out, dag != 0);
+        } else {
+            State pass, rest;
+            for (auto& e : st) (condition_satisfied(e, cond) ? pass : rest).push_back(e);
+            condrot(pass, reg_in, reg_out, dag != 0);
+            pass.insert(pass.end(), rest.begin(), rest.end());
+            st.swap(pass);
+        }
+    })
 }
 int sqo_condrot_general(void* h, uint32_t reg_in, uint32_t reg_out, const double* table, uint64_t n_values) {
     SQO_TRY({
@@ -1267,9 +1442,12 @@ int sqo_rot_general_unitary(void* h, uint32_t reg, const double* mat, uint64_t d
 }
 int sqo_hadamard_partial(void* h, uint32_t reg, const uint32_t* positions, uint32_t n, const sq_cond* cond) {
     SQO_TRY({
-        if (n != 1) throw std::invalid_argument("one position");
-        (void)cond;
-        hadamard_partial1(*static_cast<State*>(h), reg, positions[0]);
+        std::set<size_t> ps(positions, positions + n);  // the reference takes a std::set
+        for (size_t p : ps)
+            if (p >= size_of(reg)) throw std::invalid_argument("position >= register size");
+        if (ps.empty()) return 0;
+        if (ps.size() == 1) hadamard_partial1(*static_cast<State*>(h), reg, *ps.begin(), cond);
+        else hadamard_partial_multi(*static_cast<State*>(h), reg, std::vector<size_t>(ps.begin(), ps.end()), cond);
     })
 }
 int sqo_clear_zero(void* h, double eps) { SQO_TRY(clear_zero(*static_cast<State*>(h), eps)) }

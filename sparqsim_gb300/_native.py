@@ -32,9 +32,11 @@ OP = dict(
     OR_UINT_UINT=20, XOR_UINT_UINT=21, LESS_SINT_SINT=22, CARRY_UINT_UINT=23,
     OVERFLOW_SINT_SINT=24, MULOVERFLOW_UINT_UINT=25, ISZERO_UINT=26, NEGATIVE_SINT=27,
     ADD_ANYINT_INPLACE=28, ASSIGN=29, COMPARE_UINT_UINT=30, LESS_UINT_UINT=31, SWAP_GENERAL=32,
-    GETMID_UINT_UINT=33, X_BOOL=34, INIT_UNSAFE=35, QRAM_LOAD=36, PLUS_ONE_OVERFLOW=37, PHASE_BOOL=64, GLOBAL_PHASE=65,
+    GETMID_UINT_UINT=33, X_BOOL=34, INIT_UNSAFE=35, QRAM_LOAD=36, PLUS_ONE_OVERFLOW=37, BIT_GATHER=38,
+    PHASE_BOOL=64, GLOBAL_PHASE=65,
     Y_BOOL=66, REFLECTION_BOOL=67, ZERO_COND_PHASE_FLIP=68, ROT_DIAGONAL=69, ROT_OFF_DIAGONAL=70,
     PAULI_NOISE=71, TRIDIAG_ELEMENT=72, TRIDIAG_SLOT_COLUMN=73, LOOKUP_XOR=74, PARITY_PHASE=75,
+    ANGLE_XOR=76,
 )
 
 
@@ -119,6 +121,9 @@ _SIGS = [
     ("sq_qram_write", c_int, [c_void_p, c_void_p, c_uint64]),
     ("sq_qram_destroy", c_int, [c_void_p]),
     ("sq_lookup_create", c_int, [c_void_p, c_uint64, c_void_p, c_void_p, c_uint64, POINTER(c_void_p)]),
+    ("sq_angle_table_create", c_int, [c_int, c_uint32, c_uint32, c_uint32, c_void_p, c_void_p, c_uint64,
+                                      POINTER(c_void_p)]),
+    ("sq_angle_word", c_int, [c_int, c_uint32, c_uint32, c_uint32, c_uint64, c_uint64, POINTER(c_uint64)]),
     ("sq_qw_rotate_angle_words", c_int, [c_void_p, c_uint64, c_uint32, c_int, c_uint32, c_void_p]),
     ("sq_apply_program", c_int, [c_void_p, POINTER(SqInstr), c_uint32]),
     ("sq_add_uint_uint", c_int, [c_void_p, c_uint32, c_uint32, c_uint32, POINTER(SqCond)]),
@@ -146,6 +151,7 @@ _SIGS = [
     ("sq_hadamard_bool", c_int, [c_void_p, c_uint32, POINTER(SqCond)]),
     ("sq_rot_bool", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), POINTER(SqCond), c_int]),
     ("sq_condrot_rational_bool", c_int, [c_void_p, c_uint32, c_uint32, c_int]),
+    ("sq_condrot_rational_bool_cond", c_int, [c_void_p, c_uint32, c_uint32, c_int, POINTER(SqCond)]),
     ("sq_condrot_general_bool", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), c_uint64]),
     ("sq_rot_general_unitary", c_int, [c_void_p, c_uint32, POINTER(c_double), c_uint64, POINTER(SqCond), c_int]),
     ("sq_hadamard_partial", c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_uint32, POINTER(SqCond)]),
@@ -177,6 +183,10 @@ _SIGS = [
     ("sq_predictor_stats", c_int, [POINTER(c_uint64), POINTER(c_uint64)]),
     ("sq_get_fwht_arithmetic", c_int, [POINTER(c_int)]),
     ("sq_set_clearzero_eps", c_int, [c_double]),
+    ("sq_set_wait_limit", c_int, [c_uint32]),
+    ("sq_get_wait_limit", c_int, [POINTER(c_uint32)]),
+    ("sq_selftest_wait_timeout", c_int, [c_uint32]),
+    ("sq_device_allocation_count", c_int, [POINTER(c_uint64)]),
     ("sq_get_clearzero_eps", c_int, [POINTER(c_double)]),
     ("sq_clear_zero", c_int, [c_void_p, c_double]),
     ("sq_clear_zero_noalloc", c_int, [POINTER(c_void_p), c_void_p, c_uint32, c_uint64, c_double, POINTER(c_void_p),

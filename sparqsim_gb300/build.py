@@ -2,8 +2,9 @@
 
 Each CUDA translation unit under csrc/ is compiled separately and in
 parallel, then linked into one shared library placed next to this file.
-Amplitude arithmetic is compiled with --fmad=false so that no multiply-add is
-contracted: complex products and butterflies then round exactly like the
+Amplitude arithmetic is compiled with --fmad=false (and host code with
+-ffp-contract=off) so that no multiply-add is contracted: complex products,
+butterflies and the host-side angle computations then round exactly like the
 reference's CPU code.
 """
 from __future__ import annotations
@@ -30,7 +31,7 @@ UNITS = [(s, Path(s).stem, []) for s in SOURCES] + \
 HEADERS = ["sq_internal.cuh", "lookback.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
+NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
               "-I" + str(INCLUDE), "-I" + str(CSRC)]
 
 

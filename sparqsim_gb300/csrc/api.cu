@@ -8,6 +8,8 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "sq_internal.cuh"
@@ -16,6 +18,10 @@ namespace sq {
 void init_device(int device);
 uint64_t launches();
 void check_device_error();
+void set_wait_limit(unsigned polls);
+unsigned wait_limit();
+void selftest_wait_timeout(unsigned polls);
+uint64_t device_allocations();
 }  // namespace sq
 
 struct sq_state {
@@ -211,6 +217,20 @@ int sq_system_set_register_type(uint32_t id, uint32_t type) {
     SQ_API_END
 }
 
+// Live objects a graph may read: device tables by address with a generation
+// number (an address the pool hands out again gets a new one), states by
+// handle. Destroying one removes it, so that a graph launch refuses on the
+// host, before any device read, when something it reads is gone.
+static std::unordered_map<const void*, uint64_t> g_live_tables;
+static std::unordered_set<const sq_state*> g_live_states;
+static uint64_t g_table_gen = 0;
+static void table_born(const void* dev) { g_live_tables[dev] = ++g_table_gen; }
+static void table_dead(const void* dev) { g_live_tables.erase(dev); }
+static uint64_t table_generation(const void* dev) {
+    auto it = g_live_tables.find(dev);
+    return it == g_live_tables.end() ? 0 : it->second;
+}
+
 // ------------------------------------------------------------------ state
 int sq_state_create(uint64_t capacity, sq_state** out) {
     SQ_API_BEGIN
@@ -230,6 +250,7 @@ int sq_state_create(uint64_t capacity, sq_state** out) {
         delete st;
         throw;
     }
+    g_live_states.insert(st);
     *out = st;
     SQ_API_END
 }
@@ -237,6 +258,7 @@ int sq_state_create(uint64_t capacity, sq_state** out) {
 int sq_state_destroy(sq_state* st) {
     SQ_API_BEGIN
     if (!st) return SQ_OK;
+    g_live_states.erase(st);
     if (st->s.d2h_done) {  // an asynchronous download may still read the buffers
         SQ_CUDA(cudaEventSynchronize(st->s.d2h_done));
         SQ_CUDA(cudaEventDestroy(st->s.d2h_done));
@@ -425,14 +447,15 @@ struct sq_graph {
     cudaGraphExec_t exec = nullptr;
     uint64_t input_sum = 0, table_sum = 0;  // the recorded input state and tables
     std::vector<std::pair<const void*, size_t>> tables;
+    std::vector<uint64_t> table_gens;  // generation of each table when recorded
     sq_state* st = nullptr;
     State pre, post;  // the state's host-side fields before and after the captured operators
-    void* ws_p[16] = {nullptr};
+    void* ws_p[WS_COUNT_MAX] = {nullptr};
     uint64_t launches = 0;
 };
 
 static State g_capture_pre;
-static void* g_capture_ws[16];
+static void* g_capture_ws[WS_COUNT_MAX];
 static uint64_t g_capture_launch0 = 0;
 
 static bool same_buffers(const Buffers& a, const Buffers& b) {
@@ -455,6 +478,7 @@ static int g_record_cur = 0;
 static uint64_t g_record_input_sum = 0;   // the state the recording started from
 static uint64_t g_record_table_sum = 0;   // the tables its operators read
 static std::vector<std::pair<const void*, size_t>> g_record_tables;
+static std::vector<uint64_t> g_record_table_gens;
 
 // Checksum of a state's entries (key words and amplitudes): a replay runs only
 // on the input it was recorded with, so that every recorded count holds.
@@ -490,6 +514,8 @@ int sq_graph_record_end(void) {
     need((s.swaps - g_record_swaps) % 2 == 0 && s.groups.cur == g_record_cur,
          "graph: the operators leave the state's buffers in other roles (an odd number of splits)");
     g_record_tables = replay().inputs;
+    g_record_table_gens.clear();
+    for (const auto& t : g_record_tables) g_record_table_gens.push_back(table_generation(t.first));
     g_record_table_sum = device_checksum(g_record_tables);
     SQ_API_END
 }
@@ -501,7 +527,7 @@ int sq_graph_capture_begin(sq_state* st) {
     SQ_CUDA(cudaStreamSynchronize(stream()));
     need(state_checksum(s) == g_record_input_sum, "graph: the capture does not start from the recorded input");
     g_capture_pre = s;
-    for (int i = 0; i < 16; ++i) g_capture_ws[i] = ws().p[i];
+    for (int i = 0; i < WS_COUNT_MAX; ++i) g_capture_ws[i] = ws().p[i];
     g_capture_launch0 = launches();
     g_capture_state = st;
     replay().pos = 0;
@@ -531,7 +557,7 @@ int sq_graph_capture_end(sq_graph** out) {
         fail(SQ_ERR_CUDA, std::string("graph: capture failed: ") + cudaGetErrorString(ce));
     }
     bool ws_same = true;
-    for (int i = 0; i < 16; ++i) ws_same = ws_same && ws().p[i] == g_capture_ws[i];
+    for (int i = 0; i < WS_COUNT_MAX; ++i) ws_same = ws_same && ws().p[i] == g_capture_ws[i];
     if (replay().pos != replay().log.size() || !ws_same) {
         cudaGraphDestroy(g);
         fail(SQ_ERR_INVALID, "graph: the captured operators differ from the recorded ones");
@@ -548,9 +574,10 @@ int sq_graph_capture_end(sq_graph** out) {
     gr->input_sum = g_record_input_sum;
     gr->table_sum = g_record_table_sum;
     gr->tables = g_record_tables;
+    gr->table_gens = g_record_table_gens;
     gr->pre = g_capture_pre;
     gr->post = post;
-    for (int i = 0; i < 16; ++i) gr->ws_p[i] = g_capture_ws[i];
+    for (int i = 0; i < WS_COUNT_MAX; ++i) gr->ws_p[i] = g_capture_ws[i];
     gr->launches = captured;
     *out = gr;
     SQ_API_END
@@ -560,9 +587,15 @@ int sq_graph_launch(sq_graph* g) {
     SQ_API_BEGIN
     need(g != nullptr && g->exec != nullptr, "null graph");
     need(replay().mode == RP_OFF, "graph: a record or capture is open");
+    // liveness on the host first: nothing below may read a freed table or state
+    need(g_live_states.count(g->st) != 0, "graph: its state has been destroyed");
+    for (size_t i = 0; i < g->tables.size(); ++i)
+        need(g->table_gens[i] != 0 && table_generation(g->tables[i].first) == g->table_gens[i],
+             "graph: a table it reads has been destroyed");
     State& s = S(g->st);
     need(same_layout(s, g->pre), "graph: the state's size or buffers differ from the captured ones");
-    for (int i = 0; i < 16; ++i) need(ws().p[i] == g->ws_p[i], "graph: the library's workspace has been reallocated");
+    for (int i = 0; i < WS_COUNT_MAX; ++i)
+        need(ws().p[i] == g->ws_p[i], "graph: the library's workspace has been reallocated");
     // every count and offset in the graph was recorded for one input: other
     // data could take other sizes, so it is refused before anything runs
     need(state_checksum(s) == g->input_sum, "graph: the state differs from the input the graph was recorded with");
@@ -621,7 +654,7 @@ int sq_state_debug_layout(const sq_state* st, char* buf, uint64_t len) {
     }
     snprintf(line, sizeof(line), "cache valid=%d cur=%d G=%llu\n", (int)c.valid, c.cur, (unsigned long long)c.G);
     o += line;
-    for (int i = 0; i < 16; ++i) {
+    for (int i = 0; i < WS_COUNT_MAX; ++i) {
         snprintf(line, sizeof(line), "ws%d=%p size=%zu\n", i, ws().p[i], ws().sz[i]);
         o += line;
     }
@@ -667,17 +700,18 @@ int sq_qram_create(uint32_t address_size, uint32_t data_size, const uint64_t* me
         delete q;
         throw;
     }
+    table_born(q->t.dev);
     *out = q;
     SQ_API_END
 }
 
 int sq_qram_write(sq_qram* q, const uint64_t* memory, uint64_t n_words) {
     SQ_API_BEGIN
-    need(q != nullptr && !q->t.lookup, "not a QRAM table");
+    need(q != nullptr && !q->t.lookup && q->t.pair_kind < 0, "not a QRAM table");
     need(memory != nullptr && n_words >= q->t.n_words, "QRAM memory must hold 2^address_size words");
-    const uint64_t all = qram_rewrite(q->t, memory);
+    const uint64_t all = qram_rewrite(q->t, memory);  // writes nothing when a word does not fit
     const uint64_t fits = q->t.elem_bytes == 2 ? 0xffffull : q->t.elem_bytes == 4 ? 0xffffffffull : ~0ull;
-    if (all & ~fits) fail(SQ_ERR_INVALID, "QRAM write: a word wider than the table's stored width");
+    if (all & ~fits) fail(SQ_ERR_INVALID, "QRAM write: a word wider than the table's stored width (table unchanged)");
     q->t.max_word = all;
     SQ_API_END
 }
@@ -685,6 +719,7 @@ int sq_qram_write(sq_qram* q, const uint64_t* memory, uint64_t n_words) {
 int sq_qram_destroy(sq_qram* q) {
     SQ_API_BEGIN
     if (!q) return SQ_OK;
+    table_dead(q->t.dev);
     dev_free(q->t.dev);  // stream-ordered: after every launch that reads it
     delete q;
     SQ_API_END
@@ -729,6 +764,102 @@ int sq_lookup_create(const uint64_t* dense, uint64_t dense_len, const uint64_t* 
         delete q;
         throw;
     }
+    table_born(q->t.dev);
+    *out = q;
+    SQ_API_END
+}
+
+// ------------------------------------------------------------------ angle tables
+// The reference's per-entry angle computations, on the host with the C
+// library, in the reference's expression order.
+static uint64_t angle_rational(double x, uint32_t size) {  // get_rational: truncation; NaN -> 0
+    if (std::isnan(x)) return 0;
+    return (uint64_t)(x * (double)(1ull << size)) & wmask(size);
+}
+static int64_t angle_sext(uint64_t v, uint32_t w) {
+    const uint64_t sign = 1ull << (w - 1);
+    return (int64_t)((v ^ sign) - sign);
+}
+static uint64_t angle_word(int kind, uint32_t lw, uint32_t rw, uint32_t ow, uint64_t l, uint64_t r) {
+    const double pi = 3.14159265358979323846;
+    l &= wmask(lw);
+    r &= wmask(rw);
+    double out;
+    if (kind == SQ_ANGLE_DIV_SQRT_ARCCOS) {  // quantum_arithmetic.cpp:413-432
+        out = std::acos(std::sqrt(1.0 * l / r)) / pi / 2;
+    } else {  // GetRotateAngle_Int_Int, quantum_arithmetic.cpp:458-487
+        const int64_t x = angle_sext(l, lw), y = angle_sext(r, rw);
+        if (x == 0 && y >= 0) out = 0.25;
+        else if (x == 0 && y < 0) out = 0.75;
+        else {
+            out = std::atan2((double)y, (double)x) / pi / 2;
+            if (out < 0) out += 1;
+        }
+    }
+    return angle_rational(out, ow);
+}
+
+int sq_angle_word(int kind, uint32_t lhs_width, uint32_t rhs_width, uint32_t out_width, uint64_t lhs, uint64_t rhs,
+                  uint64_t* word) {
+    SQ_API_BEGIN
+    need(word != nullptr, "null pointer");
+    need(kind == SQ_ANGLE_DIV_SQRT_ARCCOS || kind == SQ_ANGLE_ROTATE, "angle: unknown kind");
+    need(lhs_width >= 1 && lhs_width <= 63 && rhs_width >= 1 && rhs_width <= 63 && out_width >= 1 && out_width <= 63,
+         "angle: widths must be 1..63");
+    *word = angle_word(kind, lhs_width, rhs_width, out_width, lhs, rhs);
+    SQ_API_END
+}
+
+int sq_angle_table_create(int kind, uint32_t lhs_width, uint32_t rhs_width, uint32_t out_width, const uint64_t* lhs,
+                          const uint64_t* rhs, uint64_t n, sq_qram** out) {
+    SQ_API_BEGIN
+    need(out != nullptr && (n == 0 || (lhs != nullptr && rhs != nullptr)), "null pointer");
+    need(kind == SQ_ANGLE_DIV_SQRT_ARCCOS || kind == SQ_ANGLE_ROTATE, "angle: unknown kind");
+    need(lhs_width >= 1 && lhs_width <= 63 && rhs_width >= 1 && rhs_width <= 63 && out_width >= 1 && out_width <= 63,
+         "angle: widths must be 1..63");
+    need(n <= (1ull << 30), "angle: more than 2^30 pairs");
+    uint64_t slots = 16;
+    while (slots < 2 * n) slots <<= 1;  // load factor <= 1/2
+    const uint64_t mask = slots - 1;
+    std::vector<uint64_t> h(3 * slots, ~0ull);
+    uint32_t probe_max = 0;
+    uint64_t stored = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint64_t l = lhs[i] & wmask(lhs_width), r = rhs[i] & wmask(rhs_width);
+        const uint64_t base = pair_slot_hash(l, r);
+        for (uint32_t p = 0;; ++p) {
+            uint64_t* slot = &h[3 * ((base + p) & mask)];
+            if (slot[0] == l && slot[1] == r) break;  // a repeat
+            if (slot[0] == ~0ull && slot[1] == ~0ull) {
+                slot[0] = l;
+                slot[1] = r;
+                slot[2] = angle_word(kind, lhs_width, rhs_width, out_width, l, r);
+                probe_max = std::max(probe_max, p);
+                ++stored;
+                break;
+            }
+        }
+    }
+    sq_qram* q = new sq_qram();
+    q->t.pair_kind = kind;
+    q->t.pair_w[0] = lhs_width;
+    q->t.pair_w[1] = rhs_width;
+    q->t.pair_w[2] = out_width;
+    q->t.pair_mask = mask;
+    q->t.pair_probe = probe_max;
+    q->t.n_words = 3 * slots;
+    q->t.elem_bytes = 8;
+    q->t.max_word = wmask(out_width);
+    try {
+        q->t.dev = dev_alloc(3 * slots * 8);
+        SQ_CUDA(cudaMemcpyAsync(q->t.dev, h.data(), 3 * slots * 8, cudaMemcpyHostToDevice, stream()));
+        SQ_CUDA(cudaStreamSynchronize(stream()));  // the host table goes out of scope
+    } catch (...) {
+        if (q->t.dev) dev_free(q->t.dev);
+        delete q;
+        throw;
+    }
+    table_born(q->t.dev);
     *out = q;
     SQ_API_END
 }
@@ -1013,6 +1144,10 @@ int sq_rot_bool(sq_state* st, uint32_t reg, uint32_t digit, const double* m8, co
 }
 
 int sq_condrot_rational_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, int dag) {
+    return sq_condrot_rational_bool_cond(st, reg_in, reg_out, dag, nullptr);
+}
+
+int sq_condrot_rational_bool_cond(sq_state* st, uint32_t reg_in, uint32_t reg_out, int dag, const sq_cond* cond) {
     SQ_API_BEGIN
     need(reg_in != reg_out, "CondRot: input and output registers must differ");
     Field fi = regtable().field(reg_in);
@@ -1025,6 +1160,7 @@ int sq_condrot_rational_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, in
     g.target = fo;
     g.aux = fi;
     g.sign = dag ? -1.0 : 1.0;
+    g.cond = resolve_cond(cond);
     g.eps = cz_eps();
     group_transform(S(st), g);
     SQ_API_END
@@ -1074,19 +1210,65 @@ int sq_rot_general_unitary(sq_state* st, uint32_t reg, const double* mat, uint64
 
 int sq_hadamard_partial(sq_state* st, uint32_t reg, const uint32_t* positions, uint32_t n_positions, const sq_cond* cond) {
     SQ_API_BEGIN
-    need(positions != nullptr && n_positions == 1,
-         "Hadamard_Partial: exactly one qubit position (the reference's active path handles one)");
+    need(positions != nullptr || n_positions == 0, "Hadamard_Partial: null positions");
     Field f = regtable().field(reg);
-    need(positions[0] < f.width, "Hadamard_Partial: position >= register size");
-    GroupSpec g;
-    memset(&g, 0, sizeof(g));
-    g.mode = GM_HADAMARD_BOOL;
-    g.target = f;
-    g.target.shift = (uint8_t)(f.shift + positions[0]);
-    g.target.width = 1;
-    g.cond = resolve_cond(cond);
-    g.eps = cz_eps();
-    group_transform(S(st), g);
+    uint64_t set = 0;  // the reference takes a std::set: repeats collapse
+    for (uint32_t i = 0; i < n_positions; ++i) {
+        need(positions[i] < f.width, "Hadamard_Partial: position >= register size");
+        set |= 1ull << positions[i];
+    }
+    const uint32_t n = (uint32_t)__builtin_popcountll(set);
+    if (n == 0) return SQ_OK;
+    if (n == 1) {  // the reference's active path: pairs equal except the bit
+        GroupSpec g;
+        memset(&g, 0, sizeof(g));
+        g.mode = GM_HADAMARD_BOOL;
+        g.target = f;
+        g.target.shift = (uint8_t)(f.shift + __builtin_ctzll(set));
+        g.target.width = 1;
+        g.cond = resolve_cond(cond);
+        g.eps = cz_eps();
+        group_transform(S(st), g);
+        return SQ_OK;
+    }
+    // Several positions: gather the set's bits to the low end of the
+    // register (member index = from_map_position), H on those n low bits
+    // (Hadamard_Int's groups and butterflies are Hadamard_Partial::operate's
+    // on the gathered index), scatter back. Conditions on this register are
+    // rewritten for the gathered layout.
+    auto gather = [&](uint64_t v) {
+        uint64_t out = 0, rest = 0;
+        uint32_t lo = 0, hi = 0;
+        for (uint32_t b = 0; b < f.width; ++b) {
+            const uint64_t bit = (v >> b) & 1ull;
+            if ((set >> b) & 1ull) out |= bit << lo++;
+            else rest |= bit << hi++;
+        }
+        return out | (hi ? rest << n : 0);
+    };
+    sq_cond c2;
+    memset(&c2, 0, sizeof(c2));
+    if (cond) c2 = *cond;
+    for (uint32_t i = 0; i < c2.count && i < SQ_MAX_CONDITIONS; ++i) {
+        sq_condition& c = c2.c[i];
+        if (c.reg != reg) continue;
+        if (c.kind == SQ_COND_BIT) {
+            need(c.param < f.width, "condition bit >= register size");
+            c.param = (uint64_t)__builtin_ctzll(gather(1ull << c.param));
+        } else if (c.kind == SQ_COND_VALUE) {
+            if (f.width >= 64 || c.param <= wmask(f.width)) c.param = gather(c.param);
+        }  // nonzero and all-ones do not depend on the bit order
+    }
+    sq_instr in;
+    memset(&in, 0, sizeof(in));
+    in.op = SQ_OP_BIT_GATHER;
+    in.reg[0] = reg;
+    in.imm[0] = set;
+    const bool low = set == wmask(n);  // already the low n bits
+    if (!low) run_program(S(st), &in, 1);
+    hadamard_passes(S(st), f, n, GM_HADAMARD_INT, resolve_cond(&c2));
+    in.dag = 1;
+    if (!low) run_program(S(st), &in, 1);
     SQ_API_END
 }
 
@@ -1148,6 +1330,30 @@ int sq_get_fwht_arithmetic(int* mode) {
     SQ_API_BEGIN
     need(mode != nullptr, "null pointer");
     *mode = get_fwht_arithmetic();
+    SQ_API_END
+}
+
+int sq_device_allocation_count(uint64_t* count) {
+    SQ_API_BEGIN
+    need(count != nullptr, "null pointer");
+    *count = device_allocations();
+    SQ_API_END
+}
+
+int sq_set_wait_limit(uint32_t polls) {
+    SQ_API_BEGIN
+    set_wait_limit(polls);
+    SQ_API_END
+}
+int sq_get_wait_limit(uint32_t* polls) {
+    SQ_API_BEGIN
+    need(polls != nullptr, "null pointer");
+    *polls = wait_limit();
+    SQ_API_END
+}
+int sq_selftest_wait_timeout(uint32_t polls) {
+    SQ_API_BEGIN
+    selftest_wait_timeout(polls);
     SQ_API_END
 }
 

@@ -150,11 +150,61 @@ void check_device_error() {
     if (v) {
         SQ_CUDA(cudaMemsetAsync(device_error_word(), 0, 4, stream()));
         if (v & 32u) fail(SQ_ERR_INVALID, "a replayed graph saw other sizes than were recorded; the state is not valid");
+        if (v & 64u) fail(SQ_ERR_INVALID, "angle: a register pair has no entry in the angle table");
         if (v & 8u) fail(SQ_ERR_INVALID, "lookup: a register value has no entry in the table");
         if (v & 4u) fail(SQ_ERR_INVALID, "batched Hadamard: an entry's digit count exceeds max_digits");
         if (v & 2u) fail(SQ_ERR_DEVICE_TIMEOUT, "hash grouping gave up (table full or a bounded wait expired)");
         fail(SQ_ERR_DEVICE_TIMEOUT, "a bounded device-side wait gave up (decoupled look-back)");
     }
+}
+
+// The poll limit of every bounded device wait (0 = kSpinLimit), word 1 of
+// the device error block; stream-ordered, so launches queued before the
+// call keep the limit they were queued with.
+static unsigned g_wait_limit = 0;
+void set_wait_limit(unsigned polls) {
+    g_wait_limit = polls;
+    SQ_CUDA(cudaMemcpyAsync(device_error_word() + 1, &g_wait_limit, 4, cudaMemcpyHostToDevice, stream()));
+    SQ_CUDA(cudaStreamSynchronize(stream()));
+}
+unsigned wait_limit() { return g_wait_limit; }
+
+// One ClearZero of 2 tiles of zero amplitudes, launched as one block whose
+// ticket is preset to tile 1: it publishes its count and waits for tile 0's,
+// which no block ever publishes. The wait gives up after `polls` polls,
+// raises the error word and the block finishes (no survivors, nothing
+// written); the host then reports SQ_ERR_DEVICE_TIMEOUT. Every index stays
+// inside the 2-tile buffers.
+void selftest_wait_timeout(unsigned polls) {
+    if (polls == 0 || polls > (1u << 20)) fail(SQ_ERR_INVALID, "wait self-test: polls must be 1..2^20");
+    check_device_error();  // start from a clean error word
+    const uint64_t n = 2 * (uint64_t)kCzTile;
+    char* buf = (char*)ws().get(WS_SCRATCH_TEST, n * 8 * 2 + n * 16 * 2);
+    uint64_t* kin = (uint64_t*)buf;
+    uint64_t* kout = kin + n;
+    double2* ain = (double2*)(kout + n);
+    double2* aout = ain + n;
+    SQ_CUDA(cudaMemsetAsync(buf, 0, n * 8 * 2 + n * 16 * 2, stream()));
+    LookbackWs lb = lookback_ws(2);
+    const unsigned one = 1;
+    SQ_CUDA(cudaMemcpyAsync(lb.counter, &one, 4, cudaMemcpyHostToDevice, stream()));
+    const unsigned prev = g_wait_limit;
+    set_wait_limit(polls);
+    ConstKeyPtrs ik;
+    KeyPtrs okp;
+    memset(&ik, 0, sizeof(ik));
+    memset(&okp, 0, sizeof(okp));
+    ik.w[0] = kin;
+    okp.w[0] = kout;
+    KeySelect none;
+    memset(&none, 0, sizeof(none));
+    clearzero_kernel<1, false><<<1, kCzBlock, 0, stream()>>>(ik, ain, okp, aout, n, 1e-14, lb, 2,
+                                                              device_error_word(), none);
+    count_launch();
+    const cudaError_t le = cudaGetLastError();
+    set_wait_limit(prev);  // synchronizes: the block has finished
+    SQ_CUDA(le);
+    check_device_error();  // fails with SQ_ERR_DEVICE_TIMEOUT when the wait gave up
 }
 
 // Compacts `in` (n entries) into `out`, returns the survivor count. `out`
@@ -467,6 +517,22 @@ extern "C" int sq_clear_zero_noalloc(const uint64_t* const* keys_in, const doubl
     if (n > 0 && (!keys_in || !amps_in || !keys_out || !amps_out)) return bad(SQ_ERR_INVALID, "null array");
     for (uint32_t w = 0; n > 0 && w < k; ++w)
         if (!keys_in[w] || !keys_out[w]) return bad(SQ_ERR_INVALID, "null key-word array");
+    // outputs are written while other blocks still read inputs: no output
+    // array may overlap an input array
+    if (n > 0) {
+        auto overlap = [](const void* a, uint64_t abytes, const void* b, uint64_t bbytes) {
+            const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b;
+            return x < y + bbytes && y < x + abytes;
+        };
+        for (uint32_t w = 0; w < k; ++w) {
+            if (overlap(keys_out[w], n * 8, amps_in, n * 16)) return bad(SQ_ERR_INVALID, "an output overlaps an input");
+            for (uint32_t v = 0; v < k; ++v)
+                if (overlap(keys_out[w], n * 8, keys_in[v], n * 8)) return bad(SQ_ERR_INVALID, "an output overlaps an input");
+        }
+        if (overlap(amps_out, n * 16, amps_in, n * 16)) return bad(SQ_ERR_INVALID, "an output overlaps an input");
+        for (uint32_t v = 0; v < k; ++v)
+            if (overlap(amps_out, n * 16, keys_in[v], n * 8)) return bad(SQ_ERR_INVALID, "an output overlaps an input");
+    }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
         return bad(SQ_ERR_CUDA, "no current CUDA device");

@@ -92,6 +92,20 @@ __device__ __forceinline__ uint64_t tri_mem(uint64_t idx, uint64_t n, uint64_t e
     return tri_window_base(t >> 2, n) + (t & 3);
 }
 
+// Parallel bit extract / deposit over the set bits of m, lowest first.
+__device__ __forceinline__ uint64_t bits_extract(uint64_t v, uint64_t m) {
+    uint64_t out = 0, b = 1;
+    for (; m; m &= m - 1, b <<= 1)
+        if (v & (m & (0ull - m))) out |= b;
+    return out;
+}
+__device__ __forceinline__ uint64_t bits_deposit(uint64_t v, uint64_t m) {
+    uint64_t out = 0, b = 1;
+    for (; m; m &= m - 1, b <<= 1)
+        if (v & b) out |= m & (0ull - m);
+    return out;
+}
+
 template <int K>
 __device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2& a, unsigned* err) {
     const Field* f = in.f;
@@ -151,6 +165,14 @@ __device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2
             const bool wrap = in.dag ? v == 0 : v == top;
             fset<K>(k, f[0], in.dag ? v - 1 : v + 1);  // stored modulo 2^width
             if (wrap) fset<K>(k, f[1], (fget<K>(k, f[1]) + 1) % 2);
+            break;
+        }
+        case SQ_OP_BIT_GATHER: {
+            const uint64_t v = fget<K>(k, f[0]);
+            const uint64_t set = in.imm[0], rest = wmask(f[0].width) & ~set;  // host: set below the width
+            const unsigned ns = (unsigned)__popcll(set);
+            fset<K>(k, f[0], in.dag ? bits_deposit(v, set) | bits_deposit(shr(v, ns), rest)
+                                    : bits_extract(v, set) | shl(bits_extract(v, rest), ns));
             break;
         }
         case SQ_OP_SUB_UINT_UINT: fset<K>(k, f[2], fget<K>(k, f[2]) ^ (fget<K>(k, f[0]) - fget<K>(k, f[1]))); break;
@@ -295,6 +317,28 @@ __device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2
         case SQ_OP_PARITY_PHASE:
             if (fget<K>(k, f[0]) & 1ull) a = make_double2(-a.x, -a.y);
             break;
+        case SQ_OP_ANGLE_XOR: {
+            const uint64_t l = fget<K>(k, f[0]), r = fget<K>(k, f[1]);
+            const uint64_t* t = static_cast<const uint64_t*>(in.table);
+            const uint64_t mask = in.imm[0];
+            const unsigned probes = (unsigned)in.imm[1];
+            const uint64_t h = pair_slot_hash(l, r);
+            uint64_t w = 0;
+            bool found = false;
+            for (unsigned i = 0; i <= probes; ++i) {
+                const uint64_t* slot = t + 3 * ((h + i) & mask);
+                const uint64_t x = __ldg(slot), y = __ldg(slot + 1);
+                if (x == l && y == r) {
+                    w = __ldg(slot + 2);
+                    found = true;
+                    break;
+                }
+                if (x == ~0ull && y == ~0ull) break;
+            }
+            if (!found) atomicOr(err, 64u);
+            fset<K>(k, f[2], fget<K>(k, f[2]) ^ w);
+            break;
+        }
         case SQ_OP_PHASE_BOOL:
             if ((fget<K>(k, f[0]) >> in.imm[0]) & 1ull) a = cmul(a, in.c[0]);
             break;
@@ -484,6 +528,10 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
             W(0); W(1);
             distinct(in.reg[0], in.reg[1], "PlusOneAndOverflow");
             break;
+        case SQ_OP_BIT_GATHER:
+            W(0);
+            if (d.f[0].width < 64 && (in.imm[0] >> d.f[0].width)) fail(SQ_ERR_INVALID, "bit gather: position >= register size");
+            break;
         case SQ_OP_NEG_UINT:
         case SQ_OP_ABS_SINT:
         case SQ_OP_SQRT_UINT:
@@ -515,6 +563,7 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
             distinct(in.reg[0], in.reg[1], "QRAMLoad");
             const QramTable* q = reinterpret_cast<const QramTable*>(in.qram);
             if (!q || !q->dev) fail(SQ_ERR_INVALID, "QRAMLoad: null table");
+            if (q->lookup || q->pair_kind >= 0) fail(SQ_ERR_INVALID, "QRAMLoad: not a QRAM table");
             if (d.f[1].width < 64 && q->max_word > wmask(d.f[1].width))
                 fail(SQ_ERR_INVALID, "QRAMLoad: table word wider than the data register");
             d.table = q->dev;
@@ -579,6 +628,21 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
             break;
         }
         case SQ_OP_PARITY_PHASE: R(0); am |= 3u; break;
+        case SQ_OP_ANGLE_XOR: {
+            R(0); R(1); W(2);
+            distinct(in.reg[0], in.reg[2], "angle");
+            distinct(in.reg[1], in.reg[2], "angle");
+            const QramTable* q = reinterpret_cast<const QramTable*>(in.qram);
+            if (!q || !q->dev || q->pair_kind < 0) fail(SQ_ERR_INVALID, "angle: not a table of sq_angle_table_create");
+            if ((int)in.imm[0] != q->pair_kind) fail(SQ_ERR_INVALID, "angle: the table was made for the other operator");
+            if (d.f[0].width != q->pair_w[0] || d.f[1].width != q->pair_w[1] || d.f[2].width != q->pair_w[2])
+                fail(SQ_ERR_INVALID, "angle: the table was made for other register widths");
+            d.table = q->dev;
+            d.imm[0] = q->pair_mask;
+            d.imm[1] = q->pair_probe;
+            replay_note_input(q->dev, q->n_words * 8);
+            break;
+        }
         case SQ_OP_PAULI_NOISE: {
             R(0); W(1); W(2); W(3);
             const QramTable* q = reinterpret_cast<const QramTable*>(in.qram);
@@ -639,7 +703,7 @@ void run_program(State& s, const sq_instr* prog, uint32_t n) {
 
 // QRAM tables are stored at the narrowest width that holds every word. The
 // words are copied as they are, then narrowed on the GPU, which also ORs them
-// together (the highest bit any word uses).
+// together (the highest bit any word uses). dst == nullptr: the OR only.
 __global__ void qram_pack_kernel(const uint64_t* __restrict__ src, uint64_t n, uint32_t eb, void* __restrict__ dst,
                                  unsigned long long* __restrict__ all) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -647,6 +711,7 @@ __global__ void qram_pack_kernel(const uint64_t* __restrict__ src, uint64_t n, u
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const uint64_t v = src[i];
         acc |= v;
+        if (!dst) continue;
         if (eb == 2) ((unsigned short*)dst)[i] = (unsigned short)v;
         else if (eb == 4) ((unsigned int*)dst)[i] = (unsigned int)v;
     }
@@ -659,7 +724,9 @@ static uint32_t width_bytes(uint64_t all) { return all <= 0xffffull ? 2 : (all <
 
 // New words for an existing table, in place and at its stored width: its
 // device address (held by queued or captured launches) does not change.
-// Returns the OR of the new words.
+// Returns the OR of the new words. The words are checked against the stored
+// width before the table is touched: when one does not fit, the table keeps
+// its content (and the caller reports the error).
 uint64_t qram_rewrite(QramTable& t, const uint64_t* host_words) {
     cudaStream_t st = stream();
     const uint64_t n = t.n_words;
@@ -667,12 +734,21 @@ uint64_t qram_rewrite(QramTable& t, const uint64_t* host_words) {
     unsigned long long* all = (unsigned long long*)dev_alloc(8);
     copy_h2d_async(raw, host_words, n * 8);
     SQ_CUDA(cudaMemsetAsync(all, 0, 8, st));
+    const bool narrow = t.elem_bytes != 8;  // 8-byte words fit whatever they are
     prof_begin("qram_pack");
-    qram_pack_kernel<<<grid_for(n, 256), 256, 0, st>>>(raw, n, t.elem_bytes, t.dev, all);
-    prof_end((double)n * (8 + (t.elem_bytes == 8 ? 0 : t.elem_bytes)));
+    qram_pack_kernel<<<grid_for(n, 256), 256, 0, st>>>(raw, n, t.elem_bytes, narrow ? nullptr : t.dev, all);
+    prof_end((double)n * 8);
     SQ_CUDA(cudaGetLastError());
     const uint64_t h = read_word_mapped(all);  // synchronises: the caller's buffer may go out of scope
-    if (raw != t.dev) dev_free(raw);
+    const uint64_t fits = t.elem_bytes == 2 ? 0xffffull : t.elem_bytes == 4 ? 0xffffffffull : ~0ull;
+    if (narrow && !(h & ~fits)) {
+        SQ_CUDA(cudaMemsetAsync(all, 0, 8, st));
+        prof_begin("qram_pack");
+        qram_pack_kernel<<<grid_for(n, 256), 256, 0, st>>>(raw, n, t.elem_bytes, t.dev, all);
+        prof_end((double)n * (8 + t.elem_bytes));
+        SQ_CUDA(cudaGetLastError());
+    }
+    if (raw != t.dev) dev_free(raw);  // stream-ordered: after the pack
     dev_free(all);
     return h;
 }

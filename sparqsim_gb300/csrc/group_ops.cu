@@ -1567,6 +1567,11 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
         if (SHAPE == H_SINGLE) continue;  // not reached: every group took the path above
         double2 v[8];
         unsigned rows = 0xffu;  // rows j that may hold a kept slot (warp-uniform)
+        // the slot of v[j]: layout A (j << 9 | tid) after the sparse-bucket
+        // product, layout P2 (tid_hi << 9 | j << 6 | tid_lo) after the FWHT;
+        // either way a warp's 32 lanes hold 32 consecutive slots of row j
+        bool p2 = FULL;
+#define SQ_B2 (((tid >> 6) << 9) | (tid & 63u))
         if (!FULL && a.mode == GM_HADAMARD_FULL && m <= 11u) {
             // sparse bucket: direct product, members in ascending target order (hadamard.cpp:267-304)
             for (unsigned j = tid; j < m; j += 512u) {
@@ -1662,15 +1667,10 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
 #pragma unroll
             for (int j = 0; j < 8; ++j) ls[swz8(b1 | ((unsigned)j << 3))] = x[j];
             __syncthreads();
-            const unsigned b2 = ((tid >> 6) << 9) | (tid & 63u);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) x[j] = ls[swz8(b2 | ((unsigned)j << 6))];
-            fwht8(x);  // P2: bits 6-8
-#pragma unroll
-            for (int j = 0; j < 8; ++j) ls[swz8(b2 | ((unsigned)j << 6))] = x[j];
-            __syncthreads();
-#pragma unroll
-            for (int j = 0; j < 8; ++j) x[j] = ls[swz8(((unsigned)j << 9) | tid)];
+            for (int j = 0; j < 8; ++j) x[j] = ls[swz8(SQ_B2 | ((unsigned)j << 6))];
+            fwht8(x);  // P2: bits 6-8; the outputs are taken from this layout
+            p2 = true;
             const int e2 = fix_out_exp(emax, 12);
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
@@ -1684,13 +1684,17 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
                 }
             }
         }
-        // kept slots in ascending slot order: row j (slot bits 9..11), then warp, then lane
+        // kept slots in ascending slot order: the 128 runs of 32 consecutive
+        // slots (run = slot >> 5), counted and ranked in run order
+        unsigned* const s_cnt_run = &s_cnt[0][0];
+        unsigned* const s_ball_run = &s_ball[0][0];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const unsigned ball = ((rows >> j) & 1u) ? __ballot_sync(0xffffffffu, keep_amp(v[j], a.eps)) : 0u;
             if (lane == 0) {
-                s_cnt[j][warp] = __popc(ball);
-                s_ball[j][warp] = ball;
+                const unsigned run = (p2 ? (SQ_B2 | ((unsigned)j << 6)) : (((unsigned)j << 9) | tid)) >> 5;
+                s_cnt_run[run] = __popc(ball);
+                s_ball_run[run] = ball;
             }
         }
         __syncthreads();
@@ -1736,16 +1740,18 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
             load_key<K>(a.in_keys, group_head<AM>(a, g, s0), gk);
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                const unsigned ball = s_ball[j][warp];
+                const unsigned slot = p2 ? (SQ_B2 | ((unsigned)j << 6)) : (((unsigned)j << 9) | tid);
+                const unsigned ball = s_ball_run[slot >> 5];
                 if (!((ball >> lane) & 1u)) continue;
                 uint64_t kk[K];
 #pragma unroll
                 for (int w = 0; w < K; ++w) kk[w] = gk[w];
-                fset<K>(kk, tg, (uint64_t)(((unsigned)j << 9) | tid));
-                store_out<K>(a, o + s_cnt[j][warp] + __popc(ball & lt), kk, v[j]);
+                fset<K>(kk, tg, (uint64_t)slot);
+                store_out<K>(a, o + s_cnt_run[slot >> 5] + __popc(ball & lt), kk, v[j]);
             }
         }
         __syncthreads();
+#undef SQ_B2
     }
     ticket_exit(a.ticket);
 }
@@ -1903,7 +1909,7 @@ __global__ void __launch_bounds__(256) hash_insert_kernel(ConstKeyPtrs keys, con
                     continue;  // lost the race: re-read this slot
                 }
                 if (v == kSlotLocked) {
-                    if (++spins > kSpinLimit) {
+                    if (++spins > spin_limit(err)) {
                         atomicOr(err, 2u);
                         break;
                     }

@@ -2,8 +2,9 @@
 //
 // Tiles take their index from an atomic counter in the order they start, so a
 // tile only ever waits on tiles that are already resident and running; that is
-// what guarantees progress. Every wait is still bounded: after kSpinLimit
-// polls the waiting tile raises bit 0 of the device error word, treats the
+// what guarantees progress. Every wait is still bounded: after a limit of
+// polls (word 1 of the device error block, sq_set_wait_limit; kSpinLimit when
+// 0) the waiting tile raises bit 0 of the device error word, treats the
 // missing predecessor as zero and finishes, and the host reports
 // SQ_ERR_DEVICE_TIMEOUT for the operation instead of hanging.
 #pragma once
@@ -13,6 +14,13 @@
 namespace sq {
 
 constexpr unsigned kSpinLimit = 1u << 22;
+
+// The poll limit of bounded waits: word 1 of the error block `err` points
+// into (written by the host between launches), kSpinLimit when it is 0.
+__device__ __forceinline__ unsigned spin_limit(const unsigned* err) {
+    const unsigned v = *(const volatile unsigned*)(err + 1);
+    return v ? v : kSpinLimit;
+}
 
 // 64-bit status word: bits 63..62 = flag (0 none, 1 aggregate, 2 inclusive
 // prefix), bits 61..0 = value.
@@ -43,6 +51,7 @@ __device__ __forceinline__ unsigned long long lb_warp_exclusive(unsigned long lo
     unsigned long long exclusive = 0;
     long long base = tile - 1;
     unsigned spins = 0;
+    const unsigned limit = spin_limit(err);
     while (true) {
         const long long idx = base - (long long)lane;
         unsigned long long s = idx >= 0 ? lb_load(&status[idx]) : kFlagPre;
@@ -52,7 +61,7 @@ __device__ __forceinline__ unsigned long long lb_warp_exclusive(unsigned long lo
         const int first_pre = pre_mask ? __ffs(pre_mask) - 1 : 32;
         const unsigned needed = first_pre >= 31 ? 0xffffffffu : ((2u << first_pre) - 1u);
         if (bad_mask & needed) {
-            if (++spins > kSpinLimit) {
+            if (++spins > limit) {
                 if (lane == 0) atomicOr(err, 1u);
                 // give up: count missing predecessors as zero
                 unsigned long long v = (lane <= (unsigned)first_pre && flag != 0u) ? (s & kValMask) : 0ull;

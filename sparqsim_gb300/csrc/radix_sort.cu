@@ -55,6 +55,7 @@ __device__ __forceinline__ unsigned rs_lookback(unsigned* status, unsigned tile,
     }
     lb32_store_relaxed(&status[(size_t)tile * kRadix + d], kFlag32Agg | cnt);
     unsigned excl = 0, spins = 0;
+    const unsigned limit = spin_limit(err);
     long long t = (long long)tile - 1;  // next predecessor to read
     while (true) {
         unsigned s[kRsWindow];
@@ -81,7 +82,7 @@ __device__ __forceinline__ unsigned rs_lookback(unsigned* status, unsigned tile,
             spins = 0;
             continue;
         }
-        if (++spins > kSpinLimit) {  // count the missing predecessors as zero
+        if (++spins > limit) {  // count the missing predecessors as zero
             atomicOr(err, 1u);
             break;
         }

@@ -172,10 +172,15 @@ int num_sms() {
     return g_sms;
 }
 
+// Device allocations made by this library (cudaMalloc and cudaMallocAsync).
+static std::atomic<uint64_t> g_dev_allocs{0};
+uint64_t device_allocations() { return g_dev_allocs.load(); }
+
 static unsigned int* g_err_word = nullptr;
 unsigned int* device_error_word() {
     if (!g_err_word) {
         (void)stream();
+        ++g_dev_allocs;
         SQ_CUDA(cudaMalloc(&g_err_word, 256));
         SQ_CUDA(cudaMemset(g_err_word, 0, 256));
     }
@@ -428,6 +433,7 @@ void* dev_alloc(size_t bytes) {
     if (capturing()) fail(SQ_ERR_UNSUPPORTED, "capture: a buffer would grow; the record pass must run the same operators");
     if (bytes == 0) bytes = 16;
     void* p = nullptr;
+    ++g_dev_allocs;
     cudaError_t e = cudaMallocAsync(&p, bytes, stream());
     if (e != cudaSuccess) {
         (void)cudaGetLastError();

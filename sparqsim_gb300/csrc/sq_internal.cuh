@@ -171,7 +171,21 @@ struct QramTable {
     bool lookup = false;
     uint64_t dense_len = 0;
     uint64_t n_sparse = 0;
+    // an angle table (SQ_OP_ANGLE_XOR): slots of 3 u64 words (lhs, rhs,
+    // word), both keys ~0 when empty; slot count pair_mask + 1
+    int pair_kind = -1;
+    uint32_t pair_w[3] = {0, 0, 0};
+    uint64_t pair_mask = 0;
+    uint32_t pair_probe = 0;  // longest insertion probe: lookups stop after it
 };
+
+// The slot of an angle table's (lhs, rhs) pair, the same on host and device.
+__host__ __device__ __forceinline__ uint64_t pair_slot_hash(uint64_t a, uint64_t b) {
+    uint64_t z = a * 0x9e3779b97f4a7c15ull ^ (b + 0x632be59bd9b4e019ull + (a << 6) + (a >> 2));
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
 
 // ------------------------------------------------------------------ state
 struct Buffers {
@@ -305,12 +319,6 @@ void free_buffers(Buffers& b);
 void swap_live_spare(State& s);
 
 // Workspace (grow-only device scratch shared by all operators).
-struct Workspace {
-    void* p[16] = {nullptr};
-    size_t sz[16] = {0};
-    void* get(int slot, size_t bytes);
-};
-Workspace& ws();
 enum WsSlot {
     WS_SORT_KEY0 = 0,
     WS_SORT_KEY1,
@@ -328,8 +336,16 @@ enum WsSlot {
     WS_CURSOR,
     WS_SKETCH,
     WS_OUTPUT,
+    WS_SCRATCH_TEST,  // buffers of the bounded-wait self-test
     WS_COUNT_MAX
 };
+struct Workspace {
+    void* p[WS_COUNT_MAX] = {nullptr};
+    size_t sz[WS_COUNT_MAX] = {0};
+    void* get(int slot, size_t bytes);
+};
+Workspace& ws();
+
 
 // ------------------------------------------------------------------ launch helpers
 inline unsigned grid_for(uint64_t n, int block, int per_sm = 8) {

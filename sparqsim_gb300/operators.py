@@ -50,7 +50,7 @@ def _run(state: SparseState, spec) -> None:
         m = (c_double * 8)(*spec[3])
         call("sq_rot_bool", h, spec[1], spec[2], m, byref(spec[4]), 0)
     elif kind == "condrot":
-        call("sq_condrot_rational_bool", h, spec[1], spec[2], 1 if spec[3] else 0)
+        call("sq_condrot_rational_bool_cond", h, spec[1], spec[2], 1 if spec[3] else 0, byref(spec[4]))
     elif kind == "condrot_general":
         tab = spec[3]
         call("sq_condrot_general_bool", h, spec[1], spec[2], tab.ctypes.data_as(ctypes.POINTER(c_double)), tab.size // 8)
@@ -611,7 +611,7 @@ class CondRot_Rational_Bool(BaseOperator):
             raise ValueError("CondRot_Rational_Bool: input must be Rational and output Boolean")
 
     def spec(self, dag=False):
-        return ("condrot", self.register_in, self.register_out, dag)
+        return ("condrot", self.register_in, self.register_out, dag, self._cond())
 
 
 CondRot_Fixed_Bool = CondRot_Rational_Bool
@@ -726,16 +726,125 @@ class PlusOneAndOverflow(ElementwiseOperator):
         ins.reg[1] = self.overflow
 
 
+SQ_ANGLE_DIV_SQRT_ARCCOS, SQ_ANGLE_ROTATE = 0, 1
+
+
+class AngleTable:
+    """The rational angle words of Div_Sqrt_Arccos_UInt_UInt or
+    GetRotateAngle_Int_Int for a set of (lhs, rhs) register pairs, computed
+    on the host with the C library exactly as the reference's CPU loop does
+    (quantum_arithmetic.cpp:413-432, 458-487) and looked up on the GPU
+    (sq_angle_table_create), so that the angle bits in the keys are the
+    CPU's."""
+
+    def __init__(self, kind: int, lhs_width: int, rhs_width: int, out_width: int, lhs, rhs):
+        import numpy as np
+        l = np.ascontiguousarray(np.asarray(lhs, dtype=np.uint64).reshape(-1))
+        r = np.ascontiguousarray(np.asarray(rhs, dtype=np.uint64).reshape(-1))
+        if l.size != r.size:
+            raise ValueError("AngleTable: lhs and rhs differ in length")
+        self.kind, self.widths = int(kind), (int(lhs_width), int(rhs_width), int(out_width))
+        self.pairs = int(l.size)
+        h = ctypes.c_void_p()
+        call("sq_angle_table_create", self.kind, *self.widths, l.ctypes.data_as(ctypes.c_void_p),
+             r.ctypes.data_as(ctypes.c_void_p), l.size, byref(h))
+        self._h = h
+
+    @staticmethod
+    def word(kind: int, lhs_width: int, rhs_width: int, out_width: int, lhs: int, rhs: int) -> int:
+        w = ctypes.c_uint64()
+        call("sq_angle_word", int(kind), int(lhs_width), int(rhs_width), int(out_width), int(lhs), int(rhs), byref(w))
+        return w.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                from ._native import lib
+                lib().sq_qram_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+class _AngleXor(_Regs, SelfAdjointOperator):
+    """out ^= angle(lhs, rhs) (XOR-out, self-adjoint). The angle comes from
+    `table` (an AngleTable made for these register widths); without one, the
+    distinct (lhs, rhs) pairs of the state are read back, their angles
+    computed on the host and applied (one round trip)."""
+
+    opcode = "ANGLE_XOR"
+    kind = SQ_ANGLE_DIV_SQRT_ARCCOS
+
+    def __init__(self, lhs, rhs, out, table: AngleTable | None = None):
+        super().__init__(lhs, rhs, out)
+        self.table = table
+
+    def _fill(self, ins, dag):
+        _set_regs(ins, *self.regs)
+        ins.imm[0] = self.kind
+        if self.table is not None:
+            ins.qram = self.table._h.value
+
+    def _table_for(self, state: SparseState) -> AngleTable:
+        import numpy as np
+        regs, _ = state.download()
+        pairs = np.unique(regs[:, self.regs[:2]], axis=0) if len(regs) else np.zeros((0, 2), dtype=np.uint64)
+        return AngleTable(self.kind, *(System.size_of(r) for r in self.regs), pairs[:, 0], pairs[:, 1])
+
+    def __call__(self, state: SparseState) -> None:
+        if self.table is None:
+            op = type(self)(*self.regs, table=self._table_for(state))
+            self.copy_control_conditions_to(op)
+            _run(state, op.spec(False))
+            return
+        super().__call__(state)
+
+    def dag(self, state: SparseState) -> None:
+        self(state)
+
+
+class Div_Sqrt_Arccos_UInt_UInt(_AngleXor):
+    """out ^= get_rational(acos(sqrt(lhs / rhs)) / (2 pi)) (quantum_arithmetic.cpp:413-432)."""
+
+    kind = SQ_ANGLE_DIV_SQRT_ARCCOS
+
+
+class GetRotateAngle_Int_Int(_AngleXor):
+    """out ^= get_rational(atan2(rhs, lhs) / (2 pi) in [0, 1)), 0.25 / 0.75 for
+    lhs = 0, of the two's-complement values (quantum_arithmetic.cpp:458-487)."""
+
+    kind = SQ_ANGLE_ROTATE
+
+
+class BitGather(ElementwiseOperator):
+    """A bit permutation of one register: the bits of `mask` move, in
+    ascending order, to the lowest bits and the others, in order, above
+    them; dag moves them back. It is the index map of Hadamard_Partial
+    (map_position / from_map_position, hadamard.cpp:443-466)."""
+
+    opcode = "BIT_GATHER"
+
+    def __init__(self, reg, mask: int):
+        super().__init__()
+        self.id = _R(reg)
+        self.mask = int(mask)
+
+    def _fill(self, ins, dag):
+        ins.reg[0] = self.id
+        ins.imm[0] = self.mask
+
+
 class Hadamard_Partial(SelfAdjointOperator):
-    """H on one bit position of a register (hadamard.cpp:470-712; the
-    reference's active path is defined for a single position)."""
+    """H on a set of bit positions of a register (hadamard.cpp:470-712): one
+    position as the reference's active path (pairs of entries equal except
+    that bit), several as H on each of them (the reference's
+    Hadamard_Partial::operate over groups equal outside the set)."""
 
     def __init__(self, reg, positions):
         super().__init__()
         self.id = _R(reg)
-        self.positions = sorted(int(p) for p in positions)
-        if len(self.positions) != 1:
-            raise ValueError("Hadamard_Partial: exactly one position is supported")
+        self.positions = sorted({int(p) for p in positions})
 
     def spec(self, dag=False):
         return ("hadamard_partial", self.id, self.positions, self._cond())

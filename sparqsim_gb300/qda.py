@@ -73,6 +73,14 @@ class Runner:
     def combine(self, first, second):
         CombineRegister(first, second)(self.state)
 
+    def add_register(self, name: str, type_, size: int):
+        from .operators import AddRegister
+        return AddRegister(name, type_, size)(self.state)
+
+    def remove_register(self, reg):
+        from .operators import RemoveRegister
+        RemoveRegister(reg)(self.state)
+
 
 def _with(op, outer):
     """A copy of `op` that also carries the conditions of `outer`."""

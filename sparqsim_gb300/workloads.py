@@ -1,5 +1,16 @@
 """Seeded synthetic workloads built on the operator API.
 
+RegisterCircuit: the register circuit at scale (a 20-bit, b 32-bit, c 32-bit
+plus a 32-bit scratch t). From |0>, each of L layers is
+
+    Hadamard_Int(a, h)                    # split: 1 -> 2^h, or merge 2^2h -> 2^h
+    b ^= QRAM[a]                          # 2^20-word table of seeded uint32
+    t ^= a*b; c += t; t ^= a*b            # c += a*b mod 2^32
+    phase exp(i theta_l) on bit 0 of c    # theta_l seeded uniform in [0, 2 pi)
+    Hadamard_Int(a, h)                    # split: fan-out to the 2^2h peak
+
+with the five elementwise operators of a layer fused into one launch.
+
 NoisyTrajectories: n instances of the register circuit (registers a, b, c of
 16 bits) with independent Pauli X/Z noise, each instance with its own Hadamard
 width h_t, so that the support of instance t alternates between 2^h_t and
@@ -31,6 +42,59 @@ from .operators import Fused, Hadamard_Int, Hadamard_Int_Batched, Mul_UInt_UInt,
     QRAMLoad
 
 REG_BITS = 16
+
+
+class RegisterCircuit:
+    A_BITS, B_BITS, C_BITS, T_BITS = 20, 32, 32, 32
+    TABLE_BITS = 20
+    SEED = 20261203
+
+    def __init__(self, h: int = 12, layers: int = 10, seed: int = SEED):
+        self.h, self.layers = int(h), int(layers)
+        rng = np.random.default_rng(seed)
+        self.table = rng.integers(0, 1 << 32, 1 << self.TABLE_BITS, dtype=np.uint64)
+        self.thetas = rng.uniform(0.0, 2 * math.pi, self.layers)
+        self.qram = None
+
+    def build(self):
+        """Declares a, b, c, t (ids 0..3, the register table cleared first) and
+        the operators."""
+        System.clear()
+        for name, w in (("a", self.A_BITS), ("b", self.B_BITS), ("c", self.C_BITS), ("t", self.T_BITS)):
+            System.add_register(name, core.UnsignedInteger, w)
+        self.qram = QRAMCircuit_qutrit(self.TABLE_BITS, 32, self.table)
+        self.H = Hadamard_Int("a", self.h)
+        self.mid = [self.mid_ops(self.qram, th) for th in self.thetas]
+        return self
+
+    @staticmethod
+    def mid_ops(qram, theta: float):
+        from .operators import Add_UInt_UInt_InPlace
+        return Fused([QRAMLoad(qram, "a", "b"), Mul_UInt_UInt("a", "b", "t"), Add_UInt_UInt_InPlace("t", "c"),
+                      Mul_UInt_UInt("a", "b", "t"), Phase_Bool("c", 0, float(theta))])
+
+    def ops(self, layers: int | None = None):
+        """The operator sequence of the first `layers` layers."""
+        out = []
+        for layer in range(self.layers if layers is None else layers):
+            out += [self.H, self.mid[layer], self.H]
+        return out
+
+    def run(self, st: SparseState, count: bool = False, reset: bool = True, layers: int | None = None) -> int:
+        """One step from |0> (`reset`); returns the update count when count=True."""
+        if reset:
+            st.reset()
+        upd = 0
+        for layer in range(self.layers if layers is None else layers):
+            n0 = st.size() if count else 0
+            self.H(st)
+            n1 = st.size() if count else 0
+            self.mid[layer](st)
+            self.H(st)
+            if count:
+                n2 = st.size()
+                upd += max(n0, n1) + 5 * n1 + max(n1, n2)
+        return upd
 
 
 class NoisyTrajectories:

@@ -137,3 +137,52 @@ def test_qram_write_in_place_and_replay_guard():
     assert np.array_equal(got_k, want_k) and np.array_equal(got_a, want_a)
     with pytest.raises(ps.SparQInvalid):
         q.write(np.full(64, 1 << 20, dtype=np.uint64))
+    # the refused write left the table as it was: the replay gate still accepts it
+    g.replay()
+    ps.synchronize()
+    got_k, got_a = _canon(st)
+    assert np.array_equal(got_k, want_k) and np.array_equal(got_a, want_a)
+
+
+def _small_graph():
+    ps.System.clear()
+    a = ps.System.add_register("a", ps.UnsignedInteger, 4)
+    b = ps.System.add_register("b", ps.UnsignedInteger, 8)
+    q = ps.QRAMCircuit_qutrit(4, 8, np.arange(16, dtype=np.uint64) * 7 % 251)
+    st = ps.SparseState()
+
+    def apply():
+        ps.Hadamard_Int(a, 4)(st)
+        ps.QRAMLoad(q, a, b)(st)
+        ps.Hadamard_Int(a, 4)(st)
+
+    return st, q, ps.Graph(st, apply, st.reset)
+
+
+def test_launch_after_table_destroyed_is_refused_on_the_host():
+    """Destroying a table a graph reads makes every later launch refuse
+    before any device work (no checksum kernel reads the freed table)."""
+    from sparqsim_gb300 import _native
+    st, q, g = _small_graph()
+    g.replay()
+    ps.synchronize()
+    _native.call("sq_qram_destroy", q._h)
+    q._h = None
+    st.reset()
+    n0 = ps.launch_count()
+    with pytest.raises(ps.SparQInvalid, match="destroyed"):
+        g.launch()
+    assert ps.launch_count() == n0  # nothing was launched
+
+
+def test_launch_after_state_destroyed_is_refused_on_the_host():
+    from sparqsim_gb300 import _native
+    st, q, g = _small_graph()
+    g.replay()
+    ps.synchronize()
+    _native.call("sq_state_destroy", st._h)
+    st._h = None
+    n0 = ps.launch_count()
+    with pytest.raises(ps.SparQInvalid, match="destroyed"):
+        g.launch()
+    assert ps.launch_count() == n0

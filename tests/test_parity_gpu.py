@@ -492,3 +492,51 @@ def test_hadamard_partial(dual, strategy):
     for pos in (0, 3, 5):
         dual.apply(ps.Hadamard_Partial("q", [pos]))
         dual.compare(exact_amp=True)
+    # conditioned: entries failing the condition stay as they are
+    dual.apply(ps.Hadamard_Partial("q", [2]).conditioned_by_bit("r", 4))
+    dual.compare(exact_amp=True)
+    dual.apply(ps.Hadamard_Partial("q", [1]).conditioned_by_nonzeros("r"))
+    dual.compare(exact_amp=True)
+
+
+@pytest.mark.parametrize("positions", [[0, 3], [1, 2, 5], [0, 1, 2], [4, 5], [0, 2, 3, 5], list(range(6)),
+                                       [2, 2, 4]])
+def test_hadamard_partial_several_positions(dual, strategy, positions):
+    """H on a set of bits: singletons fan out, full groups run the FWHT in
+    place, partial groups are completed (Hadamard_Partial::operate's three
+    cases); applied twice it merges back to the input. Conditions on another
+    register and on a bit of the target outside the set."""
+    dual.reg("q", U, 6)
+    dual.reg("r", U, 10)
+    rng = np.random.default_rng(310 + len(positions))
+    regs, amps = random_state(rng, [6, 10], 3000)
+    dual.start(regs, amps)
+    op = ps.Hadamard_Partial("q", positions)
+    dual.apply(op)
+    dual.compare(exact_amp=True)
+    dual.apply(op)
+    dual.compare(exact_amp=True)
+    assert dual.gpu.size() == 3000  # H.H = I
+    dual.apply(ps.Hadamard_Partial("q", positions).conditioned_by_bit("r", 3))
+    dual.compare(exact_amp=True)
+    rest = [b for b in range(6) if b not in positions]
+    if rest:
+        dual.apply(ps.Hadamard_Partial("q", positions).conditioned_by_bit("q", rest[-1]))
+        dual.compare(exact_amp=True)
+
+
+def test_bit_gather_round_trip(dual):
+    """The bit permutation behind several-position Hadamard_Partial, against
+    the oracle, and its inverse."""
+    dual.reg("q", U, 13)
+    dual.reg("r", U, 7)
+    rng = np.random.default_rng(320)
+    regs, amps = random_state(rng, [13, 7], 2000)
+    dual.start(regs, amps)
+    for mask in (0b1000100100001, 0b0000000000111, 0b1111111111111, 0b1010101010101):
+        g = ps.BitGather("q", mask)
+        dual.apply(g)
+        dual.compare(exact_amp=True)
+        dual.apply(g, dag=True)
+        dual.compare(exact_amp=True)
+        assert np.array_equal(np.sort(dual.gpu.download()[0][:, 0]), np.sort(regs[:, 0]))

@@ -170,3 +170,51 @@ def test_trained_model_gain():
         P.set_single_pass_limit(0)
         P.set_hash_groups_hint(0)
         ps.set_group_strategy("autotune")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("h, groups, members", [(8, 600, 60), (12, 64, 600)])
+def test_underpredicted_single_pass_falls_back_to_exact(dual, h, groups, members):
+    """The size model predicts far too few outputs (its last bias set to
+    2^-16 of the input size): the single pass overflows its capacity, writes
+    nothing past it, counts an overflow, and the exact count -> scan -> write
+    path gives the oracle's entries bit for bit, as the run without the model
+    does."""
+    import sparqsim_gb300 as ps
+    from sparqsim_gb300 import predictor as P
+
+    U = ps.UnsignedInteger
+    dual.reg("a", U, 12)
+    dual.reg("b", U, 20)
+    rng = np.random.default_rng(h * 1000 + groups)
+    b = rng.choice(1 << 20, groups, replace=False).astype(np.uint64)
+    regs = np.stack([np.concatenate([rng.choice(1 << h, members, replace=False) for _ in range(groups)]),
+                     np.repeat(b, members)], axis=1).astype(np.uint64)
+    amps = rng.normal(size=len(regs)) + 1j * rng.normal(size=len(regs))
+    amps /= np.linalg.norm(amps)
+    assert len(regs) >= 1 << 15  # the model is consulted from 2^15 entries
+    params = np.zeros(P.PARAMS, dtype=np.float32)
+    params[-1] = -1.0  # log2(outputs / N) / 16 = -1
+    results = {}
+    try:
+        ps.set_group_strategy("hash")
+        P.set_single_pass_limit(1 << 16)  # the fully populated bound exceeds this
+        for model_on in (True, False):
+            P.set_params(params)
+            P.enable(model_on)
+            dual.start(regs, amps)
+            over0 = P.stats()["single_pass_overflows"]
+            dual.apply(ps.Hadamard_Int("a", h))
+            over1 = P.stats()["single_pass_overflows"]
+            assert over1 == over0 + (1 if model_on else 0)
+            assert dual.gpu.size() > 4200  # more than the predicted capacity
+            dual.compare(exact_amp=True)
+            results[model_on] = dual.gpu.download()
+    finally:
+        P.enable(False)
+        P.set_single_pass_limit(0)
+        ps.set_group_strategy("autotune")
+    # the same entries either way (their order follows the hash grouping's)
+    (rk, ra), (bk, ba) = results[True], results[False]
+    ro, bo = np.lexsort(rk.T[::-1]), np.lexsort(bk.T[::-1])
+    assert np.array_equal(rk[ro], bk[bo]) and np.array_equal(ra[ro].view(np.float64), ba[bo].view(np.float64))

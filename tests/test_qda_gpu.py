@@ -58,6 +58,12 @@ class DualRunner:
     def combine(self, first, second):
         self.dual.combine(first, second)
 
+    def add_register(self, name, type_, size):
+        return self.dual.add_register(name, type_, size)
+
+    def remove_register(self, reg):
+        self.dual.remove_register(reg)
+
 
 @pytest.mark.gpu
 def test_plus_one_and_overflow(dual):

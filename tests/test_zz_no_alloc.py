@@ -41,13 +41,23 @@ def _run_noalloc(torch, keys_dev, amps_dev, k, n, eps):
     n_out = c_uint64()
     stream = torch.cuda.current_stream().cuda_stream
     torch.cuda.synchronize()
+    allocs0, free0 = _allocations(), torch.cuda.mem_get_info()[0]
     rc = _native.lib().sq_clear_zero_noalloc(kin, c_void_p(amps_dev), k, n, eps, kout, c_void_p(out_amps.data_ptr()),
                                              byref(n_out), c_void_p(stream))
     assert rc == 0, _native.lib().sq_last_error()
+    # the promise itself: the call made no device allocation
+    assert _allocations() == allocs0
+    assert torch.cuda.mem_get_info()[0] == free0
     m = n_out.value
     keys = np.stack([t[:m].cpu().numpy().view(np.uint64) for t in out_keys])
     amps = out_amps[: 2 * m].cpu().numpy()
     return keys, amps
+
+
+def _allocations():
+    c = c_uint64()
+    _native.call("sq_device_allocation_count", byref(c))
+    return c.value
 
 
 def _reference_clear_zero(regs, amps, eps):
@@ -80,6 +90,33 @@ def test_clear_zero_noalloc_matches_clear_zero_twice():
         assert np.array_equal(got_keys, want_keys)          # same survivors, same order
         assert np.array_equal(got_amps, want_amps)          # bit-exact amplitudes
         assert 0 < got_keys.shape[1] < n
+
+
+def test_clear_zero_noalloc_rejects_overlapping_outputs():
+    """Blocks write survivors while other blocks still read: an output array
+    that overlaps an input is refused before anything runs."""
+    torch = pytest.importorskip("torch")
+    ps.System.add_register("a", ps.UnsignedInteger, 20)
+    n = 10_000
+    keys = torch.zeros(2 * n, dtype=torch.int64, device="cuda")
+    amps = torch.zeros(4 * n, dtype=torch.float64, device="cuda")
+    n_out = c_uint64()
+    lib = _native.lib()
+    kin = (c_void_p * 1)(keys.data_ptr())
+    kout_ok = (c_void_p * 1)(keys.data_ptr() + 8 * n)
+    # amplitudes in place
+    rc = lib.sq_clear_zero_noalloc(kin, c_void_p(amps.data_ptr()), 1, n, 1e-14, kout_ok, c_void_p(amps.data_ptr()),
+                                   byref(n_out), None)
+    assert rc == _native.SQ_ERR_INVALID and b"overlaps" in lib.sq_last_error()
+    # key words shifted by one entry into the input
+    kout_bad = (c_void_p * 1)(keys.data_ptr() + 8)
+    rc = lib.sq_clear_zero_noalloc(kin, c_void_p(amps.data_ptr()), 1, n, 1e-14, kout_bad,
+                                   c_void_p(amps.data_ptr() + 16 * n), byref(n_out), None)
+    assert rc == _native.SQ_ERR_INVALID
+    # disjoint arrays are accepted
+    rc = lib.sq_clear_zero_noalloc(kin, c_void_p(amps.data_ptr()), 1, n, 1e-14, kout_ok,
+                                   c_void_p(amps.data_ptr() + 16 * n), byref(n_out), None)
+    assert rc == 0 and n_out.value == 0  # every amplitude is zero
 
 
 def test_clear_zero_noalloc_rejects_oversize_and_handles_empty():
