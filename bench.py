@@ -67,7 +67,7 @@ def sample_clocks_start(path: Path):
          "clocks_event_reasons.sw_power_cap")
     try:
         f = open(path, "w")
-        p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "100"],
+        p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "20"],
                              stdout=f, stderr=subprocess.DEVNULL)
         return p, f
     except Exception:
@@ -561,6 +561,186 @@ def run_qda(args, ext) -> dict:
     return out
 
 
+def oracle_timed_runner():
+    """A runner that applies each operator to a GPU state (which keeps the
+    register table) and to an oracle state, timing only the oracle's calls;
+    `updates` counts entries per operator as the GPU legs do (a fused
+    program counts each of its operators)."""
+    import sparqsim_gb300 as ps
+    from oracle import oracle as O
+    from sparqsim_gb300.qda import Runner
+
+    class OracleTimed(Runner):
+        def __init__(self, state, ost):
+            super().__init__(state)
+            self.ost, self.t, self.updates = ost, 0.0, 0
+
+        def op(self, o, dag=False):
+            (o.dag if dag else o)(self.state)
+            n0 = self.ost.size()
+            t0 = time.perf_counter()
+            O.apply(self.ost, o.spec(dag and not o.self_adjoint))
+            self.t += time.perf_counter() - t0
+            self.updates += (len(o.items) if hasattr(o, "items") else 1) * max(n0, self.ost.size())
+
+        def split(self, first, name, size):
+            rid = super().split(first, name, size)
+            f = ps.System.resolve(first)
+            assert O.split_register(self.ost, f, size) == rid
+            return rid
+
+        def combine(self, first, second):
+            f, s2 = ps.System.resolve(first), ps.System.resolve(second)
+            super().combine(first, second)
+            O.combine_register(self.ost, f, s2)
+
+        def add_register(self, name, type_, size):
+            rid = super().add_register(name, type_, size)
+            assert O.add_register_sync(self.ost, int(type_), size) == rid
+            return rid
+
+        def remove_register(self, reg):
+            rid = ps.System.resolve(reg)
+            super().remove_register(reg)
+            O.remove_register_sync(self.ost, rid)
+
+    return OracleTimed
+
+
+def run_qda_batched(args, ext) -> dict:
+    """B walks of the PoiseuilleQDABench system (n = 2^qda_bits) with step
+    budgets 40568 + 2000 t, t < B, side by side in one state (a log2 B-bit
+    instance register in uniform superposition; each walk's R_s by
+    CondRot_General_Bool on it; ClearZero at 1e-14 / B, where each walk's
+    |a|^2 is 1/B of its own), against the plain form: the walk of the last
+    budget alone in its own state, over the same steps. Steps
+    `--qda-warm`..+`--qda-steps` timed with CUDA events in both, updates
+    counted in separate untimed passes; the last walk of the batch is checked
+    against the plain walk (same basis entries, amplitudes times sqrt B).
+    The oracle times walk steps 0 and 1 of the plain walk on one host core."""
+    import numpy as np
+    import torch
+
+    import sparqsim_gb300 as ps
+    from sparqsim_gb300 import qda
+    B, n_bits = args.qda_batch, args.qda_bits
+    alpha, kappa, p = 2.2666666666564934, 16.0, 1.3
+    budgets = [40568 + 2000 * t for t in range(B)]
+    warm, k = max(2, args.qda_warm), args.qda_steps
+    inst_bits = max(1, (B - 1).bit_length())
+    if B != 1 << inst_bits:
+        raise ValueError("--qda-batch: a power of two (>= 2)")
+
+    class Counting(qda.Runner):
+        def __init__(self, state):
+            super().__init__(state)
+            self.count, self.updates, self.peak = False, 0, 0
+
+        def op(self, o, dag=False):
+            n0 = self.state.size() if self.count else 0
+            super().op(o, dag)
+            if self.count:
+                n1 = self.state.size()
+                self.updates += max(n0, n1)
+                self.peak = max(self.peak, n0, n1)
+
+    def walk(batched, count, timed=False):
+        ps.System.clear()
+        nb = len(budgets) if batched else 1
+        eps = 1e-14 / nb
+        ps.set_clearzero_default_eps(eps)
+        st = ps.SparseState(capacity=1 << 22)
+        run = Counting(st)
+        qda.declare_registers(run, n_bits)
+        if batched:
+            run.add_register("inst", ps.UnsignedInteger, inst_bits)
+            run.op(ps.Hadamard_Int_Full("inst"))
+        run.op(ps.Hadamard_Int_Full("main_reg"))
+        enc_A = qda.BlockEncodingTridiagonal("main_reg", "anc_UA", alpha, -1.0)
+        enc_b = qda.StatePrepHadamard("main_reg")
+
+        def step(n):
+            s = [n / b for b in budgets] if batched else n / budgets[-1]
+            qda.WalkS(enc_A, enc_b, *qda.REGS, s, kappa, p, inst_reg="inst" if batched else None).apply(run)
+            run.op(ps.ClearZero(eps))
+            run.op(ps.Normalize())
+
+        for n in range(warm):
+            step(n)
+        run.count = count
+        torch.cuda.synchronize()
+        ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev[0].record(ext)
+        for n in range(warm, warm + k):
+            step(n)
+        ev[1].record(ext)
+        ev[1].synchronize()
+        ps.set_clearzero_default_eps(1e-14)
+        return st, run, ev[0].elapsed_time(ev[1])
+
+    _, plain_c, _ = walk(False, True)
+    sp, _, plain_ms = walk(False, False)
+    _, batch_c, _ = walk(True, True)
+    sb, _, batch_ms = walk(True, False)
+    pr, pa = sp.download()
+    br, ba = sb.download()
+    ncol = len(qda.REGS)
+    sel = br[:, ncol] == B - 1
+    br, ba = br[sel][:, :ncol], ba[sel] * math.sqrt(B)
+    pr = pr[:, :ncol]
+    same_keys = len(pr) == len(br)
+    diff = None
+    if same_keys:
+        o1, o2 = np.lexsort(pr.T[::-1]), np.lexsort(br.T[::-1])
+        same_keys = bool(np.array_equal(pr[o1], br[o2]))
+        if same_keys:
+            diff = float(np.max(np.abs(pa[o1] - ba[o2])))
+    plain_ups = plain_c.updates / (plain_ms / 1e3)
+    batch_ups = batch_c.updates / (batch_ms / 1e3)
+    out = {
+        "workload": (f"{B} QDA walks of the PoiseuilleQDABench system at n=2^{n_bits} (kappa 16, p={p}) with "
+                     f"step budgets {budgets[0]}..{budgets[-1]} (+2000 each) in one state, told apart by a "
+                     f"{inst_bits}-bit instance register; steps {warm}..{warm + k - 1} of each timed"),
+        "batched": {"value": batch_ups, "unit": UNIT, "updates": batch_c.updates, "ms_per_walk_step": batch_ms / k,
+                    "peak_entries": batch_c.peak, "entries": sb.size()},
+        "plain_gpu": {"value": plain_ups, "unit": UNIT, "updates": plain_c.updates, "ms_per_walk_step": plain_ms / k,
+                      "peak_entries": plain_c.peak, "entries": sp.size(),
+                      "sample": f"the walk of budget {budgets[-1]} alone in its own state, the same steps, "
+                                "CUDA events on the library stream"},
+        "batched_over_plain": batch_ups / plain_ups,
+        "batched_s_per_walk_step_per_walk": batch_ms / k / B / 1e3,
+        "last_walk_vs_plain": {"same_basis_entries": same_keys, "max_abs_amp_diff": diff,
+                               "note": "the batch's last walk (amplitudes times sqrt B) against the plain walk of "
+                                       "the same budget after the timed steps"},
+    }
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        OracleTimed = oracle_timed_runner()
+        ps.System.clear()
+        O.clear()
+        st = ps.SparseState(capacity=1 << 22)
+        run = OracleTimed(st, O.OracleState())
+        qda.declare_registers(run, n_bits)
+        for rid in ps.System.active_ids():
+            assert O.add_register_sync(run.ost, int(ps.System.type_of(rid)), ps.System.size_of(rid)) == rid
+        run.op(ps.Hadamard_Int_Full("main_reg"))
+        enc_A = qda.BlockEncodingTridiagonal("main_reg", "anc_UA", alpha, -1.0)
+        enc_b = qda.StatePrepHadamard("main_reg")
+        run.t, run.updates = 0.0, 0
+        for n in range(2):
+            qda.WalkS(enc_A, enc_b, *qda.REGS, n / budgets[-1], kappa, p).apply(run)
+            run.op(ps.ClearZero(1e-14))
+            run.op(ps.Normalize())
+        O.clear()
+        cpu = {"value": run.updates / run.t, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"walk steps 0 and 1 at n=2^{n_bits} ({run.updates} updates in {run.t:.2f} s), one thread"}
+        out["cpu"] = cpu
+    out["target"] = {"batched_over_plain": batch_ups / plain_ups,
+                     "batched_over_cpu": batch_ups / out["cpu"]["value"] if "cpu" in out else None,
+                     "goal": ">= 5x plain GPU, >= 20x the stated-core CPU"}
+    return out
+
+
 def run_qda_config3(args, ext) -> dict:
     """The QDA solve of the banded system through the QRAM encodings: A =
     N x N symmetric, half bandwidth 4 (bandwidth 8), off-diagonals uniform in
@@ -584,15 +764,17 @@ def run_qda_config3(args, ext) -> dict:
     class Counting(Runner):
         def __init__(self, state):
             super().__init__(state)
-            self.count, self.updates, self.peak, self.ops = False, 0, 0, 0
+            self.count, self.updates, self.peak, self.ops, self.launches = False, 0, 0, 0, 0
 
         def op(self, o, dag=False):
             n0 = self.state.size() if self.count else 0
             super().op(o, dag)
-            self.ops += 1
+            k = len(o.items) if hasattr(o, "items") else 1  # a fused program counts its operators
+            self.ops += k
+            self.launches += 1
             if self.count:
                 n1 = self.state.size()
-                self.updates += max(n0, n1)
+                self.updates += k * max(n0, n1)
                 self.peak = max(self.peak, n0, n1)
 
     def problem(n_bits):
@@ -627,7 +809,7 @@ def run_qda_config3(args, ext) -> dict:
     _native.profile_enable(True)
     t0 = time.perf_counter()
     s.record(ext)
-    ops0 = run.ops
+    ops0, launches0 = run.ops, run.launches
     for i in range(2, 2 + k):
         solver.step(run, i, total)
     e.record(ext)
@@ -645,6 +827,7 @@ def run_qda_config3(args, ext) -> dict:
                      f"bits, rational 51 bits); walk steps 2..{1 + k} of a 2000-step schedule timed"),
         "n_bits": n, "kappa_matrix": solver.kappa_matrix, "kappa_walk": solver.kappa,
         "ms_per_walk_step": ms, "wall_ms_per_walk_step": wall * 1e3 / k, "operators_per_walk_step": (run.ops - ops0) / k,
+        "operator_calls_per_walk_step": (run.launches - launches0) / k,
         "projected_solve_s": ms * total / 1e3, "updates": ups, "value": ups / (ms * k / 1e3), "unit": UNIT,
         "peak_entries": peak, "entries": st.size(), "kernels": kernels, "roofline": leg_roofline(prof),
     }
@@ -672,39 +855,7 @@ def run_qda_config3(args, ext) -> dict:
     if not args.no_cpu_baseline:
         from oracle import oracle as O
 
-        class OracleTimed(Runner):
-            def __init__(self, state, ost):
-                super().__init__(state)
-                self.ost, self.t, self.updates = ost, 0.0, 0
-
-            def op(self, o, dag=False):
-                (o.dag if dag else o)(self.state)
-                n0 = self.ost.size()
-                t0 = time.perf_counter()
-                O.apply(self.ost, o.spec(dag and not o.self_adjoint))
-                self.t += time.perf_counter() - t0
-                self.updates += max(n0, self.ost.size())
-
-            def split(self, first, name, size):
-                rid = super().split(first, name, size)
-                f = ps.System.resolve(first)
-                assert O.split_register(self.ost, f, size) == rid
-                return rid
-
-            def combine(self, first, second):
-                f, s2 = ps.System.resolve(first), ps.System.resolve(second)
-                super().combine(first, second)
-                O.combine_register(self.ost, f, s2)
-
-            def add_register(self, name, type_, size):
-                rid = super().add_register(name, type_, size)
-                assert O.add_register_sync(self.ost, int(type_), size) == rid
-                return rid
-
-            def remove_register(self, reg):
-                rid = ps.System.resolve(reg)
-                super().remove_register(reg)
-                O.remove_register_sync(self.ost, rid)
+        OracleTimed = oracle_timed_runner()
 
         solver = problem(ns)
         ps.System.clear()
@@ -931,6 +1082,9 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         result["batched_trajectories"] = run_trajectories(args, ext)
     if args.qda_steps and rank == 0:
         result["qda_walk"] = run_qda(args, ext)
+        if args.qda_batch > 1:
+            result["qda_walk"]["batched"] = run_qda_batched(args, ext)
+            result["qda_walk"]["target"] = result["qda_walk"]["batched"].pop("target")
     if args.cks_terms and rank == 0:
         result["cks_walk"] = run_cks(args, ext)
     if args.qda3_steps and rank == 0:
@@ -1060,13 +1214,14 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=256, help="instances timed in the plain GPU form")
     ap.add_argument("--cpu-sample", type=int, default=16, help="instances timed in the oracle")
     ap.add_argument("--qda-steps", type=int, default=10, help="QDA walk steps timed (0 skips)")
+    ap.add_argument("--qda-batch", type=int, default=8, help="QDA walks batched in one state (0 or 1 skips)")
     ap.add_argument("--qda-bits", type=int, default=16, help="main register of the QDA walk (16 or 20)")
     ap.add_argument("--qda-warm", type=int, default=200,
                     help="untimed QDA walk steps before the timed ones (200: the state has grown to the size the "
                          "reference's published per-step times are quoted at)")
     ap.add_argument("--cks-terms", type=int, default=3, help="CKS LCU terms timed (0 skips)")
     ap.add_argument("--qda3-steps", type=int, default=3, help="QDA-via-QRAM walk steps timed (0 skips)")
-    ap.add_argument("--qda3-bits", type=int, default=8, help="N = 2^bits of the timed QDA-via-QRAM walk")
+    ap.add_argument("--qda3-bits", type=int, default=10, help="N = 2^bits of the timed QDA-via-QRAM walk")
     ap.add_argument("--qda3-solve-bits", type=int, default=4, help="N = 2^bits of the 2000-step QDA-via-QRAM solve")
     ap.add_argument("--cks-bits", type=int, default=20, help="main register of the CKS walk")
     ap.add_argument("--fwht-arithmetic", default="exact-sum", choices=["exact-sum", "reference"],

@@ -128,8 +128,8 @@ typedef enum {
     SQ_OP_PHASE_BOOL = 64,           /* basic_gates.cpp:11-54  amp *= c0 if bit imm0 of reg0 */
     SQ_OP_GLOBAL_PHASE = 65,         /* parallel_phase_operations.cpp:72-107  amp *= c0 */
     SQ_OP_Y_BOOL = 66,               /* basic_gates.cpp:418-441 */
-    SQ_OP_REFLECTION_BOOL = 67,      /* parallel_phase_operations.cpp:46-70 regs reg0..reg[imm0-1], imm1 = inverse */
-    SQ_OP_ZERO_COND_PHASE_FLIP = 68, /* parallel_phase_operations.cpp:11-31 regs reg0..reg[imm0-1] */
+    SQ_OP_REFLECTION_BOOL = 67,      /* parallel_phase_operations.cpp:46-70 imm0 = bitmask of register ids, imm1 = inverse */
+    SQ_OP_ZERO_COND_PHASE_FLIP = 68, /* parallel_phase_operations.cpp:11-31 imm0 = bitmask of register ids */
     SQ_OP_ROT_DIAGONAL = 69,         /* basic_gates.cpp:110-133 amp *= (bit ? c1 : c0) */
     SQ_OP_ROT_OFF_DIAGONAL = 70,     /* basic_gates.cpp:146-171 flip bit, amp *= (bit ? c1 : c0) */
     /* Per-trajectory Pauli noise for batched trajectories (no single reference
@@ -447,6 +447,12 @@ int sq_condrot_rational_bool_cond(sq_state* st, uint32_t reg_in, uint32_t reg_ou
  * the 1-bit out register. The callable becomes a table: table[8*v .. 8*v+7]
  * = {m00, m01, m10, m11} as (re, im) for every v < 2^width(in) = n_values. */
 int sq_condrot_general_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, const double* table, uint64_t n_values);
+/* The same on the entries that satisfy `cond` only, the others left as they
+ * are (the composite-operator form, as sq_condrot_rational_bool_cond): a walk
+ * over a batch of problems rotates its ancilla by each problem's own matrix
+ * under the problem's index, or by one matrix under the walk's conditions. */
+int sq_condrot_general_bool_cond(sq_state* st, uint32_t reg_in, uint32_t reg_out, const double* table, uint64_t n_values,
+                                 const sq_cond* cond);
 /* Rot_GeneralUnitary (rot.cpp:353-477): dense dim x dim unitary (dim = 2^width(reg),
  * width <= 8) on the whole register, row-major (re, im) pairs; dag applies M^dagger. */
 int sq_rot_general_unitary(sq_state* st, uint32_t reg, const double* mat, uint64_t dim, const sq_cond* cond, int dag);

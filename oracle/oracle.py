@@ -46,7 +46,7 @@ def lib():
             "sqo_rot_bool": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), POINTER(SqCond), c_int]),
             "sqo_condrot": (c_int, [c_void_p, c_uint32, c_uint32, c_int, POINTER(SqCond)]),
             "sqo_clear_zero": (c_int, [c_void_p, c_double]),
-            "sqo_condrot_general": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), c_uint64]),
+            "sqo_condrot_general": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), c_uint64, POINTER(SqCond)]),
             "sqo_rot_general_unitary": (c_int, [c_void_p, c_uint32, POINTER(c_double), c_uint64, POINTER(SqCond), c_int]),
             "sqo_hadamard_partial": (c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_uint32, POINTER(SqCond)]),
             "sqo_normalize": (c_int, [c_void_p, POINTER(c_double)]),
@@ -212,7 +212,8 @@ def apply(state: OracleState, spec) -> None:
         _chk(L.sqo_condrot(h, spec[1], spec[2], 1 if spec[3] else 0, byref(spec[4])))
     elif kind == "condrot_general":
         tab = spec[3]
-        _chk(L.sqo_condrot_general(h, spec[1], spec[2], tab.ctypes.data_as(POINTER(c_double)), tab.size // 8))
+        _chk(L.sqo_condrot_general(h, spec[1], spec[2], tab.ctypes.data_as(POINTER(c_double)), tab.size // 8,
+                                   byref(spec[4])))
     elif kind == "rot_general_unitary":
         mat = spec[2]
         _chk(L.sqo_rot_general_unitary(h, spec[1], mat.ctypes.data_as(POINTER(c_double)), spec[3], byref(spec[4]),

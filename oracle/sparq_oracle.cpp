@@ -1424,12 +1424,25 @@ int sqo_condrot(void* h, uint32_t reg_in, uint32_t reg_out, int dag, const sq_co
         }
     })
 }
-int sqo_condrot_general(void* h, uint32_t reg_in, uint32_t reg_out, const double* table, uint64_t n_values) {
+// with conditions: the entries that satisfy them are rotated (and pruned) as
+// a state of their own, the others kept as they are (the partition of the
+// reference's SPLIT_BY_CONDITIONS / MERGE_BY_CONDITIONS, system_operations.h:109-129)
+int sqo_condrot_general(void* h, uint32_t reg_in, uint32_t reg_out, const double* table, uint64_t n_values,
+                        const sq_cond* cond) {
     SQO_TRY({
         if (n_values != pow2(size_of(reg_in))) throw std::invalid_argument("table size");
         std::vector<complex_t> t(4 * n_values);
         for (uint64_t i = 0; i < 4 * n_values; ++i) t[i] = complex_t(table[2 * i], table[2 * i + 1]);
-        condrot_general(*static_cast<State*>(h), reg_in, reg_out, t.data());
+        State& st = *static_cast<State*>(h);
+        if (!cond || cond->count == 0) {
+            condrot_general(st, reg_in, reg_out, t.data());
+        } else {
+            State pass, rest;
+            for (auto& e : st) (condition_satisfied(e, cond) ? pass : rest).push_back(e);
+            condrot_general(pass, reg_in, reg_out, t.data());
+            pass.insert(pass.end(), rest.begin(), rest.end());
+            st.swap(pass);
+        }
     })
 }
 int sqo_rot_general_unitary(void* h, uint32_t reg, const double* mat, uint64_t dim, const sq_cond* cond, int dag) {

@@ -153,6 +153,8 @@ _SIGS = [
     ("sq_condrot_rational_bool", c_int, [c_void_p, c_uint32, c_uint32, c_int]),
     ("sq_condrot_rational_bool_cond", c_int, [c_void_p, c_uint32, c_uint32, c_int, POINTER(SqCond)]),
     ("sq_condrot_general_bool", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), c_uint64]),
+    ("sq_condrot_general_bool_cond", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_double), c_uint64,
+                                             POINTER(SqCond)]),
     ("sq_rot_general_unitary", c_int, [c_void_p, c_uint32, POINTER(c_double), c_uint64, POINTER(SqCond), c_int]),
     ("sq_hadamard_partial", c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_uint32, POINTER(SqCond)]),
     ("sq_set_group_strategy", c_int, [c_int]),

@@ -161,8 +161,11 @@ int sq_get_stream(void** s) {
 // ------------------------------------------------------------------ registers
 int sq_system_clear(void) {
     SQ_API_BEGIN
+    // the default prune threshold is a setting of its own, kept across a
+    // clear as the reference's global clearzero_default_eps
+    // (system_operations.h:577) is
     RegTable& t = regtable();
-    double eps = 1e-14;
+    const double eps = t.clearzero_eps;
     t = RegTable();
     t.clearzero_eps = eps;
     SQ_API_END
@@ -1167,6 +1170,11 @@ int sq_condrot_rational_bool_cond(sq_state* st, uint32_t reg_in, uint32_t reg_ou
 }
 
 int sq_condrot_general_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, const double* table, uint64_t n_values) {
+    return sq_condrot_general_bool_cond(st, reg_in, reg_out, table, n_values, nullptr);
+}
+
+int sq_condrot_general_bool_cond(sq_state* st, uint32_t reg_in, uint32_t reg_out, const double* table, uint64_t n_values,
+                                 const sq_cond* cond) {
     SQ_API_BEGIN
     need(reg_in != reg_out, "CondRot_General_Bool: input and output registers must differ");
     need(table != nullptr, "null matrix table");
@@ -1183,6 +1191,7 @@ int sq_condrot_general_bool(sq_state* st, uint32_t reg_in, uint32_t reg_out, con
     g.target = fo;
     g.aux = fi;
     g.mtable = dev;
+    g.cond = resolve_cond(cond);
     g.eps = cz_eps();
     group_transform(S(st), g);
     SQ_API_END

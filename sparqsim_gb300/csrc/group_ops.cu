@@ -810,6 +810,123 @@ __global__ void __launch_bounds__(256) emit_fanout_kernel(const __grid_constant_
     }
 }
 
+__device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
+    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+__device__ __forceinline__ longlong2 shfl_xor_l2(longlong2 v, int m) {
+    return make_longlong2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
+// Rows of the register FWHT below: slot r * 32 + lane in v[r]; the stage of
+// target bit 5 + log2(HR) pairs rows r and r | HR.
+template <int HR, typename T, typename F>
+__device__ __forceinline__ void fwht_rows(T (&v)[8], F bfly) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+        if ((r & HR) == 0) bfly(v[r], v[r | HR]);
+}
+
+// Single-pass integer Hadamard (Hadamard_Int or Hadamard_Int_Full) of a full
+// cached range of S = 2^n members, 2 <= S <= 256, by one warp: the range was
+// written by the previous split in ascending target order with every slot
+// kept, so member c has target c (the same layout the 12-bit kernel reads
+// directly), and the group never touches shared memory. Lane t holds slots
+// r * 32 + t of rows r < 8: the stages of target bits 0..4 exchange with lane
+// t ^ 2^q by shuffles, those of bits 5..7 pair rows in registers, in
+// ascending stage order as the shared-memory form (hadamard.cpp:44-59,
+// 100-131), with either arithmetic; the kept slots are counted by one ballot
+// per row, reserved with one atomic and written in ascending target order.
+// Outputs are bit-identical to the shared-memory form of emit_hadamard_kernel.
+template <int K>
+__device__ __forceinline__ void hadamard_full_range_warp(const EmitArgs& a, uint64_t g, unsigned s0, int nbits,
+                                                         const uint64_t (&gk)[K], Field tg) {
+    const unsigned t = threadIdx.x & 31u;
+    const unsigned S = 1u << nbits;
+    const int nrows = (int)((S + 31u) >> 5);
+    double2 v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const unsigned c = ((unsigned)r << 5) | t;
+        v[r] = c < S ? __ldcs(a.in_amp + s0 + c) : make_double2(0.0, 0.0);
+    }
+    if (a.fix) {
+        // exact-sum arithmetic: integer grid, n exact stages, one rounding
+        int emax = 1;
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+            if ((((unsigned)r << 5) | t) < S) emax = max(emax, amp_exp(v[r]));
+        emax = (int)__reduce_max_sync(0xffffffffu, (unsigned)emax);
+        const int F = 62 - nbits;
+        longlong2 L[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) L[r] = to_fixed2(v[r], emax, F);
+        for (int q = 0; q < nbits && q < 5; ++q) {
+            const int h = 1 << q;
+            const bool hi = (t & (unsigned)h) != 0u;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                if (r >= nrows) break;  // rows past the range hold zeros: no stage needed
+                const longlong2 p = shfl_xor_l2(L[r], h);
+                L[r] = hi ? lsub(p, L[r]) : ladd(L[r], p);
+            }
+        }
+        auto bl = [](longlong2& x0, longlong2& x1) {
+            const longlong2 y0 = ladd(x0, x1), y1 = lsub(x0, x1);
+            x0 = y0;
+            x1 = y1;
+        };
+        if (nbits > 5) fwht_rows<1>(L, bl);
+        if (nbits > 6) fwht_rows<2>(L, bl);
+        if (nbits > 7) fwht_rows<4>(L, bl);
+        const int e2 = fix_out_exp(emax, nbits);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = from_fixed2(L[r], e2, nbits & 1, a.sqrt2inv);
+    } else {
+        const double s2 = a.sqrt2inv;
+        for (int q = 0; q < nbits && q < 5; ++q) {
+            const int h = 1 << q;
+            const bool hi = (t & (unsigned)h) != 0u;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                if (r >= nrows) break;
+                const double2 p = shfl_xor_d2(v[r], h);
+                v[r] = hi ? cscale(csub(p, v[r]), s2) : cscale(cadd(v[r], p), s2);
+            }
+        }
+        auto bd = [s2](double2& x0, double2& x1) {
+            const double2 y0 = cscale(cadd(x0, x1), s2), y1 = cscale(csub(x0, x1), s2);
+            x0 = y0;
+            x1 = y1;
+        };
+        if (nbits > 5) fwht_rows<1>(v, bd);
+        if (nbits > 6) fwht_rows<2>(v, bd);
+        if (nbits > 7) fwht_rows<4>(v, bd);
+    }
+    unsigned ball[8], total = 0;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const unsigned c = ((unsigned)r << 5) | t;
+        ball[r] = __ballot_sync(0xffffffffu, c < S && keep_amp(v[r], a.eps));
+        total += __popc(ball[r]);
+    }
+    bool fits = true;
+    const unsigned long long o = reserve_out<32>(a, g, total, fits, nullptr);
+    if (!fits) return;
+    const unsigned below = (1u << t) - 1u;
+    unsigned rank = 0;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        if ((ball[r] >> t) & 1u) {
+            uint64_t kk[K];
+#pragma unroll
+            for (int w = 0; w < K; ++w) kk[w] = gk[w];
+            fset<K>(kk, tg, (uint64_t)(((unsigned)r << 5) | t));
+            store_out<K>(a, o + rank + __popc(ball[r] & below), kk, v[r]);
+        }
+        rank += __popc(ball[r]);
+    }
+}
+
 template <int K, int W, bool WRITE, int AM>
 __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constant__ EmitArgs a) {
     extern __shared__ double2 s_slots[];
@@ -839,6 +956,11 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
         Field tg = a.target;
         tg.width = (uint8_t)nbits;
         const bool sparse_full = a.mode == GM_HADAMARD_FULL && m <= (unsigned)(nbits - 1);
+        if (W == 32 && AM == 2 && WRITE && a.cursor && m == S && S >= 2u && S <= 256u &&
+            (a.mode == GM_HADAMARD_INT || a.mode == GM_HADAMARD_FULL)) {
+            hadamard_full_range_warp<K>(a, g, s0, nbits, gk, tg);
+            continue;
+        }
         if (a.mode == GM_HADAMARD_INT && m == 1) {
             // singleton: a * 2^{-n/2}, sign (-1)^{popcount(t & v)} (hadamard.cpp:27-42)
             uint64_t v0;
@@ -1210,10 +1332,6 @@ __device__ __forceinline__ double2 sel_neg(bool lower, double2 p, double2 v) {
                         __longlong_as_double((long long)(lower ? (unsigned long long)__double_as_longlong(p.y) : sy)));
 }
 
-
-__device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
-    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
-}
 
 // The reference FP64 arithmetic (the exact-sum arithmetic runs in
 // emit_h4096x_kernel below).
@@ -2888,7 +3006,13 @@ static void run_group(State& s, const GroupSpec& gs) {
                         : am < 2 && gs.mode == GM_HADAMARD_INT && G == P && !gs.varw.width ? 4 + am
                                                                                           : am;
         const size_t sm = 4096 * sizeof(double2);
-        prof_begin(mode == EMIT_COUNT ? "emit_h4096_count" : mode == EMIT_WRITE ? "emit_h4096_write" : "emit_h4096_single_pass");
+        // the single-pass forms are named apart: the merge of full cached
+        // ranges and the split of singletons bound differently
+        prof_begin(mode == EMIT_COUNT   ? "emit_h4096_count"
+                   : mode == EMIT_WRITE ? "emit_h4096_write"
+                   : amx == 3           ? "emit_h4096_merge"
+                   : amx >= 4           ? "emit_h4096_split"
+                                        : "emit_h4096_single_pass");
         if (mode == EMIT_COUNT) launch_h4096<K, EMIT_COUNT>(amx, grid, sm, st, ea);
         else if (mode == EMIT_WRITE) launch_h4096<K, EMIT_WRITE>(amx, grid, sm, st, ea);
         else launch_h4096<K, EMIT_ATOMIC>(amx, grid, sm, st, ea);
@@ -2917,10 +3041,11 @@ static void run_group(State& s, const GroupSpec& gs) {
             prof_end((double)P * E);
             SQ_CUDA(cudaGetLastError());
         } else {
-            prof_begin("emit_hadamard_single_pass");
-            const unsigned fgrid = (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8);
             // a fresh grouping (no empty groups) with as many groups as entries: all singletons
-            if (W == 32 && gs.mode == GM_HADAMARD_INT && am < 2 && G == P) {
+            const bool fanout = W == 32 && gs.mode == GM_HADAMARD_INT && am < 2 && G == P;
+            prof_begin(fanout ? "emit_fanout_single_pass" : "emit_hadamard_single_pass");
+            const unsigned fgrid = (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8);
+            if (fanout) {
                 ea.err = device_error_word();
                 if (am == 1) emit_fanout_kernel<K, 1><<<fgrid, 256, 0, st>>>(ea);
                 else emit_fanout_kernel<K, 0><<<fgrid, 256, 0, st>>>(ea);

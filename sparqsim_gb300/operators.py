@@ -53,7 +53,8 @@ def _run(state: SparseState, spec) -> None:
         call("sq_condrot_rational_bool_cond", h, spec[1], spec[2], 1 if spec[3] else 0, byref(spec[4]))
     elif kind == "condrot_general":
         tab = spec[3]
-        call("sq_condrot_general_bool", h, spec[1], spec[2], tab.ctypes.data_as(ctypes.POINTER(c_double)), tab.size // 8)
+        call("sq_condrot_general_bool_cond", h, spec[1], spec[2], tab.ctypes.data_as(ctypes.POINTER(c_double)),
+             tab.size // 8, byref(spec[4]))
     elif kind == "rot_general_unitary":
         mat = spec[2]
         call("sq_rot_general_unitary", h, spec[1], mat.ctypes.data_as(ctypes.POINTER(c_double)), spec[3],
@@ -621,7 +622,8 @@ class CondRot_General_Bool(BaseOperator):
     """2x2 unitary func(v) on the 1-bit `out`, v = value of `in`
     (CondRot_General_Bool_Fast<F>, condrot.h:149-300). `func(v)` returns the
     four elements (m00, m01, m10, m11); it is evaluated on the host for every
-    v < 2^width(in) and the table is uploaded."""
+    v < 2^width(in) and the table is uploaded. Conditions restrict it to the
+    entries that satisfy them."""
 
     has_dag = False
 
@@ -638,8 +640,18 @@ class CondRot_General_Bool(BaseOperator):
             tab[v] = [m[0].real, m[0].imag, m[1].real, m[1].imag, m[2].real, m[2].imag, m[3].real, m[3].imag]
         self.table = np.ascontiguousarray(tab.reshape(-1))
 
+    @classmethod
+    def from_table(cls, reg_in, reg_out, mats):
+        """From a list of 2^width(in) matrices (m00, m01, m10, m11); values of
+        `in` past the list's end get the identity."""
+        n = 1 << System.size_of(_R(reg_in))
+        if len(mats) > n:
+            raise ValueError("CondRot_General_Bool: more matrices than values of the input register")
+        eye = (1, 0, 0, 1)
+        return cls(reg_in, reg_out, lambda v: mats[v] if v < len(mats) else eye)
+
     def spec(self, dag=False):
-        return ("condrot_general", self.in_id, self.out_id, self.table)
+        return ("condrot_general", self.in_id, self.out_id, self.table, self._cond())
 
 
 class Rot_GeneralUnitary(BaseOperator):

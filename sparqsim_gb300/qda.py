@@ -35,8 +35,8 @@ import math
 import numpy as np
 
 from .core import SparseState, System
-from .operators import (CombineRegister, GlobalPhase, Hadamard_Bool, Hadamard_Int_Full, PlusOneAndOverflow,
-                        Reflection_Bool, Rot_Bool, Rot_GeneralStatePrep, SplitRegister, X_Bool)
+from .operators import (CombineRegister, CondRot_General_Bool, GlobalPhase, Hadamard_Bool, Hadamard_Int_Full,
+                        PlusOneAndOverflow, Reflection_Bool, Rot_Bool, Rot_GeneralStatePrep, SplitRegister, X_Bool)
 from . import core
 
 
@@ -172,14 +172,33 @@ class StatePrepHadamard(Composite):
 
 
 class BlockEncodingHs(Composite):
-    """Block encoding of H(s) = (1 - f) H_0 + f H_1 (qda_fundamental.h:92-130)."""
+    """Block encoding of H(s) = (1 - f) H_0 + f H_1 (qda_fundamental.h:92-130).
 
-    def __init__(self, enc_A, enc_b, main_reg, anc_UA, anc_1, anc_2, anc_3, anc_4, fs: float):
+    Batched: with `inst_reg`, the state holds several walks of the same
+    system side by side, told apart by the value of `inst_reg`, and `fs` is a
+    list with one f(s) per value; the only operator that depends on s, the
+    rotation R_s of anc_2, then rotates each walk by its own matrix
+    (CondRot_General_Bool on inst_reg). Every other operator is the same for
+    all walks and maps each walk's entries among themselves."""
+
+    def __init__(self, enc_A, enc_b, main_reg, anc_UA, anc_1, anc_2, anc_3, anc_4, fs, inst_reg=None):
         super().__init__()
         self.enc_A, self.enc_b = enc_A, enc_b
         self.main_reg, self.anc_UA = main_reg, anc_UA
         self.a1, self.a2, self.a3, self.a4 = anc_1, anc_2, anc_3, anc_4
-        self.R = rotation_R(fs)
+        self.inst = inst_reg
+        fs = list(fs) if isinstance(fs, (list, tuple)) else [fs]
+        if inst_reg is None and len(fs) != 1:
+            raise ValueError("BlockEncodingHs: several f(s) need an instance register")
+        self.R = [rotation_R(f) for f in fs]
+
+    def _rot(self):
+        """R_s on anc_2: Rot_Bool when every walk is at the same f(s) (the
+        plain walk; at s = 0 R is diagonal and Rot_Bool's in-place form makes
+        no new entries), else one matrix per value of the instance register."""
+        if self.inst is None or all(r == self.R[0] for r in self.R):
+            return Rot_Bool(self.a2, self.R[0])
+        return CondRot_General_Bool.from_table(self.inst, self.a2, self.R)
 
     def apply(self, run):
         a1, a2, a3, a4 = self.a1, self.a2, self.a3, self.a4
@@ -191,7 +210,7 @@ class BlockEncodingHs(Composite):
         d(run, X_Bool(a1, 0))
         self.enc_b.conditioned(self).apply(run)
         d(run, X_Bool(a4, 0))
-        d(run, Rot_Bool(a2, self.R).conditioned_by_all_ones(a4))
+        d(run, self._rot().conditioned_by_all_ones(a4))
         d(run, X_Bool(a4, 0))
         d(run, Hadamard_Bool(a2).conditioned_by_all_ones(a4))
         enc = self.enc_A.conditioned(self)
@@ -204,7 +223,7 @@ class BlockEncodingHs(Composite):
         d(run, X_Bool(a4, 0))
         d(run, Hadamard_Bool(a2).conditioned_by_all_ones(a4))
         d(run, X_Bool(a4, 0))
-        d(run, Rot_Bool(a2, self.R).conditioned_by_all_ones(a4))
+        d(run, self._rot().conditioned_by_all_ones(a4))
         d(run, X_Bool(a4, 0))
         self.enc_b.conditioned(self).apply_dag(run)
         d(run, X_Bool(a1, 0))
@@ -218,11 +237,15 @@ class WalkS(Composite):
     """One walk step at s: U_H(s), then the reflection about anc_UA = anc_2 =
     anc_3 = 0, then the global phase i (qda_fundamental.h:344-470)."""
 
-    def __init__(self, enc_A, enc_b, main_reg, anc_UA, anc_1, anc_2, anc_3, anc_4, s: float, kappa: float,
-                 p: float):
+    def __init__(self, enc_A, enc_b, main_reg, anc_UA, anc_1, anc_2, anc_3, anc_4, s, kappa: float,
+                 p: float, inst_reg=None):
         super().__init__()
-        self.fs = schedule_f(s, kappa, p)
-        self.enc_Hs = BlockEncodingHs(enc_A, enc_b, main_reg, anc_UA, anc_1, anc_2, anc_3, anc_4, self.fs)
+        if isinstance(s, (list, tuple)):  # batched: one s per value of inst_reg
+            self.fs = [schedule_f(x, kappa, p) for x in s]
+        else:
+            self.fs = schedule_f(s, kappa, p)
+        self.enc_Hs = BlockEncodingHs(enc_A, enc_b, main_reg, anc_UA, anc_1, anc_2, anc_3, anc_4, self.fs,
+                                      inst_reg=inst_reg)
         self.refl = [anc_UA, anc_2, anc_3]
 
     def apply(self, run):

@@ -46,11 +46,11 @@ import numpy as np
 from . import core
 from .core import QRAMCircuit_qutrit, System
 from .operators import (SQ_ANGLE_DIV_SQRT_ARCCOS, SQ_ANGLE_ROTATE, Add_ConstUInt_InPlace,
-                        Add_Mult_UInt_ConstUInt_InPlace, Add_UInt_UInt_InPlace, AngleTable, ClearZero,
-                        CondRot_Fixed_Bool, Div_Sqrt_Arccos_UInt_UInt, GetRotateAngle_Int_Int,
-                        Mult_UInt_ConstUInt, QRAMLoad, ShiftLeft_InPlace, ShiftRight_InPlace,
-                        Swap_General_General, X_Bool)
-from .qda import Composite
+                        Add_Mult_UInt_ConstUInt_InPlace, Add_UInt_UInt_InPlace, AngleTable, BaseOperator,
+                        ClearZero, CondRot_Fixed_Bool, Div_Sqrt_Arccos_UInt_UInt, ElementwiseOperator,
+                        GetRotateAngle_Int_Int, Mult_UInt_ConstUInt, QRAMLoad, ShiftLeft_InPlace,
+                        ShiftRight_InPlace, Swap_General_General, X_Bool)
+from .qda import Composite, _with
 
 U64 = (1 << 64) - 1
 
@@ -160,12 +160,76 @@ def _pow2(k: int) -> int:
     return 1 << k
 
 
+class _Program(BaseOperator):
+    """Consecutive elementwise operators of a descent as one launch of the
+    fused elementwise kernel. Each entry maps on its own under every one of
+    them, so the sequence applied entry by entry is the sequence applied
+    operator by operator. The instructions are built when the operator is
+    queued (register types can change between two queued operators)."""
+
+    has_dag = False
+
+    def __init__(self, items):
+        super().__init__()
+        self.items = items  # [(operator, dagger)], in order
+        self.instrs = [o.instr(d and not o.self_adjoint) for o, d in items]
+
+    def spec(self, dag: bool = False):
+        if dag:
+            raise NotImplementedError("a fused program is applied forward only")
+        return ("prog", list(self.instrs))
+
+
 class _QRAMComposite(Composite):
+    """The descents queue their elementwise operators and apply each run of
+    them as one fused program; anything else (a split of amplitudes, a
+    register change, ClearZero) applies the queue first."""
+
+    def __init__(self):
+        super().__init__()
+        self._queue = []
+
+    def conditioned(self, outer):
+        o = super().conditioned(outer)
+        o._queue = []
+        return o
+
+    def _do(self, run, op, dag=False, outer=None):
+        o = _with(op, outer if outer is not None else self)
+        if isinstance(o, ElementwiseOperator):
+            self._queue.append((o, dag))
+        else:
+            self._flush(run)
+            run.op(o, dag)
+
+    def _flush(self, run):
+        if self._queue:
+            prog = _Program(self._queue)
+            self._queue = []
+            run.op(prog)
+
     def _set_boolean(self, reg):
         System.set_register_type(reg, core.Boolean)
 
     def _add(self, run, name, type_, size):
+        self._flush(run)
         return run.add_register(name, type_, size)
+
+    def _remove(self, run, reg):
+        self._flush(run)
+        run.remove_register(reg)
+
+    def _split(self, run, first, name, size):
+        self._flush(run)
+        return run.split(first, name, size)
+
+    def _combine(self, run, first, second):
+        self._flush(run)
+        run.combine(first, second)
+
+    def _clear(self, run):
+        self._flush(run)
+        run.op(ClearZero())
 
 
 class U_R(_QRAMComposite):
@@ -188,8 +252,8 @@ class U_R(_QRAMComposite):
 
     def _close(self, run):
         for r in ("data_parent", "addr_child", "data_child", "temp_bit", "div_result"):
-            run.remove_register(r)
-        run.op(ClearZero())
+            self._remove(run, r)
+        self._clear(run)
 
     def _rotate(self, run, dag: bool):
         q, tr, d, col = self.tree.qram, self.tree, self._do, self.col
@@ -198,7 +262,7 @@ class U_R(_QRAMComposite):
         d(run, tr.div("data_child", "data_parent", "div_result"))
         self._set_boolean("rotation")
         d(run, CondRot_Fixed_Bool("div_result", "rotation"), dag=dag)
-        run.op(ClearZero())
+        self._clear(run)
         d(run, tr.div("data_child", "data_parent", "div_result"))
         d(run, QRAMLoad(q, "addr_child", "data_child") if not dag else QRAMLoad(q, col, "data_parent"))
         d(run, QRAMLoad(q, col, "data_parent") if not dag else QRAMLoad(q, "addr_child", "data_child"))
@@ -207,8 +271,8 @@ class U_R(_QRAMComposite):
         n, col, d = self.addr_size, self.col, self._do
         self._open(run)
         for k in range(n):
-            run.split(col, "rotation", 1)
-            run.combine(col, "temp_bit")
+            self._split(run, col, "rotation", 1)
+            self._combine(run, col, "temp_bit")
             d(run, ShiftRight_InPlace(col, 1))
             d(run, Add_ConstUInt_InPlace(col, _pow2(k) - 1))
             d(run, Mult_UInt_ConstUInt(col, 2, "addr_child"))
@@ -218,8 +282,8 @@ class U_R(_QRAMComposite):
             d(run, Mult_UInt_ConstUInt(col, 2, "addr_child"))
             d(run, Add_ConstUInt_InPlace(col, _pow2(n) - _pow2(k) + 1))
             d(run, ShiftLeft_InPlace(col, 1))
-            run.split(col, "temp_bit", 1)
-            run.combine(col, "rotation")
+            self._split(run, col, "temp_bit", 1)
+            self._combine(run, col, "rotation")
             d(run, ShiftLeft_InPlace(col, 1))
         d(run, ShiftRight_InPlace(col, 1))
         self._close(run)
@@ -230,8 +294,8 @@ class U_R(_QRAMComposite):
         d(run, ShiftLeft_InPlace(col, 1))
         for k in range(n):
             d(run, ShiftRight_InPlace(col, 1))
-            run.split(col, "rotation", 1)
-            run.combine(col, "temp_bit")
+            self._split(run, col, "rotation", 1)
+            self._combine(run, col, "temp_bit")
             d(run, ShiftRight_InPlace(col, 1))
             d(run, Add_ConstUInt_InPlace(col, _pow2(n - 1 - k) - 1))
             d(run, Mult_UInt_ConstUInt(col, 2, "addr_child"))
@@ -241,8 +305,8 @@ class U_R(_QRAMComposite):
             d(run, Mult_UInt_ConstUInt(col, 2, "addr_child"))
             d(run, Add_ConstUInt_InPlace(col, _pow2(n) - _pow2(n - 1 - k) + 1))
             d(run, ShiftLeft_InPlace(col, 1))
-            run.split(col, "temp_bit", 1)
-            run.combine(col, "rotation")
+            self._split(run, col, "temp_bit", 1)
+            self._combine(run, col, "rotation")
         self._close(run)
 
 
@@ -254,7 +318,7 @@ class _TreeDescent(_QRAMComposite):
 
     def _level(self, run, k: int, last: bool, dag: bool, addr_terms):
         q, tr, d, work = self.tree.qram, self.tree, self._do, self.work
-        run.split(work, "rotation", 1)
+        self._split(run, work, "rotation", 1)
         self._set_boolean("rotation")
         d(run, Add_ConstUInt_InPlace("addr_parent", _pow2(k) - 1))
         addr_terms(run, False)
@@ -270,7 +334,7 @@ class _TreeDescent(_QRAMComposite):
             d(run, tr.div("data_child", "data_parent", "div_result"))
             d(run, CondRot_Fixed_Bool("div_result", "rotation"), dag=dag)
             if dag or self.prune_forward:
-                run.op(ClearZero())
+                self._clear(run)
             d(run, tr.div("data_child", "data_parent", "div_result"))
             for o in loads:
                 d(run, o)
@@ -283,7 +347,7 @@ class _TreeDescent(_QRAMComposite):
             d(run, tr.rot("data_parent", "data_child", "div_result"))
             d(run, CondRot_Fixed_Bool("div_result", "rotation"), dag=dag)
             if dag or self.prune_forward:
-                run.op(ClearZero())
+                self._clear(run)
             d(run, tr.rot("data_parent", "data_child", "div_result"))
             for o in loads:
                 d(run, o)
@@ -295,7 +359,7 @@ class _TreeDescent(_QRAMComposite):
         d(run, Add_UInt_UInt_InPlace(work, "addr_parent"), dag=True)
         addr_terms(run, True)
         d(run, Add_ConstUInt_InPlace("addr_parent", _pow2(k) - 1), dag=True)
-        run.combine(work, "rotation")
+        self._combine(run, work, "rotation")
 
 
 class U_L(_TreeDescent):
@@ -319,8 +383,8 @@ class U_L(_TreeDescent):
 
     def _close(self, run):
         for r in ("addr_parent", "data_parent", "addr_child", "data_child", "div_result"):
-            run.remove_register(r)
-        run.op(ClearZero())
+            self._remove(run, r)
+        self._clear(run)
 
     def _col_term(self, k):
         def terms(run, undo):
@@ -412,10 +476,12 @@ class Block_Encoding_via_QRAM(_QRAMComposite):
         ul.apply(run)
         ur.apply_dag(run)
         self._do(run, Swap_General_General(self.row, self.col))
+        self._flush(run)
 
     def apply_dag(self, run):
         ul, ur = self._parts()
         self._do(run, Swap_General_General(self.row, self.col))
+        self._flush(run)
         ur.apply(run)
         ul.apply_dag(run)
 

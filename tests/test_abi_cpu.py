@@ -122,3 +122,16 @@ def test_fused_dag_reverses_and_inverts():
     assert [i.dag for i in inv] == [0, 1, 1]
     with pytest.raises(TypeError):
         ps.Fused([ps.Hadamard_Int("a", 2)])
+
+
+def test_clearzero_default_eps_survives_system_clear():
+    """clearzero_default_eps is a global of its own
+    (system_operations.h:577): System::clear leaves it as it was."""
+    saved = ps.get_clearzero_default_eps()
+    try:
+        ps.set_clearzero_default_eps(3e-15)
+        ps.System.clear()
+        assert ps.get_clearzero_default_eps() == 3e-15
+    finally:
+        ps.set_clearzero_default_eps(saved)
+        ps.System.clear()

@@ -481,6 +481,13 @@ def test_condrot_general_bool(dual, strategy, w_in):
     op = ps.CondRot_General_Bool("in", "out", lambda v: mats[v].reshape(-1))
     dual.apply(op)
     dual.compare(exact_amp=True)
+    # conditioned: entries failing the condition stay as they are (a pair with
+    # one member on each side is two unpaired members of the rotated part)
+    dual.apply(op.conditioned_by_bit("r", 2))
+    dual.compare(exact_amp=True)
+    dual.apply(ps.CondRot_General_Bool.from_table("in", "out", [m.reshape(-1) for m in mats[:3]])
+               .conditioned_by_value("r", 5).conditioned_by_nonzeros("in"))
+    dual.compare(exact_amp=True)
 
 
 def test_hadamard_partial(dual, strategy):

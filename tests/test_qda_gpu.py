@@ -263,3 +263,50 @@ def test_poiseuille_dim256_rate_0_1(tmp_path):
     assert abs(summary["final_fidelity_vs_classical"] - 0.999438) <= 5e-7, summary
     assert abs(summary["final_success_prob"] - 0.5969) <= 5e-5, summary
     assert 17_400 <= summary["max_system_size"] <= 17_600, summary
+
+
+@pytest.mark.gpu
+def test_batched_walk_matches_plain_walks():
+    """Two walks of the Poisson benchmark with different step budgets (60 and
+    90) run side by side in one state, told apart by a 1-bit instance
+    register, against the same walks run alone: per instance the same basis
+    entries, and amplitudes (times sqrt 2, the instance superposition's
+    factor) within 1e-12 after 12 steps. The batched run prunes at half the
+    threshold, where each walk's |a|^2 is half its own."""
+    n_bits, budgets, steps, eps0 = 4, [60, 90], 12, 1e-14
+    alpha, kappa, p = POISSON_ALPHA, 16.0, 1.3
+
+    def walk(budget_list, inst):
+        ps.System.clear()
+        st = ps.SparseState()
+        run = qda.Runner(st)
+        qda.declare_registers(run, n_bits)
+        if inst:
+            run.add_register("inst", U, 1)
+            run.op(ps.Hadamard_Int_Full("inst"))
+        run.op(ps.Hadamard_Int_Full("main_reg"))
+        enc_A = qda.BlockEncodingTridiagonal("main_reg", "anc_UA", alpha, -1.0)
+        enc_b = qda.StatePrepHadamard("main_reg")
+        eps = eps0 / len(budget_list)
+        for i in range(steps):
+            s = [i / b for b in budget_list] if inst else i / budget_list[0]
+            qda.WalkS(enc_A, enc_b, *qda.REGS, s, kappa, p, inst_reg="inst" if inst else None).apply(run)
+            run.op(ps.ClearZero(eps))
+            run.op(ps.Normalize())
+        return st.download()
+
+    eps_saved = ps.get_clearzero_default_eps()
+    try:
+        plain = [walk([b], False) for b in budgets]
+        ps.set_clearzero_default_eps(eps0 / 2)  # the ClearZero calls inside the walk
+        regs, amps = walk(budgets, True)
+    finally:
+        ps.set_clearzero_default_eps(eps_saved)
+    ncol = len(qda.REGS)
+    for t, (pr, pa) in enumerate(plain):
+        sel = regs[:, ncol] == t
+        br, ba = regs[sel][:, :ncol], amps[sel] * math.sqrt(2)
+        assert len(ba) == len(pa) > 1 << n_bits
+        o1, o2 = np.lexsort(pr[:, :ncol].T[::-1]), np.lexsort(br.T[::-1])
+        assert np.array_equal(pr[o1, :ncol], br[o2])
+        assert np.max(np.abs(pa[o1] - ba[o2])) <= 1e-12
