@@ -1082,13 +1082,18 @@ static void rot_general_unitary(State& st, size_t id, const complex_t* mat, bool
 }
 
 // ---------------------------------------------------------------- Hadamard_Partial
-// One position: the reference's active path, Hadamard_Partial::operator()
-// with use_hash (hadamard.cpp:619-711): buckets of entries equal except the
-// chosen bit, pairs combined as a*sqrt2inv +- b*sqrt2inv, lone entries given
-// their partner. That path never tests the operator's conditions; this
-// restatement leaves the entries that fail them untouched (every other
-// controllable split operator of the reference does so), which is the same
-// result wherever no condition is set.
+// One position: the pair arithmetic of the reference's active path,
+// Hadamard_Partial::operator() with use_hash (hadamard.cpp:619-711): entries
+// equal except the chosen bit combined as a*sqrt2inv +- b*sqrt2inv
+// (operate_pair), lone entries given their partner (operate_alone_zero /
+// _one). The reference's buckets never actually pair two entries (their
+// order, StateLessExceptQubits, ends on the whole register,
+// quantum_interfere_basic.cpp:151-177), so it leaves partners as duplicate
+// keys; here they are paired, which is the transform, and equals the
+// reference wherever no two entries are partners. That path also never tests
+// the operator's conditions; this restatement leaves the entries that fail
+// them untouched (every other controllable split operator of the reference
+// does so), which is the same result wherever no condition is set.
 static void hadamard_partial1(State& st, size_t id, size_t pos, const sq_cond* cond) {
     if (st.empty()) return;
     uint64_t bit = pow2(pos);

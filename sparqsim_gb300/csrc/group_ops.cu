@@ -526,28 +526,13 @@ __device__ __forceinline__ void group_range(const EmitArgs& a, uint64_t g, unsig
     }
 }
 
-// Pair modes (1-bit target): one thread per group.
-// The two outputs of pair group g and whether each survives the prune.
-template <int K, bool BUCKET>
-__device__ __forceinline__ void pair_outputs(const EmitArgs& a, uint64_t g, uint64_t (&k0)[K], double2& rz,
-                                             double2& ro, bool& kz, bool& ko) {
+// Pair modes (1-bit target): the two outputs of a pair (az: the member
+// with target bit 0, ao: bit 1; either may be absent) and whether each
+// survives the prune. k0 is a member's key (the other registers).
+template <int K>
+__device__ __forceinline__ void pair_math(const EmitArgs& a, const uint64_t (&k0)[K], double2 az, double2 ao,
+                                          bool has_z, bool has_o, double2& rz, double2& ro, bool& kz, bool& ko) {
     {
-        const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
-        const unsigned m = s1 - s0;
-        load_key<K>(a.in_keys, group_head<BUCKET>(a, g, s0), k0);
-        uint64_t t0;
-        double2 v0;
-        member_at<BUCKET>(a, s0, t0, v0);
-        const bool b0 = t0 & 1ull;
-        double2 az = make_double2(0.0, 0.0), ao = make_double2(0.0, 0.0);
-        bool has_z = false, has_o = false;
-        if (b0) { ao = v0; has_o = true; } else { az = v0; has_z = true; }
-        if (m >= 2) {
-            uint64_t t1;
-            double2 v1;
-            member_at<BUCKET>(a, s0 + 1, t1, v1);
-            if (b0) { az = v1; has_z = true; } else { ao = v1; has_o = true; }
-        }
         const double2 zero = make_double2(0.0, 0.0);
         if (a.mode == GM_HADAMARD_BOOL) {
             const double s = a.sqrt2inv;
@@ -592,6 +577,29 @@ __device__ __forceinline__ void pair_outputs(const EmitArgs& a, uint64_t g, uint
         kz = keep_amp(rz, a.eps);
         ko = keep_amp(ro, a.eps);
     }
+}
+
+// Pair modes: one thread per group of the grouping.
+template <int K, bool BUCKET>
+__device__ __forceinline__ void pair_outputs(const EmitArgs& a, uint64_t g, uint64_t (&k0)[K], double2& rz,
+                                             double2& ro, bool& kz, bool& ko) {
+    const unsigned s0 = a.seg[g], s1 = a.seg[g + 1];
+    const unsigned m = s1 - s0;
+    load_key<K>(a.in_keys, group_head<BUCKET>(a, g, s0), k0);
+    uint64_t t0;
+    double2 v0;
+    member_at<BUCKET>(a, s0, t0, v0);
+    const bool b0 = t0 & 1ull;
+    double2 az = make_double2(0.0, 0.0), ao = make_double2(0.0, 0.0);
+    bool has_z = false, has_o = false;
+    if (b0) { ao = v0; has_o = true; } else { az = v0; has_z = true; }
+    if (m >= 2) {
+        uint64_t t1;
+        double2 v1;
+        member_at<BUCKET>(a, s0 + 1, t1, v1);
+        if (b0) { az = v1; has_z = true; } else { ao = v1; has_o = true; }
+    }
+    pair_math<K>(a, k0, az, ao, has_z, has_o, rz, ro, kz, ko);
 }
 
 // One thread per group of at most two members (the target is one bit). In
@@ -826,28 +834,52 @@ __device__ __forceinline__ void fwht_rows(T (&v)[8], F bfly) {
         if ((r & HR) == 0) bfly(v[r], v[r | HR]);
 }
 
-// Single-pass integer Hadamard (Hadamard_Int or Hadamard_Int_Full) of a full
-// cached range of S = 2^n members, 2 <= S <= 256, by one warp: the range was
-// written by the previous split in ascending target order with every slot
-// kept, so member c has target c (the same layout the 12-bit kernel reads
-// directly), and the group never touches shared memory. Lane t holds slots
-// r * 32 + t of rows r < 8: the stages of target bits 0..4 exchange with lane
-// t ^ 2^q by shuffles, those of bits 5..7 pair rows in registers, in
-// ascending stage order as the shared-memory form (hadamard.cpp:44-59,
-// 100-131), with either arithmetic; the kept slots are counted by one ballot
-// per row, reserved with one atomic and written in ascending target order.
-// Outputs are bit-identical to the shared-memory form of emit_hadamard_kernel.
-template <int K>
-__device__ __forceinline__ void hadamard_full_range_warp(const EmitArgs& a, uint64_t g, unsigned s0, int nbits,
-                                                         const uint64_t (&gk)[K], Field tg) {
+// Single-pass integer Hadamard (Hadamard_Int or Hadamard_Int_Full) of a
+// full group of S = 2^n members, 2 <= S <= 256, by one warp, the group's
+// slots held in registers. A full cached range (AM = 2) was written by the
+// previous split in ascending target order with every slot kept, so member c
+// has target c and is loaded straight into its slot (the same layout the
+// 12-bit kernel reads directly); the members of a bucket (AM = 1) or a sorted
+// run (AM = 0) are placed by target through the warp's shared slots once.
+// Lane t holds slots r * 32 + t of rows r < 8: the stages of target bits
+// 0..4 exchange with lane t ^ 2^q by shuffles, those of bits 5..7 pair rows
+// in registers, in ascending stage order as the shared-memory form
+// (hadamard.cpp:44-59, 100-131), with either arithmetic; the kept slots are
+// counted by one ballot per row, reserved with one atomic and written in
+// ascending target order. Outputs are bit-identical to the shared-memory form
+// of emit_hadamard_kernel.
+template <int K, int AM>
+__device__ __forceinline__ void hadamard_full_group_warp(const EmitArgs& a, uint64_t g, unsigned s0, int nbits,
+                                                         const uint64_t (&gk)[K], Field tg, double2* slots) {
     const unsigned t = threadIdx.x & 31u;
     const unsigned S = 1u << nbits;
     const int nrows = (int)((S + 31u) >> 5);
     double2 v[8];
+    if (AM == 2) {
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
-        const unsigned c = ((unsigned)r << 5) | t;
-        v[r] = c < S ? __ldcs(a.in_amp + s0 + c) : make_double2(0.0, 0.0);
+        for (int r = 0; r < 8; ++r) {
+            const unsigned c = ((unsigned)r << 5) | t;
+            v[r] = c < S ? __ldcs(a.in_amp + s0 + c) : make_double2(0.0, 0.0);
+        }
+    } else {
+        // the S members' targets are S distinct values below S: every slot is written once
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const unsigned j = ((unsigned)r << 5) | t;
+            if (j < S) {
+                uint64_t tj;
+                double2 aj;
+                member_at<AM>(a, s0 + j, tj, aj);
+                slots[tj & (S - 1u)] = aj;
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const unsigned c = ((unsigned)r << 5) | t;
+            v[r] = c < S ? slots[c] : make_double2(0.0, 0.0);
+        }
+        __syncwarp();  // the slots are the next group's
     }
     if (a.fix) {
         // exact-sum arithmetic: integer grid, n exact stages, one rounding
@@ -956,9 +988,9 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
         Field tg = a.target;
         tg.width = (uint8_t)nbits;
         const bool sparse_full = a.mode == GM_HADAMARD_FULL && m <= (unsigned)(nbits - 1);
-        if (W == 32 && AM == 2 && WRITE && a.cursor && m == S && S >= 2u && S <= 256u &&
+        if (W == 32 && WRITE && a.cursor && m == S && S >= 2u && S <= 256u &&
             (a.mode == GM_HADAMARD_INT || a.mode == GM_HADAMARD_FULL)) {
-            hadamard_full_range_warp<K>(a, g, s0, nbits, gk, tg);
+            hadamard_full_group_warp<K, AM>(a, g, s0, nbits, gk, tg, slots);
             continue;
         }
         if (a.mode == GM_HADAMARD_INT && m == 1) {
@@ -2694,6 +2726,175 @@ static Grouping group_by_hash(State& s, const GroupSpec& gs, uint64_t* dg, uint6
     return out;
 }
 
+// ------------------------------------------------------------------ pair splits by partner lookup
+// A 1-bit split pairs each entry with the entry whose key differs in the
+// target bit alone. Instead of grouping (hash buckets or a sort of the keys
+// without the bit), the entries that pass the conditions go into an
+// open-addressing table by their whole key (keys are unique), and every
+// entry looks its partner up: the member with bit 0 of a pair, or a member
+// without a partner, writes the pair's outputs (pair_math, the arithmetic of
+// the grouped path); the member with bit 1 of a pair writes nothing; entries
+// that fail the conditions are copied. A slot is (fingerprint 24 | index + 1),
+// zero empty; the table holds at least twice the entries, so every probe
+// sequence ends at an empty slot.
+struct PairTable {
+    unsigned long long* slots;
+    unsigned long long mask;  // capacity - 1
+};
+template <int K>
+__device__ __forceinline__ unsigned long long full_key_hash(const uint64_t (&k)[K]) {
+    unsigned long long hv = 0x9e3779b97f4a7c15ull;
+#pragma unroll
+    for (int w = 0; w < K; ++w) hv = mix64(hv ^ k[w] ^ (0x632be59bd9b4e019ull * (w + 1)));
+    return hv;
+}
+
+template <int K>
+__global__ void __launch_bounds__(256) pair_table_build_kernel(ConstKeyPtrs keys, uint64_t n, DCondSet cond,
+                                                               PairTable t) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint64_t k[K];
+        load_key<K>(keys, i, k);
+        if (!cond_ok<K>(k, cond)) continue;
+        const unsigned long long hv = full_key_hash<K>(k);
+        const unsigned long long tag = ((hv >> 40) << 32) | (unsigned long long)(i + 1);
+        unsigned long long slot = hv & t.mask;
+        // at most capacity probes; a lost race re-reads the slot it lost
+        // (filled now), so the loop moves on after at most one retry per slot
+        for (unsigned long long probes = 0; probes <= t.mask;) {
+            const unsigned long long v = t.slots[slot];
+            if (v == 0ull) {
+                if (atomicCAS(&t.slots[slot], 0ull, tag) == 0ull) break;
+                continue;
+            }
+            slot = (slot + 1) & t.mask;
+            ++probes;
+        }
+    }
+}
+
+// The entry index holding key pk, or -1.
+template <int K>
+__device__ __forceinline__ long long pair_find(const PairTable& t, const ConstKeyPtrs& keys, const uint64_t (&pk)[K]) {
+    const unsigned long long hv = full_key_hash<K>(pk);
+    const unsigned long long fp = hv >> 40;
+    unsigned long long slot = hv & t.mask;
+    for (unsigned long long probes = 0; probes <= t.mask; ++probes) {
+        const unsigned long long v = __ldg(t.slots + slot);
+        if (v == 0ull) return -1;
+        if ((v >> 32) == fp) {
+            const unsigned long long j = (v & 0xffffffffull) - 1ull;
+            bool eq = true;
+#pragma unroll
+            for (int w = 0; w < K; ++w) eq = eq && (__ldg(keys.w[w] + j) == pk[w]);
+            if (eq) return (long long)j;
+        }
+        slot = (slot + 1) & t.mask;
+    }
+    return -1;
+}
+
+// One thread per entry; the lanes of a warp reserve their outputs with one
+// atomic, in lane order. Writes nothing past a.capacity (the bound 2n is
+// exact, so that only matters to a graph replayed on other data).
+template <int K>
+__global__ void __launch_bounds__(256) pair_partner_emit_kernel(const __grid_constant__ EmitArgs a, uint64_t n,
+                                                                DCondSet cond, PairTable t) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t bit = 1ull << a.target.shift;
+    for (uint64_t gb = (uint64_t)blockIdx.x * blockDim.x; gb < n; gb += stride) {  // warp-uniform trips
+        const uint64_t i = gb + threadIdx.x;
+        const bool valid = i < n;
+        uint64_t k[K];
+        double2 rz = make_double2(0.0, 0.0), ro = make_double2(0.0, 0.0);
+        bool kz = false, ko = false, copy = false;
+        if (valid) {
+            load_key<K>(a.in_keys, i, k);
+            const double2 ai = a.in_amp[i];
+            if (!cond_ok<K>(k, cond)) {
+                copy = true;
+                rz = ai;
+            } else {
+                const bool one = (k[a.target.word] & bit) != 0ull;
+                uint64_t pk[K];
+#pragma unroll
+                for (int w = 0; w < K; ++w) pk[w] = k[w];
+                pk[a.target.word] ^= bit;
+                const long long j = pair_find<K>(t, a.in_keys, pk);
+                if (!(one && j >= 0)) {  // the bit-0 member of a pair, or a lone member
+                    const double2 aj = j >= 0 ? a.in_amp[j] : make_double2(0.0, 0.0);
+                    const double2 az = one ? aj : ai, ao = one ? ai : aj;
+                    pair_math<K>(a, k, az, ao, !one || j >= 0, one || j >= 0, rz, ro, kz, ko);
+                }
+            }
+        }
+        const unsigned c = copy ? 1u : (unsigned)kz + (unsigned)ko;
+        unsigned inc = c;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned v = __shfl_up_sync(0xffffffffu, inc, d);
+            if (lane >= (unsigned)d) inc += v;
+        }
+        const unsigned total = __shfl_sync(0xffffffffu, inc, 31);
+        unsigned long long base = 0;
+        if (lane == 31 && total) base = atomicAdd(a.cursor, (unsigned long long)total);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        if (!valid || c == 0 || base + total > a.capacity) continue;
+        unsigned long long o = base + (inc - c);
+        if (copy) {
+            store_out<K>(a, o, k, rz);
+            continue;
+        }
+        if (kz) {
+            fset<K>(k, a.target, 0);
+            store_out<K>(a, o++, k, rz);
+        }
+        if (ko) {
+            fset<K>(k, a.target, 1);
+            store_out<K>(a, o, k, ro);
+        }
+    }
+}
+
+// Pair split by partner lookup: table build, one emit pass with reserved
+// outputs (at most 2N: two per passing entry, one per copied entry).
+template <int K>
+static void run_pair_partner(State& s, const GroupSpec& gs, EmitArgs& ea) {
+    const uint64_t N = s.n;
+    cudaStream_t st = stream();
+    uint64_t cap = 1024;
+    while (cap < 2 * N) cap <<= 1;
+    PairTable t;
+    t.slots = (unsigned long long*)ws().get(WS_PAIR_TABLE, cap * 8);
+    t.mask = cap - 1;
+    SQ_CUDA(cudaMemsetAsync(t.slots, 0, cap * 8, st));
+    const DCondSet dc = gs.cond;
+    prof_begin("pair_table_build");
+    pair_table_build_kernel<K><<<grid_for(N, 256, 8), 256, 0, st>>>(ea.in_keys, N, dc, t);
+    prof_end((double)N * 8.0 * K + (double)cap * 8);
+    SQ_CUDA(cudaGetLastError());
+    const uint64_t capT = 2 * N;
+    ensure_buffers(s.spare, capT, regtable().k, 0);
+    for (int w = 0; w < SQ_KMAX; ++w) ea.out_keys.w[w] = s.spare.keys[w];
+    ea.out_amp = s.spare.amp;
+    unsigned long long* cur = (unsigned long long*)ws().get(WS_CURSOR, 64);
+    ea.cursor = cur;
+    ea.capacity = capT;
+    SQ_CUDA(cudaMemsetAsync(cur, 0, 8, st));
+    prof_begin("emit_pair_partner");
+    pair_partner_emit_kernel<K><<<grid_for(N, 256, 8), 256, 0, st>>>(ea, N, dc, t);
+    prof_end((double)N * (8.0 * K + 16));
+    SQ_CUDA(cudaGetLastError());
+    unsigned long long T = 0;
+    host_read(&T, cur, 8);
+    if (T > capT) fail(SQ_ERR_CAPACITY, "pair split wrote past its bound");
+    prof_add_bytes_last((double)T * (8 * K + 16));
+    swap_live_spare(s);
+    s.n = T;
+}
+
 constexpr uint64_t kModelMinEntries = 1ull << 15;  // below this a prediction costs more than it saves
 
 // Features of the size model (layout in sparq_gb300.h).
@@ -2822,6 +3023,35 @@ static void run_group(State& s, const GroupSpec& gs) {
     cudaStream_t st = stream();
     ConstKeyPtrs ik;
     for (int w = 0; w < SQ_KMAX; ++w) ik.w[w] = s.live.keys[w];
+
+    // 1-bit splits: partner lookup instead of a grouping, under the default
+    // strategies with single-pass sizing (the 'sort' and 'hash' strategies
+    // and exact sizing keep the grouped path, the same arithmetic)
+    {
+        const bool pair_mode = gs.mode == GM_HADAMARD_BOOL || gs.mode == GM_ROT || gs.mode == GM_CONDROT;
+        const int strat0 = get_group_strategy();
+        bool partner = pair_mode && !gs.varw.width && (strat0 == 0 || strat0 == 3) && get_output_sizing() == 0;
+        host_decision(&partner, sizeof(partner));
+        if (partner) {
+            s.groups.valid = false;
+            EmitArgs ea;
+            memset(&ea, 0, sizeof(ea));
+            ea.in_keys = ik;
+            ea.in_amp = s.live.amp;
+            ea.target = gs.target;
+            ea.aux = gs.aux;
+            ea.mode = gs.mode;
+            ea.nbits = 1;
+            ea.sqrt2inv = 1.0 / std::sqrt(2.0);
+            ea.eps = gs.eps;
+            ea.sign2pi = gs.sign * 2 * 3.14159265358979323846;
+            for (int i = 0; i < 4; ++i) ea.m[i] = gs.m[i];
+            ea.mtable = gs.mtable;
+            ea.err = device_error_word();
+            run_pair_partner<K>(s, gs, ea);
+            return;
+        }
+    }
 
     // group mask: active bits except the target bits
     uint64_t gmask[SQ_KMAX];

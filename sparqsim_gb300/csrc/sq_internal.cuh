@@ -336,6 +336,7 @@ enum WsSlot {
     WS_CURSOR,
     WS_SKETCH,
     WS_OUTPUT,
+    WS_PAIR_TABLE,    // partner table of the 1-bit splits
     WS_SCRATCH_TEST,  // buffers of the bounded-wait self-test
     WS_COUNT_MAX
 };

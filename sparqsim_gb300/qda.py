@@ -35,8 +35,9 @@ import math
 import numpy as np
 
 from .core import SparseState, System
-from .operators import (CombineRegister, CondRot_General_Bool, GlobalPhase, Hadamard_Bool, Hadamard_Int_Full,
-                        PlusOneAndOverflow, Reflection_Bool, Rot_Bool, Rot_GeneralStatePrep, SplitRegister, X_Bool)
+from .operators import (CombineRegister, CondRot_General_Bool, ElementwiseOperator, GlobalPhase, Hadamard_Bool,
+                        Hadamard_Int_Full, PlusOneAndOverflow, Reflection_Bool, Rot_Bool, Rot_GeneralStatePrep,
+                        SplitRegister, X_Bool, _run)
 from . import core
 
 
@@ -59,27 +60,60 @@ def rotation_R(fs: float) -> list:
 
 # ------------------------------------------------------------------ runners
 class Runner:
-    """Applies operators to one GPU state."""
+    """Applies operators to one GPU state.
 
-    def __init__(self, state: SparseState):
+    Consecutive elementwise operators are queued and applied as one fused
+    program (one pass over the entries instead of one per operator: each
+    entry maps on its own under every one of them, so the order within the
+    run is kept entry by entry). Anything else (a split of amplitudes, a
+    register change, ClearZero, Normalize) applies the queue first, and
+    `flush()` applies it on demand; the walk drivers flush at the end of each
+    step, before the state is read. `fuse=False` applies every operator as it
+    comes."""
+
+    def __init__(self, state: SparseState, fuse: bool = True):
         self.state = state
+        self.fuse = fuse
+        self._queue = []
 
     def op(self, o, dag: bool = False):
+        if self.fuse and isinstance(o, ElementwiseOperator):
+            if dag and not o.has_dag:
+                raise NotImplementedError("Dagger is not implemented.")
+            self._queue.append(o.instr(dag and not o.self_adjoint))
+            return
+        self.flush()
         (o.dag if dag else o)(self.state)
 
+    def flush(self):
+        if self._queue:
+            q, self._queue = self._queue, []
+            _run(self.state, ("prog", q))
+
     def split(self, first, name: str, size: int):
+        self.flush()
         return SplitRegister(first, name, size)(self.state)
 
     def combine(self, first, second):
+        self.flush()
         CombineRegister(first, second)(self.state)
 
     def add_register(self, name: str, type_, size: int):
         from .operators import AddRegister
+        self.flush()
         return AddRegister(name, type_, size)(self.state)
 
     def remove_register(self, reg):
         from .operators import RemoveRegister
+        self.flush()
         RemoveRegister(reg)(self.state)
+
+
+def flush(run):
+    """Apply whatever a runner has queued (runners without a queue: nothing)."""
+    f = getattr(run, "flush", None)
+    if f is not None:
+        f()
 
 
 def _with(op, outer):
@@ -252,6 +286,7 @@ class WalkS(Composite):
         self.enc_Hs.conditioned(self).apply(run)
         self._do(run, Reflection_Bool(self.refl, False))
         run.op(GlobalPhase(complex(0, 1)))  # outside the conditions, as in the reference
+        flush(run)
 
 
 # ------------------------------------------------------------------ driver
@@ -266,6 +301,7 @@ def tridiagonal_matrix(n: int, alpha: float, beta: float) -> np.ndarray:
 def declare_registers(run, n_bits: int):
     """main register (n bits), anc_UA (4 bits), anc_1..anc_4 (1 bit each)."""
     from .operators import AddRegister
+    flush(run)
     state = run.state
     AddRegister("main_reg", core.UnsignedInteger, n_bits)(state)
     AddRegister("anc_UA", core.UnsignedInteger, 4)(state)

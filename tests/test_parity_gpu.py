@@ -18,11 +18,12 @@ pytestmark = pytest.mark.gpu
 U = ps.UnsignedInteger
 
 
-@pytest.fixture(params=["sort", "hash", "hash-exact", "sort-fix", "hash-fix"])
+@pytest.fixture(params=["sort", "hash", "hash-exact", "sort-fix", "hash-fix", "auto"])
 def strategy(request, dual):
     """Grouping strategy x output sizing x FWHT arithmetic. The '-fix' cases
     run the Hadamard butterflies in exact-sum arithmetic: keys stay bit-exact,
-    amplitudes are held to 1e-12 relative (of the largest) instead of bit-exact."""
+    amplitudes are held to 1e-12 relative (of the largest) instead of bit-exact.
+    'auto' (as the default 'autotune') runs 1-bit splits by partner lookup."""
     ps.set_group_strategy(request.param.split("-")[0])
     ps.set_output_sizing("exact" if request.param.endswith("exact") else "auto")
     if request.param.endswith("fix"):
