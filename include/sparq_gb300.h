@@ -602,6 +602,10 @@ int sq_norm_sq(const sq_state* st, double* out);
  * equal keys summed, |a|^2 < eps dropped. */
 int sq_add_systems(sq_state* dst, const sq_state* src, double coef);
 /* AddRegister (system_operations.cpp:269-290): new zeroed register. */
+/* AddRegisterWithHadamard (system_operations.cpp:281-305): a new register
+ * of `width` bits, every entry copied 2^width times with the register taking
+ * every value, amplitudes unchanged (no 2^(-width/2) factor, no prune). */
+int sq_add_register_with_hadamard(sq_state* st, uint32_t type, uint32_t width, uint32_t* id_out);
 int sq_add_register_sync(sq_state* st, uint32_t type, uint32_t width, uint32_t* id_out);
 /* RemoveRegister / remove_register_synchronous (basic_components.cpp:398-430). */
 int sq_remove_register_sync(sq_state* st, uint32_t id);

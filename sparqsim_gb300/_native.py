@@ -197,6 +197,7 @@ _SIGS = [
     ("sq_norm_sq", c_int, [c_void_p, POINTER(c_double)]),
     ("sq_add_systems", c_int, [c_void_p, c_void_p, c_double]),
     ("sq_add_register_sync", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_uint32)]),
+    ("sq_add_register_with_hadamard", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_uint32)]),
     ("sq_remove_register_sync", c_int, [c_void_p, c_uint32]),
     ("sq_split_register", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_uint32)]),
     ("sq_combine_register", c_int, [c_void_p, c_uint32, c_uint32]),

@@ -1493,6 +1493,31 @@ int sq_add_register_sync(sq_state* st, uint32_t type, uint32_t width, uint32_t* 
     SQ_API_END
 }
 
+int sq_add_register_with_hadamard(sq_state* st, uint32_t type, uint32_t width, uint32_t* id_out) {
+    SQ_API_BEGIN
+    need(id_out != nullptr, "null pointer");
+    State& s = S(st);
+    drop_groups(s);
+    const uint32_t id = regtable().add(type, width);
+    *id_out = id;
+    Field f = regtable().field(id);
+    zero_field(s, f);
+    // every entry is alone in its group (the new register is 0 everywhere):
+    // the singleton fan-out, its factor 1 instead of 2^(-n/2), no prune
+    for (uint32_t lo = 0; lo < width; lo += 12) {
+        GroupSpec g;
+        memset(&g, 0, sizeof(g));
+        g.mode = GM_HADAMARD_INT;
+        g.target = f;
+        g.target.shift = (uint8_t)(f.shift + lo);
+        g.target.width = (uint8_t)std::min<uint32_t>(12, width - lo);
+        g.eps = -1.0;
+        g.unscaled = 1;
+        group_transform(s, g);
+    }
+    SQ_API_END
+}
+
 int sq_remove_register_sync(sq_state* st, uint32_t id) {
     SQ_API_BEGIN
     State& s = S(st);

@@ -821,143 +821,6 @@ __global__ void __launch_bounds__(256) emit_fanout_kernel(const __grid_constant_
 __device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
     return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
 }
-__device__ __forceinline__ longlong2 shfl_xor_l2(longlong2 v, int m) {
-    return make_longlong2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
-}
-
-// Rows of the register FWHT below: slot r * 32 + lane in v[r]; the stage of
-// target bit 5 + log2(HR) pairs rows r and r | HR.
-template <int HR, typename T, typename F>
-__device__ __forceinline__ void fwht_rows(T (&v)[8], F bfly) {
-#pragma unroll
-    for (int r = 0; r < 8; ++r)
-        if ((r & HR) == 0) bfly(v[r], v[r | HR]);
-}
-
-// Single-pass integer Hadamard (Hadamard_Int or Hadamard_Int_Full) of a
-// full group of S = 2^n members, 2 <= S <= 256, by one warp, the group's
-// slots held in registers. A full cached range (AM = 2) was written by the
-// previous split in ascending target order with every slot kept, so member c
-// has target c and is loaded straight into its slot (the same layout the
-// 12-bit kernel reads directly); the members of a bucket (AM = 1) or a sorted
-// run (AM = 0) are placed by target through the warp's shared slots once.
-// Lane t holds slots r * 32 + t of rows r < 8: the stages of target bits
-// 0..4 exchange with lane t ^ 2^q by shuffles, those of bits 5..7 pair rows
-// in registers, in ascending stage order as the shared-memory form
-// (hadamard.cpp:44-59, 100-131), with either arithmetic; the kept slots are
-// counted by one ballot per row, reserved with one atomic and written in
-// ascending target order. Outputs are bit-identical to the shared-memory form
-// of emit_hadamard_kernel.
-template <int K, int AM>
-__device__ __forceinline__ void hadamard_full_group_warp(const EmitArgs& a, uint64_t g, unsigned s0, int nbits,
-                                                         const uint64_t (&gk)[K], Field tg, double2* slots) {
-    const unsigned t = threadIdx.x & 31u;
-    const unsigned S = 1u << nbits;
-    const int nrows = (int)((S + 31u) >> 5);
-    double2 v[8];
-    if (AM == 2) {
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            const unsigned c = ((unsigned)r << 5) | t;
-            v[r] = c < S ? __ldcs(a.in_amp + s0 + c) : make_double2(0.0, 0.0);
-        }
-    } else {
-        // the S members' targets are S distinct values below S: every slot is written once
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            const unsigned j = ((unsigned)r << 5) | t;
-            if (j < S) {
-                uint64_t tj;
-                double2 aj;
-                member_at<AM>(a, s0 + j, tj, aj);
-                slots[tj & (S - 1u)] = aj;
-            }
-        }
-        __syncwarp();
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            const unsigned c = ((unsigned)r << 5) | t;
-            v[r] = c < S ? slots[c] : make_double2(0.0, 0.0);
-        }
-        __syncwarp();  // the slots are the next group's
-    }
-    if (a.fix) {
-        // exact-sum arithmetic: integer grid, n exact stages, one rounding
-        int emax = 1;
-#pragma unroll
-        for (int r = 0; r < 8; ++r)
-            if ((((unsigned)r << 5) | t) < S) emax = max(emax, amp_exp(v[r]));
-        emax = (int)__reduce_max_sync(0xffffffffu, (unsigned)emax);
-        const int F = 62 - nbits;
-        longlong2 L[8];
-#pragma unroll
-        for (int r = 0; r < 8; ++r) L[r] = to_fixed2(v[r], emax, F);
-        for (int q = 0; q < nbits && q < 5; ++q) {
-            const int h = 1 << q;
-            const bool hi = (t & (unsigned)h) != 0u;
-#pragma unroll
-            for (int r = 0; r < 8; ++r) {
-                if (r >= nrows) break;  // rows past the range hold zeros: no stage needed
-                const longlong2 p = shfl_xor_l2(L[r], h);
-                L[r] = hi ? lsub(p, L[r]) : ladd(L[r], p);
-            }
-        }
-        auto bl = [](longlong2& x0, longlong2& x1) {
-            const longlong2 y0 = ladd(x0, x1), y1 = lsub(x0, x1);
-            x0 = y0;
-            x1 = y1;
-        };
-        if (nbits > 5) fwht_rows<1>(L, bl);
-        if (nbits > 6) fwht_rows<2>(L, bl);
-        if (nbits > 7) fwht_rows<4>(L, bl);
-        const int e2 = fix_out_exp(emax, nbits);
-#pragma unroll
-        for (int r = 0; r < 8; ++r) v[r] = from_fixed2(L[r], e2, nbits & 1, a.sqrt2inv);
-    } else {
-        const double s2 = a.sqrt2inv;
-        for (int q = 0; q < nbits && q < 5; ++q) {
-            const int h = 1 << q;
-            const bool hi = (t & (unsigned)h) != 0u;
-#pragma unroll
-            for (int r = 0; r < 8; ++r) {
-                if (r >= nrows) break;
-                const double2 p = shfl_xor_d2(v[r], h);
-                v[r] = hi ? cscale(csub(p, v[r]), s2) : cscale(cadd(v[r], p), s2);
-            }
-        }
-        auto bd = [s2](double2& x0, double2& x1) {
-            const double2 y0 = cscale(cadd(x0, x1), s2), y1 = cscale(csub(x0, x1), s2);
-            x0 = y0;
-            x1 = y1;
-        };
-        if (nbits > 5) fwht_rows<1>(v, bd);
-        if (nbits > 6) fwht_rows<2>(v, bd);
-        if (nbits > 7) fwht_rows<4>(v, bd);
-    }
-    unsigned ball[8], total = 0;
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-        const unsigned c = ((unsigned)r << 5) | t;
-        ball[r] = __ballot_sync(0xffffffffu, c < S && keep_amp(v[r], a.eps));
-        total += __popc(ball[r]);
-    }
-    bool fits = true;
-    const unsigned long long o = reserve_out<32>(a, g, total, fits, nullptr);
-    if (!fits) return;
-    const unsigned below = (1u << t) - 1u;
-    unsigned rank = 0;
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-        if ((ball[r] >> t) & 1u) {
-            uint64_t kk[K];
-#pragma unroll
-            for (int w = 0; w < K; ++w) kk[w] = gk[w];
-            fset<K>(kk, tg, (uint64_t)(((unsigned)r << 5) | t));
-            store_out<K>(a, o + rank + __popc(ball[r] & below), kk, v[r]);
-        }
-        rank += __popc(ball[r]);
-    }
-}
 
 template <int K, int W, bool WRITE, int AM>
 __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constant__ EmitArgs a) {
@@ -972,15 +835,28 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
     double2* slots = s_slots + (size_t)wid * Smax;
     const uint64_t workers_per_block = blockDim.x / W;
     const uint64_t stride = (uint64_t)gridDim.x * workers_per_block;
-    for (uint64_t g = (uint64_t)blockIdx.x * workers_per_block + wid; g < a.groups; g += stride) {
-        unsigned s0, m;
-        group_range<AM>(a, g, s0, m);
+    // a group's range and key are a chain of dependent reads: the next
+    // group's are issued while the current one is transformed
+    uint64_t g = (uint64_t)blockIdx.x * workers_per_block + wid;
+    unsigned s0_next = 0, m_next = 0;
+    uint64_t gk_next[K] = {};
+    if (g < a.groups) {
+        group_range<AM>(a, g, s0_next, m_next);
+        if (m_next) load_key<K>(a.in_keys, group_head<AM>(a, g, s0_next), gk_next);
+    }
+    for (; g < a.groups; g += stride) {
+        const unsigned s0 = s0_next, m = m_next;
+        uint64_t gk[K];
+#pragma unroll
+        for (int w = 0; w < K; ++w) gk[w] = gk_next[w];
+        if (g + stride < a.groups) {
+            group_range<AM>(a, g + stride, s0_next, m_next);
+            if (m_next) load_key<K>(a.in_keys, group_head<AM>(a, g + stride, s0_next), gk_next);
+        }
         if (m == 0) {  // an emptied cached range
             if (!WRITE && t == 0) a.cnt[g] = 0u;
             continue;
         }
-        uint64_t gk[K];
-        load_key<K>(a.in_keys, group_head<AM>(a, g, s0), gk);
         // batched Hadamard: this group's digit count comes from its key
         const int nbits = a.varw.width ? (int)fget<K>(gk, a.varw) : a.nbits;
         const unsigned S = 1u << nbits;
@@ -988,11 +864,6 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
         Field tg = a.target;
         tg.width = (uint8_t)nbits;
         const bool sparse_full = a.mode == GM_HADAMARD_FULL && m <= (unsigned)(nbits - 1);
-        if (W == 32 && WRITE && a.cursor && m == S && S >= 2u && S <= 256u &&
-            (a.mode == GM_HADAMARD_INT || a.mode == GM_HADAMARD_FULL)) {
-            hadamard_full_group_warp<K, AM>(a, g, s0, nbits, gk, tg, slots);
-            continue;
-        }
         if (a.mode == GM_HADAMARD_INT && m == 1) {
             // singleton: a * 2^{-n/2}, sign (-1)^{popcount(t & v)} (hadamard.cpp:27-42)
             uint64_t v0;
@@ -3138,7 +3009,7 @@ static void run_group(State& s, const GroupSpec& gs) {
     ea.aux = gs.aux;
     ea.mode = gs.mode;
     ea.nbits = gs.target.width;
-    ea.extra = 1.0 / std::sqrt((double)(1ull << gs.target.width));
+    ea.extra = gs.unscaled ? 1.0 : 1.0 / std::sqrt((double)(1ull << gs.target.width));
     ea.sqrt2inv = 1.0 / std::sqrt(2.0);
     ea.eps = gs.eps;
     ea.sign2pi = gs.sign * 2 * 3.14159265358979323846;
@@ -3273,7 +3144,11 @@ static void run_group(State& s, const GroupSpec& gs) {
         } else {
             // a fresh grouping (no empty groups) with as many groups as entries: all singletons
             const bool fanout = W == 32 && gs.mode == GM_HADAMARD_INT && am < 2 && G == P;
-            prof_begin(fanout ? "emit_fanout_single_pass" : "emit_hadamard_single_pass");
+            // named apart by what the groups mostly are: members of several-member
+            // groups (merges) or singletons fanned out
+            prof_begin(fanout          ? "emit_fanout_single_pass"
+                       : 2 * G <= P    ? "emit_hadamard_merge"
+                                       : "emit_hadamard_single_pass");
             const unsigned fgrid = (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8);
             if (fanout) {
                 ea.err = device_error_word();

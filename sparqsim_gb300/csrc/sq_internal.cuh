@@ -387,6 +387,7 @@ struct GroupSpec {
     const double2* umat;    // device: Rot_GeneralUnitary matrix
     int udag;
     Field varw;             // batched Hadamard: register holding each entry's digit count (width 0: unused)
+    int unscaled;           // Hadamard singleton fan-out without the 2^(-n/2) factor (AddRegisterWithHadamard)
 };
 void group_transform(State& s, const GroupSpec& g);
 void set_group_strategy(int s);

@@ -18,7 +18,7 @@ import ctypes
 import math
 from ctypes import byref, c_double, c_uint32
 
-from ._native import OP, SQ_ERR_INVALID, SQ_MAX_PROGRAM, SparQInvalid, SqInstr, call
+from ._native import OP, SQ_ERR_BAD_RESULT, SQ_ERR_INVALID, SQ_MAX_PROGRAM, SparQError, SparQInvalid, SqInstr, call
 from .core import Controllable, QRAMCircuit_qutrit, SparseState, StateStorageType, System
 
 PI = math.pi
@@ -934,6 +934,49 @@ class AddRegister:
 
     def __call__(self, state: SparseState) -> int:
         return System.add_register_synchronous(self.name, self.type, self.size, state)
+
+
+class AddRegisterWithHadamard:
+    """New register of `size` bits, every entry copied once per value of it
+    with the amplitude unchanged: no 2^(-size/2) factor, no prune
+    (system_operations.cpp:281-305); returns its id."""
+
+    def __init__(self, name: str, type_: StateStorageType, size: int):
+        if size > 64:
+            raise ValueError("register size > 64")
+        self.name, self.type, self.size = name, type_, int(size)
+
+    def __call__(self, state: SparseState) -> int:
+        rid = c_uint32()
+        call("sq_add_register_with_hadamard", state._h, int(self.type), self.size, byref(rid))
+        System._set_name(rid.value, self.name)
+        return rid.value
+
+
+class CheckNormalization:
+    """Raise (the reference's throw_bad_result) unless |sum |a|^2 - 1| <
+    threshold (debugger.cpp:12-27); the state is left as it is."""
+
+    def __init__(self, threshold: float = 1e-5):
+        self.threshold = float(threshold)
+
+    def __call__(self, state: SparseState) -> None:
+        f = state.norm_sq()
+        if math.isnan(f) or not abs(f - 1.0) < self.threshold:
+            raise SparQError(SQ_ERR_BAD_RESULT, f"State is not normalized (sum |a|^2 = {f!r}).")
+
+    dag = __call__
+
+
+class CheckNan:
+    """Raise (throw_bad_result) if an amplitude is NaN (debugger.cpp:52-66):
+    the sum of |a|^2 is NaN exactly then."""
+
+    def __call__(self, state: SparseState) -> None:
+        if math.isnan(state.norm_sq()):
+            raise SparQError(SQ_ERR_BAD_RESULT, "NaN amplitude in the state.")
+
+    dag = __call__
 
 
 class RemoveRegister:

@@ -15,14 +15,16 @@ U = ps.UnsignedInteger
 
 
 def test_autotuner_decides_and_matches_oracle(dual):
+    """(1-bit splits take the partner lookup and no grouping; a 2-bit
+    Hadamard is grouped, so it is the autotuned operator here.)"""
     assert ps.get_group_strategy() == "autotune"
     dual.reg("a", U, 6)
     dual.reg("b", U, 16)
     rng = np.random.default_rng(12)
-    half = 10000  # complete pairs in bit 2 of a: the rotation keeps the entry count (one shape class)
-    a0 = rng.integers(0, 64, half) & ~4
-    b = rng.permutation(1 << 16)[:half]
-    regs = np.concatenate([np.stack([a0, b], axis=1), np.stack([a0 | 4, b], axis=1)]).astype(np.uint64)
+    quarter = 5000  # complete groups on bits 0-1 of a: the Hadamard keeps the entry count (one shape class)
+    a0 = rng.integers(0, 64, quarter) & ~3
+    b = rng.permutation(1 << 16)[:quarter]
+    regs = np.concatenate([np.stack([a0 | j, b], axis=1) for j in range(4)]).astype(np.uint64)
     n = len(regs)
     amps = rng.normal(size=n) + 1j * rng.normal(size=n)
     dual.start(regs, amps / np.linalg.norm(amps))
@@ -30,11 +32,11 @@ def test_autotuner_decides_and_matches_oracle(dual):
     for i in range(4):
         _native.profile_reset()
         _native.profile_enable(True)
-        dual.apply(ps.Rot_Bool("a", 2, [0.6, 0.8, 0.8, -0.6]))
+        dual.apply(ps.Hadamard_Int("a", 2))
         _native.profile_enable(False)
         names = _native.profile_read()
         ran.append("sort" if any(k.startswith("radix") or k == "group_heads" for k in names) else "hash")
-        dual.compare(exact_amp=True)
+        dual.compare()
         dual.apply(ps.Add_ConstUInt_InPlace("b", 1))  # key change: no cached ranges
     assert ran[0] == "sort" and ran[1] == "hash"
     assert ran[2] == ran[3]
