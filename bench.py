@@ -271,6 +271,109 @@ def run_cks(args, ext) -> dict:
     return out
 
 
+def run_cks_qram(args, ext) -> dict:
+    """Config 5's CKS solve through the QRAM walk: an N = 2^cks_qram_bits
+    symmetric banded matrix (half bandwidth 4, off-diagonals uniform in
+    [-1, 1], the diagonal set for kappa ~ 100) as a SparseMatrix in QRAM
+    (24-bit elements), least-squares 1/x coefficients of Chebyshev degree
+    201 (J = 100) on the encoded matrix's Gershgorin interval, b uniform. The
+    reference's T rotates by the element's magnitude (its angle ignores the
+    sign), so the walk encodes |A|. Timed: `--cks-qram-terms` LCU terms after
+    FirstStep and one term, plain, then with the size model trained on the
+    split sizes logged by an untimed repeat of the same terms (learned); the
+    two accumulators are compared (same entries, amplitudes within 1e-12)."""
+    import numpy as np
+    import torch
+
+    import sparqsim_gb300 as ps
+    from sparqsim_gb300 import _native, cks, cks_qram
+    from sparqsim_gb300 import predictor as P
+    n_bits, terms = args.cks_qram_bits, args.cks_qram_terms
+    n = 1 << n_bits
+    A = cks_qram.banded_symmetric(n, 4, 100.0, seed=SEED + n_bits)
+
+    def solve(learned: bool, log: bool):
+        ps.System.clear()
+        mat = cks_qram.SparseMatrix(A, 24)
+        # Gershgorin interval of the encoded matrix |A| / (max|A| nnz_col)
+        absA_rows = np.asarray(abs(A).sum(axis=1)).ravel()
+        diag = np.abs(A.diagonal())
+        scale = mat.amax * mat.nnz_col
+        lo = max(float(np.min(2 * diag - absA_rows)) / scale, 1e-3 / scale)
+        hi = float(np.max(absA_rows)) / scale
+        obj = cks_qram.LCU_Container_NoiseFree(mat, 100.0, 0.01, checks=False)
+        obj.set_inverse_coefficients(cks.ChebyshevInverseCoefficients(lo, hi, 100))
+        st = obj.step_state
+        ps.Hadamard_Int(obj.GetInputVecReg(), n_bits)(st)
+        ps.ClearZero()(st)
+        P.log(log)  # the untimed first steps log their split sizes too
+        t0 = time.perf_counter()
+        obj.quantum_walk_obj.FirstStep(obj.run)
+        obj.Step()
+        obj.Step()
+        torch.cuda.synchronize()
+        setup_s = time.perf_counter() - t0
+        P.enable(learned)
+        pred0 = P.stats()["predictions"]
+        over0 = P.stats()["single_pass_overflows"]
+        if not log:
+            _native.profile_reset()
+            _native.profile_enable(True)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(ext)
+        for _ in range(terms):
+            obj.Step()
+        e.record(ext)
+        e.synchronize()
+        _native.profile_enable(False)
+        P.log(False)
+        P.enable(False)
+        st_ = P.stats()
+        return (obj, mat, s.elapsed_time(e), setup_s, _native.profile_read(),
+                st_["predictions"] - pred0, st_["single_pass_overflows"] - over0)
+
+    obj, mat, ms, setup_s, prof, _, _ = solve(False, False)
+    plain_r, plain_a = obj.current_state.download()
+    peak = obj.max_system_size
+    walk_entries = obj.step_state.size()
+    del obj
+    P.clear_log()
+    solve(False, True)  # logs the split sizes of the same terms
+    x_log, t_log = P.read_log()
+    learned = None
+    if x_log.shape[0] >= 8:
+        P.reset(seed=31)
+        loss = P.train(x_log, t_log, epochs=200, batch=64, lr=2e-3, seed=32)
+        obj2, _, lms, _, _, preds, overs = solve(True, False)
+        lr, la = obj2.current_state.download()
+        same = len(la) == len(plain_a)
+        diff = None
+        if same:
+            o1, o2 = np.lexsort(plain_r.T[::-1]), np.lexsort(lr.T[::-1])
+            same = bool(np.array_equal(plain_r[o1], lr[o2]))
+            if same:
+                diff = float(np.max(np.abs(plain_a[o1] - la[o2])) / max(np.max(np.abs(plain_a)), 1e-300))
+        learned = {"s_per_term": lms / terms / 1e3, "training_rows": int(x_log.shape[0]), "final_loss": loss,
+                   "predictions": preds, "overflows": overs, "same_entries_as_plain": same,
+                   "max_rel_amp_diff_vs_plain": diff}
+        del obj2
+    tot = sum(v[1] for v in prof.values()) or 1.0
+    kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot, 4)}
+               for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:10]}
+    return {
+        "workload": (f"CKS through the QRAM walk: N=2^{n_bits} symmetric banded matrix (half bandwidth 4, "
+                     "off-diagonals U[-1,1], kappa ~100) as a SparseMatrix in QRAM (24-bit elements, "
+                     f"nnz_col {mat.nnz_col}), least-squares 1/x coefficients of degree 201 (J=100); LCU terms "
+                     f"3..{2 + terms} timed (two walk steps and one add_systems merge each)"),
+        "terms_timed": terms, "s_per_term": ms / terms / 1e3, "projected_degree_201_solve_s": ms / terms / 1e3 * 101,
+        "setup_s": setup_s, "entries_walk_state": walk_entries, "peak_walk_entries": peak,
+        "key_words": ps.System.key_words(), "kernels": kernels, "kernel_s_per_term": tot / terms / 1e3,
+        "roofline": leg_roofline(prof), "learned": learned,
+        "note": "the reference's QRAM T rotates by the element's magnitude (GetQWRotateAngle_Int_Int_Int "
+                "then CondRot_Fixed_Bool), so a signed matrix is walked as |A|",
+    }
+
+
 def leg_roofline(prof: dict) -> dict:
     """The kernel with the largest device time in a leg's profile: its
     algorithmic bytes per launch over its event-timed duration, against the
@@ -1126,6 +1229,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         result["cks_walk"] = run_cks(args, ext)
     if args.qda3_steps and rank == 0:
         result["qda_config3"] = run_qda_config3(args, ext)
+    if args.cks_qram_terms and rank == 0:
+        result["cks_qram"] = run_cks_qram(args, ext)
     return result
 
 
@@ -1262,6 +1367,8 @@ def main():
     ap.add_argument("--qda3-cpu-bits", type=int, default=8, help="N = 2^bits of the oracle's QDA-via-QRAM sample")
     ap.add_argument("--qda3-solve-bits", type=int, default=4, help="N = 2^bits of the 2000-step QDA-via-QRAM solve")
     ap.add_argument("--cks-bits", type=int, default=20, help="main register of the CKS walk")
+    ap.add_argument("--cks-qram-terms", type=int, default=2, help="LCU terms of the QRAM CKS walk timed (0 skips)")
+    ap.add_argument("--cks-qram-bits", type=int, default=18, help="N = 2^bits of the QRAM CKS walk")
     ap.add_argument("--fwht-arithmetic", default="exact-sum", choices=["exact-sum", "reference"],
                     help="Hadamard butterfly arithmetic of the headline run (the other one is timed too)")
     ap.add_argument("--cuda-profiler-range", default="none", choices=["none", "qda", "cks"],

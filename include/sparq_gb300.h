@@ -167,7 +167,18 @@ typedef enum {
      * GetRotateAngle_Int_Int (quantum_arithmetic.cpp:458-487). A pair the
      * table does not hold XORs 0 and is reported as SQ_ERR_INVALID at the
      * next synchronising call. */
-    SQ_OP_ANGLE_XOR = 76
+    SQ_OP_ANGLE_XOR = 76,
+    /* The address arithmetic of the sparse-matrix oracles:
+     * reg3 ^= reg0 + imm0 * reg1 (+ reg2 when imm1 = 1), the sum in 64 bits,
+     * XORed into reg3 within its width: GetRowAddr (imm1 = 0) and GetDataAddr
+     * (imm1 = 1), SparQ_Algorithm/src/hamiltonian_simulation.cpp:222-253. */
+    SQ_OP_ADDR_XOR = 77,
+    /* QuantumBinarySearch_Fast (hamiltonian_simulation.cpp:182-220): with the
+     * QRAM table in `qram`, l = reg0, r = l + imm0, imm1 rounds of
+     * mid = (l + r) / 2 compared with reg1 (equal: the result is mid; word <
+     * target: l = mid, else r = mid); reg2 ^= the result (0 when not found).
+     * Addresses are taken modulo the table's size. */
+    SQ_OP_QBS_XOR = 78
 } sq_opcode;
 
 /* One elementwise instruction. Register ids in reg[], integer constants in

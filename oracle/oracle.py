@@ -180,7 +180,7 @@ def apply(state: OracleState, spec) -> None:
         for ins in spec[1]:
             c = SqInstr()
             ctypes.pointer(c)[0] = ins
-            if ins.op in (OP["QRAM_LOAD"], OP["PAULI_NOISE"]):
+            if ins.op in (OP["QRAM_LOAD"], OP["PAULI_NOISE"], OP["QBS_XOR"]):
                 c.qram = _qram_map[ins.qram].h
             instrs.append(c)
         arr = (SqInstr * len(instrs))(*instrs)

@@ -433,6 +433,30 @@ static void apply_instr_entry(System& s, const sq_instr& in) {
             s.get(r[1]) ^= q->memory[addr];
             return;
         }
+        case SQ_OP_ADDR_XOR: {  // GetRowAddr / GetDataAddr (hamiltonian_simulation.cpp:222-253)
+            // the reference XORs the whole sum in; a register here holds its width
+            uint64_t v = get_as(s, r[0]) + in.imm[0] * get_as(s, r[1]);
+            if (in.imm[1]) v += get_as(s, r[2]);
+            s.get(r[3]) = (s.get(r[3]) ^ v) & width_mask(size_of(r[3]));
+            return;
+        }
+        case SQ_OP_QBS_XOR: {  // QuantumBinarySearch_Fast (hamiltonian_simulation.cpp:182-220)
+            const Qram* q = reinterpret_cast<const Qram*>(in.qram);
+            const uint64_t target = get_as(s, r[1]);
+            uint64_t l = get_as(s, r[0]), rr = l + in.imm[0], found = 0;
+            for (uint64_t i = 0; i < in.imm[1]; ++i) {
+                const uint64_t mid = (l + rr) / 2;
+                const uint64_t word = q->memory[mid % pow2(q->address_size)];
+                if (word == target) {
+                    found = mid;
+                    break;
+                }
+                if (word < target) l = mid;
+                else rr = mid;
+            }
+            s.get(r[2]) = (s.get(r[2]) ^ found) & width_mask(size_of(r[2]));
+            return;
+        }
         case SQ_OP_PHASE_BOOL: {  // basic_gates.cpp:11-54 (c0 precomputed, conj for dag)
             if ((s.get(r[0]) >> in.imm[0]) & 1) s.amplitude = cmul(s.amplitude, complex_t(in.c[0], in.c[1]));
             return;

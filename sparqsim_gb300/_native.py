@@ -36,7 +36,7 @@ OP = dict(
     PHASE_BOOL=64, GLOBAL_PHASE=65,
     Y_BOOL=66, REFLECTION_BOOL=67, ZERO_COND_PHASE_FLIP=68, ROT_DIAGONAL=69, ROT_OFF_DIAGONAL=70,
     PAULI_NOISE=71, TRIDIAG_ELEMENT=72, TRIDIAG_SLOT_COLUMN=73, LOOKUP_XOR=74, PARITY_PHASE=75,
-    ANGLE_XOR=76,
+    ANGLE_XOR=76, ADDR_XOR=77, QBS_XOR=78,
 )
 
 

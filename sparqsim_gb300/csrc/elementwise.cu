@@ -270,6 +270,32 @@ __device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2
             fset<K>(k, f[1], fget<K>(k, f[1]) ^ word);
             break;
         }
+        case SQ_OP_ADDR_XOR: {
+            uint64_t v = fget<K>(k, f[0]) + in.imm[0] * fget<K>(k, f[1]);
+            if (in.imm[1]) v += fget<K>(k, f[2]);
+            fset<K>(k, f[3], fget<K>(k, f[3]) ^ v);
+            break;
+        }
+        case SQ_OP_QBS_XOR: {
+            const uint64_t amask = wmask(in.addr_bits);
+            const uint64_t target = fget<K>(k, f[1]);
+            uint64_t l = fget<K>(k, f[0]), r = l + in.imm[0], found = 0;
+            for (uint64_t i = 0; i < in.imm[1]; ++i) {
+                const uint64_t mid = (l + r) / 2;
+                uint64_t word;
+                if (in.elem_bytes == 2) word = __ldg((const unsigned short*)in.table + (mid & amask));
+                else if (in.elem_bytes == 4) word = __ldg((const unsigned int*)in.table + (mid & amask));
+                else word = __ldg((const unsigned long long*)in.table + (mid & amask));
+                if (word == target) {
+                    found = mid;
+                    break;
+                }
+                if (word < target) l = mid;
+                else r = mid;
+            }
+            fset<K>(k, f[2], fget<K>(k, f[2]) ^ found);
+            break;
+        }
         case SQ_OP_TRIDIAG_ELEMENT: {
             const uint64_t idx = fget<K>(k, f[0]) + 4 * fget<K>(k, f[1]) + fget<K>(k, f[2]);
             fset<K>(k, f[3], fget<K>(k, f[3]) ^ tri_mem(idx, in.imm[0], in.imm[1]));
@@ -628,6 +654,28 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
             break;
         }
         case SQ_OP_PARITY_PHASE: R(0); am |= 3u; break;
+        case SQ_OP_ADDR_XOR:
+            R(0); R(1);
+            if (in.imm[1]) R(2);
+            W(3);
+            distinct(in.reg[0], in.reg[3], "GetRowAddr/GetDataAddr");
+            distinct(in.reg[1], in.reg[3], "GetRowAddr/GetDataAddr");
+            if (in.imm[1]) distinct(in.reg[2], in.reg[3], "GetDataAddr");
+            break;
+        case SQ_OP_QBS_XOR: {
+            R(0); R(1); W(2);
+            distinct(in.reg[0], in.reg[2], "QuantumBinarySearch_Fast");
+            distinct(in.reg[1], in.reg[2], "QuantumBinarySearch_Fast");
+            const QramTable* q = reinterpret_cast<const QramTable*>(in.qram);
+            if (!q || !q->dev) fail(SQ_ERR_INVALID, "QuantumBinarySearch_Fast: null table");
+            if (q->lookup || q->pair_kind >= 0) fail(SQ_ERR_INVALID, "QuantumBinarySearch_Fast: not a QRAM table");
+            if (in.imm[1] > 64) fail(SQ_ERR_INVALID, "QuantumBinarySearch_Fast: more than 64 rounds");
+            d.table = q->dev;
+            replay_note_input(q->dev, q->n_words * q->elem_bytes);
+            d.elem_bytes = q->elem_bytes;
+            d.addr_bits = q->address_size;
+            break;
+        }
         case SQ_OP_ANGLE_XOR: {
             R(0); R(1); W(2);
             distinct(in.reg[0], in.reg[2], "angle");

@@ -1031,8 +1031,9 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
     }
 }
 
-// Hadamard_Int, Hadamard_Int_Full and Rot_GeneralUnitary on targets of 1 to 3
-// bits: one thread per group, the group's 2^NB slots in registers. The
+// Hadamard_Int and Hadamard_Int_Full on targets of 1 to 4 bits, and
+// Rot_GeneralUnitary on 1 to 3 bits: one thread per group, the group's 2^NB
+// slots in registers. The
 // arithmetic and its order are those of emit_hadamard_kernel, so the results
 // are bit-identical; what changes is that millions of small groups no longer
 // run one after another on a warp (a chain of dependent loads per group, with
@@ -1064,30 +1065,40 @@ __global__ void __launch_bounds__(256) emit_small_kernel(const __grid_constant__
                 single = true;
                 keepm = keep_amp(base, a.eps) ? (1u << S) - 1u : 0u;
             } else if (!UNI && a.mode == GM_HADAMARD_FULL && m <= (unsigned)(NB - 1)) {
-                // Hadamard_Int_Full sparse bucket (hadamard.cpp:267-304): at most two
-                // members, summed in ascending target value
-                uint64_t t0 = 0, t1 = 0;
-                double2 a0 = make_double2(0.0, 0.0), a1 = make_double2(0.0, 0.0);
-                member_at<AM>(a, s0, t0, a0);
-                if (m == 2) {
-                    member_at<AM>(a, s0 + 1, t1, a1);
-                    if (t1 < t0) {
-                        const uint64_t tt = t0;
-                        t0 = t1;
-                        t1 = tt;
-                        const double2 ta = a0;
-                        a0 = a1;
-                        a1 = ta;
+                // Hadamard_Int_Full sparse bucket (hadamard.cpp:267-304): at most
+                // NB - 1 members, summed in ascending target value
+                constexpr int MM = NB > 1 ? NB - 1 : 1;
+                uint64_t ts[MM];
+                double2 as[MM];
+#pragma unroll
+                for (int j = 0; j < MM; ++j) {
+                    ts[j] = ~0ull;  // absent members sort last
+                    as[j] = make_double2(0.0, 0.0);
+                    if ((unsigned)j < m) member_at<AM>(a, s0 + j, ts[j], as[j]);
+                }
+#pragma unroll
+                for (int i = 0; i < MM - 1; ++i) {  // bubble passes over at most three registers
+#pragma unroll
+                    for (int j = 0; j < MM - 1 - i; ++j) {
+                        if (ts[j + 1] < ts[j]) {
+                            const uint64_t tt = ts[j];
+                            ts[j] = ts[j + 1];
+                            ts[j + 1] = tt;
+                            const double2 ta = as[j];
+                            as[j] = as[j + 1];
+                            as[j + 1] = ta;
+                        }
                     }
                 }
 #pragma unroll
                 for (unsigned c = 0; c < S; ++c) {
                     double2 acc = make_double2(0.0, 0.0);
-                    double2 term = cscale(a0, (__popcll((uint64_t)c & t0) & 1) ? -1. : 1.);
-                    acc = cadd(acc, cscale(term, a.extra));
-                    if (m == 2) {
-                        term = cscale(a1, (__popcll((uint64_t)c & t1) & 1) ? -1. : 1.);
-                        acc = cadd(acc, cscale(term, a.extra));
+#pragma unroll
+                    for (int j = 0; j < MM; ++j) {
+                        if ((unsigned)j < m) {
+                            const double2 term = cscale(as[j], (__popcll((uint64_t)c & ts[j]) & 1) ? -1. : 1.);
+                            acc = cadd(acc, cscale(term, a.extra));
+                        }
                     }
                     v[c] = acc;
                 }
@@ -2849,7 +2860,8 @@ template <int K, bool WRITE>
 static void launch_small(int am, int nb, unsigned grid, cudaStream_t st, const EmitArgs& ea) {
     if (nb == 1) launch_small_nb<K, 1, WRITE>(am, grid, st, ea);
     else if (nb == 2) launch_small_nb<K, 2, WRITE>(am, grid, st, ea);
-    else launch_small_nb<K, 3, WRITE>(am, grid, st, ea);
+    else if (nb == 3) launch_small_nb<K, 3, WRITE>(am, grid, st, ea);
+    else launch_small_am<K, 4, WRITE, false>(am, grid, st, ea);  // Hadamards only
 }
 template <int K>
 static void set_emit_smem_limits() {
@@ -3054,8 +3066,10 @@ static void run_group(State& s, const GroupSpec& gs) {
         smem = (size_t)(W == 32 ? 8 : 1) * S * sizeof(double2);
     }
     const bool bk = gr.bucket;
-    // targets of 1 to 3 bits (not batched): one thread per group
-    const bool small = !pair && gs.mode != GM_MERGE && nb >= 1 && nb <= 3 && !gs.varw.width;
+    // targets of 1 to 3 bits, and Hadamards on 4 bits (not batched): one
+    // thread per group (a 16-slot unitary is 256 complex products a thread)
+    const bool small = !pair && gs.mode != GM_MERGE && !gs.varw.width && nb >= 1 &&
+                       (nb <= 3 || (nb == 4 && gs.mode != GM_UNITARY));
     uint64_t T = 0;
     // Hadamard on 12 bits: register FWHT kernel; single pass when the output
     // bound (every group fully populated) fits a modest multiple of the input

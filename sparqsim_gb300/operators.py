@@ -441,6 +441,60 @@ class QRAMLoad(ElementwiseOperator, SelfAdjointOperator):
 QRAMLoadFast = QRAMLoad
 
 
+class GetRowAddr(ElementwiseOperator, SelfAdjointOperator):
+    """row_offset ^= offset + row_sz * row (hamiltonian_simulation.cpp:222-237);
+    the sum is kept to the output register's width."""
+
+    opcode = "ADDR_XOR"
+
+    def __init__(self, reg_offset, reg_row, row_sz: int, reg_row_offset):
+        super().__init__()
+        self.offset_id, self.row_id, self.out_id = _R(reg_offset), _R(reg_row), _R(reg_row_offset)
+        self.row_sz = int(row_sz)
+
+    def _fill(self, ins, dag):
+        ins.reg[0], ins.reg[1], ins.reg[3] = self.offset_id, self.row_id, self.out_id
+        ins.imm[0], ins.imm[1] = self.row_sz, 0
+
+
+class GetDataAddr(ElementwiseOperator, SelfAdjointOperator):
+    """data_offset ^= offset + row_sz * row + col_sparse
+    (hamiltonian_simulation.cpp:239-253)."""
+
+    opcode = "ADDR_XOR"
+
+    def __init__(self, reg_offset, reg_row, reg_col_sparse, row_sz: int, reg_data_offset):
+        super().__init__()
+        self.offset_id, self.row_id, self.col_id = _R(reg_offset), _R(reg_row), _R(reg_col_sparse)
+        self.out_id, self.row_sz = _R(reg_data_offset), int(row_sz)
+
+    def _fill(self, ins, dag):
+        ins.reg[0], ins.reg[1], ins.reg[2], ins.reg[3] = self.offset_id, self.row_id, self.col_id, self.out_id
+        ins.imm[0], ins.imm[1] = self.row_sz, 1
+
+
+class QuantumBinarySearch_Fast(ElementwiseOperator, SelfAdjointOperator):
+    """result ^= the address in [offset, offset + total_length) of the QRAM
+    word equal to target, by floor(log2(total_length)) + 1 rounds of
+    bisection, or 0 (hamiltonian_simulation.cpp:146-220)."""
+
+    opcode = "QBS_XOR"
+
+    def __init__(self, qram: QRAMCircuit_qutrit, reg_offset, total_length: int, reg_target, reg_result):
+        super().__init__()
+        if qram is None:
+            raise ValueError("null QRAM")
+        self.qram = qram
+        self.offset_id, self.target_id, self.result_id = _R(reg_offset), _R(reg_target), _R(reg_result)
+        self.total_length = int(total_length)
+        self.max_step = int(math.log2(self.total_length)) + 1 if self.total_length > 0 else 1
+
+    def _fill(self, ins, dag):
+        ins.reg[0], ins.reg[1], ins.reg[2] = self.offset_id, self.target_id, self.result_id
+        ins.imm[0], ins.imm[1] = self.total_length, self.max_step
+        ins.qram = self.qram._h.value
+
+
 class Fused(ElementwiseOperator):
     """A chain of elementwise operators applied in one pass over the state
     (one kernel launch per 32 instructions). dag applies the chain's inverse:

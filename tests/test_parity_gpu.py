@@ -203,6 +203,52 @@ def test_qram_load(dual, addr_bits, data_bits):
     dual.compare(exact_amp=True)
 
 
+def test_sparse_matrix_address_and_search(dual):
+    """GetRowAddr / GetDataAddr (XOR of offset + row_sz * row (+ col)) and
+    QuantumBinarySearch_Fast (a bisection of sorted runs of QRAM words per
+    entry, hamiltonian_simulation.cpp:182-253): keys bit-exact; hits, misses
+    and a conditioned form."""
+    dual.reg("off", U, 10)
+    dual.reg("row", U, 6)
+    dual.reg("col", U, 3)
+    dual.reg("out", U, 12)
+    dual.reg("tgt", U, 12)
+    dual.reg("res", U, 12)
+    dual.reg("x", U, 2)
+    rng = np.random.default_rng(77)
+    # 64 rows of 8 sorted distinct words at 512 + 8 row: searched by row
+    table = np.zeros(1 << 10, dtype=np.uint64)
+    for r in range(64):
+        table[512 + 8 * r: 512 + 8 * r + 8] = np.sort(rng.choice(4000, 8, replace=False))
+    q = dual.qram(10, 12, table)
+    n = 3000
+    rows = rng.integers(0, 64, n)
+    tg = np.where(rng.random(n) < 0.7, table[512 + 8 * rows + rng.integers(0, 8, n)], rng.integers(0, 4096, n))
+    regs = np.stack([np.full(n, 512), rows, rng.integers(0, 8, n), rng.integers(0, 4096, n), tg,
+                     np.zeros(n), rng.integers(0, 4, n)], axis=1).astype(np.uint64)
+    regs = np.unique(regs, axis=0)
+    amps = rng.normal(size=len(regs)) + 1j * rng.normal(size=len(regs))
+    dual.start(regs, amps / np.linalg.norm(amps))
+    dual.apply(ps.GetRowAddr("off", "row", 8, "out"))
+    dual.compare(exact_amp=True)
+    dual.apply(ps.GetDataAddr("off", "row", "col", 8, "out"))
+    dual.compare(exact_amp=True)
+    dual.apply(ps.GetRowAddr("off", "row", 8, "out"))  # out = its start value ^ data_addr
+    dual.compare(exact_amp=True)
+    dual.apply(ps.Init_Unsafe("out", 0))
+    dual.apply(ps.GetRowAddr("off", "row", 8, "out"))  # out = 512 + 8 row
+    dual.apply(ps.QuantumBinarySearch_Fast(q, "out", 8, "tgt", "res"))
+    dual.compare(exact_amp=True)
+    dual.apply(ps.QuantumBinarySearch_Fast(q, "out", 8, "tgt", "res").conditioned_by_nonzeros("x"))
+    dual.compare(exact_amp=True)
+    r, _ = dual.gpu.download()
+    ids = {name: ps.System.resolve(name) for name in ("tgt", "res", "x")}
+    sel = r[:, ids["x"]] == 0  # searched once: res holds the hit's address, 0 on a miss
+    res, tgt = r[sel, ids["res"]].astype(np.int64), r[sel, ids["tgt"]]
+    assert np.all(table[res[res > 0]] == tgt[res > 0])
+    assert (res > 0).any() and (res == 0).any()
+
+
 def test_multiword_keys(dual):
     # 3 words of packed keys; ops touching registers in different words
     for i, w in enumerate([40, 40, 40, 30, 20]):

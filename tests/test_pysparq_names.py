@@ -20,12 +20,9 @@ ALGORITHMS = Path("/root/reference/PySparQ/pysparq/algorithms")
 NOT_PROVIDED = {
     "CondRot_General_Bool_QW_fast": "the QRAM CKS walk (SparseMatrix oracles) is not built",
     "CustomArithmetic": "an arbitrary Python callable per entry has no device form",
-    "GetDataAddr": "the QRAM CKS walk is not built",
     "GetQWRotateAngle_Int_Int_Int": "the QRAM CKS walk's angle (the tridiagonal walk's is cks.GetQWRotateAngle_Int_Int_Int)",
-    "GetRowAddr": "the QRAM CKS walk is not built",
     "InverseQFT": "QFT is outside the gate-application path",
     "PartialTrace": "measurement sampling is outside the path (PartialTraceSelect is provided)",
-    "QuantumBinarySearch_Fast": "the QRAM CKS walk is not built",
     "SparseMatrix": "the QRAM CKS walk is not built",
     "combine_systems": "condition split/merge is per entry in this engine (conditioned operators)",
     "split_systems": "condition split/merge is per entry in this engine (conditioned operators)",
