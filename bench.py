@@ -1179,6 +1179,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
                       "alg_GBps": round(v[2] / (v[1] / 1e3) / 1e9, 1) if v[1] > 0 else 0}
                for name, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
 
+    at_scale = elementwise_at_scale(circ, st, peak, peak_kind)
+
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -1206,6 +1208,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
                      "traffic": traffic, "alg_bytes_per_launch": d_bytes / max(n_l, 1),
                      "avg_launch_ms": d_ms / max(n_l, 1)},
         "kernels": kernels,
+        "elementwise_at_scale": at_scale,
     }
     if clocks:
         result["clocks"] = clocks
@@ -1232,6 +1235,58 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     if args.cks_qram_terms and rank == 0:
         result["cks_qram"] = run_cks_qram(args, ext)
     return result
+
+
+def elementwise_at_scale(circ, st, peak: float, peak_kind: str, reps: int = 10) -> dict:
+    """The layer's fused elementwise program (b ^= QRAM[a], t = a*b,
+    c += t, t = a*b, phase on c bit 0: one launch) applied to the state the
+    last split left (2^24 entries, 0.54 GB). In the circuit the program runs
+    on the 4096 entries between a merge and a split, so it is timed here at
+    full size: per launch it reads and writes both key words and the
+    amplitude (64 B per entry) and gathers from the 4 MB table, which stays
+    in L2."""
+    from sparqsim_gb300 import _native
+    n = st.size()
+    _native.profile_reset()
+    _native.profile_enable(True)
+    for i in range(reps):
+        circ.mid[i % len(circ.mid)](st)
+    _native.profile_enable(False)
+    n_l, ms, nbytes = _native.profile_read()["elementwise_program"]
+    achieved = nbytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    return {"entries": n, "launches": n_l, "avg_launch_ms": ms / max(n_l, 1),
+            "alg_bytes_per_launch": nbytes / max(n_l, 1), "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+            "updates_per_s": 5 * n * n_l / (ms / 1e3) if ms > 0 else 0.0}
+
+
+def profile_case(args) -> None:
+    """Small cases of single kernels for ncu (no JSON line): see --profile-case."""
+    import torch
+
+    import sparqsim_gb300 as ps
+    from sparqsim_gb300 import _native
+    _native.call("sq_init", 0)
+    if args.profile_case == "elementwise":
+        from sparqsim_gb300.workloads import RegisterCircuit
+        circ = RegisterCircuit(args.hadamard_bits, 2, seed=SEED).build()
+        st = ps.SparseState(capacity=1 << (2 * args.hadamard_bits))
+        circ.run(st, layers=1)  # program_kernel launch 1 runs on 2^h entries; the state then holds 2^2h
+        for _ in range(3):
+            circ.mid[0](st)  # program_kernel launches 2..4 on the full state
+        print("elementwise case:", st.size(), "entries")
+    else:
+        from sparqsim_gb300.workloads import NoisyTrajectories
+        w = NoisyTrajectories(n_traj=args.trajectories, layers=6).build_batched()
+        st = ps.SparseState(capacity=1 << 26)
+        w.run_batched(st)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        w.run_batched(st)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        print("trajectories case:", st.size(), "entries")
+    ps.synchronize()
 
 
 def ctypes_void_p():
@@ -1376,7 +1431,15 @@ def main():
                          "(for ncu --profile-from-start off)")
     ap.add_argument("--group-strategy", default="autotune", choices=["autotune", "hash", "sort"],
                     help="how split operators group entries (autotune: timed per shape class)")
+    ap.add_argument("--profile-case", default="none", choices=["none", "elementwise", "trajectories"],
+                    help="run only a small case for an ncu capture and exit: 'elementwise' = one layer of the "
+                         "register circuit, then the layer's fused program three times on its 2^24 entries; "
+                         "'trajectories' = the batched trajectories (--trajectories instances) twice, the second "
+                         "run inside cudaProfilerStart/Stop")
     args = ap.parse_args()
+    if args.profile_case != "none":
+        profile_case(args)
+        return
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
     rank = int(os.environ.get("RANK", "0"))

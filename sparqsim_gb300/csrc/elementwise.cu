@@ -16,12 +16,45 @@
 
 namespace sq {
 
+// A register field with its masks computed on the host, so that a field
+// access costs a word select, a shift and an AND per entry
+struct DField {
+    uint8_t word;
+    uint8_t shift;
+    uint8_t width;
+    uint8_t type;
+    uint32_t pad;
+    uint64_t mask;   // wmask(width)
+    uint64_t smask;  // mask << shift
+};
+static DField dfield(const Field& f) {
+    DField d;
+    d.word = f.word;
+    d.shift = f.shift;
+    d.width = f.width;
+    d.type = f.type;
+    d.pad = 0;
+    d.mask = wmask(f.width);
+    d.smask = d.mask << f.shift;
+    return d;
+}
+template <int K>
+__device__ __forceinline__ uint64_t fget(const uint64_t (&k)[K], const DField& f) {
+    return (kword<K>(k, f.word) >> f.shift) & f.mask;
+}
+template <int K>
+__device__ __forceinline__ void fset(uint64_t (&k)[K], const DField& f, uint64_t v) {
+    const uint64_t w = kword<K>(k, f.word);
+    kword_set<K>(k, f.word, (w & ~f.smask) | ((v << f.shift) & f.smask));
+}
+
 struct DInstr {
     uint16_t op;
     uint8_t dag;
     uint8_t pad;
     uint32_t addr_bits;
-    Field f[4];
+    uint64_t amask;  // wmask(addr_bits)
+    DField f[4];
     uint64_t imm[3];
     double2 c[2];
     const void* table;
@@ -108,7 +141,7 @@ __device__ __forceinline__ uint64_t bits_deposit(uint64_t v, uint64_t m) {
 
 template <int K>
 __device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2& a, unsigned* err) {
-    const Field* f = in.f;
+    const DField* f = in.f;
     switch (in.op) {
         case SQ_OP_FLIP_BOOLS: fset<K>(k, f[0], ~fget<K>(k, f[0])); break;
         case SQ_OP_SWAP_BOOL_BOOL: {
@@ -262,7 +295,7 @@ __device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2
         case SQ_OP_X_BOOL: fset<K>(k, f[0], fget<K>(k, f[0]) ^ (1ull << in.imm[0])); break;
         case SQ_OP_INIT_UNSAFE: fset<K>(k, f[0], in.imm[0]); break;
         case SQ_OP_QRAM_LOAD: {
-            const uint64_t addr = fget<K>(k, f[0]) & wmask(in.addr_bits);
+            const uint64_t addr = fget<K>(k, f[0]) & in.amask;
             uint64_t word;
             if (in.elem_bytes == 2) word = __ldg((const unsigned short*)in.table + addr);
             else if (in.elem_bytes == 4) word = __ldg((const unsigned int*)in.table + addr);
@@ -421,18 +454,23 @@ __device__ __forceinline__ void exec(const DInstr& in, uint64_t (&k)[K], double2
 template <int K, int MAXI>
 __global__ void __launch_bounds__(256) program_kernel(const __grid_constant__ ProgramArgs<MAXI> p, KeyPtrs keys,
                                                       double2* __restrict__ amp, uint64_t n) {
+    // warp-uniform trips (the entry index is per lane, the loop is not), so
+    // that the instruction index is uniform and the instruction's fields are
+    // uniform loads
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x; b < n; b += stride) {
+        const uint64_t i = b + threadIdx.x;
+        const bool valid = i < n;
         uint64_t k[K];
 #pragma unroll
-        for (int w = 0; w < K; ++w) k[w] = ((p.read_words >> w) & 1u) ? keys.w[w][i] : 0ull;
+        for (int w = 0; w < K; ++w) k[w] = (valid && ((p.read_words >> w) & 1u)) ? keys.w[w][i] : 0ull;
         double2 a = make_double2(0.0, 0.0);
-        if (p.amp_mode & 1u) a = amp[i];
+        if (valid && (p.amp_mode & 1u)) a = amp[i];
         for (uint32_t j = 0; j < p.n; ++j) {
             const DInstr& in = p.ins[j];
-            if (!cond_ok<K>(k, in.cond)) continue;
-            exec<K>(in, k, a, p.err);
+            if (valid && cond_ok<K>(k, in.cond)) exec<K>(in, k, a, p.err);
         }
+        if (!valid) continue;
 #pragma unroll
         for (int w = 0; w < K; ++w)
             if ((p.write_words >> w) & 1u) keys.w[w][i] = k[w];
@@ -500,8 +538,9 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
     for (uint32_t i = 0; i < d.cond.n; ++i) rw |= 1u << d.cond.c[i].word;
     RegTable& t = regtable();
     auto F = [&](int slot) {
-        d.f[slot] = t.field(in.reg[slot]);
-        return d.f[slot];
+        const Field f = t.field(in.reg[slot]);
+        d.f[slot] = dfield(f);
+        return f;
     };
     auto R = [&](int slot) { rw |= word_bit(F(slot)); };
     auto W = [&](int slot) {
@@ -704,6 +743,7 @@ static void translate(const sq_instr& in, DInstr& d, uint32_t& rw, uint32_t& ww,
         }
         default: fail(SQ_ERR_INVALID, "unknown opcode " + std::to_string(in.op));
     }
+    d.amask = wmask(d.addr_bits);
 }
 
 void run_program(State& s, const sq_instr* prog, uint32_t n) {

@@ -145,10 +145,21 @@ __device__ __forceinline__ double fixed_to_double(long long Y, int e2) {
     if (be <= 0 || be >= 2047) return fixed_to_double_scaled(Y, e2);
     return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (q & 0xfffffffffffffull)));
 }
+// An exactly zero component stays +0.0 without the FP64 multiply (0 * s2 is
+// +0.0): merges leave most slots zero, and FP64 issue is scarce on GB300.
 __device__ __forceinline__ double2 from_fixed2(longlong2 v, int e2, bool odd, double s2) {
     double2 r = make_double2(fixed_to_double(v.x, e2), fixed_to_double(v.y, e2));
-    if (odd) r = cscale(r, s2);
+    if (odd && (v.x | v.y)) r = cscale(r, s2);
     return r;
+}
+// 1/sqrt(2^n) for a batched group's width n (0..63), as 1.0 / sqrt(2^n)
+// rounds it, built from exponent bits instead of an FP64 square root and
+// division: 2^(-n/2) for even n; for odd n sqrt(2^n) = 2^((n-1)/2) sqrt(2)
+// scales exactly, so the quotient is sqrt2inv (= 1/sqrt(2) rounded) times
+// 2^(-(n-1)/2).
+__device__ __forceinline__ double inv_sqrt_pow2(int n, double sqrt2inv) {
+    if (n & 1) return __longlong_as_double(__double_as_longlong(sqrt2inv) - ((long long)(n >> 1) << 52));
+    return __longlong_as_double((long long)(1023 - (n >> 1)) << 52);
 }
 __device__ __forceinline__ longlong2 ladd(longlong2 a, longlong2 b) { return make_longlong2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ longlong2 lsub(longlong2 a, longlong2 b) { return make_longlong2(a.x - b.x, a.y - b.y); }
@@ -754,67 +765,82 @@ __device__ __forceinline__ unsigned worker_rank(bool f, unsigned* s_tmp, unsigne
 
 // Single-pass integer Hadamard of up to 8 bits (or a batched width) whose
 // groups are all singletons (a fresh grouping with as many groups as
-// condition-passing entries):
-// a warp per group fans the entry out to its 2^n outputs. A group's data is
-// a chain of dependent reads (range, member, key), so each warp reads the
-// next group's while it writes the current one; groups are taken in a fixed
-// grid-stride order. Arithmetic and output order are those of the singleton
-// case of emit_hadamard_kernel.
+// condition-passing entries). Each lane of a warp fetches one of 32
+// consecutive groups (their chains of dependent reads run side by side), the
+// warp reserves the 32 groups' outputs with one atomic on the output cursor
+// (a reservation per group put up to a million same-address atomics in one
+// launch), then fans the groups out one after another, 32 outputs per store
+// instruction. Arithmetic and per-group output order are those of the
+// singleton case of emit_hadamard_kernel; groups land in the output in lane
+// order within a warp.
 template <int K, int AM>
 __global__ void __launch_bounds__(256) emit_fanout_kernel(const __grid_constant__ EmitArgs a) {
     const unsigned lane = threadIdx.x & 31u;
-    const uint64_t warps = (uint64_t)gridDim.x * 8u;
-    struct One {
+    const uint64_t step = (uint64_t)gridDim.x * 256u;  // groups per grid-wide round (32 per warp)
+    for (uint64_t gb = ((uint64_t)blockIdx.x * 8u + (threadIdx.x >> 5)) * 32u; gb < a.groups; gb += step) {
+        const uint64_t g = gb + lane;
+        const bool valid = g < a.groups;
         unsigned s0 = 0, m = 0;
         uint64_t v0 = 0;
         double2 a0 = make_double2(0.0, 0.0);
         uint64_t gk[K] = {};
-    };
-    auto fetch = [&](uint64_t gg, One& d) {
-        group_range<AM>(a, gg, d.s0, d.m);
-        if (d.m == 1u) {
-            member_at<AM>(a, d.s0, d.v0, d.a0);
-            load_key<K>(a.in_keys, group_head<AM>(a, gg, d.s0), d.gk);
+        if (valid) {
+            group_range<AM>(a, g, s0, m);
+            if (m == 1u) {
+                member_at<AM>(a, s0, v0, a0);
+                load_key<K>(a.in_keys, group_head<AM>(a, g, s0), gk);
+            }
         }
-    };
-    uint64_t g = (uint64_t)blockIdx.x * 8u + (threadIdx.x >> 5);
-    One cur;
-    if (g < a.groups) fetch(g, cur);
-    for (; g < a.groups; g += warps) {
-        One nxt;
-        if (g + warps < a.groups) fetch(g + warps, nxt);
         // a group that is not a singleton only arises in a graph replayed on
         // other data: nothing is written for it and the replay is reported
-        const bool one = cur.m == 1u;
-        const int nbits = a.varw.width ? (int)fget<K>(cur.gk, a.varw) : a.nbits;
+        const bool one = valid && m == 1u;
+        if (valid && !one) atomicOr(a.err, 32u);
+        const int nbits = a.varw.width ? (int)fget<K>(gk, a.varw) : a.nbits;
         const unsigned S = 1u << nbits;
-        const double extra = a.varw.width ? 1.0 / sqrt((double)S) : a.extra;
-        Field tg = a.target;
-        tg.width = (uint8_t)nbits;
+        const double extra = a.varw.width ? inv_sqrt_pow2(nbits, a.sqrt2inv) : a.extra;
         // singleton: a * 2^{-n/2}, sign (-1)^{popcount(t & v)} (hadamard.cpp:27-42)
-        const double2 base = cscale(cur.a0, extra);
+        const double2 base = cscale(a0, extra);
         // batched width 0: the entry is left as it is, never pruned
         const bool keep = one && ((a.varw.width && nbits == 0) || keep_amp(base, a.eps));
-        unsigned long long o = 0;
-        if (lane == 0) {
-            if (!one) atomicOr(a.err, 32u);
-            o = keep ? atomicAdd(a.cursor, (unsigned long long)S) : 0ull;
-            if (a.ocnt) {
-                a.ostart[g] = o;
-                a.ocnt[g] = keep ? S : 0u;
-            }
+        const unsigned cnt = keep ? S : 0u;
+        unsigned inc = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned t = __shfl_up_sync(0xffffffffu, inc, d);
+            if (lane >= (unsigned)d) inc += t;
         }
-        o = __shfl_sync(0xffffffffu, o, 0);
-        if (keep && o + S <= a.capacity) {
-            for (unsigned c = lane; c < S; c += 32u) {
+        const unsigned total = __shfl_sync(0xffffffffu, inc, 31);
+        unsigned long long wbase = 0;
+        if (lane == 31 && total) wbase = atomicAdd(a.cursor, (unsigned long long)total);
+        wbase = __shfl_sync(0xffffffffu, wbase, 31);
+        const unsigned long long o = wbase + (inc - cnt);
+        if (valid && a.ocnt) {
+            a.ostart[g] = keep ? o : 0ull;
+            a.ocnt[g] = cnt;
+        }
+        // past the output capacity (uniform over the warp): nothing is
+        // written, the host sees the cursor beyond it and reruns exactly
+        if (wbase + total > a.capacity) continue;
+        for (unsigned j = 0; j < 32u; ++j) {
+            const unsigned cj = __shfl_sync(0xffffffffu, cnt, j);
+            if (!cj) continue;  // uniform: the group is empty or pruned
+            const unsigned long long oj = __shfl_sync(0xffffffffu, o, j);
+            const uint64_t vj = __shfl_sync(0xffffffffu, v0, j);
+            const double2 bj = make_double2(__shfl_sync(0xffffffffu, base.x, j), __shfl_sync(0xffffffffu, base.y, j));
+            const int nj = __shfl_sync(0xffffffffu, nbits, j);
+            uint64_t kj[K];
+#pragma unroll
+            for (int w = 0; w < K; ++w) kj[w] = __shfl_sync(0xffffffffu, gk[w], j);
+            Field tg = a.target;
+            tg.width = (uint8_t)nj;
+            for (unsigned c = lane; c < cj; c += 32u) {
                 uint64_t kk[K];
 #pragma unroll
-                for (int w = 0; w < K; ++w) kk[w] = cur.gk[w];
+                for (int w = 0; w < K; ++w) kk[w] = kj[w];
                 fset<K>(kk, tg, (uint64_t)c);
-                store_out_sign<K>(a, o + c, kk, base, __popcll((uint64_t)c & cur.v0) & 1);
+                store_out_sign<K>(a, oj + c, kk, bj, __popcll((uint64_t)c & vj) & 1);
             }
         }
-        cur = nxt;
     }
 }
 
@@ -822,8 +848,13 @@ __device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
     return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
 }
 
+// A warp per group (W = 32, targets up to 8 bits) or a CTA per group. The
+// warp form is latency-bound (a chain of dependent loads and shared-memory
+// stages per group), so it asks for 4 CTAs per SM at one key word and 3 at
+// two (a few bytes of spills outside the stage loops), to keep more groups
+// in flight.
 template <int K, int W, bool WRITE, int AM>
-__global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constant__ EmitArgs a) {
+__global__ void __launch_bounds__(256, W == 32 ? (K == 1 ? 4 : K == 2 ? 3 : 1) : 1) emit_hadamard_kernel(const __grid_constant__ EmitArgs a) {
     extern __shared__ double2 s_slots[];
     __shared__ unsigned s_tmp[8];
     __shared__ uint64_t s_member_t[8][64];
@@ -860,7 +891,7 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
         // batched Hadamard: this group's digit count comes from its key
         const int nbits = a.varw.width ? (int)fget<K>(gk, a.varw) : a.nbits;
         const unsigned S = 1u << nbits;
-        const double extra = a.varw.width ? 1.0 / sqrt((double)S) : a.extra;
+        const double extra = a.varw.width ? inv_sqrt_pow2(nbits, a.sqrt2inv) : a.extra;
         Field tg = a.target;
         tg.width = (uint8_t)nbits;
         const bool sparse_full = a.mode == GM_HADAMARD_FULL && m <= (unsigned)(nbits - 1);
@@ -999,6 +1030,34 @@ __global__ void __launch_bounds__(256) emit_hadamard_kernel(const __grid_constan
         // count / write the kept slots in ascending target order
         unsigned long long o = 0;
         bool fits = true;
+        if (W == 32 && WRITE && a.cursor) {
+            // single pass, a warp per group (S <= 256): the rows' keep masks
+            // stay in registers between the count and the write
+            unsigned ball[8];
+            unsigned total = 0;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const unsigned c = (unsigned)r * 32u + t;
+                ball[r] = (unsigned)r * 32u < S ? __ballot_sync(0xffffffffu, c < S && keep_amp(slots[c], a.eps)) : 0u;
+                total += __popc(ball[r]);
+            }
+            o = reserve_out<W>(a, g, total, fits, &s_base);
+            unsigned kept = 0;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const unsigned c = (unsigned)r * 32u + t;
+                if (fits && ((ball[r] >> t) & 1u)) {
+                    uint64_t kk[K];
+#pragma unroll
+                    for (int w = 0; w < K; ++w) kk[w] = gk[w];
+                    fset<K>(kk, tg, (uint64_t)c);
+                    store_out<K>(a, o + kept + __popc(ball[r] & ((1u << t) - 1u)), kk, slots[c]);
+                }
+                kept += __popc(ball[r]);
+            }
+            worker_sync<W>();
+            continue;
+        }
         if (WRITE && a.cursor) {  // single pass: count, reserve, then write
             unsigned total = 0;
             for (unsigned r = 0; r < S; r += W) {
@@ -3166,8 +3225,10 @@ static void run_group(State& s, const GroupSpec& gs) {
             const unsigned fgrid = (unsigned)std::min<uint64_t>((G + 7) / 8, (uint64_t)num_sms() * 8);
             if (fanout) {
                 ea.err = device_error_word();
-                if (am == 1) emit_fanout_kernel<K, 1><<<fgrid, 256, 0, st>>>(ea);
-                else emit_fanout_kernel<K, 0><<<fgrid, 256, 0, st>>>(ea);
+                // 256 groups per CTA and round (a group per lane)
+                const unsigned ogrid = (unsigned)std::min<uint64_t>((G + 255) / 256, (uint64_t)num_sms() * 8);
+                if (am == 1) emit_fanout_kernel<K, 1><<<ogrid, 256, 0, st>>>(ea);
+                else emit_fanout_kernel<K, 0><<<ogrid, 256, 0, st>>>(ea);
             } else if (W == 32) launch_hadamard<K, 32, true>(am, fgrid, smem, st, ea);
             else launch_hadamard<K, 256, true>(am, (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2), smem, st, ea);
             prof_end((double)P * E);

@@ -127,6 +127,7 @@ DCondSet resolve_cond(const sq_cond* c) {
         d.c[i].word = f.word;
         d.c[i].shift = f.shift;
         d.c[i].width = f.width;
+        d.c[i].mask = wmask(f.width);
         d.c[i].param = q.param;
         if (q.kind == SQ_COND_BIT && q.param >= 64) fail(SQ_ERR_INVALID, "condition bit >= 64");
     }

@@ -108,6 +108,7 @@ struct DCond {
     uint8_t width;
     uint32_t pad;
     uint64_t param;
+    uint64_t mask;  // wmask(width), computed on the host
 };
 struct DCondSet {
     uint32_t n;
@@ -145,10 +146,10 @@ __device__ __forceinline__ bool cond_ok(const uint64_t (&k)[K], const DCondSet& 
     bool ok = true;
     for (uint32_t i = 0; i < cs.n; ++i) {
         const DCond& c = cs.c[i];
-        const uint64_t v = (kword<K>(k, c.word) >> c.shift) & wmask(c.width);
+        const uint64_t v = (kword<K>(k, c.word) >> c.shift) & c.mask;
         switch (c.kind) {
             case SQ_COND_NONZERO: ok = ok && (v != 0); break;
-            case SQ_COND_ALL_ONES: ok = ok && (v == wmask(c.width)); break;
+            case SQ_COND_ALL_ONES: ok = ok && (v == c.mask); break;
             case SQ_COND_BIT: ok = ok && (c.param < 64) && ((v >> c.param) & 1ull); break;
             default: ok = ok && (v == c.param); break;
         }
