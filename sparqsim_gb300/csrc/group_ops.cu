@@ -438,6 +438,8 @@ struct EmitArgs {
     int fix;                   // FWHT arithmetic: 0 the reference's FP64 butterflies, 1 exact sums
     unsigned long long* ticket;  // dynamic group order: next group, CTAs finished (zero between launches)
     unsigned* err;               // device error word
+    unsigned* glist;             // groups left by a singleton fan-out, and their number (glist_n);
+    unsigned* glist_n;           // emit_hadamard_kernel then runs over these groups only
 };
 
 // Dynamic group order for the persistent emit kernels. A grid of two CTAs
@@ -791,10 +793,15 @@ __global__ void __launch_bounds__(256) emit_fanout_kernel(const __grid_constant_
                 load_key<K>(a.in_keys, group_head<AM>(a, g, s0), gk);
             }
         }
-        // a group that is not a singleton only arises in a graph replayed on
-        // other data: nothing is written for it and the replay is reported
+        // a group of several members (a few collisions among mostly singleton
+        // groups) is listed for emit_hadamard_kernel; without a list it only
+        // arises in a graph replayed on other data: nothing is written for it
+        // and the replay is reported
         const bool one = valid && m == 1u;
-        if (valid && !one) atomicOr(a.err, 32u);
+        if (valid && !one) {
+            if (a.glist) a.glist[atomicAdd(a.glist_n, 1u)] = (unsigned)g;  // several members: left for the next kernel
+            else atomicOr(a.err, 32u);
+        }
         const int nbits = a.varw.width ? (int)fget<K>(gk, a.varw) : a.nbits;
         const unsigned S = 1u << nbits;
         const double extra = a.varw.width ? inv_sqrt_pow2(nbits, a.sqrt2inv) : a.extra;
@@ -868,21 +875,27 @@ __global__ void __launch_bounds__(256, W == 32 ? (K == 1 ? 4 : K == 2 ? 3 : 1) :
     const uint64_t stride = (uint64_t)gridDim.x * workers_per_block;
     // a group's range and key are a chain of dependent reads: the next
     // group's are issued while the current one is transformed
-    uint64_t g = (uint64_t)blockIdx.x * workers_per_block + wid;
+    // every group, or the groups a fan-out listed (their number written by
+    // that kernel, earlier on the same stream)
+    const uint64_t ng = a.glist ? (uint64_t)*a.glist_n : a.groups;
+    uint64_t i = (uint64_t)blockIdx.x * workers_per_block + wid;
     unsigned s0_next = 0, m_next = 0;
     uint64_t gk_next[K] = {};
-    if (g < a.groups) {
-        group_range<AM>(a, g, s0_next, m_next);
-        if (m_next) load_key<K>(a.in_keys, group_head<AM>(a, g, s0_next), gk_next);
+    if (i < ng) {
+        const uint64_t gn = a.glist ? (uint64_t)a.glist[i] : i;
+        group_range<AM>(a, gn, s0_next, m_next);
+        if (m_next) load_key<K>(a.in_keys, group_head<AM>(a, gn, s0_next), gk_next);
     }
-    for (; g < a.groups; g += stride) {
+    for (; i < ng; i += stride) {
+        const uint64_t g = a.glist ? (uint64_t)a.glist[i] : i;
         const unsigned s0 = s0_next, m = m_next;
         uint64_t gk[K];
 #pragma unroll
         for (int w = 0; w < K; ++w) gk[w] = gk_next[w];
-        if (g + stride < a.groups) {
-            group_range<AM>(a, g + stride, s0_next, m_next);
-            if (m_next) load_key<K>(a.in_keys, group_head<AM>(a, g + stride, s0_next), gk_next);
+        if (i + stride < ng) {
+            const uint64_t gn = a.glist ? (uint64_t)a.glist[i + stride] : i + stride;
+            group_range<AM>(a, gn, s0_next, m_next);
+            if (m_next) load_key<K>(a.in_keys, group_head<AM>(a, gn, s0_next), gk_next);
         }
         if (m == 0) {  // an emptied cached range
             if (!WRITE && t == 0) a.cnt[g] = 0u;
@@ -3215,8 +3228,10 @@ static void run_group(State& s, const GroupSpec& gs) {
             prof_end((double)P * E);
             SQ_CUDA(cudaGetLastError());
         } else {
-            // a fresh grouping (no empty groups) with as many groups as entries: all singletons
-            const bool fanout = W == 32 && gs.mode == GM_HADAMARD_INT && am < 2 && G == P;
+            // a fresh grouping (no empty groups) whose groups are all (G == P) or
+            // mostly (2G > P) singletons: the fan-out kernel, which lists the
+            // groups of several members for the warp-per-group kernel after it
+            const bool fanout = W == 32 && gs.mode == GM_HADAMARD_INT && am < 2 && 2 * G > P;
             // named apart by what the groups mostly are: members of several-member
             // groups (merges) or singletons fanned out
             prof_begin(fanout          ? "emit_fanout_single_pass"
@@ -3227,8 +3242,19 @@ static void run_group(State& s, const GroupSpec& gs) {
                 ea.err = device_error_word();
                 // 256 groups per CTA and round (a group per lane)
                 const unsigned ogrid = (unsigned)std::min<uint64_t>((G + 255) / 256, (uint64_t)num_sms() * 8);
+                if (G < P) {  // the list's length, then the group ids
+                    unsigned* gl = (unsigned*)ws().get(WS_GROUP_LIST, (G + 16) * 4);
+                    SQ_CUDA(cudaMemsetAsync(gl, 0, 4, st));
+                    ea.glist_n = gl;
+                    ea.glist = gl + 16;
+                }
                 if (am == 1) emit_fanout_kernel<K, 1><<<ogrid, 256, 0, st>>>(ea);
                 else emit_fanout_kernel<K, 0><<<ogrid, 256, 0, st>>>(ea);
+                if (G < P) {
+                    SQ_CUDA(cudaGetLastError());
+                    launch_hadamard<K, 32, true>(am, fgrid, smem, st, ea);
+                    ea.glist = ea.glist_n = nullptr;
+                }
             } else if (W == 32) launch_hadamard<K, 32, true>(am, fgrid, smem, st, ea);
             else launch_hadamard<K, 256, true>(am, (unsigned)std::min<uint64_t>(G, (uint64_t)num_sms() * 2), smem, st, ea);
             prof_end((double)P * E);

@@ -338,6 +338,7 @@ enum WsSlot {
     WS_SKETCH,
     WS_OUTPUT,
     WS_PAIR_TABLE,    // partner table of the 1-bit splits
+    WS_GROUP_LIST,    // groups a singleton fan-out leaves to the warp-per-group emit
     WS_SCRATCH_TEST,  // buffers of the bounded-wait self-test
     WS_COUNT_MAX
 };

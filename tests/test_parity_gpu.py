@@ -265,8 +265,11 @@ def test_multiword_keys(dual):
 
 # ----------------------------------------------------------------- split / merge
 @pytest.mark.parametrize("n_digits", [1, 2, 3, 5, 8, 10, 12])
-@pytest.mark.parametrize("fill", ["singleton", "full", "mixed"])
+@pytest.mark.parametrize("fill", ["singleton", "full", "mixed", "collide"])
 def test_hadamard_int(dual, strategy, n_digits, fill):
+    """'collide': mostly singleton groups with every tenth holding two or
+    three members (the fan-out kernel lists those for the warp-per-group
+    kernel, targets up to 8 bits)."""
     dual.reg("x", U, 14)
     dual.reg("y", U, 9)
     dual.reg("z", U, 6)
@@ -277,6 +280,8 @@ def test_hadamard_int(dual, strategy, n_digits, fill):
         f = lambda g: 1  # noqa: E731
     elif fill == "full":
         f = lambda g: S  # noqa: E731
+    elif fill == "collide":
+        f = lambda g: min(S, 2 + g % 20 // 10) if g % 10 == 0 else 1  # noqa: E731
     else:
         f = lambda g: int(rng.integers(1, S + 1))  # noqa: E731
     regs, amps = grouped_state(rng, [9, 14, 6], 1, n_digits, groups, f)
