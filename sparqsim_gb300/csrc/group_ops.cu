@@ -971,15 +971,24 @@ __global__ void __launch_bounds__(256, W == 32 ? (K == 1 ? 4 : K == 2 ? 3 : 1) :
             worker_sync<W>();
         } else {
             // zero-filled slots, scatter members, stage-ascending FWHT (hadamard.cpp:44-59, 100-131)
-            for (unsigned c = t; c < S; c += W) slots[c] = make_double2(0.0, 0.0);
-            worker_sync<W>();
             int emax = 1;
-            for (unsigned j = t; j < m; j += W) {
-                uint64_t tj;
-                double2 aj;
-                member_at<AM>(a, s0 + j, tj, aj);
-                slots[tj & (S - 1u)] = aj;  // cached ranges of a batched split: only the group's own n bits
-                emax = max(emax, amp_exp(aj));
+            if (AM == 2 && m == S) {
+                // a full cached range: member c has target c, read as amplitudes only
+                for (unsigned c = t; c < S; c += W) {
+                    const double2 ac = __ldcs(a.in_amp + s0 + c);
+                    slots[c] = ac;
+                    emax = max(emax, amp_exp(ac));
+                }
+            } else {
+                for (unsigned c = t; c < S; c += W) slots[c] = make_double2(0.0, 0.0);
+                worker_sync<W>();
+                for (unsigned j = t; j < m; j += W) {
+                    uint64_t tj;
+                    double2 aj;
+                    member_at<AM>(a, s0 + j, tj, aj);
+                    slots[tj & (S - 1u)] = aj;  // cached ranges of a batched split: only the group's own n bits
+                    emax = max(emax, amp_exp(aj));
+                }
             }
             const bool fix = a.fix && a.mode != GM_UNITARY;
             if (fix) emax = worker_max<W>(emax, s_tmp);
