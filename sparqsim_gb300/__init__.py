@@ -29,5 +29,7 @@ from .operators import (Abs_SInt, Add_AnyInt_AnyInt_InPlace, Add_ConstUInt_InPla
                         Sqrt_UInt, Sub_UInt_UInt, Swap_Bool_Bool, Swap_General_General, T_Bool, X_Bool,
                         Xor_UInt_UInt, Y_Bool, Z_Bool, ZeroConditionalPhaseFlip, add_systems, get_output,
                         synchronize)
+from .cks import GetQWRotateAngle_Int_Int_Int
+from .cks_qram import SparseMatrix
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -46,10 +46,26 @@ class SparseMatrix(cks.SparseMatrix):
     """A sparse n x n matrix (n a power of two; a dense array or a
     scipy.sparse matrix) as the QRAM words the walk reads, with at most
     nnz_col nonzeros per row (nnz_col the next power of two of the densest
-    row)."""
+    row).
 
-    def __init__(self, A, data_size: int, positive_only: bool | None = None):
+    pysparq's constructor form is accepted too (PySparQ/pysparq/_core.pyi
+    SparseMatrix, as PySparQ/pysparq/algorithms/cks_solver.py:278 and :344
+    call it): SparseMatrix(elements, sparsity, data_size, nnz_col, n_row,
+    positive_only), row j's slots at [nnz_col j, nnz_col (j + 1)) of both
+    lists, values already scaled into (-1, 1) and quantised against full
+    scale 1.0; slots whose value is 0 are padding."""
+
+    def __init__(self, A, data_size: int, *args, positive_only: bool | None = None):
         import scipy.sparse as sp
+        full_scale = None
+        if len(args) == 4:  # pysparq form: (elements, sparsity, data_size, nnz_col, n_row, positive_only)
+            A, positive_only = self._from_slot_lists(A, data_size, args[1], args[2]), bool(args[3])
+            data_size, full_scale = int(args[0]), 1.0
+        elif len(args) == 1:
+            positive_only = args[0]
+        elif args:
+            raise TypeError("SparseMatrix(A, data_size[, positive_only]) or "
+                            "SparseMatrix(elements, sparsity, data_size, nnz_col, n_row, positive_only)")
         C = sp.csr_matrix(A, dtype=np.float64)
         C.eliminate_zeros()
         C.sort_indices()
@@ -67,7 +83,12 @@ class SparseMatrix(cks.SparseMatrix):
         self.nnz_col = 1 << max(0, (dens - 1).bit_length())
         if n + self.nnz_col > (1 << self.data_size):
             raise ValueError("SparseMatrix: column indices do not fit data_size bits")
-        self.amax = float(np.max(np.abs(vals))) if vals.size else 1.0
+        if full_scale is not None:
+            if vals.size and float(np.max(np.abs(vals))) > full_scale:
+                raise ValueError("SparseMatrix: elements must lie in [-1, 1] in the slot-list form")
+            self.amax = full_scale
+        else:
+            self.amax = float(np.max(np.abs(vals))) if vals.size else 1.0
         nn = self.nnz_col
         off = n * nn
         # slot s of row j: the s-th nonzero in ascending column order, then padding
@@ -81,6 +102,35 @@ class SparseMatrix(cks.SparseMatrix):
         data[off:] = cols
         self._data = data
         self._angle_tables: dict = {}
+
+    @staticmethod
+    def _from_slot_lists(elements, sparsity, nnz_col, n_row):
+        """The n_row x n_row matrix of pysparq's slot lists (padding slots,
+        value 0, dropped; a column named twice in a row is an error)."""
+        import scipy.sparse as sp
+        nn, n = int(nnz_col), int(n_row)
+        vals = np.asarray(elements, dtype=np.float64)
+        cols = np.asarray(sparsity, dtype=np.int64)
+        if nn < 1 or n < 1 or vals.shape != (n * nn,) or cols.shape != (n * nn,):
+            raise ValueError("SparseMatrix: elements and sparsity need n_row * nnz_col slots each")
+        rows = np.repeat(np.arange(n), nn)
+        keep = vals != 0
+        if np.any((cols[keep] < 0) | (cols[keep] >= n)):
+            raise ValueError("SparseMatrix: a column index is outside the matrix")
+        pairs = rows[keep] * n + cols[keep]
+        if np.unique(pairs).size != pairs.size:
+            raise ValueError("SparseMatrix: a row names the same column twice")
+        return sp.csr_matrix((vals[keep], (rows[keep], cols[keep])), shape=(n, n))
+
+    @property
+    def elements(self) -> list:
+        """The quantised element words, nnz_col per row (pysparq's `elements`)."""
+        return [int(v) for v in self._data[: self.get_sparsity_offset()]]
+
+    @property
+    def sparsity(self) -> list:
+        """The column words, nnz_col per row (pysparq's `sparsity`)."""
+        return [int(v) for v in self._data[self.get_sparsity_offset():]]
 
     def quantise_array(self, a) -> np.ndarray:
         ds = self.data_size

@@ -7,7 +7,7 @@
 // The group count sizes the hash table (no overflow retry); the output count
 // gives the single-pass emit a capacity where the "fully populated" bound is
 // too large to allocate. The exact count-then-scan path stays the fallback and
-// the judge of every prediction: a single pass whose outputs overflow the
+// the check on every prediction: a single pass whose outputs overflow the
 // predicted capacity is redone exactly, so results never depend on the model.
 //
 // Training data is logged by the split operators themselves (features before,

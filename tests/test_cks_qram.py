@@ -50,6 +50,55 @@ def test_sparse_matrix_layout():
     assert np.allclose(ms.dequantised() * ms.amax, S, atol=ms.amax / ((1 << 11) - 1))
 
 
+def _slot_lists(M, nnz_col):
+    """pysparq's slot lists of a matrix already scaled into (-1, 1): row j's
+    nonzeros in ascending column order, then padding slots (column 0, value
+    0), as PySparQ/pysparq/algorithms/cks_solver.py:329-341 lays them out."""
+    values, sparsity = [], []
+    for row in M:
+        cols = list(np.nonzero(row)[0])
+        for pos in range(nnz_col):
+            sparsity.append(int(cols[pos]) if pos < len(cols) else 0)
+            values.append(float(row[cols[pos]]) if pos < len(cols) else 0.0)
+    return values, sparsity
+
+
+@pytest.mark.parametrize("signed", [False, True])
+def test_sparse_matrix_pysparq_form(signed):
+    """ps.SparseMatrix(elements, sparsity, data_size, nnz_col, n_row,
+    positive_only), the constructor the reference's Python CKS solver calls:
+    the same words as the dense form, quantised against full scale 1.0."""
+    A = _positive_banded(16, 2, 4.0, 3)
+    if signed:
+        A[2, 3] = A[3, 2] = -0.7
+    M = A / np.linalg.norm(A, 2)
+    vals, cols = _slot_lists(M, 5)
+    m = ps.SparseMatrix(vals, cols, 14, 5, 16, not signed)
+    assert isinstance(m, cks_qram.SparseMatrix)
+    assert (m.n_row, m.nnz_col, m.data_size, m.positive_only, m.amax) == (16, 8, 14, not signed, 1.0)
+    full = (1 << 14) - 1 if not signed else (1 << 13) - 1
+    assert np.allclose(m.dequantised(), M, atol=1.0 / full)
+    # the layout is the dense form's, only the full scale differs
+    dense = cks_qram.SparseMatrix(M, 14, positive_only=not signed)
+    off = m.get_sparsity_offset()
+    assert off == dense.get_sparsity_offset() == 16 * 8
+    assert m.sparsity == dense.sparsity == [int(v) for v in m.get_data()[off:]]
+    assert m.elements == [int(v) for v in m.get_data()[:off]]
+    nz = np.nonzero(M)
+    enc = m.quantise_array(M[nz])
+    slots = [8 * j + int(np.searchsorted(np.nonzero(M[j])[0], c)) for j, c in zip(*nz)]
+    assert [m.elements[s] for s in slots] == [int(v) for v in enc]
+    # malformed slot lists are refused
+    with pytest.raises(ValueError):
+        ps.SparseMatrix(vals[:-1], cols, 14, 5, 16, not signed)
+    bad = list(cols)
+    bad[1] = bad[0]  # row 0 names one column twice
+    with pytest.raises(ValueError):
+        ps.SparseMatrix(vals, bad, 14, 5, 16, not signed)
+    with pytest.raises(ValueError):
+        ps.SparseMatrix([2.0 * v for v in vals], cols, 14, 5, 16, not signed)
+
+
 # ------------------------------------------------------------------ GPU
 class DualRun:
     def __init__(self, dual):
@@ -68,8 +117,14 @@ class DualRun:
         o(self.dual.gpu)
 
 
-def _walk(dual, A, ds=16):
-    mat = cks_qram.SparseMatrix(A, ds)
+def _walk(dual, A, ds=16, form="dense"):
+    if form == "dense":
+        mat = cks_qram.SparseMatrix(A, ds)
+    else:  # pysparq's slot lists of A / ||A||_2, as the reference's Python solver builds them
+        M = A / np.linalg.norm(A, 2)
+        nnz = int(np.max(np.sum(M != 0, axis=1)))
+        vals, cols = _slot_lists(M, nnz)
+        mat = ps.SparseMatrix(vals, cols, ds, nnz, A.shape[0], bool(np.all(M >= 0)))
     w = cks_qram.QuantumWalkNSteps(mat)
     w.InitEnvironment(declare=dual.reg)
     dual.O.register_qram(w.qram)
@@ -107,13 +162,19 @@ def test_sparse_oracles_parity(dual):
 
 
 @pytest.mark.gpu
-def test_walk_parity_with_oracle(dual):
+@pytest.mark.parametrize("form", ["dense", "pysparq", "pysparq_signed"])
+def test_walk_parity_with_oracle(dual, form):
     """Input preparation, FirstStep and two walk steps over a QRAM matrix at
     n = 8, every operator against the oracle: keys bit-exact, amplitudes
-    within 1e-12 (CondRot takes sin and cos on the GPU)."""
+    within 1e-12 (CondRot takes sin and cos on the GPU). The matrix is built
+    from a dense array, or from pysparq's slot lists (ps.SparseMatrix's
+    constructor form), positive or with signed elements."""
     dual.relaxed = True
     A = _positive_banded(8, 1, 3.0, 3)
-    mat, w = _walk(dual, A)
+    if form == "pysparq_signed":
+        A[1, 2] = A[2, 1] = -A[1, 2]
+    mat, w = _walk(dual, A, form=form)
+    assert mat.positive_only == (form != "pysparq_signed")
     dual.start()
     run = DualRun(dual)
     for o in w.init_ops():

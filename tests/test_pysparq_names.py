@@ -18,12 +18,11 @@ ALGORITHMS = Path("/root/reference/PySparQ/pysparq/algorithms")
 
 # not provided, and why
 NOT_PROVIDED = {
-    "CondRot_General_Bool_QW_fast": "the QRAM CKS walk (SparseMatrix oracles) is not built",
+    "CondRot_General_Bool_QW_fast": "removed from the reference's own bindings (PySparQ/core.cpp:1477); "
+                                    "signed matrices take GetQWRotateAngle_Int_Int_Int + CondRot_Fixed_Bool",
     "CustomArithmetic": "an arbitrary Python callable per entry has no device form",
-    "GetQWRotateAngle_Int_Int_Int": "the QRAM CKS walk's angle (the tridiagonal walk's is cks.GetQWRotateAngle_Int_Int_Int)",
     "InverseQFT": "QFT is outside the gate-application path",
     "PartialTrace": "measurement sampling is outside the path (PartialTraceSelect is provided)",
-    "SparseMatrix": "the QRAM CKS walk is not built",
     "combine_systems": "condition split/merge is per entry in this engine (conditioned operators)",
     "split_systems": "condition split/merge is per entry in this engine (conditioned operators)",
 }
