@@ -2094,19 +2094,41 @@ constexpr unsigned kSmallGroupMax = 8192;  // entries
 constexpr unsigned kSmallPer = kSmallGroupMax / 1024;
 
 template <int K>
-__device__ __forceinline__ void group_key(const ConstKeyPtrs& keys, unsigned e, const uint64_t (&gm)[K], Field tgt,
-                                          Field varw, uint64_t (&k)[K]) {
+__device__ __forceinline__ void group_key_of(const uint64_t (&full)[K], const uint64_t (&gm)[K], Field tgt, Field varw,
+                                             uint64_t (&k)[K]) {
 #pragma unroll
-    for (int w = 0; w < K; ++w) k[w] = keys.w[w][e] & gm[w];
+    for (int w = 0; w < K; ++w) k[w] = full[w] & gm[w];
     if (varw.width) {
-        uint64_t full[K];
-#pragma unroll
-        for (int w = 0; w < K; ++w) full[w] = keys.w[w][e];
         const unsigned nd = (unsigned)fget<K>(full, varw);
         kword_set<K>(k, tgt.word, kword<K>(k, tgt.word) & ~(wmask(nd) << tgt.shift));
     }
 }
+template <int K>
+__device__ __forceinline__ void group_key(const ConstKeyPtrs& keys, unsigned e, const uint64_t (&gm)[K], Field tgt,
+                                          Field varw, uint64_t (&k)[K]) {
+    uint64_t full[K];
+#pragma unroll
+    for (int w = 0; w < K; ++w) full[w] = keys.w[w][e];
+    group_key_of<K>(full, gm, tgt, varw, k);
+}
 
+// an entry's target digits (its own width when the width is per entry) and amplitude
+__device__ __forceinline__ void small_member(const ConstKeyPtrs& keys, const double2* __restrict__ amp, unsigned e,
+                                             Field tgt, Field varw, unsigned& t, double2& a) {
+    const unsigned nd = varw.width ? (unsigned)((keys.w[varw.word][e] >> varw.shift) & wmask(varw.width)) : tgt.width;
+    t = (unsigned)((keys.w[tgt.word][e] >> tgt.shift) & wmask(nd));
+    a = amp[e];
+}
+template <int K>
+__host__ __device__ constexpr unsigned small_batch() { return K <= 2 ? 4u : K <= 4 ? 2u : 1u; }  // no spills
+
+// A thread's entries are handled in batches of small_batch<K>(), whose key words
+// (and, when written out, amplitudes) are loaded before any of them is used,
+// so that a batch costs one memory round trip instead of one per entry.
+// When every entry passes the conditions and no two entries share a group key
+// (the split that follows a merge, as a rule), every group is a singleton: the
+// groups are the entries in entry order, written without the scan over the
+// table and the bucket pass.
 template <int K>
 __global__ void __launch_bounds__(1024) group_small_kernel(const __grid_constant__ ConstKeyPtrs keys,
                                                            const uint64_t* __restrict__ gmask,
@@ -2117,56 +2139,97 @@ __global__ void __launch_bounds__(1024) group_small_kernel(const __grid_constant
                                                            unsigned* __restrict__ seg, unsigned* __restrict__ ghead,
                                                            unsigned* __restrict__ btgt, double2* __restrict__ bamp,
                                                            unsigned* __restrict__ pass_list, unsigned* err) {
+    constexpr unsigned kSmallBatch = small_batch<K>();
     extern __shared__ unsigned s_tab[];  // cap slots | cap counts
     unsigned* table = s_tab;
     unsigned* cnt = s_tab + cap;
-    __shared__ unsigned s_F, s_scan[32][2];
+    __shared__ unsigned s_F, s_dup, s_scan[32][2];
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     for (unsigned i = tid; i < 2 * cap; i += 1024u) s_tab[i] = 0u;
-    if (tid == 0) s_F = 0u;
+    if (tid == 0) {
+        s_F = 0u;
+        s_dup = 0u;
+    }
     uint64_t gm[K];
 #pragma unroll
     for (int w = 0; w < K; ++w) gm[w] = gmask[w];
     __syncthreads();
     unsigned myslot[kSmallPer];
 #pragma unroll
-    for (unsigned q = 0; q < kSmallPer; ++q) {
-        const unsigned e = tid + q * 1024u;
-        myslot[q] = ~0u;
-        if (e >= n) continue;
-        uint64_t full[K];
+    for (unsigned qb = 0; qb < kSmallPer; qb += kSmallBatch) {
+        uint64_t full[kSmallBatch][K];
 #pragma unroll
-        for (int w = 0; w < K; ++w) full[w] = keys.w[w][e];
-        bool pass = cond_ok<K>(full, cond);
-        if (pass && varw.width && (unsigned)fget<K>(full, varw) > max_digits) {
-            atomicOr(err, 4u);
-            pass = false;
-        }
-        if (!pass) {
-            pass_list[atomicAdd(&s_F, 1u)] = e;
-            continue;
-        }
-        uint64_t k[K];
-        group_key<K>(keys, e, gm, tgt, varw, k);
-        unsigned long long hv = 0x9e3779b97f4a7c15ull;
+        for (unsigned qi = 0; qi < kSmallBatch; ++qi) {
+            const unsigned e = tid + (qb + qi) * 1024u;
 #pragma unroll
-        for (int w = 0; w < K; ++w) hv = mix64(hv ^ k[w] ^ (0x632be59bd9b4e019ull * (w + 1)));
-        unsigned slot = (unsigned)hv & (cap - 1u);
-        for (unsigned probes = 0; probes < cap; ++probes) {  // the table holds 2x the entries: always ends
-            const unsigned old = atomicCAS(&table[slot], 0u, e + 1u);
-            if (old == 0u) break;
-            uint64_t hk[K];
-            group_key<K>(keys, old - 1u, gm, tgt, varw, hk);
-            bool eq = true;
-#pragma unroll
-            for (int w = 0; w < K; ++w) eq = eq && hk[w] == k[w];
-            if (eq) break;
-            slot = (slot + 1u) & (cap - 1u);
+            for (int w = 0; w < K; ++w) full[qi][w] = e < n ? keys.w[w][e] : 0ull;
         }
-        myslot[q] = slot;
-        atomicAdd(&cnt[slot], 1u);
+#pragma unroll
+        for (unsigned qi = 0; qi < kSmallBatch; ++qi) {
+            const unsigned q = qb + qi, e = tid + q * 1024u;
+            myslot[q] = ~0u;
+            if (e >= n) continue;
+            bool pass = cond_ok<K>(full[qi], cond);
+            if (pass && varw.width && (unsigned)fget<K>(full[qi], varw) > max_digits) {
+                atomicOr(err, 4u);
+                pass = false;
+            }
+            if (!pass) {
+                pass_list[atomicAdd(&s_F, 1u)] = e;
+                continue;
+            }
+            uint64_t k[K];
+            group_key_of<K>(full[qi], gm, tgt, varw, k);
+            unsigned long long hv = 0x9e3779b97f4a7c15ull;
+#pragma unroll
+            for (int w = 0; w < K; ++w) hv = mix64(hv ^ k[w] ^ (0x632be59bd9b4e019ull * (w + 1)));
+            unsigned slot = (unsigned)hv & (cap - 1u);
+            for (unsigned probes = 0; probes < cap; ++probes) {  // the table holds 2x the entries: always ends
+                const unsigned old = atomicCAS(&table[slot], 0u, e + 1u);
+                if (old == 0u) break;
+                uint64_t hk[K];
+                group_key<K>(keys, old - 1u, gm, tgt, varw, hk);
+                bool eq = true;
+#pragma unroll
+                for (int w = 0; w < K; ++w) eq = eq && hk[w] == k[w];
+                if (eq) {
+                    s_dup = 1u;  // a group of two or more members
+                    break;
+                }
+                slot = (slot + 1u) & (cap - 1u);
+            }
+            myslot[q] = slot;
+            atomicAdd(&cnt[slot], 1u);
+        }
     }
     __syncthreads();
+    if (s_F == 0u && s_dup == 0u) {  // uniform over the CTA
+#pragma unroll
+        for (unsigned qb = 0; qb < kSmallPer; qb += kSmallBatch) {
+            double2 av[kSmallBatch];
+            unsigned tv[kSmallBatch];
+#pragma unroll
+            for (unsigned qi = 0; qi < kSmallBatch; ++qi) {
+                const unsigned e = tid + (qb + qi) * 1024u;
+                if (e < n) small_member(keys, amp, e, tgt, varw, tv[qi], av[qi]);
+            }
+#pragma unroll
+            for (unsigned qi = 0; qi < kSmallBatch; ++qi) {
+                const unsigned e = tid + (qb + qi) * 1024u;
+                if (e >= n) continue;
+                seg[e] = e;
+                ghead[e] = e;
+                btgt[e] = tv[qi];
+                bamp[e] = av[qi];
+            }
+        }
+        if (tid == 0) {
+            counts[0] = n;
+            counts[1] = 0u;
+            seg[n] = n;
+        }
+        return;
+    }
     // dense group ids and member offsets: one block-wide scan over the slots in order
     const unsigned per = cap / 1024u;  // cap >= 1024
     const unsigned s0 = tid * per;
@@ -2222,14 +2285,22 @@ __global__ void __launch_bounds__(1024) group_small_kernel(const __grid_constant
     __syncthreads();
     // members, contiguous per group
 #pragma unroll
-    for (unsigned q = 0; q < kSmallPer; ++q) {
-        const unsigned e = tid + q * 1024u;
-        if (myslot[q] == ~0u) continue;
-        const unsigned pos = atomicAdd(&cnt[myslot[q]], 1u);
-        const unsigned nd = varw.width ? (unsigned)((keys.w[varw.word][e] >> varw.shift) & wmask(varw.width))
-                                       : tgt.width;
-        btgt[pos] = (unsigned)((keys.w[tgt.word][e] >> tgt.shift) & wmask(nd));
-        bamp[pos] = amp[e];
+    for (unsigned qb = 0; qb < kSmallPer; qb += kSmallBatch) {
+        double2 av[kSmallBatch];
+        unsigned tv[kSmallBatch];
+#pragma unroll
+        for (unsigned qi = 0; qi < kSmallBatch; ++qi) {
+            const unsigned e = tid + (qb + qi) * 1024u;
+            if (myslot[qb + qi] != ~0u) small_member(keys, amp, e, tgt, varw, tv[qi], av[qi]);
+        }
+#pragma unroll
+        for (unsigned qi = 0; qi < kSmallBatch; ++qi) {
+            const unsigned q = qb + qi;
+            if (myslot[q] == ~0u) continue;
+            const unsigned pos = atomicAdd(&cnt[myslot[q]], 1u);
+            btgt[pos] = tv[qi];
+            bamp[pos] = av[qi];
+        }
     }
 }
 
