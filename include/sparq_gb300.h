@@ -598,7 +598,10 @@ int sq_clear_zero(sq_state* st, double eps);
  * at SQ_NOALLOC_MAX_ENTRIES; larger n returns SQ_ERR_CAPACITY. Work is issued
  * on `stream` (NULL = the default stream) and the call waits for it. The
  * first call on each device looks up that array's device address with the
- * device current; make that first call before capturing any stream. All calls
+ * device current; make that first call before capturing any stream. Under
+ * CUDA's lazy module loading that first call is also when the driver places
+ * the library's device code and the array in device memory, so device memory
+ * in use can grow once there; later calls leave it unchanged. All calls
  * share the array: calls that overlap on the GPU race. No output array may
  * overlap an input array (blocks write outputs while others still read
  * inputs): overlapping arrays return SQ_ERR_INVALID. */
