@@ -1763,7 +1763,11 @@ __global__ void __launch_bounds__(512, 2) emit_h4096x_kernel(const __grid_consta
                 x[j] = make_longlong2(to_fixed_right(d.x, emax, 50), to_fixed_right(d.y, emax, 50));
             }
             fwht8(x);  // layout A: slot bits 9-11
-            __syncthreads();  // every thread has read its slots as doubles
+            // every thread has read its slots as doubles before they are overwritten; a
+            // direct range was read from global memory, and the barrier after the
+            // exponent exchange already orders this group's writes after every
+            // use of the slots by the previous group
+            if (!direct) __syncthreads();
 #pragma unroll
             for (int j = 0; j < 8; ++j) ls[swz8(((unsigned)j << 9) | tid)] = x[j];
             __syncthreads();
