@@ -293,6 +293,46 @@ def test_hadamard_int(dual, strategy, n_digits, fill):
     dual.compare(exact_amp=True)
 
 
+@pytest.mark.parametrize("arith", ["reference", "exact-sum"])
+@pytest.mark.parametrize("n", [4097, 7000, 8192])
+@pytest.mark.parametrize("case", ["singletons", "one-pair", "one-failing"])
+def test_hadamard_int_one_cta_grouping(dual, n, case, arith):
+    """States of 4097 to 8192 entries (the most one CTA groups) with two key
+    words, so that every thread of the one-CTA grouping has entries in both
+    of its load batches: every group a singleton (written in entry order
+    without the scan and bucket pass), one group of two members, and one
+    entry failing the condition (both through the scan and bucket pass).
+    Split on 2 bits and merged back, against the oracle."""
+    ps.set_group_strategy("hash")
+    ps.set_fwht_arithmetic(arith)
+    dual.relaxed = arith == "exact-sum"
+    try:
+        dual.reg("x", U, 10)
+        dual.reg("y", U, 50)
+        dual.reg("z", U, 8)
+        dual.reg("c", ps.Boolean, 1)
+        assert ps.System.key_words() == 2
+        rng = np.random.default_rng(n * 3 + len(case))
+        y = rng.permutation(np.arange(n, dtype=np.uint64) * np.uint64(7919) + np.uint64(12345))  # distinct groups
+        x = rng.integers(0, 1 << 10, n).astype(np.uint64)
+        z = rng.integers(0, 1 << 8, n).astype(np.uint64)
+        c = np.ones(n, dtype=np.uint64)
+        if case == "one-pair":  # entry 1 joins entry 0's group with another target
+            y[1], z[1], x[1] = y[0], z[0], x[0] ^ np.uint64(1)
+        if case == "one-failing":
+            c[n // 2] = 0
+        regs = np.stack([x, y, z, c], axis=1)
+        amps = rng.normal(size=n) + 1j * rng.normal(size=n)
+        dual.start(regs, amps / np.linalg.norm(amps))
+        op = ps.Hadamard_Int("x", 2).conditioned_by_nonzeros("c")
+        dual.apply(op)
+        dual.compare(exact_amp=True)
+        dual.apply(op)
+        dual.compare(exact_amp=True)
+    finally:
+        ps.set_group_strategy("autotune")
+
+
 def test_hadamard_int_conditioned(dual, strategy):
     dual.reg("x", U, 6)
     dual.reg("y", U, 8)
